@@ -1,0 +1,22 @@
+"""GB300-native (sm_103a) body-of-revolution MoM monostatic RCS path.
+
+Drop-in modules mirroring the reference project's entry points:
+
+    bor_solver     solve_bor, solve_bor_pec, BorPecSolver, sphere_generatrix, ...
+    bor_streaming  StreamingFarBlocks, estimate_streaming_gb
+
+All numerics run on one GPU through libghost_bor.so (C ABI in include/ghost_bor.h).
+"""
+
+from . import bodies, geometry  # noqa: F401
+from .build import build  # noqa: F401
+
+__all__ = ["bodies", "geometry", "build", "bor_solver", "bor_streaming", "engine"]
+
+
+def __getattr__(name):
+    # the GPU modules import torch lazily so that a CPU-only import stays cheap
+    if name in ("bor_solver", "bor_streaming", "engine", "_native"):
+        import importlib
+        return importlib.import_module(f".{name}", __name__)
+    raise AttributeError(name)

@@ -1,0 +1,706 @@
+// lu.cu -- batched dense complex LU with partial pivoting, triangular solves,
+// mixed-precision residuals and small matrix helpers.  Replaces the LAPACK
+// zgesv behind np.linalg.solve (bor_solver.py:753) and its residual
+// (bor_solver.py:754-756) for every azimuthal mode at once.
+//
+// Right-looking blocked LU per matrix (one batch entry per mode):
+//   panel   one CTA per matrix factors an NB-wide column panel (pivot search
+//           with the LAPACK izamax rule |re| + |im|, first maximum wins)
+//   laswp   row interchanges applied to the columns outside the panel
+//   trsm    U12 = L11^-1 A12, one thread per column, L11 in shared memory
+//   gemm    A22 -= L21 U12 (complex rank-NB update, 64 x 64 tiles)
+// The same trsm/gemm kernels run the forward/back substitutions.
+#include "common.cuh"
+
+namespace gb {
+namespace {
+
+template <class R> struct LuCfg;
+template <> struct LuCfg<float> { static constexpr int NB = 64; };
+template <> struct LuCfg<double> { static constexpr int NB = 32; };
+
+constexpr int PANEL_THREADS = 512;
+constexpr int GT = 64;               // gemm tile (rows and columns)
+
+// ---------------------------------------------------------------------------
+// panel factorisation (one CTA per batch matrix)
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(PANEL_THREADS)
+panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long long sa,
+             int *__restrict__ ipiv, int *__restrict__ info)
+{
+    using CT = C<R>;
+    const int b = blockIdx.x;
+    CT *Ab = A + (size_t)b * sa;
+    int *piv = ipiv + (size_t)b * n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = PANEL_THREADS / 32;
+    __shared__ R s_val[NW];
+    __shared__ int s_idx[NW];
+    __shared__ int s_piv;
+    __shared__ CT s_prow[64];
+
+    for (int jj = 0; jj < nb; ++jj) {
+        const int col = k0 + jj;
+        // --- pivot search: max |re|+|im|, smallest index on ties
+        R best = R(-1);
+        int bi = n;
+        for (int i = col + tid; i < n; i += PANEL_THREADS) {
+            const R v = cabs1(Ab[(size_t)i * lda + col]);
+            if (v > best) { best = v; bi = i; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const R ov = __shfl_down_sync(0xffffffffu, best, off);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+            if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (lane == 0) { s_val[warp] = best; s_idx[warp] = bi; }
+        __syncthreads();
+        if (warp == 0) {
+            best = lane < NW ? s_val[lane] : R(-1);
+            bi = lane < NW ? s_idx[lane] : n;
+            for (int off = 16; off > 0; off >>= 1) {
+                const R ov = __shfl_down_sync(0xffffffffu, best, off);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+            }
+            if (lane == 0) {
+                const int p = (bi < n) ? bi : col;
+                s_piv = p;
+                piv[col] = p;
+                if (!(best > R(0)) && info[b] == 0) info[b] = col + 1;
+            }
+        }
+        __syncthreads();
+        const int p = s_piv;
+        // --- swap rows col <-> p inside the panel columns
+        if (p != col) {
+            for (int c = k0 + tid; c < k0 + nb; c += PANEL_THREADS) {
+                const CT t = Ab[(size_t)col * lda + c];
+                Ab[(size_t)col * lda + c] = Ab[(size_t)p * lda + c];
+                Ab[(size_t)p * lda + c] = t;
+            }
+        }
+        __syncthreads();
+        const CT pv = Ab[(size_t)col * lda + col];
+        const int ncol = k0 + nb - col - 1;           // trailing panel columns
+        for (int c = tid; c < ncol; c += PANEL_THREADS) s_prow[c] = Ab[(size_t)col * lda + col + 1 + c];
+        __syncthreads();
+        if (pv.x != R(0) || pv.y != R(0)) {
+            // reciprocal of the pivot (LAPACK scales by 1/pivot)
+            const R den = pv.x * pv.x + pv.y * pv.y;
+            const CT inv = mk<R>(pv.x / den, -pv.y / den);
+            // warps over rows, lanes over trailing columns (nb <= 64: two passes)
+            for (int i = col + 1 + warp; i < n; i += NW) {
+                CT l;
+                if (lane == 0) {
+                    l = cmul(Ab[(size_t)i * lda + col], inv);
+                    Ab[(size_t)i * lda + col] = l;
+                }
+                l.x = __shfl_sync(0xffffffffu, l.x, 0);
+                l.y = __shfl_sync(0xffffffffu, l.y, 0);
+                for (int c = lane; c < ncol; c += 32) {
+                    CT *dst = Ab + (size_t)i * lda + col + 1 + c;
+                    *dst = cfms(l, s_prow[c], *dst);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// apply the panel's interchanges to the columns outside [k0, k0 + nb)
+template <class R>
+__global__ void laswp_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long long sa,
+                             const int *__restrict__ ipiv)
+{
+    const int b = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncols = n - nb;
+    if (t >= ncols) return;
+    const int c = (t < k0) ? t : t + nb;
+    C<R> *Ab = A + (size_t)b * sa;
+    const int *piv = ipiv + (size_t)b * n;
+    for (int jj = 0; jj < nb; ++jj) {
+        const int r = k0 + jj, p = piv[r];
+        if (p != r) {
+            const C<R> x = Ab[(size_t)r * lda + c];
+            Ab[(size_t)r * lda + c] = Ab[(size_t)p * lda + c];
+            Ab[(size_t)p * lda + c] = x;
+        }
+    }
+}
+
+// row interchanges of a right-hand-side block, all n pivots in order
+template <class R>
+__global__ void laswp_rhs_kernel(int n, int nrhs, C<R> *__restrict__ B, long long ldb, long long sb,
+                                 const int *__restrict__ ipiv)
+{
+    const int b = blockIdx.y;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nrhs) return;
+    C<R> *Bb = B + (size_t)b * sb;
+    const int *piv = ipiv + (size_t)b * n;
+    for (int r = 0; r < n; ++r) {
+        const int p = piv[r];
+        if (p != r) {
+            const C<R> x = Bb[(size_t)r * ldb + c];
+            Bb[(size_t)r * ldb + c] = Bb[(size_t)p * ldb + c];
+            Bb[(size_t)p * ldb + c] = x;
+        }
+    }
+}
+
+// X := L^-1 X (unit lower) or U^-1 X (non-unit upper) for an nb-row block,
+// one thread per column.  T points at the nb x nb diagonal block.
+template <class R, int NB, bool UPPER>
+__global__ void __launch_bounds__(128)
+trsm_kernel(int nb, int ncols, const C<R> *__restrict__ T, long long ldt, long long st,
+            C<R> *__restrict__ X, long long ldx, long long sx)
+{
+    using CT = C<R>;
+    __shared__ CT Ts[NB][NB + 1];
+    __shared__ CT Dinv[NB];
+    const int b = blockIdx.y;
+    const CT *Tb = T + (size_t)b * st;
+    for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) {
+        const int r = i / nb, c = i % nb;
+        Ts[r][c] = Tb[(size_t)r * ldt + c];
+    }
+    __syncthreads();
+    if (UPPER) {
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+            const CT d = Ts[i][i];
+            const R den = d.x * d.x + d.y * d.y;
+            Dinv[i] = mk<R>(d.x / den, -d.y / den);
+        }
+        __syncthreads();
+    }
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    CT *Xb = X + (size_t)b * sx + c;
+    CT x[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) x[i] = (i < nb) ? Xb[(size_t)i * ldx] : mk<R>(0, 0);
+    if (!UPPER) {
+#pragma unroll
+        for (int i = 1; i < NB; ++i) {
+            if (i < nb) {
+                CT s = x[i];
+#pragma unroll
+                for (int j = 0; j < i; ++j) s = cfms(Ts[i][j], x[j], s);
+                x[i] = s;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = NB - 1; i >= 0; --i) {
+            if (i < nb) {
+                CT s = x[i];
+#pragma unroll
+                for (int j = i + 1; j < NB; ++j)
+                    if (j < nb) s = cfms(Ts[i][j], x[j], s);
+                x[i] = cmul(s, Dinv[i]);
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+        if (i < nb) Xb[(size_t)i * ldx] = x[i];
+}
+
+// C -= A B,  A: rows x K, B: K x cols, K <= NB; 64 x 64 tiles, 4 x 4 per thread
+template <class R, int NB>
+__global__ void __launch_bounds__(256)
+gemm_update_kernel(int rows, int cols, int K,
+                   const C<R> *__restrict__ A, long long lda, long long sa,
+                   const C<R> *__restrict__ B, long long ldb, long long sb,
+                   C<R> *__restrict__ Cm, long long ldc, long long sc)
+{
+    using CT = C<R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CT *As = reinterpret_cast<CT *>(smem_raw);            // [GT][NB+1]
+    CT *Bs = As + GT * (NB + 1);                          // [NB][GT]
+    const int b = blockIdx.z;
+    const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
+    const CT *Ab = A + (size_t)b * sa;
+    const CT *Bb = B + (size_t)b * sb;
+    CT *Cb = Cm + (size_t)b * sc;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < GT * K; i += 256) {
+        const int r = i / K, kk = i % K;
+        As[r * (NB + 1) + kk] = (r0 + r < rows) ? Ab[(size_t)(r0 + r) * lda + kk] : mk<R>(0, 0);
+    }
+    for (int i = tid; i < K * GT; i += 256) {
+        const int kk = i / GT, c = i % GT;
+        Bs[kk * GT + c] = (c0 + c < cols) ? Bb[(size_t)kk * ldb + c0 + c] : mk<R>(0, 0);
+    }
+    __syncthreads();
+    const int ty = tid >> 4, tx = tid & 15;
+    CT acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = mk<R>(0, 0);
+    for (int kk = 0; kk < K; ++kk) {
+        CT a[4], bv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[(ty + 16 * i) * (NB + 1) + kk];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = Bs[kk * GT + tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], bv[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty + 16 * i;
+        if (r >= rows) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tx + 16 * j;
+            if (c < cols) {
+                CT *dst = Cb + (size_t)r * ldc + c;
+                *dst = csub(*dst, acc[i][j]);
+            }
+        }
+    }
+}
+
+template <class R>
+int gemm_update(int batch, int rows, int cols, int K, const C<R> *A, long long lda, long long sa,
+                const C<R> *B, long long ldb, long long sb, C<R> *Cm, long long ldc, long long sc,
+                cudaStream_t st)
+{
+    if (rows <= 0 || cols <= 0 || K <= 0) return GHOST_BOR_OK;
+    constexpr int NB = LuCfg<R>::NB;
+    const size_t smem = sizeof(C<R>) * ((size_t)GT * (NB + 1) + (size_t)NB * GT);
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(gemm_update_kernel<R, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return check_launch("gemm_update: smem attribute");
+        attr_set = true;
+    }
+    dim3 grid((cols + GT - 1) / GT, (rows + GT - 1) / GT, batch);
+    gemm_update_kernel<R, NB><<<grid, 256, smem, st>>>(rows, cols, K, A, lda, sa, B, ldb, sb, Cm, ldc, sc);
+    return check_launch("gemm_update");
+}
+
+template <class R>
+int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv, int *info, cudaStream_t st)
+{
+    constexpr int NB = LuCfg<R>::NB;
+    if (cudaMemsetAsync(info, 0, sizeof(int) * batch, st) != cudaSuccess) return check_launch("getrf: memset");
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        panel_kernel<R><<<batch, PANEL_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+        int rc = check_launch("getrf: panel");
+        if (rc) return rc;
+        if (n - nb > 0) {
+            dim3 g((n - nb + 255) / 256, batch);
+            laswp_kernel<R><<<g, 256, 0, st>>>(n, k0, nb, A, lda, sa, ipiv);
+            if ((rc = check_launch("getrf: laswp"))) return rc;
+        }
+        const int rest = n - k0 - nb;
+        if (rest > 0) {
+            dim3 g((rest + 127) / 128, batch);
+            trsm_kernel<R, NB, false><<<g, 128, 0, st>>>(nb, rest, A + (size_t)k0 * lda + k0, lda, sa,
+                                                          A + (size_t)k0 * lda + k0 + nb, lda, sa);
+            if ((rc = check_launch("getrf: trsm"))) return rc;
+            rc = gemm_update<R>(batch, rest, rest, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
+                                A + (size_t)k0 * lda + k0 + nb, lda, sa,
+                                A + (size_t)(k0 + nb) * lda + k0 + nb, lda, sa, st);
+            if (rc) return rc;
+        }
+    }
+    return GHOST_BOR_OK;
+}
+
+template <class R>
+int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long long sa, const int *ipiv,
+               C<R> *B, long long ldb, long long sb, cudaStream_t st)
+{
+    constexpr int NB = LuCfg<R>::NB;
+    {
+        dim3 g((nrhs + 127) / 128, batch);
+        laswp_rhs_kernel<R><<<g, 128, 0, st>>>(n, nrhs, B, ldb, sb, ipiv);
+        int rc = check_launch("getrs: laswp");
+        if (rc) return rc;
+    }
+    dim3 gt((nrhs + 127) / 128, batch);
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = min(NB, n - k0);
+        trsm_kernel<R, NB, false><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)k0 * lda + k0, lda, sa,
+                                                       B + (size_t)k0 * ldb, ldb, sb);
+        int rc = check_launch("getrs: trsm L");
+        if (rc) return rc;
+        rc = gemm_update<R>(batch, n - k0 - nb, nrhs, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
+                            B + (size_t)k0 * ldb, ldb, sb, B + (size_t)(k0 + nb) * ldb, ldb, sb, st);
+        if (rc) return rc;
+    }
+    const int last = ((n - 1) / NB) * NB;
+    for (int k0 = last; k0 >= 0; k0 -= NB) {
+        const int nb = min(NB, n - k0);
+        trsm_kernel<R, NB, true><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)k0 * lda + k0, lda, sa,
+                                                      B + (size_t)k0 * ldb, ldb, sb);
+        int rc = check_launch("getrs: trsm U");
+        if (rc) return rc;
+        rc = gemm_update<R>(batch, k0, nrhs, nb, A + k0, lda, sa, B + (size_t)k0 * ldb, ldb, sb,
+                            B, ldb, sb, st);
+        if (rc) return rc;
+    }
+    return GHOST_BOR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// residuals
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool is_masked(const int *mr, int r)
+{
+    return mr[0] == r || mr[1] == r || mr[2] == r || mr[3] == r;
+}
+
+// R = B - Zf X - band X ;  Zf float, X / B / R double.  64 x 64 tiles over
+// (rows, rhs), K in chunks of 32 accumulated in FP32 then added in FP64.
+constexpr int RK = 32;
+__global__ void __launch_bounds__(256)
+residual_mixed_kernel(int n, int nrhs, int Nn, const float2 *__restrict__ Zf, long long ldz, long long sz,
+                      const double2 *__restrict__ band, const int *__restrict__ mask_rows,
+                      const double2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
+                      double2 *__restrict__ R, float2 *__restrict__ Rlo, double *__restrict__ norms)
+{
+    __shared__ float2 Zs[GT][RK + 1];
+    __shared__ float2 Xs[RK][GT];
+    __shared__ double red[2][8];
+    const int b = blockIdx.z;
+    const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
+    const float2 *Zb = Zf + (size_t)b * sz;
+    const double2 *Xb = X + (size_t)b * sbb;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    double2 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0, 0);
+    for (int k0 = 0; k0 < n; k0 += RK) {
+        __syncthreads();
+        for (int i = tid; i < GT * RK; i += 256) {
+            const int r = i / RK, kk = i % RK;
+            Zs[r][kk] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_float2(0, 0);
+        }
+        for (int i = tid; i < RK * GT; i += 256) {
+            const int kk = i / GT, c = i % GT;
+            double2 v = (k0 + kk < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kk) * ldb + c0 + c] : make_double2(0, 0);
+            Xs[kk][c] = make_float2((float)v.x, (float)v.y);
+        }
+        __syncthreads();
+        float2 ac[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) ac[i][j] = make_float2(0, 0);
+#pragma unroll 8
+        for (int kk = 0; kk < RK; ++kk) {
+            float2 a[4], x[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = Zs[ty + 16 * i][kk];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) x[j] = Xs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) ac[i][j] = cfma(a[i], x[j], ac[i][j]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { acc[i][j].x += ac[i][j].x; acc[i][j].y += ac[i][j].y; }
+    }
+    const int *mr = mask_rows + 4 * b;
+    const double2 *Bb = B + (size_t)b * sbb;
+    double rn = 0.0, bn = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty + 16 * i;
+        if (r >= n) continue;
+        const bool masked = is_masked(mr, r);
+        const int half = r >= Nn ? 1 : 0, node = r - half * Nn;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tx + 16 * j;
+            if (c >= nrhs) continue;
+            const double2 bv = Bb[(size_t)r * ldb + c];
+            double2 rv = make_double2(bv.x - acc[i][j].x, bv.y - acc[i][j].y);
+            if (band) {
+                for (int ch = 0; ch < 2; ++ch) {
+                    const double2 *bd = band + (((size_t)b * 4 + 2 * half + ch) * Nn + node) * 5;
+                    for (int d = 0; d < 5; ++d) {
+                        const int jn = node + d - 2;
+                        if (jn < 0 || jn >= Nn) continue;
+                        rv = cfms(bd[d], Xb[(size_t)(ch * Nn + jn) * ldb + c], rv);
+                    }
+                }
+            }
+            if (masked) rv = make_double2(0, 0);
+            R[(size_t)b * sbb + (size_t)r * ldb + c] = rv;
+            if (Rlo) Rlo[(size_t)b * sbb + (size_t)r * ldb + c] = make_float2((float)rv.x, (float)rv.y);
+            rn += rv.x * rv.x + rv.y * rv.y;
+            bn += bv.x * bv.x + bv.y * bv.y;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        rn += __shfl_down_sync(0xffffffffu, rn, off);
+        bn += __shfl_down_sync(0xffffffffu, bn, off);
+    }
+    if ((tid & 31) == 0) { red[0][tid >> 5] = rn; red[1][tid >> 5] = bn; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0, c = 0;
+        for (int w = 0; w < 8; ++w) { a += red[0][w]; c += red[1][w]; }
+        atomicAdd(norms + 2 * b, a);
+        atomicAdd(norms + 2 * b + 1, c);
+    }
+}
+
+constexpr int RK64 = 16;
+__global__ void __launch_bounds__(256)
+residual64_kernel(int n, int nrhs, const double2 *__restrict__ Z, long long ldz, long long sz,
+                  const double2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
+                  double2 *__restrict__ R, double *__restrict__ norms)
+{
+    __shared__ double2 Zs[GT][RK64 + 1];
+    __shared__ double2 Xs[RK64][GT];
+    __shared__ double red[2][8];
+    const int b = blockIdx.z;
+    const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
+    const double2 *Zb = Z + (size_t)b * sz;
+    const double2 *Xb = X + (size_t)b * sbb;
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    double2 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0, 0);
+    for (int k0 = 0; k0 < n; k0 += RK64) {
+        __syncthreads();
+        for (int i = tid; i < GT * RK64; i += 256) {
+            const int r = i / RK64, kk = i % RK64;
+            Zs[r][kk] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
+        }
+        for (int i = tid; i < RK64 * GT; i += 256) {
+            const int kk = i / GT, c = i % GT;
+            Xs[kk][c] = (k0 + kk < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kk) * ldb + c0 + c] : make_double2(0, 0);
+        }
+        __syncthreads();
+        for (int kk = 0; kk < RK64; ++kk) {
+            double2 a[4], x[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = Zs[ty + 16 * i][kk];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) x[j] = Xs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], x[j], acc[i][j]);
+        }
+    }
+    const double2 *Bb = B + (size_t)b * sbb;
+    double rn = 0.0, bn = 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty + 16 * i;
+        if (r >= n) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tx + 16 * j;
+            if (c >= nrhs) continue;
+            const double2 bv = Bb[(size_t)r * ldb + c];
+            const double2 rv = make_double2(bv.x - acc[i][j].x, bv.y - acc[i][j].y);
+            if (R) R[(size_t)b * sbb + (size_t)r * ldb + c] = rv;
+            rn += rv.x * rv.x + rv.y * rv.y;
+            bn += bv.x * bv.x + bv.y * bv.y;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        rn += __shfl_down_sync(0xffffffffu, rn, off);
+        bn += __shfl_down_sync(0xffffffffu, bn, off);
+    }
+    if ((tid & 31) == 0) { red[0][tid >> 5] = rn; red[1][tid >> 5] = bn; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0, c = 0;
+        for (int w = 0; w < 8; ++w) { a += red[0][w]; c += red[1][w]; }
+        atomicAdd(norms + 2 * b, a);
+        atomicAdd(norms + 2 * b + 1, c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// compose / mask / convert
+// ---------------------------------------------------------------------------
+__global__ void compose_kernel(int n, int Nn, const float2 *__restrict__ Zf, long long ldz, long long sz,
+                               const double2 *__restrict__ band, const int *__restrict__ mask_rows,
+                               float2 *__restrict__ A, long long lda, long long sa)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    const int b = blockIdx.z;
+    if (j >= n) return;
+    const int *mr = mask_rows + 4 * b;
+    float2 out;
+    if (is_masked(mr, i) || is_masked(mr, j)) {
+        out = make_float2(i == j ? 1.f : 0.f, 0.f);
+    } else {
+        const float2 z = Zf[(size_t)b * sz + (size_t)i * ldz + j];
+        double2 v = make_double2((double)z.x, (double)z.y);
+        if (band) {
+            const int a = i >= Nn, ch = j >= Nn;
+            const int ii = i - a * Nn, jj = j - ch * Nn;
+            const int d = jj - ii + 2;
+            if (d >= 0 && d <= 4) {
+                const double2 bv = band[(((size_t)b * 4 + 2 * a + ch) * Nn + ii) * 5 + d];
+                v.x += bv.x; v.y += bv.y;
+            }
+        }
+        out = make_float2((float)v.x, (float)v.y);
+    }
+    A[(size_t)b * sa + (size_t)i * lda + j] = out;
+}
+
+__global__ void mask64_kernel(int n, const int *__restrict__ mask_rows, double2 *__restrict__ Z,
+                              long long ldz, long long sz)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int slot = blockIdx.y;
+    const int b = blockIdx.z;
+    const int r = mask_rows[4 * b + slot];
+    if (r < 0 || r >= n || t >= n) return;
+    double2 *Zb = Z + (size_t)b * sz;
+    const double2 v = make_double2(t == r ? 1.0 : 0.0, 0.0);
+    Zb[(size_t)r * ldz + t] = v;
+    Zb[(size_t)t * ldz + r] = v;
+}
+
+__global__ void convert_kernel(int dir, int rows, int cols, const void *__restrict__ src, long long lds,
+                               long long ss, void *__restrict__ dst, long long ldd, long long sd)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    const int b = blockIdx.z;
+    if (c >= cols) return;
+    if (dir == 0) {
+        const double2 v = reinterpret_cast<const double2 *>(src)[(size_t)b * ss + (size_t)r * lds + c];
+        reinterpret_cast<float2 *>(dst)[(size_t)b * sd + (size_t)r * ldd + c] = make_float2((float)v.x, (float)v.y);
+    } else {
+        const float2 v = reinterpret_cast<const float2 *>(src)[(size_t)b * ss + (size_t)r * lds + c];
+        double2 *o = reinterpret_cast<double2 *>(dst) + (size_t)b * sd + (size_t)r * ldd + c;
+        if (dir == 1) *o = make_double2(v.x, v.y);
+        else { double2 t = *o; t.x += v.x; t.y += v.y; *o = t; }
+    }
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long long stride_a,
+                               int *ipiv, int *info, void *stream)
+{
+    if (batch < 1 || n < 1 || !A || !ipiv || !info || lda < n || stride_a < lda * n) return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (prec == GHOST_BOR_F32) return getrf_impl<float>(batch, n, reinterpret_cast<float2 *>(A), lda, stride_a, ipiv, info, st);
+    if (prec == GHOST_BOR_F64) return getrf_impl<double>(batch, n, reinterpret_cast<double2 *>(A), lda, stride_a, ipiv, info, st);
+    return GHOST_BOR_EINVAL;
+}
+
+extern "C" int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
+                               const void *A, long long lda, long long stride_a, const int *ipiv,
+                               void *B, long long ldb, long long stride_b, void *stream)
+{
+    if (batch < 1 || n < 1 || nrhs < 1 || !A || !ipiv || !B || lda < n || ldb < nrhs ||
+        stride_a < lda * n || stride_b < ldb * n)
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (prec == GHOST_BOR_F32)
+        return getrs_impl<float>(batch, n, nrhs, reinterpret_cast<const float2 *>(A), lda, stride_a, ipiv,
+                                 reinterpret_cast<float2 *>(B), ldb, stride_b, st);
+    if (prec == GHOST_BOR_F64)
+        return getrs_impl<double>(batch, n, nrhs, reinterpret_cast<const double2 *>(A), lda, stride_a, ipiv,
+                                  reinterpret_cast<double2 *>(B), ldb, stride_b, st);
+    return GHOST_BOR_EINVAL;
+}
+
+extern "C" int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
+                                  const void *Zf, long long ldz, long long stride_z,
+                                  const double *band, const int *mask_rows,
+                                  const double *X, const double *B, long long ldb, long long stride_b,
+                                  double *R, float *Rlo, double *norms, void *stream)
+{
+    if (batch < 1 || n < 1 || nrhs < 1 || !Zf || !mask_rows || !X || !B || !R || !norms ||
+        ldz < n || ldb < nrhs || n != 2 * Nn)
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual: memset");
+    dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
+    residual_mixed_kernel<<<grid, 256, 0, st>>>(n, nrhs, Nn, reinterpret_cast<const float2 *>(Zf), ldz, stride_z,
+                                                reinterpret_cast<const double2 *>(band), mask_rows,
+                                                reinterpret_cast<const double2 *>(X), reinterpret_cast<const double2 *>(B),
+                                                ldb, stride_b, reinterpret_cast<double2 *>(R),
+                                                reinterpret_cast<float2 *>(Rlo), norms);
+    return check_launch("residual");
+}
+
+extern "C" int ghost_bor_residual64(int batch, int n, int nrhs,
+                                    const double *Z, long long ldz, long long stride_z,
+                                    const double *X, const double *B, long long ldb, long long stride_b,
+                                    double *R, double *norms, void *stream)
+{
+    if (batch < 1 || n < 1 || nrhs < 1 || !Z || !X || !B || !norms || ldz < n || ldb < nrhs)
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual64: memset");
+    dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
+    residual64_kernel<<<grid, 256, 0, st>>>(n, nrhs, reinterpret_cast<const double2 *>(Z), ldz, stride_z,
+                                            reinterpret_cast<const double2 *>(X), reinterpret_cast<const double2 *>(B),
+                                            ldb, stride_b, reinterpret_cast<double2 *>(R), norms);
+    return check_launch("residual64");
+}
+
+extern "C" int ghost_bor_compose(int batch, int n, int Nn, const void *Zf, long long ldz, long long stride_z,
+                                 const double *band, const int *mask_rows,
+                                 void *A, long long lda, long long stride_a, void *stream)
+{
+    if (batch < 1 || n < 1 || n != 2 * Nn || !Zf || !mask_rows || !A || ldz < n || lda < n) return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    dim3 grid((n + 255) / 256, n, batch);
+    compose_kernel<<<grid, 256, 0, st>>>(n, Nn, reinterpret_cast<const float2 *>(Zf), ldz, stride_z,
+                                         reinterpret_cast<const double2 *>(band), mask_rows,
+                                         reinterpret_cast<float2 *>(A), lda, stride_a);
+    return check_launch("compose");
+}
+
+extern "C" int ghost_bor_mask64(int batch, int n, const int *mask_rows, double *Z, long long ldz, long long stride_z,
+                                void *stream)
+{
+    if (batch < 1 || n < 1 || !mask_rows || !Z || ldz < n) return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    dim3 grid((n + 255) / 256, 4, batch);
+    mask64_kernel<<<grid, 256, 0, st>>>(n, mask_rows, reinterpret_cast<double2 *>(Z), ldz, stride_z);
+    return check_launch("mask64");
+}
+
+extern "C" int ghost_bor_convert(int dir, int batch, int rows, int cols,
+                                 const void *src, long long lds, long long stride_s,
+                                 void *dst, long long ldd, long long stride_d, void *stream)
+{
+    if (dir < 0 || dir > 2 || batch < 1 || rows < 1 || cols < 1 || !src || !dst || lds < cols || ldd < cols)
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    dim3 grid((cols + 255) / 256, rows, batch);
+    convert_kernel<<<grid, 256, 0, st>>>(dir, rows, cols, src, lds, stride_s, dst, ldd, stride_d);
+    return check_launch("convert");
+}

@@ -1,0 +1,273 @@
+"""GPU sweep engine: one body, one frequency, every azimuthal mode at once.
+
+Stages (each a C-ABI call on one CUDA stream):
+
+  far fill      ghost_bor_far_efie   Z_far[m], m = 0..M (FP32 or FP64)
+  near fill     ghost_bor_near_efie  FP64 near/self blocks (band store or dense)
+  compose       ghost_bor_compose    A32 = fl32(Z_far + Z_near), masked
+  excitation    ghost_bor_rhs        B[m][row][2*it + pol] (FP64)
+  LU + solve    ghost_bor_getrf/getrs
+  refinement    ghost_bor_residual   R = B - (Z_far + Z_near) X in FP64 (FP32 products,
+                                     FP64 accumulation) then A32^-1 R, <= 3 passes
+  far field     ghost_bor_farfield   dF[m][col] by reciprocity
+
+Only modes m >= 0 are factored: Z(-m) = D Z(m) D with D = diag(I, -I) and the
+excitation obeys V(-m) = +-D V(m), so each -m system has the solution
++-D x(m) and contributes exactly the same far field; the mode sum weights
+m > 0 by two (checked against the per-mode reference in the tests).
+
+Precisions: "fp64" is the plain FP64 path (the comparator); "fp32ir" fills
+the far part and factors in FP32, keeps near/self blocks, the residual and the
+mode sum in FP64, and refines up to three times.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional
+
+import numpy as np
+
+from . import _native as nat
+from .geometry import (C0, ETA0, Generatrix, dct_tables, default_n_modes, gauss_on_generatrix,
+                       mask_rows, n_xi_efie, near_tables, pack_geo)
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the GB300 BoR path needs a CUDA device; there is no CPU fallback")
+    return torch
+
+
+@dataclass
+class SweepResult:
+    dF: np.ndarray                 # [M+1, 2 (VV, HH), n_theta] complex128, m = 0..M (mode weight applied)
+    residual: np.ndarray           # [M+1] ||AX - B|| / ||B|| per mode
+    refine_iters: int
+    timings: Dict[str, float] = field(default_factory=dict)
+    info: Optional[np.ndarray] = None
+    gpu_launches: int = 0
+
+
+class BorGpuProblem:
+    """Host tables (FP64) and their device copies for one body at one frequency."""
+
+    def __init__(self, points, freq_hz: float, thetas_deg, m_max: Optional[int] = None,
+                 gauss_order: int = 4, device=None):
+        if gauss_order != 4:
+            raise NotImplementedError("the GPU kernels are specialised for gauss_order=4")
+        torch = _torch()
+        nat.load()
+        self.torch = torch
+        self.device = torch.device("cuda" if device is None else device)
+        self.gen = Generatrix(points)
+        self.g = gauss_on_generatrix(self.gen, gauss_order)
+        self.freq_hz = float(freq_hz)
+        self.k = 2.0 * math.pi * self.freq_hz / C0
+        self.thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+        self.rho_max = float(np.max(self.gen.nodes[:, 0]))
+        if m_max is None:
+            m_max = default_n_modes(self.k, self.rho_max, self.thetas)
+        self.m_max = int(m_max)
+        self.N = self.gen.n_elems
+        if self.N < 3:
+            raise ValueError("the GPU path needs at least 3 generatrix elements")
+        self.Nn = self.gen.n_nodes
+        self.n = 2 * self.Nn
+        self.P = 4 * self.N
+        self.T = len(self.thetas)
+        self.nrhs = 2 * self.T
+        self.n_xi = n_xi_efie(self.k, self.rho_max, self.m_max)
+        dct, sin2 = dct_tables(self.n_xi, self.m_max + 2)
+        self.near = near_tables(self.gen, self.k, self.m_max)
+        self.masks = mask_rows(self.gen, self.m_max)
+        dev = self.device
+        f64 = torch.float64
+        elem = np.stack([self.gen.lengths, self.gen.trho, self.gen.tz])
+        self.d_geo = torch.as_tensor(pack_geo(self.g), dtype=f64, device=dev)
+        self.d_dct = torch.as_tensor(dct, dtype=f64, device=dev)
+        self.d_sin2 = torch.as_tensor(sin2, dtype=f64, device=dev)
+        self.d_nodes = torch.as_tensor(np.ascontiguousarray(self.gen.nodes), dtype=f64, device=dev)
+        self.d_elem = torch.as_tensor(np.ascontiguousarray(elem), dtype=f64, device=dev)
+        self.d_pairs = torch.as_tensor(self.near.pairs, dtype=torch.int32, device=dev)
+        self.d_tails = torch.as_tensor(self.near.tails, dtype=torch.int32, device=dev)
+        self.d_cells = torch.as_tensor(self.near.cells, dtype=f64, device=dev)
+        self.d_core = torch.as_tensor(self.near.core_gl, dtype=f64, device=dev)
+        self.d_tail = torch.as_tensor(self.near.tail_gl, dtype=f64, device=dev)
+        self.d_masks = torch.as_tensor(self.masks, dtype=torch.int32, device=dev)
+        self.d_thetas = torch.as_tensor(self.thetas, dtype=f64, device=dev)
+        w = np.full(self.m_max + 1, 2.0)
+        w[0] = 1.0
+        self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
+        self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
+
+    # -- memory -----------------------------------------------------------
+    def bytes_needed(self, precision: str) -> int:
+        Mb = self.m_max + 1
+        nn = self.n * self.n
+        rhs = self.n * self.nrhs
+        if precision == "fp64":
+            return Mb * (2 * nn * 16 + 3 * rhs * 16)
+        return Mb * (2 * nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16)
+
+    # -- stages -----------------------------------------------------------
+    def fill_far(self, Z, precision: int, scale: complex, stream: int):
+        ld = Z.shape[-1]
+        nat.call("ghost_bor_far_efie", precision, self.N, self.m_max, self.n_xi, self.k,
+                 scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_dct),
+                 nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), stream)
+
+    def fill_near(self, scale: complex, stream: int, band=None, Z=None):
+        ld = 0 if Z is None else Z.shape[-1]
+        ms = 0 if Z is None else Z.stride(0)
+        nat.call("ghost_bor_near_efie", nat.F64, self.N, self.m_max, self.k, scale.real, scale.imag,
+                 nat.ptr(self.d_nodes), nat.ptr(self.d_elem), len(self.near.pairs),
+                 nat.ptr(self.d_pairs), nat.ptr(self.d_tails), nat.ptr(self.d_cells),
+                 self.near.cells.shape[1], nat.ptr(self.d_core), nat.ptr(self.d_tail),
+                 self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms, stream)
+
+    def excitation(self, B, coef_e: float, coef_h: float, stream: int):
+        torch = self.torch
+        lib = nat.load()
+        nbytes = int(lib.ghost_bor_rhs_workspace(self.N, self.m_max, self.T))
+        work = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        nat.call("ghost_bor_rhs", self.N, self.m_max, self.T, self.k, coef_e, coef_h,
+                 nat.ptr(self.d_geo), nat.ptr(self.d_thetas), nat.ptr(self.d_masks),
+                 nat.ptr(B), B.shape[-1], B.stride(0), nat.ptr(work), stream)
+        return work
+
+    def assemble_modes_fp64(self, stream: Optional[int] = None):
+        """Dense FP64 Z(m), m = 0..M, unmasked, C factor applied: the
+        assemble_mode operator of the reference for every m >= 0."""
+        torch = self.torch
+        st = nat.stream_handle() if stream is None else stream
+        Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
+        self.fill_far(Z, nat.F64, self.C, st)
+        self.fill_near(self.C, st, Z=Z)
+        return Z
+
+    # -- the sweep ---------------------------------------------------------
+    def sweep(self, precision: str = "fp32ir", max_refine: int = 3,
+              check_abort: Optional[Callable] = None, keep: bool = False) -> SweepResult:
+        torch = self.torch
+        if precision not in ("fp64", "fp32ir"):
+            raise ValueError("precision must be 'fp64' or 'fp32ir'")
+        free, _ = torch.cuda.mem_get_info(self.device)
+        need = self.bytes_needed(precision)
+        if need > 0.92 * free:
+            raise MemoryError(f"GPU sweep needs {need / 1e9:.1f} GB, {free / 1e9:.1f} GB free")
+        st = nat.stream_handle()
+        Mb, n, nrhs, Nn = self.m_max + 1, self.n, self.nrhs, self.Nn
+        ev = {}
+        launches = 0
+
+        def mark(name):
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            ev[name] = e
+
+        def abort():
+            if check_abort is not None:
+                check_abort()
+
+        mark("start")
+        c128, c64 = torch.complex128, torch.complex64
+        B = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
+        ipiv = torch.empty((Mb, n), dtype=torch.int32, device=self.device)
+        info = torch.empty((Mb,), dtype=torch.int32, device=self.device)
+        norms = torch.empty((Mb, 2), dtype=torch.float64, device=self.device)
+        iters = 0
+        if precision == "fp64":
+            Z = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
+            self.fill_far(Z, nat.F64, self.C, st); mark("far"); abort()
+            self.fill_near(self.C, st, Z=Z); mark("near")
+            nat.call("ghost_bor_mask64", Mb, n, nat.ptr(self.d_masks), nat.ptr(Z), n, Z.stride(0), st)
+            Zc = Z.clone()
+            mark("compose"); abort()
+            work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
+            X = B.clone()
+            nat.call("ghost_bor_getrf", nat.F64, Mb, n, nat.ptr(Z), n, Z.stride(0), nat.ptr(ipiv),
+                     nat.ptr(info), st); mark("lu"); abort()
+            nat.call("ghost_bor_getrs", nat.F64, Mb, n, nrhs, nat.ptr(Z), n, Z.stride(0), nat.ptr(ipiv),
+                     nat.ptr(X), nrhs, X.stride(0), st); mark("solve")
+            nat.call("ghost_bor_residual64", Mb, n, nrhs, nat.ptr(Zc), n, Zc.stride(0), nat.ptr(X),
+                     nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(norms), st); mark("residual")
+            del Zc
+        else:
+            Zf = torch.zeros((Mb, n, n), dtype=c64, device=self.device)
+            band = torch.zeros((Mb, 4, Nn, 5), dtype=c128, device=self.device)
+            self.fill_far(Zf, nat.F32, self.C, st); mark("far"); abort()
+            self.fill_near(self.C, st, band=band); mark("near")
+            A = torch.empty((Mb, n, n), dtype=c64, device=self.device)
+            nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
+                     nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st); mark("compose"); abort()
+            work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
+            X32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
+            nat.call("ghost_bor_convert", 0, Mb, n, nrhs, nat.ptr(B), nrhs, B.stride(0), nat.ptr(X32),
+                     nrhs, X32.stride(0), st)
+            nat.call("ghost_bor_getrf", nat.F32, Mb, n, nat.ptr(A), n, A.stride(0), nat.ptr(ipiv),
+                     nat.ptr(info), st); mark("lu"); abort()
+            nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0), nat.ptr(ipiv),
+                     nat.ptr(X32), nrhs, X32.stride(0), st)
+            X = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
+            nat.call("ghost_bor_convert", 1, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(X),
+                     nrhs, X.stride(0), st); mark("solve")
+            R = torch.empty_like(B)
+            prev = None
+            for it in range(max_refine + 1):
+                nat.call("ghost_bor_residual", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
+                         nat.ptr(self.d_masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0), nat.ptr(R),
+                         nat.ptr(X32), nat.ptr(norms), st)
+                rel = float(torch.sqrt(torch.max(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300))))
+                if it == max_refine or rel < 1e-14 or (prev is not None and rel > 0.5 * prev):
+                    break
+                prev = rel
+                nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
+                         nat.ptr(ipiv), nat.ptr(X32), nrhs, X32.stride(0), st)
+                nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
+                         nat.ptr(X), nrhs, X.stride(0), st)
+                iters += 1
+                abort()
+            mark("residual")
+            if not keep:
+                del Zf, A, R, X32, band
+        dF = torch.empty((Mb, nrhs), dtype=c128, device=self.device)
+        nat.call("ghost_bor_farfield", nat.F64, Mb, n, nrhs, Nn, self.k, nat.ptr(self.d_mode_w),
+                 nat.ptr(B), nrhs, B.stride(0), nat.ptr(X), nrhs, X.stride(0), nat.ptr(dF), st)
+        mark("farfield")
+        dF_h = dF.cpu().numpy()
+        res = torch.sqrt(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300)).cpu().numpy()
+        info_h = info.cpu().numpy()
+        torch.cuda.synchronize()
+        names = list(ev)
+        tm = {f"{b}_s": ev[a].elapsed_time(ev[b]) / 1e3 for a, b in zip(names[:-1], names[1:])}
+        tm["gpu_total_s"] = ev[names[0]].elapsed_time(ev[names[-1]]) / 1e3
+        dF_h = dF_h.reshape(Mb, self.T, 2).transpose(0, 2, 1)
+        out = SweepResult(dF=np.ascontiguousarray(dF_h), residual=res, refine_iters=iters, timings=tm,
+                          info=info_h)
+        if keep:
+            out.X = X
+            out.B = B
+        return out
+
+
+def replay_truncation(dF: np.ndarray, mode_tol: float):
+    """The reference's mode loop in strict mode order (bor_solver.py:777-794):
+    accumulate per-|m| contributions, stop after two consecutive quiet modes."""
+    F = np.zeros(dF.shape[1:], dtype=np.complex128)
+    quiet = 0
+    used = 0
+    for am in range(dF.shape[0]):
+        F += dF[am]
+        used = am
+        scale = max(float(np.max(np.abs(F))), 1e-30)
+        if float(np.max(np.abs(dF[am]))) < mode_tol * scale:
+            quiet += 1
+            if quiet >= 2:
+                break
+        else:
+            quiet = 0
+    return F, used

@@ -1,0 +1,283 @@
+"""Host-side FP64 set-up of one body of revolution for the GPU kernels.
+
+Everything here is O(N) or O(N * cells) NumPy work that fixes the discrete
+problem exactly as the reference defines it:
+
+* generatrix checks, element lengths and tangents (bor_kernels.py:38-82)
+* 4-point Gauss data per element (bor_kernels.py:103-125), packed as the
+  ``geo`` array the kernels read
+* azimuth sample counts (bor_streaming.py:109-116) and the half-grid DCT /
+  sin^2 tables equivalent to the reference's FFT over xi
+* the graded near-cell quadrature (bor_solver.py:54-110), the per-pair tail
+  order of the near kernel (bor_kernels.py:238-240), Gauss-Legendre tables
+* the per-mode basis masks (bor_solver.py:611-622) as masked row indices
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+C0 = 299_792_458.0
+ETA0 = 376.730313668
+AXIS_TOL = 1e-12
+GEO_ROWS = 11      # rho, z, w, T0 w rho, T1 w rho, T0 w, T1 w, dRT0 w, dRT1 w, t_rho, t_z
+
+
+class Generatrix:
+    """Polyline generatrix in the (rho, z) half-plane, traversed from the +z
+    axis end to the -z axis end (bor_kernels.py:38-82)."""
+
+    def __init__(self, nodes):
+        pts = np.array(nodes, dtype=float)
+        if pts.ndim != 2 or pts.shape[1] != 2 or pts.shape[0] < 2:
+            raise ValueError("Generatrix needs an (Nn, 2) array of (rho, z) nodes.")
+        if np.any(pts[:, 0] < -1e-12):
+            raise ValueError("Generatrix rho coordinates must be >= 0.")
+        pts[:, 0] = np.maximum(pts[:, 0], 0.0)
+        self.nodes = pts
+        d = pts[1:] - pts[:-1]
+        self.lengths = np.hypot(d[:, 0], d[:, 1])
+        if np.any(self.lengths <= 0):
+            raise ValueError("Generatrix has a zero-length element.")
+        self.trho = d[:, 0] / self.lengths
+        self.tz = d[:, 1] / self.lengths
+        self.elem_n0 = np.arange(len(self.lengths))
+        self.elem_n1 = self.elem_n0 + 1
+
+    @property
+    def n_elems(self) -> int:
+        return len(self.lengths)
+
+    @property
+    def n_nodes(self) -> int:
+        return len(self.nodes)
+
+    def node_on_axis(self, i: int) -> bool:
+        return self.nodes[i, 0] <= AXIS_TOL * max(1.0, float(np.max(self.nodes[:, 0])))
+
+
+@dataclass
+class GaussData:
+    """Per-Gauss-point geometry (bor_kernels.py:84-101)."""
+    elem: np.ndarray
+    s: np.ndarray
+    w: np.ndarray
+    rho: np.ndarray
+    z: np.ndarray
+    trho: np.ndarray
+    tz: np.ndarray
+    T0: np.ndarray
+    T1: np.ndarray
+    dRT0: np.ndarray
+    dRT1: np.ndarray
+
+
+def gauss_on_generatrix(gen: Generatrix, order: int = 4) -> GaussData:
+    xg, wg = np.polynomial.legendre.leggauss(order)
+    s = 0.5 * (xg + 1.0)
+    w = 0.5 * wg
+    ne = gen.n_elems
+    S = np.tile(s, ne)
+    L = np.repeat(gen.lengths, order)
+    r0 = gen.nodes[gen.elem_n0]
+    r1 = gen.nodes[gen.elem_n1]
+    drho = np.repeat(r1[:, 0] - r0[:, 0], order)
+    rho = np.repeat(r0[:, 0], order) + S * drho
+    z = np.repeat(r0[:, 1], order) + S * np.repeat(r1[:, 1] - r0[:, 1], order)
+    return GaussData(
+        elem=np.repeat(np.arange(ne), order), s=S, w=np.tile(w, ne) * L, rho=rho, z=z,
+        trho=np.repeat(gen.trho, order), tz=np.repeat(gen.tz, order),
+        T0=1.0 - S, T1=S, dRT0=(drho * (1.0 - S) - rho) / L, dRT1=(drho * S + rho) / L)
+
+
+def pack_geo(g: GaussData) -> np.ndarray:
+    """[GEO_ROWS][P] array read by the far, excitation and far-field kernels."""
+    wr = g.w * g.rho
+    return np.ascontiguousarray(np.stack([
+        g.rho, g.z, g.w, g.T0 * wr, g.T1 * wr, g.T0 * g.w, g.T1 * g.w,
+        g.dRT0 * g.w, g.dRT1 * g.w, g.trho, g.tz]))
+
+
+def n_xi_efie(k: float, rho_max: float, m_max: int) -> int:
+    """Azimuth samples of the Green's function sweep (bor_streaming.py:109-111)."""
+    osc = 2.0 * abs(k) * rho_max
+    return int(2 ** math.ceil(math.log2(max(64, 4 * (m_max + 2), 6 * (osc + 4)))))
+
+
+def n_xi_bracket(k: float, rho_max: float, m_max: int) -> int:
+    """Azimuth samples of the MFIE bracket sweep (bor_streaming.py:114-116)."""
+    osc = 2.0 * abs(k) * rho_max
+    return int(2 ** math.ceil(math.log2(max(128, 6 * (m_max + 2), 8 * (osc + 4)))))
+
+
+def dct_tables(n_xi: int, n_orders: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Half-grid trapezoid/DCT-I weights equivalent to the reference's
+    FFT over xi_l = -pi + 2 pi l / n_xi for an even integrand:
+
+        G_n = (pi/h) [g_0 + (-1)^n g_h + 2 sum_{j=1}^{h-1} g_j cos(pi n j / h)],
+
+    h = n_xi/2, g_j = g(pi j / h).  Returns dct [h+1, n_orders] and
+    sin2 [h+1] = sin^2(pi j / n_xi)."""
+    h = n_xi // 2
+    j = np.arange(h + 1)
+    n = np.arange(n_orders)
+    c = np.full(h + 1, 2.0)
+    c[0] = c[h] = 1.0
+    # exact integer reduction of (n j) mod 2h keeps cos accurate for large n j
+    nj = np.outer(j, n) % (2 * h)
+    ang = np.pi * nj / h
+    dct = (np.pi / h) * c[:, None] * np.cos(ang)
+    sin2 = np.sin(0.5 * np.pi * j / h) ** 2
+    return np.ascontiguousarray(dct), np.ascontiguousarray(sin2)
+
+
+# ---------------------------------------------------------------------------
+# graded near cells (bor_solver.py:54-110)
+# ---------------------------------------------------------------------------
+
+def graded_cells(kind: str, depth: int = 4) -> List[Tuple[float, float, float, float]]:
+    """Cells (s0, s1, s'0, s'1) of [0,1]^2 refined toward the singular set:
+    the diagonal (``diag``) or a shared corner (``cornerAB``: s = A, s' = B)."""
+    cells: List[Tuple[float, float, float, float]] = []
+
+    def singular(a0, a1, b0, b1):
+        if kind == "diag":
+            return not (a1 <= b0 or b1 <= a0)
+        ca = 0.0 if kind[6] == "0" else 1.0
+        cb = 0.0 if kind[7] == "0" else 1.0
+        return a0 <= ca <= a1 and b0 <= cb <= b1
+
+    def visit(a0, a1, b0, b1, level):
+        if level >= depth or not singular(a0, a1, b0, b1):
+            cells.append((a0, a1, b0, b1))
+            return
+        am, bm = 0.5 * (a0 + a1), 0.5 * (b0 + b1)
+        visit(a0, am, b0, bm, level + 1)
+        visit(a0, am, bm, b1, level + 1)
+        visit(am, a1, b0, bm, level + 1)
+        visit(am, a1, bm, b1, level + 1)
+
+    visit(0.0, 1.0, 0.0, 1.0, 0)
+    return cells
+
+
+def cell_points(kind: str, gorder: int = 4) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Test points (order ``gorder``), source points (order ``gorder + 1``, so a
+    test and a source point never coincide) and weights over the cells."""
+    xs, ws = np.polynomial.legendre.leggauss(gorder)
+    xq, wq = np.polynomial.legendre.leggauss(gorder + 1)
+    us, vs = 0.5 * (xs + 1.0), 0.5 * ws
+    uq, vq = 0.5 * (xq + 1.0), 0.5 * wq
+    S, Q, W = [], [], []
+    for (a0, a1, b0, b1) in graded_cells(kind):
+        ha, hb = a1 - a0, b1 - b0
+        ss, qq = np.meshgrid(a0 + us * ha, b0 + uq * hb, indexing="ij")
+        S.append(ss.ravel())
+        Q.append(qq.ravel())
+        W.append(np.outer(vs * ha, vq * hb).ravel())
+    return np.concatenate(S), np.concatenate(Q), np.concatenate(W)
+
+
+_NEAR_KINDS = ("diag", "corner10", "corner01")
+
+
+@dataclass
+class NearTables:
+    pairs: np.ndarray        # [n_pairs, 4] int32: e, f, cell offset, cell count
+    tails: np.ndarray        # [n_pairs, 2] int32: tail offset, n_tail
+    cells: np.ndarray        # [3, n_cells_total]
+    core_gl: np.ndarray      # [2, 48]
+    tail_gl: np.ndarray      # [2, n_tail_total]
+    n_tail: np.ndarray = field(default=None)
+
+
+def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> NearTables:
+    """Element pairs |e - f| <= 1, their cell sets and the tail Gauss order
+    n_tail = clip(ceil(4 (max|k| a / pi + m_max + 2)), 64, 1024) with
+    a = sqrt(4 rho rho') over the pair's non-axis point pairs, bit-identical to
+    the reference's choice (bor_kernels.py:199-204, 238-240)."""
+    ne = gen.n_elems
+    kinds = {}
+    off = 0
+    blocks = []
+    for kind in _NEAR_KINDS:
+        s, sp_, w = cell_points(kind)
+        kinds[kind] = (off, len(s), s, sp_)
+        blocks.append(np.stack([s, sp_, w]))
+        off += len(s)
+    cells = np.ascontiguousarray(np.concatenate(blocks, axis=1))
+    pairs = []
+    ntails = []
+    x0 = gen.nodes[:-1]
+    x1 = gen.nodes[1:]
+    for kind, df in (("diag", 0), ("corner10", 1), ("corner01", -1)):
+        e = np.arange(max(0, -df), ne - max(0, df))
+        f = e + df
+        coff, cnt, s, sp_ = kinds[kind]
+        rho_p = x0[e, 0][:, None] + s[None, :] * (x1[e, 0] - x0[e, 0])[:, None]
+        rho_q = x0[f, 0][:, None] + sp_[None, :] * (x1[f, 0] - x0[f, 0])[:, None]
+        rr4 = 4.0 * rho_p * rho_q
+        a = np.sqrt(np.where(rr4 > 1e-30, rr4, 0.0))
+        osc = np.max(abs(complex(k)) * a, axis=1) / math.pi + (m_max + 2)
+        nt = np.minimum(1024, np.maximum(64, np.ceil(4.0 * osc))).astype(np.int64)
+        nt[~np.any(rr4 > 1e-30, axis=1)] = 0
+        for i in range(len(e)):
+            pairs.append((int(e[i]), int(f[i]), coff, cnt))
+            ntails.append(int(nt[i]))
+    pairs = np.asarray(pairs, dtype=np.int32)
+    ntails = np.asarray(ntails, dtype=np.int64)
+    order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+    pairs = pairs[order]
+    ntails = ntails[order]
+    uniq = sorted(set(int(n) for n in ntails if n > 0))
+    tab_u, tab_w, offs = [], [], {}
+    o = 0
+    for n in uniq:
+        x, wt = np.polynomial.legendre.leggauss(n)
+        tab_u.append(0.5 * (x + 1.0))
+        tab_w.append(0.5 * wt)
+        offs[n] = o
+        o += n
+    tail_gl = (np.ascontiguousarray(np.stack([np.concatenate(tab_u), np.concatenate(tab_w)]))
+               if uniq else np.zeros((2, 1)))
+    tails = np.asarray([(offs.get(int(n), 0), int(n)) for n in ntails], dtype=np.int32)
+    xc, wc = np.polynomial.legendre.leggauss(core_order)
+    core_gl = np.ascontiguousarray(np.stack([0.5 * (xc + 1.0), 0.5 * wc]))
+    return NearTables(pairs=np.ascontiguousarray(pairs), tails=np.ascontiguousarray(tails),
+                      cells=cells, core_gl=core_gl, tail_gl=tail_gl, n_tail=ntails)
+
+
+def basis_mask(gen: Generatrix, m: int) -> np.ndarray:
+    """Active (J_t, J_phi) bases of mode m (bor_solver.py:611-622)."""
+    Nn = gen.n_nodes
+    t_act = np.ones(Nn, dtype=bool)
+    f_act = np.ones(Nn, dtype=bool)
+    for end in (0, Nn - 1):
+        if gen.node_on_axis(end):
+            t_act[end] = abs(m) == 1
+            f_act[end] = False
+        else:
+            t_act[end] = False
+            f_act[end] = True
+    return np.concatenate([t_act, f_act])
+
+
+def mask_rows(gen: Generatrix, m_max: int) -> np.ndarray:
+    """[m_max+1, 4] int32 masked row indices per mode m >= 0 (-1 = unused)."""
+    out = np.full((m_max + 1, 4), -1, dtype=np.int32)
+    for m in range(m_max + 1):
+        rows = np.flatnonzero(~basis_mask(gen, m))
+        if len(rows) > 4:
+            raise ValueError("basis mask removes more than four rows")
+        out[m, :len(rows)] = rows
+    return out
+
+
+def default_n_modes(k: float, rho_max: float, thetas_deg) -> int:
+    """bor_solver.py:845-847."""
+    st = float(np.max(np.abs(np.sin(np.radians(np.atleast_1d(thetas_deg))))))
+    return int(math.ceil(k * rho_max * max(st, 0.05))) + 12

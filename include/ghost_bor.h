@@ -1,0 +1,213 @@
+/*
+ * ghost_bor.h -- C ABI of the GB300 (sm_103a) body-of-revolution MoM path.
+ *
+ * Every function takes DEVICE pointers (caller-owned, allocated by the caller),
+ * explicit sizes, and a CUDA stream passed as `void *` (NULL = legacy default
+ * stream).  Kernels are launched asynchronously on that stream; the return
+ * value only reports argument and launch errors.  Device-side numerical status
+ * (zero pivots, iteration limits) is written to caller buffers named `info`.
+ *
+ * Complex arrays are interleaved (re, im) pairs of float (precision
+ * GHOST_BOR_F32) or double (GHOST_BOR_F64).  Matrices are row-major with an
+ * explicit leading dimension (elements between rows); batches of matrices are
+ * separated by an explicit batch stride (elements).
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   sample_g / sample_mfie  bor_stream_kernel.c:26-48, 65-106 (ctypes binding
+ *                           bor_streaming.py:50-73)
+ *   far fill                bor_streaming.py:220-268 + 352-407
+ *                           (StreamingFarBlocks._build_range, efie_blocks,
+ *                           bracket_blocks)
+ *   near fill               bor_solver.py:270-336 + bor_kernels.py:170-257
+ *                           (_near_pair_data, modal_kernels_near, near loop of
+ *                           assemble_mode); MFIE: bor_solver.py:372-435,
+ *                           bor_kernels.py:334-431
+ *   excitation              bor_solver.py:437-461, 625-645 (rhs_mfie_mode,
+ *                           rhs_mode) for all modes x angles x polarisations
+ *   LU + solves             bor_solver.py:753 (np.linalg.solve = zgesv)
+ *   far field + mode sum    bor_solver.py:659-708, 771-801 (farfield_mode,
+ *                           _mode_sweep accumulation)
+ */
+#ifndef GHOST_BOR_H
+#define GHOST_BOR_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GHOST_BOR_OK            0
+#define GHOST_BOR_EINVAL        1   /* bad argument (size, pointer, alignment) */
+#define GHOST_BOR_ECUDA         2   /* kernel launch / CUDA runtime error */
+#define GHOST_BOR_EUNSUPPORTED  3   /* valid but unsupported configuration */
+
+/* precisions */
+#define GHOST_BOR_F32 0
+#define GHOST_BOR_F64 1
+
+/* Library version (major*10000 + minor*100 + patch). */
+int ghost_bor_version(void);
+
+/* Human-readable text of the last CUDA error seen by this library (thread-local). */
+const char *ghost_bor_last_error(void);
+
+/* Number of kernels this library has launched since it was loaded. */
+long long ghost_bor_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Drop-in device samplers.  Same argument meaning and output layout as the
+ * reference ctypes functions, with device pointers and a stream:
+ *   out[i][j][l] (interleaved complex double), i < nr, j < np_, l < nxi.
+ * Replaces sample_g (bor_stream_kernel.c:26-48).
+ */
+int ghost_bor_sample_g(int nr, int np_, int nxi,
+                       const double *rho_p, const double *z_p,
+                       const double *rho_q, const double *z_q,
+                       double k, const double *sin2_tab, double *out,
+                       void *stream);
+
+/* Replaces sample_mfie (bor_stream_kernel.c:65-106). */
+int ghost_bor_sample_mfie(int nr, int np_, int nxi,
+                          const double *rho_p, const double *z_p,
+                          const double *tr_p, const double *tz_p,
+                          const double *rho_q, const double *z_q,
+                          const double *tr_q, const double *tz_q,
+                          double k, const double *cos_tab, const double *sin_tab,
+                          double *o_tt, double *o_tf, double *o_ft, double *o_ff,
+                          void *stream);
+
+/* ------------------------------------------------------------------------
+ * Fused EFIE far fill: for every far element pair (|e - f| >= 2) sample the
+ * Green's function on the half azimuth grid xi_j = pi j / (nxi/2), take the
+ * even DCT to orders 0..m_max+1, contract with the Galerkin weights and
+ * combine the orders into the mode-m blocks, m = 0..m_max, then ADD
+ * scale * [[ztt, ztf], [zft, zff]] into Z[m] (rows 0..Nn-1 = J_t tests,
+ * Nn..2Nn-1 = J_phi tests).  Z must be zeroed (or hold other terms) first.
+ *
+ *   geo   [11][P] doubles, P = 4 n_elem (Gauss points, element-major):
+ *         rho, z, w, T0*w*rho, T1*w*rho, T0*w, T1*w, dRT0*w, dRT1*w, t_rho, t_z
+ *   dct   [nxi/2+1][m_max+2]  (pi/h) * c_j * cos(pi n j / h), c_0 = c_h = 1, else 2
+ *   sin2  [nxi/2+1]           sin^2(pi j / nxi)
+ *   Z     complex, precision `prec`, Z[m] at Z + m*mode_stride, row stride ldz
+ * Replaces StreamingFarBlocks._build_range + efie_blocks
+ * (bor_streaming.py:220-268, 320-376, 388-407).
+ */
+int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
+                       double scale_re, double scale_im,
+                       const double *geo, const double *dct, const double *sin2,
+                       void *Z, long long ldz, long long mode_stride,
+                       void *stream);
+
+/* ------------------------------------------------------------------------
+ * FP64 near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
+ * the graded-cell + sinh-core + Gauss-tail quadrature of the reference.
+ *   nodes     [Nn][2] (rho, z);  elem [3][n_elem] (length, t_rho, t_z)
+ *   pairs     [n_pairs][4] ints: e, f, cell-table offset, cell count
+ *   tails     [n_pairs][2] ints: tail-table offset, n_tail
+ *   cells     [3][n_cells_total] (s, s', w)
+ *   core_gl   [2][48] (u01, w01);  tail_gl [2][n_tail_total] (u01, w01)
+ * Output: if band != NULL, ADD scale * block into band[m][blk][Nn][5]
+ * (complex double, blk = tt, tf, ft, ff; column offset -2..2); else into the
+ * dense Z[m] (precision prec, like ghost_bor_far_efie).
+ * Replaces _near_pair_data + modal_kernels_near + the near loop of
+ * assemble_mode (bor_solver.py:270-336, bor_kernels.py:170-257).
+ */
+int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
+                        double scale_re, double scale_im,
+                        const double *nodes, const double *elem,
+                        int n_pairs, const int *pairs, const int *tails,
+                        const double *cells, int n_cells_total,
+                        const double *core_gl, const double *tail_gl, int n_tail_total,
+                        double *band, void *Z, long long ldz, long long mode_stride,
+                        void *stream);
+
+/* ------------------------------------------------------------------------
+ * Excitation for all modes 0..m_max, angles and both polarisations:
+ *   B[m][row][2*it + pol] (complex double, row stride ldb, mode stride),
+ *   pol 0 = VV (theta), 1 = HH (phi).  Rows flagged in mask_rows[m][4]
+ *   (-1 = unused) are written as zero.
+ *   coef_e multiplies the EFIE excitation <W, E_inc> (rhs_mode),
+ *   coef_h multiplies the rotated MFIE excitation <W, n x H_inc>
+ *   (rhs_mfie_mode); either may be 0.
+ *   geo as in ghost_bor_far_efie; thetas_deg [n_theta].
+ *   work: caller scratch of ghost_bor_rhs_workspace() bytes.
+ * Bessel J_n by Miller's backward recurrence (FP64).
+ */
+long long ghost_bor_rhs_workspace(int n_elem, int m_max, int n_theta);
+int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
+                  double coef_e, double coef_h,
+                  const double *geo, const double *thetas_deg,
+                  const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                  void *work, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Batched complex LU with partial pivoting (|re|+|im| pivot rule, as LAPACK
+ * izamax) of n x n matrices A[b] = A + b*stride_a, row-major, b < batch.
+ * ipiv[b][n] receives 0-based pivot rows; info[b] = 0 or (first zero pivot
+ * column + 1).  In place.
+ */
+int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long long stride_a,
+                    int *ipiv, int *info, void *stream);
+
+/* Solve A X = B with the factors of ghost_bor_getrf for nrhs columns
+ * (B row-major n x nrhs, in place).  precisions of A and B are equal. */
+int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
+                    const void *A, long long lda, long long stride_a, const int *ipiv,
+                    void *B, long long ldb, long long stride_b, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Mixed-precision residual for iterative refinement, per batch b:
+ *   R = B - (Zf + band) X        with Zf complex float (far part), band
+ *   complex double [Nn blocks as in ghost_bor_near_efie] (may be NULL), X and
+ *   B complex double; rows in mask_rows[b] produce R = 0.
+ * If Rlo != NULL the residual is also written as complex float to Rlo.
+ * norms[b][2] receives (||R||_F^2, ||B||_F^2).
+ * Products accumulate in FP32 over 64-term chunks and in FP64 across chunks.
+ */
+int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
+                       const void *Zf, long long ldz, long long stride_z,
+                       const double *band, const int *mask_rows,
+                       const double *X, const double *B, long long ldb, long long stride_b,
+                       double *R, float *Rlo, double *norms, void *stream);
+
+/* FP64 residual R = B - Z X (all complex double); norms as above. */
+int ghost_bor_residual64(int batch, int n, int nrhs,
+                         const double *Z, long long ldz, long long stride_z,
+                         const double *X, const double *B, long long ldb, long long stride_b,
+                         double *R, double *norms, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Far field by reciprocity + mode weights:
+ *   dF[b][c] = pref * wt[b] * sgn(c) * sum_i d_i Ve[b][i][c] X[b][i][c]
+ * d_i = +1 for rows < Nn (J_t), -1 otherwise; sgn(c) = +1 for even c (VV),
+ * -1 for odd c (HH); pref = -j k eta0 / (4 pi).  X precision prec; Ve double.
+ * Replaces farfield_mode (bor_solver.py:659-708).
+ */
+int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
+                       const double *mode_weight,
+                       const double *Ve, long long ldv, long long stride_v,
+                       const void *X, long long ldx, long long stride_x,
+                       double *dF, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Small helpers used between stages.
+ * ghost_bor_compose: A32[b] = fl32(Zf[b] + band[b]) with masked rows/columns
+ *   replaced by identity rows/columns (band may be NULL).
+ * ghost_bor_mask64: apply the same identity masking to a complex double Z.
+ * ghost_bor_convert: elementwise complex double <-> float copy of a strided
+ *   batch of row blocks (dir 0: double->float, 1: float->double, 2: float
+ *   added into double).
+ */
+int ghost_bor_compose(int batch, int n, int Nn, const void *Zf, long long ldz, long long stride_z,
+                      const double *band, const int *mask_rows,
+                      void *A, long long lda, long long stride_a, void *stream);
+int ghost_bor_mask64(int batch, int n, const int *mask_rows,
+                     double *Z, long long ldz, long long stride_z, void *stream);
+int ghost_bor_convert(int dir, int batch, int rows, int cols,
+                      const void *src, long long lds, long long stride_s,
+                      void *dst, long long ldd, long long stride_d, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GHOST_BOR_H */

@@ -1,0 +1,772 @@
+"""CPU oracle for the BoR-MoM monostatic path -- TEST INFRASTRUCTURE ONLY.
+
+A NumPy restatement of the reference's PEC body-of-revolution solver
+(``bor_solver.solve_bor`` with ``formulation`` "efie" / "cfie",
+``table_precision="double"``, ``assembly="streaming"``).  It is the checker
+that the CUDA product is compared against; the product never imports it.
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs may
+import, call or time anything under ``oracle/``.
+
+Parity pinned: ``tests/test_oracle_golden.py`` checks this module against
+golden vectors produced by running the reference itself
+(``tests/golden/make_golden.py``).
+
+Every function cites the reference lines it restates (paths relative to the
+reference project root).  The far-field assembly follows the reference's
+streaming algorithm: uniform xi sampling (C sampler ``oracle/sampler.c`` when
+built, NumPy otherwise), FFT over xi, zeroing of same/adjacent-element pairs,
+contraction to nodal per-order primitives (bor_streaming.py:220-407).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import threading
+from concurrent.futures import ThreadPoolExecutor
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+from scipy import special as sp
+
+C0 = 299_792_458.0          # bor_kernels.py:29
+ETA0 = 376.730313668        # bor_kernels.py:30
+AXIS_TOL = 1e-12            # bor_kernels.py:31
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+# ---------------------------------------------------------------------------
+# optional C sampler (oracle/sampler.c, built by oracle/build_oracle.py)
+# ---------------------------------------------------------------------------
+
+def _load_sampler():
+    path = os.path.join(_HERE, "_build", "liboracle_sampler.so")
+    if not os.path.exists(path):
+        return None
+    try:
+        lib = ctypes.CDLL(path)
+    except OSError:
+        return None
+    dp = ctypes.POINTER(ctypes.c_double)
+    ci, cd = ctypes.c_int, ctypes.c_double
+    lib.oracle_sample_g.argtypes = [ci, ci, ci, dp, dp, dp, dp, cd, dp, dp]
+    lib.oracle_sample_g.restype = None
+    lib.oracle_sample_mfie.argtypes = [ci, ci, ci] + [dp] * 8 + [cd, dp, dp] + [dp] * 4
+    lib.oracle_sample_mfie.restype = None
+    return lib
+
+
+_SAMPLER = _load_sampler()
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+# ---------------------------------------------------------------------------
+# geometry: bor_kernels.py:38-125, bor_solver.py:230-242
+# ---------------------------------------------------------------------------
+
+class Geom:
+    """Generatrix polyline + Gauss data (bor_kernels.py:38-82, 103-125)."""
+
+    def __init__(self, points, gauss_order: int = 4):
+        pts = np.array(points, dtype=float)
+        if pts.ndim != 2 or pts.shape[1] != 2 or pts.shape[0] < 2:
+            raise ValueError("Generatrix needs an (Nn, 2) array of (rho, z) nodes.")
+        if np.any(pts[:, 0] < -1e-12):
+            raise ValueError("Generatrix rho coordinates must be >= 0.")
+        pts[:, 0] = np.maximum(pts[:, 0], 0.0)
+        self.nodes = pts
+        seg = pts[1:] - pts[:-1]
+        self.lengths = np.hypot(seg[:, 0], seg[:, 1])
+        if np.any(self.lengths <= 0):
+            raise ValueError("Generatrix has a zero-length element.")
+        self.trho = seg[:, 0] / self.lengths
+        self.tz = seg[:, 1] / self.lengths
+        self.ne = len(self.lengths)
+        self.Nn = len(pts)
+        # Gauss-Legendre on each element, local s in [0, 1]
+        xg, wg = np.polynomial.legendre.leggauss(gauss_order)
+        s = 0.5 * (xg + 1.0)
+        w = 0.5 * wg
+        go = gauss_order
+        self.go = go
+        self.elem = np.repeat(np.arange(self.ne), go)
+        S = np.tile(s, self.ne)
+        L = np.repeat(self.lengths, go)
+        r0 = pts[:-1]
+        r1 = pts[1:]
+        d_rho = np.repeat(r1[:, 0] - r0[:, 0], go)
+        self.s = S
+        self.w = np.tile(w, self.ne) * L
+        self.rho = np.repeat(r0[:, 0], go) + S * d_rho
+        self.z = np.repeat(r0[:, 1], go) + S * np.repeat(r1[:, 1] - r0[:, 1], go)
+        self.ptr = np.repeat(self.trho, go)
+        self.ptz = np.repeat(self.tz, go)
+        self.T0 = 1.0 - S
+        self.T1 = S
+        self.dRT0 = (d_rho * (1.0 - S) - self.rho) / L
+        self.dRT1 = (d_rho * S + self.rho) / L
+        self.P = len(S)
+        # dense nodal shape matrices (bor_solver.py:230-242)
+        self.BT = np.zeros((self.Nn, self.P))
+        self.BD = np.zeros((self.Nn, self.P))
+        idx = np.arange(self.P)
+        self.BT[self.elem, idx] = self.T0
+        self.BT[self.elem + 1, idx] = self.T1
+        self.BD[self.elem, idx] = self.dRT0
+        self.BD[self.elem + 1, idx] = self.dRT1
+
+    def on_axis(self, i: int) -> bool:
+        """bor_kernels.py:80-81."""
+        return self.nodes[i, 0] <= AXIS_TOL * max(1.0, float(np.max(self.nodes[:, 0])))
+
+    def points_on_element(self, e: int, s: np.ndarray):
+        """bor_solver.py:117-127."""
+        r0, r1 = self.nodes[e], self.nodes[e + 1]
+        rho = r0[0] + s * (r1[0] - r0[0])
+        z = r0[1] + s * (r1[1] - r0[1])
+        L = self.lengths[e]
+        drho = r1[0] - r0[0]
+        d0 = (drho * (1.0 - s) - rho) / L
+        d1 = (drho * s + rho) / L
+        return rho, z, 1.0 - s, s, d0, d1, L
+
+
+def n_xi_efie(k: float, rho_max: float, m_max: int) -> int:
+    """bor_streaming.py:109-111 (= bor_kernels.py:149-152)."""
+    osc = 2.0 * abs(k) * rho_max
+    return int(2 ** math.ceil(math.log2(max(64, 4 * (m_max + 2), 6 * (osc + 4)))))
+
+
+def n_xi_bracket(k: float, rho_max: float, m_max: int) -> int:
+    """bor_streaming.py:114-116 (= bor_kernels.py:315-319)."""
+    osc = 2.0 * abs(k) * rho_max
+    return int(2 ** math.ceil(math.log2(max(128, 6 * (m_max + 2), 8 * (osc + 4)))))
+
+
+# ---------------------------------------------------------------------------
+# graded near cells: bor_solver.py:54-110
+# ---------------------------------------------------------------------------
+
+def graded_cells(kind: str, depth: int = 4) -> List[Tuple[float, float, float, float]]:
+    """Quadtree of [0,1]^2 refined toward the singular set (bor_solver.py:54-78)."""
+    out: List[Tuple[float, float, float, float]] = []
+
+    def hits(a0, a1, b0, b1):
+        if kind == "diag":
+            return not (a1 <= b0 or b1 <= a0)
+        sa = 0.0 if kind[6] == "0" else 1.0
+        sb = 0.0 if kind[7] == "0" else 1.0
+        return a0 <= sa <= a1 and b0 <= sb <= b1
+
+    def split(a0, a1, b0, b1, level):
+        if level >= depth or not hits(a0, a1, b0, b1):
+            out.append((a0, a1, b0, b1))
+            return
+        am, bm = 0.5 * (a0 + a1), 0.5 * (b0 + b1)
+        for (x0, x1) in ((a0, am), (am, a1)):
+            for (y0, y1) in ((b0, bm), (bm, b1)):
+                split(x0, x1, y0, y1, level + 1)
+
+    split(0.0, 1.0, 0.0, 1.0, 0)
+    return out
+
+
+_CELLS: Dict[str, Tuple[np.ndarray, np.ndarray, np.ndarray]] = {}
+
+
+def cell_points(kind: str, gorder: int = 4):
+    """(s, s', weight) over the graded cells; source axis one order higher
+    so test/source points never coincide (bor_solver.py:84-110)."""
+    key = f"{kind}:{gorder}"
+    if key not in _CELLS:
+        xs, ws = np.polynomial.legendre.leggauss(gorder)
+        xq, wq = np.polynomial.legendre.leggauss(gorder + 1)
+        us, vs = 0.5 * (xs + 1.0), 0.5 * ws
+        uq, vq = 0.5 * (xq + 1.0), 0.5 * wq
+        S, Q, W = [], [], []
+        for (a0, a1, b0, b1) in graded_cells(kind):
+            ha, hb = a1 - a0, b1 - b0
+            ss, qq = np.meshgrid(a0 + us * ha, b0 + uq * hb, indexing="ij")
+            S.append(ss.ravel())
+            Q.append(qq.ravel())
+            W.append(np.outer(vs * ha, vq * hb).ravel())
+        _CELLS[key] = (np.concatenate(S), np.concatenate(Q), np.concatenate(W))
+    return _CELLS[key]
+
+
+def near_kind(e: int, f: int) -> str:
+    """bor_solver.py:276-282."""
+    if e == f:
+        return "diag"
+    return "corner10" if f == e + 1 else "corner01"
+
+
+# ---------------------------------------------------------------------------
+# near modal kernels: bor_kernels.py:170-257, 334-431
+# ---------------------------------------------------------------------------
+
+def _near_grid(d, a, k, m_max, order=48, s0_axis=None):
+    """Sinh-graded core + Gauss tail xi grid shared by the near kernels
+    (bor_kernels.py:216-254, 380-404).  Returns the core's s = sin(xi/2),
+    core xi / weights and tail xi / weights, each [n_pairs, n_q]."""
+    s0 = np.minimum(0.25, 20.0 * d / a)
+    if s0_axis is not None:
+        s0 = np.where(s0_axis, 1.0, s0)
+    xg, wg = np.polynomial.legendre.leggauss(order)
+    u01, w01 = 0.5 * (xg + 1.0), 0.5 * wg
+    vmax = np.arcsinh((a / d) * s0)
+    v = u01[None, :] * vmax[:, None]
+    wv = w01[None, :] * vmax[:, None]
+    s = np.minimum((d / a)[:, None] * np.sinh(v), 1.0)
+    xi_c = 2.0 * np.arcsin(s)
+    ds_dv = (d / a)[:, None] * np.cosh(v)
+    w_c = wv * 2.0 * ds_dv / np.sqrt(np.maximum(1.0 - s ** 2, 1e-15))
+    osc = float(np.max(abs(complex(k)) * a)) / math.pi + (m_max + 2)
+    n_tail = int(min(1024, max(64, math.ceil(4.0 * osc))))
+    xt, wt = np.polynomial.legendre.leggauss(n_tail)
+    xi0 = 2.0 * np.arcsin(np.minimum(s0, 1.0))
+    span = np.pi - xi0
+    xi_t = xi0[:, None] + 0.5 * (xt + 1.0)[None, :] * span[:, None]
+    w_t = 0.5 * wt[None, :] * span[:, None]
+    return s, xi_c, w_c, xi_t, w_t
+
+
+def near_G(rho_p, z_p, rho_q, z_q, k, m_max, order=48):
+    """G_m, m = 0..m_max+1, at near point pairs (bor_kernels.py:170-257)."""
+    rho_p = np.atleast_1d(np.asarray(rho_p, float))
+    rho_q = np.atleast_1d(np.asarray(rho_q, float))
+    z_p = np.atleast_1d(np.asarray(z_p, float))
+    z_q = np.atleast_1d(np.asarray(z_q, float))
+    d2 = (rho_p - rho_q) ** 2 + (z_p - z_q) ** 2
+    rr4 = 4.0 * rho_p * rho_q
+    out = np.zeros((rho_p.size, m_max + 2), dtype=np.complex128)
+    m = np.arange(m_max + 2)
+    axis = rr4 <= 1e-30
+    if np.any(axis):
+        R0 = np.sqrt(d2[axis])
+        out[axis, 0] = 2.0 * np.pi * np.exp(-1j * k * R0) / (4.0 * np.pi * np.maximum(R0, 1e-300))
+    idx = np.flatnonzero(~axis)
+    if idx.size == 0:
+        return out
+    d = np.sqrt(np.maximum(d2[idx], 1e-300))
+    a = np.sqrt(rr4[idx])
+    s_c, xi_c, w_c, xi_t, w_t = _near_grid(d, a, k, m_max, order)
+    acc = np.zeros((idx.size, m_max + 2), dtype=np.complex128)
+    # core: R from s directly (bor_kernels.py:228); tail: from sin(xi/2) (:248-249)
+    for R, xi, w in ((np.sqrt(d[:, None] ** 2 + (a[:, None] * s_c) ** 2), xi_c, w_c),
+                     (np.sqrt(d[:, None] ** 2 + (a[:, None] * np.sin(0.5 * xi_t)) ** 2), xi_t, w_t)):
+        gw = np.exp(-1j * k * R) / (4.0 * np.pi * R) * w
+        cm = np.cos(xi[:, :, None] * m[None, None, :])
+        acc += 2.0 * (np.einsum("pv,pvm->pm", gw.real, cm)
+                      + 1j * np.einsum("pv,pvm->pm", gw.imag, cm))
+    out[idx, :] = acc
+    return out
+
+
+def _mfie_bracket_grid(rp, zp, trp, tzp, rq, zq, trq, tzq, k, xi):
+    """Four MFIE brackets on per-pair xi grids (bor_kernels.py:409-426);
+    test at phi = 0, source at phi' = -xi, n = (-tz, 0, tr)."""
+    cx, sx = np.cos(xi), np.sin(xi)
+    Rx = rp[:, None] - rq[:, None] * cx
+    Ry = rq[:, None] * sx
+    Rz = (zp - zq)[:, None] * np.ones_like(cx)
+    R = np.maximum(np.sqrt(Rx ** 2 + Ry ** 2 + Rz ** 2), 1e-300)
+    p = (1.0 + 1j * k * R) * np.exp(-1j * k * R) / (4.0 * np.pi * R ** 3)
+    WtR = trp[:, None] * Rx + tzp[:, None] * Rz
+    nR = -tzp[:, None] * Rx + trp[:, None] * Rz
+    n_tq = -(tzp * trq)[:, None] * cx + (trp * tzq)[:, None]
+    n_fq = -tzp[:, None] * sx
+    Wt_tq = (trp * trq)[:, None] * cx + (tzp * tzq)[:, None]
+    Wt_fq = trp[:, None] * sx
+    Wf_tq = -trq[:, None] * sx
+    Wf_fq = cx
+    return (-p * (WtR * n_tq - Wt_tq * nR), -p * (WtR * n_fq - Wt_fq * nR),
+            -p * (Ry * n_tq - Wf_tq * nR), -p * (Ry * n_fq - Wf_fq * nR))
+
+
+def near_mfie(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m_max, order=48):
+    """Near MFIE modal brackets for m = -m_max..m_max (bor_kernels.py:360-431)."""
+    rho_p = np.atleast_1d(np.asarray(rho_p, float))
+    rho_q = np.atleast_1d(np.asarray(rho_q, float))
+    z_p = np.atleast_1d(np.asarray(z_p, float))
+    z_q = np.atleast_1d(np.asarray(z_q, float))
+    tr_p = np.broadcast_to(np.asarray(tr_p, float), rho_p.shape)
+    tz_p = np.broadcast_to(np.asarray(tz_p, float), rho_p.shape)
+    tr_q = np.broadcast_to(np.asarray(tr_q, float), rho_q.shape)
+    tz_q = np.broadcast_to(np.asarray(tz_q, float), rho_q.shape)
+    d2 = (rho_p - rho_q) ** 2 + (z_p - z_q) ** 2
+    rr4 = 4.0 * rho_p * rho_q
+    d = np.sqrt(np.maximum(d2, 1e-300))
+    a = np.sqrt(np.maximum(rr4, 1e-300))
+    a_safe = np.maximum(a, 1e-300)
+    _, xi_c, w_c, xi_t, w_t = _near_grid(d, a_safe, k, m_max, order, s0_axis=rr4 <= 1e-30)
+    # the tail order uses a (not a_safe) exactly like the reference
+    xi_pos = np.concatenate([xi_c, xi_t], axis=1)
+    w_pos = np.concatenate([w_c, w_t], axis=1)
+    m = np.arange(-m_max, m_max + 1)
+    Fp = _mfie_bracket_grid(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, xi_pos)
+    Fm = _mfie_bracket_grid(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, -xi_pos)
+    arg = xi_pos[:, :, None] * m[None, None, :]
+    cm, sm = np.cos(arg), np.sin(arg)
+    outs = []
+    for fp, fm in zip(Fp, Fm):
+        S = (fp + fm) * w_pos
+        D = (fp - fm) * w_pos
+        pc = np.einsum("pv,pvm->pm", S.real, cm) + 1j * np.einsum("pv,pvm->pm", S.imag, cm)
+        ps = np.einsum("pv,pvm->pm", D.real, sm) + 1j * np.einsum("pv,pvm->pm", D.imag, sm)
+        outs.append(pc - 1j * ps)
+    return tuple(outs)
+
+
+# ---------------------------------------------------------------------------
+# the solver
+# ---------------------------------------------------------------------------
+
+class OracleSolver:
+    """Restatement of BorPecSolver (bor_solver.py:175-708) on the streaming
+    far path (bor_streaming.py:119-421), FP64 throughout."""
+
+    _COMBOS = (("r", "r"), ("z", "z"), ("r", "1"), ("1", "r"), ("1", "1"),
+               ("d", "d"), ("d", "s"), ("s", "d"), ("s", "s"))  # bor_streaming.py:370-371
+
+    def __init__(self, points, freq_hz: float, gauss_order: int = 4):
+        self.geo = Geom(points, gauss_order)
+        self.k = 2.0 * math.pi * freq_hz / C0
+        self.eta = ETA0
+        self.freq_hz = freq_hz
+        g = self.geo
+        wrho = g.w * g.rho
+        self.lv = {                                         # bor_streaming.py:145-152
+            "r": np.stack([g.T0 * wrho * g.ptr, g.T1 * wrho * g.ptr]),
+            "z": np.stack([g.T0 * wrho * g.ptz, g.T1 * wrho * g.ptz]),
+            "1": np.stack([g.T0 * wrho, g.T1 * wrho]),
+            "s": np.stack([g.T0 * g.w, g.T1 * g.w]),
+            "d": np.stack([g.dRT0 * g.w, g.dRT1 * g.w]),
+        }
+        self.Zp = None      # EFIE primitives [9, M+2, Nn, Nn]
+        self.Kb = None      # MFIE brackets [4, 2M+1, Nn, Nn]
+        self._near: Dict = {}
+        self._lock = threading.Lock()
+
+    # ---- far sampling (bor_streaming.py:320-341, 271-317) ----
+    def _sample_g(self, rows: slice, n_xi: int) -> np.ndarray:
+        g = self.geo
+        xi = 2.0 * np.pi * np.arange(n_xi) / n_xi - np.pi
+        sin2 = np.ascontiguousarray(np.sin(0.5 * xi) ** 2)
+        rp = np.ascontiguousarray(g.rho[rows])
+        zp = np.ascontiguousarray(g.z[rows])
+        if _SAMPLER is not None:
+            out = np.empty((len(rp), g.P, n_xi), dtype=np.complex128)
+            _SAMPLER.oracle_sample_g(len(rp), g.P, n_xi, _dp(rp), _dp(zp),
+                                     _dp(np.ascontiguousarray(g.rho)),
+                                     _dp(np.ascontiguousarray(g.z)), float(self.k),
+                                     _dp(sin2), _dp(out))
+            return out
+        d2 = (rp[:, None] - g.rho[None, :]) ** 2 + (zp[:, None] - g.z[None, :]) ** 2
+        rr4 = 4.0 * rp[:, None] * g.rho[None, :]
+        R = np.maximum(np.sqrt(d2[..., None] + rr4[..., None] * sin2), 1e-300)
+        return np.exp(-1j * self.k * R) / (4.0 * np.pi * R)
+
+    def _sample_mfie(self, rows: slice, n_xi: int):
+        g = self.geo
+        xi = 2.0 * np.pi * np.arange(n_xi) / n_xi - np.pi
+        nr = rows.stop - rows.start
+        if _SAMPLER is not None:
+            outs = tuple(np.empty((nr, g.P, n_xi), dtype=np.complex128) for _ in range(4))
+            a = [np.ascontiguousarray(v[rows]) for v in (g.rho, g.z, g.ptr, g.ptz)]
+            b = [np.ascontiguousarray(v) for v in (g.rho, g.z, g.ptr, g.ptz)]
+            _SAMPLER.oracle_sample_mfie(nr, g.P, n_xi, *[_dp(v) for v in a],
+                                        *[_dp(v) for v in b], float(self.k),
+                                        _dp(np.ascontiguousarray(np.cos(xi))),
+                                        _dp(np.ascontiguousarray(np.sin(xi))),
+                                        *[_dp(o) for o in outs])
+            return outs
+        one = np.ones((nr, g.P))
+        rp = (g.rho[rows][:, None] * one).ravel()
+        zp = (g.z[rows][:, None] * one).ravel()
+        trp = (g.ptr[rows][:, None] * one).ravel()
+        tzp = (g.ptz[rows][:, None] * one).ravel()
+        rq = (g.rho[None, :] * one).ravel()
+        zq = (g.z[None, :] * one).ravel()
+        trq = (g.ptr[None, :] * one).ravel()
+        tzq = (g.ptz[None, :] * one).ravel()
+        F = _mfie_bracket_grid(rp, zp, trp, tzp, rq, zq, trq, tzq, self.k,
+                               np.broadcast_to(xi, (rp.size, n_xi)))
+        return tuple(f.reshape(nr, g.P, n_xi) for f in F)
+
+    def _zero_near(self, K, e0, e1):
+        """bor_streaming.py:343-349."""
+        go, ne = self.geo.go, self.geo.ne
+        for e in range(e0, e1):
+            K[(e - e0) * go:(e - e0 + 1) * go, max(0, e - 1) * go:min(ne, e + 2) * go] = 0.0
+
+    def _contract(self, Kn, lv_rows, rv, e0, re, out):
+        """bor_streaming.py:352-368."""
+        go, ne = self.geo.go, self.geo.ne
+        Kr = Kn.reshape(re, go, ne, go, -1)
+        L = lv_rows.reshape(2, re, go)
+        R = rv.reshape(2, ne, go)
+        M = np.einsum("aeg,egfhm,bfh->maebf", L, Kr, R, optimize=True)
+        with self._lock:
+            out[:, e0:e0 + re, 0:ne] += M[:, 0, :, 0, :]
+            out[:, e0:e0 + re, 1:ne + 1] += M[:, 0, :, 1, :]
+            out[:, e0 + 1:e0 + re + 1, 0:ne] += M[:, 1, :, 0, :]
+            out[:, e0 + 1:e0 + re + 1, 1:ne + 1] += M[:, 1, :, 1, :]
+
+    def _tile_elems(self, n_xi, n_arrays, workers):
+        g = self.geo
+        budget = 512e6 / max(1, workers)
+        rows = max(g.go, int(budget / (g.P * n_xi * 16.0 * n_arrays)))
+        return max(1, rows // g.go)
+
+    def build_far(self, m_max: int, efie: bool = True, mfie: bool = False,
+                  workers: int = 1, elem_range: Optional[Tuple[int, int]] = None):
+        """Far blocks for all orders in one sweep (bor_streaming.py:220-268).
+        elem_range restricts the sweep to a slice of test elements (used only
+        to time a bounded sample of the build)."""
+        g = self.geo
+        Nn, ne, go = g.Nn, g.ne, g.go
+        rho_max = float(np.max(g.nodes[:, 0]))
+        nx_e = n_xi_efie(self.k, rho_max, m_max)
+        nx_b = n_xi_bracket(self.k, rho_max, m_max)
+        orders = np.arange(0, m_max + 2)
+        ph_e = np.exp(1j * np.pi * orders) * (2.0 * np.pi / nx_e)
+        ms = np.arange(-m_max, m_max + 1)
+        bins = np.where(ms >= 0, ms, nx_b + ms)
+        ph_b = np.exp(1j * np.pi * ms) * (2.0 * np.pi / nx_b)
+        if efie:
+            self.Zp = np.zeros((9, m_max + 2, Nn, Nn), dtype=np.complex128)
+        if mfie:
+            self.Kb = np.zeros((4, 2 * m_max + 1, Nn, Nn), dtype=np.complex128)
+        te = self._tile_elems(max(nx_e, nx_b if mfie else 0), 6 if mfie else 2, workers)
+        lo, hi = (0, ne) if elem_range is None else elem_range
+
+        def tile(e0):
+            e1 = min(e0 + te, hi)
+            rows = slice(e0 * go, e1 * go)
+            re = e1 - e0
+            if efie:
+                spec = np.fft.fft(self._sample_g(rows, nx_e), axis=-1)
+                Gn = spec[..., 0:m_max + 2] * ph_e
+                self._zero_near(Gn, e0, e1)
+                for ci, (lx, rx) in enumerate(self._COMBOS):
+                    self._contract(Gn, self.lv[lx][:, rows], self.lv[rx], e0, re, self.Zp[ci])
+            if mfie:
+                Fs = self._sample_mfie(rows, nx_b)
+                for uv, F in enumerate(Fs):
+                    spec = np.fft.fft(F, axis=-1)
+                    Km = spec[..., bins] * (2.0 * np.pi * ph_b)
+                    self._zero_near(Km, e0, e1)
+                    self._contract(Km, self.lv["1"][:, rows], self.lv["1"], e0, re, self.Kb[uv])
+
+        starts = list(range(lo, hi, te))
+        if workers <= 1:
+            for e0 in starts:
+                tile(e0)
+        else:
+            with ThreadPoolExecutor(max_workers=workers) as ex:
+                list(ex.map(tile, starts))
+
+    def efie_far_blocks(self, m: int):
+        """Per-mode far EFIE blocks from the primitives (bor_streaming.py:388-407)."""
+        am = abs(m)
+        k = self.k
+        lo, hi = abs(am - 1), am + 1
+        Z = self.Zp
+        ztt = 0.5 * (Z[0, lo] + Z[0, hi]) + Z[1, am] - (1.0 / k ** 2) * Z[5, am]
+        ztf = (Z[2, lo] - Z[2, hi]) / 2j - (1j * am / k ** 2) * Z[6, am]
+        zft = -(Z[3, lo] - Z[3, hi]) / 2j + (1j * am / k ** 2) * Z[7, am]
+        zff = 0.5 * (Z[4, lo] + Z[4, hi]) - (am ** 2 / k ** 2) * Z[8, am]
+        if m < 0:
+            ztf, zft = -ztf, -zft
+        return ztt.copy(), ztf.copy(), zft.copy(), zff.copy()
+
+    # ---- near pairs (bor_solver.py:270-290, 372-387) ----
+    def near_pairs(self):
+        ne = self.geo.ne
+        return [(e, f) for e in range(ne) for f in (e - 1, e, e + 1) if 0 <= f < ne]
+
+    def near_efie_data(self, e: int, f: int, m_max: int):
+        key = ("efie", m_max, e, f)
+        if key in self._near:
+            return self._near[key]
+        g = self.geo
+        s, sp_, w = cell_points(near_kind(e, f))
+        rp, zp, T0p, T1p, D0p, D1p, Lp = g.points_on_element(e, s)
+        rq, zq, T0q, T1q, D0q, D1q, Lq = g.points_on_element(f, sp_)
+        Gm = near_G(rp, zp, rq, zq, self.k, m_max)
+        data = (w * Lp * Lq, rp, np.vstack([T0p, T1p]), np.vstack([D0p, D1p]),
+                rq, np.vstack([T0q, T1q]), np.vstack([D0q, D1q]), Gm)
+        self._near[key] = data
+        return data
+
+    def near_mfie_data(self, e: int, f: int, m_max: int):
+        key = ("mfie", m_max, e, f)
+        if key in self._near:
+            return self._near[key]
+        g = self.geo
+        s, sp_, w = cell_points(near_kind(e, f))
+        rp, zp, T0p, T1p, _, _, Lp = g.points_on_element(e, s)
+        rq, zq, T0q, T1q, _, _, Lq = g.points_on_element(f, sp_)
+        Kn = near_mfie(rp, zp, np.full_like(rp, g.trho[e]), np.full_like(rp, g.tz[e]),
+                       rq, zq, np.full_like(rq, g.trho[f]), np.full_like(rq, g.tz[f]),
+                       self.k, m_max)
+        data = (w * Lp * Lq, rp, np.vstack([T0p, T1p]), rq, np.vstack([T0q, T1q]), Kn)
+        self._near[key] = data
+        return data
+
+    def prepare(self, m_max: int, efie=True, mfie=False, workers=1,
+                pairs: Optional[List[Tuple[int, int]]] = None):
+        """Far sweep + near caches (bor_solver.py:578-608)."""
+        if pairs is None:
+            self.build_far(m_max, efie=efie, mfie=mfie, workers=workers)
+            pairs = self.near_pairs()
+        jobs = []
+        if efie:
+            jobs += [(self.near_efie_data, p) for p in pairs]
+        if mfie:
+            jobs += [(self.near_mfie_data, p) for p in pairs]
+        if workers <= 1:
+            for fn, (e, f) in jobs:
+                fn(e, f, m_max)
+        else:
+            with ThreadPoolExecutor(max_workers=workers) as ex:
+                list(ex.map(lambda j: j[0](j[1][0], j[1][1], m_max), jobs))
+
+    # ---- per-mode operators ----
+    def assemble_efie(self, m: int, m_max: int) -> np.ndarray:
+        """bor_solver.py:293-345 on streamed far blocks."""
+        g = self.geo
+        k = self.k
+        ztt, ztf, zft, zff = self.efie_far_blocks(m)
+        am = abs(m)
+        for (e, f) in self.near_pairs():
+            w, rp, Tp, Dp, rq, Tq, Dq, Gm = self.near_efie_data(e, f, m_max)
+            Gn = Gm[:, am]
+            Gc = 0.5 * (Gm[:, abs(am - 1)] + Gm[:, am + 1])
+            Gs = (Gm[:, abs(am - 1)] - Gm[:, am + 1]) / 2j
+            if m < 0:
+                Gs = -Gs
+            rr = rp * rq * w
+            ktt = rr * (g.trho[e] * g.trho[f] * Gc + g.tz[e] * g.tz[f] * Gn)
+            ksc = w * Gn
+            ktf = rr * (g.trho[e] * Gs)
+            kft = -rr * (g.trho[f] * Gs)
+            kff = rr * Gc
+            c = lambda A, kk, B: np.einsum("ip,p,jp->ij", A, kk, B)
+            rs, cs = slice(e, e + 2), slice(f, f + 2)
+            ztt[rs, cs] += c(Tp, ktt, Tq) - (1.0 / k ** 2) * c(Dp, ksc, Dq)
+            ztf[rs, cs] += c(Tp, ktf, Tq) - (1j * m / k ** 2) * c(Dp, ksc, Tq)
+            zft[rs, cs] += c(Tp, kft, Tq) + (1j * m / k ** 2) * c(Tp, ksc, Dq)
+            zff[rs, cs] += c(Tp, kff, Tq) - (m ** 2 / k ** 2) * c(Tp, ksc, Tq)
+        C = 1j * k * self.eta * 2.0 * np.pi
+        return C * np.block([[ztt, ztf], [zft, zff]])
+
+    def mass(self) -> np.ndarray:
+        """bor_solver.py:389-397."""
+        g = self.geo
+        return 2.0 * np.pi * (g.BT * (g.w * g.rho)[None, :]) @ g.BT.T
+
+    def assemble_mfie(self, m: int, m_max: int) -> np.ndarray:
+        """Z_MFIE = M/2 - K (bor_solver.py:399-435) on streamed brackets."""
+        mi = m + m_max
+        blocks = [self.Kb[uv, mi].copy() for uv in range(4)]
+        for (e, f) in self.near_pairs():
+            w, rp, Tp, rq, Tq, Kn = self.near_mfie_data(e, f, m_max)
+            rr = rp * rq * w
+            for uv in range(4):
+                blocks[uv][e:e + 2, f:f + 2] += 2.0 * np.pi * np.einsum(
+                    "ip,p,jp->ij", Tp, rr * Kn[uv][:, mi], Tq)
+        M = self.mass()
+        ktt, ktf, kft, kff = blocks
+        return np.block([[0.5 * M - ktt, -ktf], [-kft, 0.5 * M - kff]])
+
+    def basis_mask(self, m: int) -> np.ndarray:
+        """bor_solver.py:611-622."""
+        Nn = self.geo.Nn
+        t = np.ones(Nn, dtype=bool)
+        f = np.ones(Nn, dtype=bool)
+        for end in (0, Nn - 1):
+            if self.geo.on_axis(end):
+                t[end] = abs(m) == 1
+                f[end] = False
+            else:
+                t[end] = False
+                f[end] = True
+        return np.concatenate([t, f])
+
+    # ---- excitation / far field, vectorised over angles ----
+    def _bessel_parts(self, m: int, thetas_deg: np.ndarray, sign: int):
+        g = self.geo
+        th = np.radians(thetas_deg)
+        st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+        u = self.k * g.rho[None, :] * st
+        P = np.exp(1j * self.k * ct * g.z[None, :])
+        jm = lambda n: (1j) ** n * sp.jv(n, u)
+        J0 = jm(m)
+        Jlo, Jhi = jm(m - sign), jm(m + sign)
+        Ic = math.pi * (Jlo + Jhi)
+        Is = (math.pi / 1j) * (Jlo - Jhi)
+        I1 = 2.0 * math.pi * J0
+        return st, ct, P, Ic, Is, I1
+
+    def rhs_efie(self, m: int, thetas_deg, pol: str) -> np.ndarray:
+        """rhs_mode (bor_solver.py:625-645) for every angle: [n_theta, 2Nn]."""
+        g = self.geo
+        st, ct, P, Ic, Is, I1 = self._bessel_parts(m, np.atleast_1d(thetas_deg), 1)
+        if pol == "VV":
+            et = ct * g.ptr * Ic - st * g.ptz * I1
+            ef = -ct * Is
+        else:
+            et = g.ptr * Is
+            ef = Ic
+        c = g.w * g.rho * P
+        return np.concatenate([(c * et) @ g.BT.T, (c * ef) @ g.BT.T], axis=1)
+
+    def rhs_mfie(self, m: int, thetas_deg, pol: str) -> np.ndarray:
+        """rhs_mfie_mode (bor_solver.py:437-461) for every angle."""
+        g = self.geo
+        st, ct, P, Ic, Is, I1 = self._bessel_parts(m, np.atleast_1d(thetas_deg), 1)
+        if pol == "VV":
+            et = Ic / ETA0
+            ef = -(g.ptr * Is) / ETA0
+        else:
+            et = (ct * Is) / ETA0
+            ef = (ct * g.ptr * Ic - st * g.ptz * I1) / ETA0
+        c = g.w * g.rho * P
+        return np.concatenate([(c * et) @ g.BT.T, (c * ef) @ g.BT.T], axis=1)
+
+    def farfield(self, m: int, sols: np.ndarray, thetas_deg) -> Tuple[np.ndarray, np.ndarray]:
+        """farfield_mode (bor_solver.py:659-708, PEC) for solution rows
+        sols [n_theta, 2Nn] at the matching angles: (F_theta, F_phi)."""
+        g = self.geo
+        Nn = g.Nn
+        st, ct, P, Icos, Isin, I1 = self._bessel_parts(m, np.atleast_1d(thetas_deg), -1)
+        Jt = sols[:, :Nn] @ g.BT
+        Jf = sols[:, Nn:] @ g.BT
+        common = g.w * g.rho * P
+        pth = np.sum(common * (Jt * (ct * g.ptr * Icos - st * g.ptz * I1) + Jf * (-ct * Isin)), axis=1)
+        pph = np.sum(common * (Jt * g.ptr * Isin + Jf * Icos), axis=1)
+        pref = -1j * self.k * ETA0 / (4.0 * math.pi)
+        return pref * pth, pref * pph
+
+
+def default_n_modes(points, freq_hz: float, thetas_deg) -> int:
+    """bor_solver.py:845-847."""
+    pts = np.asarray(points, float)
+    k = 2.0 * math.pi * freq_hz / C0
+    st = float(np.max(np.abs(np.sin(np.radians(np.atleast_1d(thetas_deg))))))
+    return int(math.ceil(k * float(np.max(pts[:, 0])) * max(st, 0.05))) + 12
+
+
+def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
+              cfie_alpha: float = 0.5, n_modes: Optional[int] = None,
+              mode_tol: float = 1e-6, gauss_order: int = 4, workers: int = 1,
+              keep_per_mode: bool = False, modes_subset=None,
+              timings: Optional[Dict[str, float]] = None) -> Dict:
+    """Monostatic PEC RCS (bor_solver.py:820-1004 with table_precision
+    "double", assembly "streaming") and the mode loop (bor_solver.py:711-801).
+
+    modes_subset (tuple of |m|) solves only those |m| -- used to time a bounded
+    sample; the result then holds partial sums."""
+    import time
+    form = formulation.strip().lower()
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    if n_modes is None:
+        n_modes = default_n_modes(points, freq_hz, thetas)
+    m_max = int(n_modes)
+    alpha = float(cfie_alpha) if form == "cfie" else (1.0 if form == "efie" else 0.0)
+    sol = OracleSolver(points, freq_hz, gauss_order)
+    Nn = sol.geo.Nn
+    t0 = time.perf_counter()
+    sol.prepare(m_max, efie=alpha > 0.0, mfie=alpha < 1.0, workers=workers)
+    t1 = time.perf_counter()
+    pols = ("VV", "HH")
+    F = np.zeros((2, len(thetas)), dtype=np.complex128)
+    per_mode = {}
+
+    def solve_am(am):
+        dF = np.zeros_like(F)
+        res = 0.0
+        for m in ([0] if am == 0 else [am, -am]):
+            Z = np.zeros((2 * Nn, 2 * Nn), dtype=np.complex128)
+            if alpha > 0.0:
+                Z += alpha * sol.assemble_efie(m, m_max)
+            if alpha < 1.0:
+                Z += (1.0 - alpha) * ETA0 * sol.assemble_mfie(m, m_max)
+            mask = sol.basis_mask(m)
+            A = Z[np.ix_(mask, mask)]
+            cols = []
+            for pol in pols:
+                V = np.zeros((len(thetas), 2 * Nn), dtype=np.complex128)
+                if alpha > 0.0:
+                    V += alpha * sol.rhs_efie(m, thetas, pol)
+                if alpha < 1.0:
+                    V += (1.0 - alpha) * ETA0 * sol.rhs_mfie(m, thetas, pol)
+                cols.append(V)
+            # column order theta-major, pol-minor (bor_solver.py:750-751)
+            B = np.stack([cols[0], cols[1]], axis=1)            # [n_theta, 2, 2Nn]
+            B = B.transpose(2, 0, 1).reshape(2 * Nn, 2 * len(thetas))[mask]
+            X = np.linalg.solve(A, B)
+            bn = float(np.linalg.norm(B))
+            if bn > 0.0:
+                res = max(res, float(np.linalg.norm(A @ X - B)) / bn)
+            full = np.zeros((2 * Nn, X.shape[1]), dtype=np.complex128)
+            full[mask] = X
+            xs = full.T.reshape(len(thetas), 2, 2 * Nn)
+            fth, _ = sol.farfield(m, xs[:, 0, :], thetas)
+            _, fph = sol.farfield(m, xs[:, 1, :], thetas)
+            dF[0] += fth
+            dF[1] += fph
+            if keep_per_mode:
+                per_mode[m] = (A, B, X)
+        return dF, res
+
+    modes_used = 0
+    quiet = 0
+    max_res = 0.0
+    am_list = list(range(m_max + 1)) if modes_subset is None else list(modes_subset)
+    dFs = []
+    with ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        results = list(ex.map(solve_am, am_list))
+    for am, (dF, res) in zip(am_list, results):
+        dFs.append(dF)
+        if modes_subset is not None:
+            F += dF
+            max_res = max(max_res, res)
+            modes_used = am
+            continue
+        F += dF
+        max_res = max(max_res, res)
+        modes_used = am
+        scale = max(float(np.max(np.abs(F))), 1e-30)
+        if float(np.max(np.abs(dF))) < mode_tol * scale:
+            quiet += 1
+            if quiet >= 2:
+                break
+        else:
+            quiet = 0
+    t2 = time.perf_counter()
+    if timings is not None:
+        timings["prepare_s"] = t1 - t0
+        timings["modes_s"] = t2 - t1
+    out = {
+        "theta_deg": thetas.tolist(),
+        "sigma_vv": (4.0 * math.pi * np.abs(F[0]) ** 2).tolist(),
+        "sigma_hh": (4.0 * math.pi * np.abs(F[1]) ** 2).tolist(),
+        "amp_vv": F[0].tolist(),
+        "amp_hh": F[1].tolist(),
+        "modes_used": modes_used,
+        "n_unknowns": int(2 * Nn),
+        "formulation": form,
+        "linear_residual": max_res,
+        "dF": np.array(dFs),
+    }
+    if keep_per_mode:
+        out["per_mode"] = per_mode
+    return out

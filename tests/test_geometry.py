@@ -1,0 +1,91 @@
+"""Host-side set-up of the package (product code) against the oracle/golden."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+
+def test_cells_match_golden(pkg):
+    G = load_golden("kernels")
+    for kind in ("diag", "corner10", "corner01"):
+        s, sp, w = pkg.geometry.cell_points(kind)
+        np.testing.assert_array_equal(np.stack([s, sp, w]), G[f"cells_{kind}"])
+
+
+def test_nxi_rules(pkg):
+    G = load_golden("kernels")
+    for (k, r, m), (ne, nb) in zip(((10, 1, 20), (80, .5, 50), (200, .5, 120), (40, .6, 30), (3, .1, 2)),
+                                   G["n_xi"]):
+        assert pkg.geometry.n_xi_efie(k, r, m) == ne
+        assert pkg.geometry.n_xi_bracket(k, r, m) == nb
+
+
+@pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40", "openshell_n20"])
+def test_gauss_and_masks(pkg, oracle, name):
+    D = load_golden(name)
+    geo = pkg.geometry
+    gen = geo.Generatrix(D["points"])
+    g = geo.gauss_on_generatrix(gen)
+    o = oracle.Geom(D["points"])
+    for a, b in ((g.rho, o.rho), (g.z, o.z), (g.w, o.w), (g.dRT0, o.dRT0), (g.dRT1, o.dRT1)):
+        np.testing.assert_array_equal(a, b)
+    M = int(D["m_max"])
+    rows = geo.mask_rows(gen, M)
+    for m in range(M + 1):
+        want = np.flatnonzero(~D[f"mask_{m}"]) if f"mask_{m}" in D else np.flatnonzero(
+            ~oracle.OracleSolver(D["points"], float(D["freq_hz"])).basis_mask(m))
+        got = rows[m][rows[m] >= 0]
+        np.testing.assert_array_equal(np.sort(got), want)
+
+
+def test_dct_equals_fft(pkg):
+    """The half-grid DCT tables reproduce the reference's full-grid FFT of an
+    even integrand (bor_kernels.py:160-167) to rounding."""
+    rng = np.random.default_rng(3)
+    n_xi, M = 64, 10
+    rp, rq, zp, zq = rng.uniform(0.2, 1.0, 4)
+    k = 5.0
+    xi = 2 * np.pi * np.arange(n_xi) / n_xi - np.pi
+    R = np.sqrt((rp - rq) ** 2 + (zp - zq) ** 2 + 4 * rp * rq * np.sin(xi / 2) ** 2)
+    g = np.exp(-1j * k * R) / (4 * np.pi * R)
+    ref = np.fft.fft(g)[:M + 2] * np.exp(1j * np.pi * np.arange(M + 2)) * (2 * np.pi / n_xi)
+    dct, sin2 = pkg.geometry.dct_tables(n_xi, M + 2)
+    Rh = np.sqrt((rp - rq) ** 2 + (zp - zq) ** 2 + 4 * rp * rq * sin2)
+    gh = np.exp(-1j * k * Rh) / (4 * np.pi * Rh)
+    got = gh @ dct
+    assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40"])
+def test_near_tail_orders(pkg, oracle, name):
+    """n_tail per element pair equals the order the reference's near kernel picks."""
+    D = load_golden(name)
+    geo = pkg.geometry
+    gen = geo.Generatrix(D["points"])
+    k = 2 * math.pi * float(D["freq_hz"]) / geo.C0
+    M = int(D["m_max"])
+    nt = geo.near_tables(gen, k, M)
+    og = oracle.Geom(D["points"])
+    for (e, f, _, _), n in zip(nt.pairs, nt.n_tail):
+        s, sp, _ = oracle.cell_points(oracle.near_kind(int(e), int(f)))
+        rp = og.points_on_element(int(e), s)[0]
+        rq = og.points_on_element(int(f), sp)[0]
+        rr4 = 4.0 * rp * rq
+        a = np.sqrt(rr4[rr4 > 1e-30])
+        osc = float(np.max(abs(complex(k)) * a)) / math.pi + (M + 2)
+        assert n == int(min(1024, max(64, math.ceil(4.0 * osc))))
+
+
+def test_bodies(pkg):
+    b = pkg.bodies
+    p = b.cone_sphere_generatrix(0.5, 15.0, 120)
+    seg = np.hypot(*np.diff(p, axis=0).T)
+    assert p[0, 0] == 0.0 and p[-1, 0] == 0.0 and abs(p[0, 1] - 0.5 / math.sin(math.radians(15))) < 1e-12
+    assert np.all(np.diff(p[:, 1]) < 0)
+    assert seg.max() / seg.min() < 1.001
+    bodies = b.random_bodies(4)
+    assert all(200 <= x["n"] <= 1600 for x in bodies)
+    s = b.sphere_generatrix(1.0, 8)
+    np.testing.assert_allclose(np.hypot(s[:, 0], s[:, 1]), 1.0)

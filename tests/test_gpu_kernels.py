@@ -1,0 +1,152 @@
+"""GPU kernels through the C ABI against the CPU oracle / reference goldens."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+def test_sample_g_and_mfie(pkg, oracle, torch):
+    """Drop-in device samplers vs the oracle's C restatement (bit-level formulas, FP64)."""
+    nat = pkg._native
+    rng = np.random.default_rng(1)
+    nr, npp, nx = 6, 13, 48
+    a = [rng.uniform(0.01, 1, nr) for _ in range(4)]
+    b = [rng.uniform(0.01, 1, npp) for _ in range(4)]
+    xi = 2 * np.pi * np.arange(nx) / nx - np.pi
+    s2 = np.sin(0.5 * xi) ** 2
+    d = lambda v: torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64, device="cuda")
+    out = torch.empty((nr, npp, nx), dtype=torch.complex128, device="cuda")
+    nat.call("ghost_bor_sample_g", nr, npp, nx, nat.ptr(d(a[0])), nat.ptr(d(a[1])), nat.ptr(d(b[0])),
+             nat.ptr(d(b[1])), 7.5, nat.ptr(d(s2)), nat.ptr(out), nat.stream_handle())
+    dR = (a[0][:, None] - b[0][None, :]) ** 2 + (a[1][:, None] - b[1][None, :]) ** 2
+    R = np.sqrt(dR[..., None] + 4 * (a[0][:, None] * b[0][None, :])[..., None] * s2)
+    assert rel(out.cpu().numpy(), np.exp(-7.5j * R) / (4 * np.pi * R)) < 1e-14
+    outs = [torch.empty((nr, npp, nx), dtype=torch.complex128, device="cuda") for _ in range(4)]
+    args = [nat.ptr(d(v)) for v in a] + [nat.ptr(d(v)) for v in b]
+    nat.call("ghost_bor_sample_mfie", nr, npp, nx, *args, 7.5, nat.ptr(d(np.cos(xi))),
+             nat.ptr(d(np.sin(xi))), *[nat.ptr(o) for o in outs], nat.stream_handle())
+    one = np.ones((nr, npp))
+    F = oracle._mfie_bracket_grid(
+        (a[0][:, None] * one).ravel(), (a[1][:, None] * one).ravel(), (a[2][:, None] * one).ravel(),
+        (a[3][:, None] * one).ravel(), (b[0][None, :] * one).ravel(), (b[1][None, :] * one).ravel(),
+        (b[2][None, :] * one).ravel(), (b[3][None, :] * one).ravel(), 7.5,
+        np.broadcast_to(xi, (nr * npp, nx)))
+    for o, f in zip(outs, F):
+        assert rel(o.cpu().numpy(), f.reshape(nr, npp, nx)) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40", "openshell_n20"])
+def test_far_blocks(pkg, oracle, name):
+    """Fused far fill (FP64 and FP32) vs the oracle's streamed far blocks."""
+    D = load_golden(name)
+    M = int(D["m_max"])
+    o = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    o.build_far(M, efie=True)
+    bs = pkg.bor_solver
+    s = bs.BorPecSolver(D["points"], float(D["freq_hz"]))
+    for dtype, tol in ((np.complex128, 1e-12), (np.complex64, 2e-5)):
+        s.enable_streaming(M, single_blocks=dtype == np.complex64)
+        for m in list(range(M + 1)) + [-1, -M]:
+            got = s._stream.efie_blocks(m)
+            want = o.efie_far_blocks(m)
+            scale = max(np.max(np.abs(w)) for w in want)
+            err = max(np.max(np.abs(g - w)) for g, w in zip(got, want)) / scale
+            assert err < tol, (dtype, m, err)
+
+
+@pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40", "openshell_n20"])
+def test_full_operator_and_excitation(pkg, name):
+    """assemble_mode (far + near), rhs_mode and farfield_mode vs the reference goldens."""
+    D = load_golden(name)
+    M = int(D["m_max"])
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]))
+    s.prepare_operators(M)
+    for m in D["modes"]:
+        m = int(m)
+        assert rel(s.assemble_mode(m, M), D[f"Ze_{m}"]) < 1e-12, m
+        np.testing.assert_array_equal(s.basis_mask(m), D[f"mask_{m}"])
+        for it, th in enumerate(D["thetas"][::3]):
+            for pol in ("VV", "HH"):
+                assert rel(s.rhs_mode(m, th, pol), D[f"Ve_{m}_{pol}"][3 * it]) < 1e-12
+        x = D[f"ffx_{m}"]
+        ff = np.array([s.farfield_mode(m, x, th) for th in D["thetas"][::4]])
+        assert rel(ff, D[f"ff_{m}"][::4]) < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-11), ("f32", 5e-4)])
+def test_batched_lu(pkg, torch, prec, tol):
+    """ghost_bor_getrf / getrs vs numpy on random complex systems, including a
+    size that is not a multiple of the panel width and pivoting-heavy rows."""
+    nat = pkg._native
+    rng = np.random.default_rng(5)
+    batch, n, nrhs = 3, 173, 37
+    A = rng.standard_normal((batch, n, n)) + 1j * rng.standard_normal((batch, n, n))
+    A[:, 0, :] *= 1e-3                          # force pivoting
+    B = rng.standard_normal((batch, n, nrhs)) + 1j * rng.standard_normal((batch, n, nrhs))
+    X_ref = np.linalg.solve(A, B)
+    dt = torch.complex128 if prec == "f64" else torch.complex64
+    p = nat.F64 if prec == "f64" else nat.F32
+    dA = torch.as_tensor(A, device="cuda").to(dt).contiguous()
+    dB = torch.as_tensor(B, device="cuda").to(dt).contiguous()
+    ipiv = torch.empty((batch, n), dtype=torch.int32, device="cuda")
+    info = torch.empty((batch,), dtype=torch.int32, device="cuda")
+    st = nat.stream_handle()
+    nat.call("ghost_bor_getrf", p, batch, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info), st)
+    nat.call("ghost_bor_getrs", p, batch, n, nrhs, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(dB),
+             nrhs, n * nrhs, st)
+    X = dB.cpu().numpy()
+    assert np.all(info.cpu().numpy() == 0)
+    assert rel(X, X_ref) < tol
+    # partial pivoting: |L| <= 1 below the diagonal
+    LU = dA.cpu().numpy()
+    L = np.tril(LU, -1)
+    assert np.max(np.abs(L)) <= 1.0 + 1e-6
+
+
+def test_singular_pivot_reported(pkg, torch):
+    nat = pkg._native
+    n = 70
+    A = np.eye(n, dtype=np.complex128)
+    A[40, 40] = 0.0
+    dA = torch.as_tensor(A[None], device="cuda").contiguous()
+    ipiv = torch.empty((1, n), dtype=torch.int32, device="cuda")
+    info = torch.empty((1,), dtype=torch.int32, device="cuda")
+    nat.call("ghost_bor_getrf", nat.F64, 1, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info),
+             nat.stream_handle())
+    assert int(info.cpu()[0]) == 41
+
+
+def test_bessel_rhs_against_scipy(pkg, torch):
+    """Miller-recurrence Bessel tables inside the excitation kernel vs scipy jv,
+    through rhs_mode at large orders and arguments."""
+    from scipy import special as sp
+    pts = pkg.bodies.sphere_generatrix(1.0, 30)
+    k = 30.0
+    f = k * 299_792_458.0 / (2 * math.pi)
+    s = pkg.bor_solver.BorPecSolver(pts, f)
+    g = s.g
+    for m in (0, 7, 29, 40):
+        for th in (0.0, 37.0, 90.0, 180.0):
+            v = s.rhs_mode(m, th, "HH")
+            t = math.radians(th)
+            u = k * g.rho * math.sin(t)
+            jm = lambda n: (1j) ** n * sp.jv(n, u)
+            Ic = math.pi * (jm(m - 1) + jm(m + 1))
+            Is = (math.pi / 1j) * (jm(m - 1) - jm(m + 1))
+            P = np.exp(1j * k * math.cos(t) * g.z)
+            want = np.concatenate([s.B_T @ (g.w * g.rho * P * g.trho * Is), s.B_T @ (g.w * g.rho * P * Ic)])
+            assert rel(v, want) < 1e-12, (m, th)

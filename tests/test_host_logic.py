@@ -1,0 +1,51 @@
+"""Host logic of the GPU engine checked on the CPU oracle: the +-m folding
+and reciprocity identities the engine relies on, and the truncation replay."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+
+def test_mode_symmetry_and_reciprocity(oracle):
+    D = load_golden("conesphere_n40")
+    s = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    M = int(D["m_max"])
+    s.prepare(M, efie=True)
+    Nn = s.geo.Nn
+    d = np.concatenate([np.ones(Nn), -np.ones(Nn)])
+    th = D["thetas"]
+    c = -1j * s.k * oracle.ETA0 / (4 * np.pi)
+    for m in (1, 3, 8):
+        Zp, Zm = s.assemble_efie(m, M), s.assemble_efie(-m, M)
+        assert np.max(np.abs(Zm - d[:, None] * Zp * d[None, :])) <= 1e-13 * np.max(np.abs(Zp))
+        Vv, Vh = s.rhs_efie(m, th, "VV"), s.rhs_efie(m, th, "HH")
+        Vvm, Vhm = s.rhs_efie(-m, th, "VV"), s.rhs_efie(-m, th, "HH")
+        assert np.allclose(Vvm, Vv * d, rtol=0, atol=1e-13 * np.abs(Vv).max())
+        assert np.allclose(Vhm, -Vh * d, rtol=0, atol=1e-13 * np.abs(Vh).max())
+        rng = np.random.default_rng(m)
+        x = rng.standard_normal((len(th), 2 * Nn)) + 1j * rng.standard_normal((len(th), 2 * Nn))
+        fth, fph = s.farfield(m, x, th)
+        assert np.allclose(fth, c * np.sum(d * Vv * x, axis=1), rtol=1e-12, atol=0)
+        assert np.allclose(fph, -c * np.sum(d * Vh * x, axis=1), rtol=1e-12, atol=0)
+
+
+def test_truncation_replay(pkg, oracle):
+    """replay_truncation reproduces the reference loop's modes_used and F."""
+    eng = pytest.importorskip("importlib").import_module("20260722_ghost_gb300.engine")
+    rng = np.random.default_rng(0)
+    dF = rng.standard_normal((12, 2, 5)) + 1j * rng.standard_normal((12, 2, 5))
+    dF *= np.exp(-np.arange(12))[:, None, None]
+    for tol in (0.0, 1e-6, 1e-3, 1e-1):
+        F, used = eng.replay_truncation(dF, tol)
+        Fr = np.zeros((2, 5), complex)
+        quiet, used_r = 0, 0
+        for am in range(12):
+            Fr += dF[am]
+            used_r = am
+            if np.max(np.abs(dF[am])) < tol * max(np.max(np.abs(Fr)), 1e-30):
+                quiet += 1
+                if quiet >= 2:
+                    break
+            else:
+                quiet = 0
+        assert used == used_r and np.array_equal(F, Fr)
