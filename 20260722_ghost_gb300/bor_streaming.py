@@ -53,8 +53,7 @@ class StreamingFarBlocks:
         prob = BorGpuProblem(solver._points, solver.freq_hz, (0.0,), m_max=self.m_max,
                              gauss_order=solver.gauss_order)
         single = np.dtype(dtype) == np.complex64
-        tdt = torch.complex64 if single else torch.complex128
-        Z = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=tdt, device=prob.device)
+        Z = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
         prob.fill_far(Z, nat.F32 if single else nat.F64, 1.0 + 0.0j, nat.stream_handle())
         self.Z = Z
         self.K = None
@@ -65,7 +64,9 @@ class StreamingFarBlocks:
         if am > self.m_max:
             raise ValueError(f"mode {m} outside the built range 0..{self.m_max}")
         Nn = self.Nn
-        Zm = self.Z[am].to(dtype=self.Z.dtype).cpu().numpy().astype(np.complex128)
+        Zm = self.Z[am].cpu().numpy()
+        if np.dtype(self.dtype) == np.complex64:
+            Zm = Zm.astype(np.complex64).astype(np.complex128)
         ztt, ztf = Zm[:Nn, :Nn].copy(), Zm[:Nn, Nn:].copy()
         zft, zff = Zm[Nn:, :Nn].copy(), Zm[Nn:, Nn:].copy()
         if m < 0:

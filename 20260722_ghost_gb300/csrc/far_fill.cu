@@ -19,8 +19,16 @@
 // per element), combines orders |m-1|, m, m+1 into the four mode-m blocks
 // and adds scale * block into Z[m].
 //
-// FP32 path: R^2, R and k R are carried as double-float (hi + lo) so the
-// phase is accurate to ~3e-7 rad before the FP32 sin/cos, independent of kR.
+// Precision: the sampling and the DCT (all but a few percent of the flops)
+// run in the requested precision; contraction, mode combination and the
+// node accumulation always run in FP64 and Z is complex double.  The EFIE
+// scalar-potential entries of a node pair are double differences of the
+// element-pair contributions (the two elements at a node carry charges of
+// opposite sign), which cancels ~(1/kL)^2 ~ 30x at 30 elements per wavelength,
+// so any rounding before the node sum is amplified by that factor.  In the
+// FP32 path R^2, R and k R are carried as double-float so the phase is exact
+// to ~1e-7 rad before an accurate sincosf, and the DCT is summed in blocks
+// of 8 samples folded in with Kahan compensation.
 #include "common.cuh"
 
 namespace gb {
@@ -31,11 +39,12 @@ constexpr int TPB = EPB * 16;     // one thread per Gauss-point pair
 constexpr int JC = 32;            // azimuth samples staged per smem chunk
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
-constexpr float kTwoPiA = 6.28125f;                                     // 8 significant bits
-constexpr float kTwoPiB = (float)(kTwoPi - 6.28125);
-constexpr float kTwoPiC = (float)(kTwoPi - 6.28125 - (double)(float)(kTwoPi - 6.28125));
+// 2 pi = A + B + C; A (8 bits) and B (12 bits) are short enough that q*A and
+// q*B are exact in FP32 for every reduction count q < 2^11 (k R < 12800).
+constexpr float kTwoPiA = 6.28125f;
+constexpr float kTwoPiB = 4059.0f / 2097152.0f;
+constexpr float kTwoPiC = (float)(kTwoPi - 6.28125 - 4059.0 / 2097152.0);
 constexpr float kInvTwoPi = (float)(1.0 / kTwoPi);
-constexpr float kInv4Pi = (float)(1.0 / (4.0 * GB_PI));
 
 // ---------------------------------------------------------------------------
 // per-pair samplers
@@ -52,7 +61,7 @@ template <> struct GreenSampler<double> {
         R = fmax(R, 1e-30);
         double sn, cs;
         sincos(k * R, &sn, &cs);
-        const double amp = 1.0 / (4.0 * GB_PI * R);
+        const double amp = 1.0 / R;                  // 1/(4 pi) is folded into the DCT table
         return make_double2(amp * cs, -amp * sn);
     }
 };
@@ -85,32 +94,40 @@ template <> struct GreenSampler<float> {
         const float r = R2 * rs;
         const float e = fmaf(-r, r, R2) + R2l;
         const float rl = 0.5f * e * rs;
-        // phase k R in double-float, reduced mod 2 pi (Cody-Waite, 3 parts)
+        // phase k R in double-float (ph + phl), reduced mod 2 pi: ph - q A is
+        // exact, the subtraction of q B is made exact with a two-sum, and the
+        // remaining small terms form a first-order correction dt.
         const float ph = kh * r;
         const float phe = fmaf(kh, r, -ph);
         const float phl = phe + fmaf(kh, rl, kl * r);
         const float q = rintf(ph * kInvTwoPi);
-        float th = fmaf(-q, kTwoPiA, ph);
-        th = fmaf(-q, kTwoPiB, th);
-        th = fmaf(-q, kTwoPiC, th);
-        th += phl;
+        const float t1 = fmaf(-q, kTwoPiA, ph);
+        const float qb = -q * kTwoPiB;
+        const float t2 = t1 + qb;
+        const float tb = t2 - t1;
+        const float t2e = (t1 - (t2 - tb)) + (qb - tb);
+        const float dt = fmaf(-q, kTwoPiC, phl) + t2e;
         float sn, cs;
-        __sincosf(th, &sn, &cs);
-        const float amp = rs * kInv4Pi;
-        return make_float2(amp * cs, -amp * sn);
+        sincosf(t2, &sn, &cs);
+        const float s1 = fmaf(dt, cs, sn);            // sin(t2 + dt)
+        const float c1 = fmaf(-dt, sn, cs);           // cos(t2 + dt)
+        // 1/R = 1/(r + rl) from an IEEE reciprocal and a first-order correction
+        const float ir = __frcp_rn(r);
+        const float amp = ir * fmaf(-rl, ir, 1.0f);  // 1/(4 pi) is folded into the DCT table
+        return make_float2(amp * c1, -amp * s1);
     }
 };
 
 template <class R> struct SmemLayout {
-    // Gs   [EPB][NO][16]  C<R>  per-pair orders, later the mode-local blocks
-    // P11s [EPB][NO][4]   C<R>
+    // Gs   [EPB][NO][16]  double2  per-pair orders, later the mode-local blocks
+    // P11s [EPB][NO][4]   double2
     // dcts [JC][NO]       R
     // s2s  [JC]           S2
-    // wts  [EPB+1][6][4]  R     (index EPB = test element)
+    // wts  [EPB+1][6][4]  double   (index EPB = test element)
     static size_t bytes(int NO) {
-        return sizeof(C<R>) * (size_t)EPB * NO * 16 + sizeof(C<R>) * (size_t)EPB * NO * 4 +
+        return sizeof(double2) * (size_t)EPB * NO * 16 + sizeof(double2) * (size_t)EPB * NO * 4 +
                sizeof(R) * (size_t)JC * NO + sizeof(typename GreenSampler<R>::S2) * JC +
-               sizeof(R) * (size_t)(EPB + 1) * 24;
+               sizeof(double) * (size_t)(EPB + 1) * 24;
     }
 };
 
@@ -118,18 +135,18 @@ template <class R, int NO>
 __global__ void __launch_bounds__(TPB)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
-                const double *__restrict__ sin2, C<R> *__restrict__ Z,
+                const double *__restrict__ sin2, double2 *__restrict__ Z,
                 long long ldz, long long mode_stride)
 {
     using CT = C<R>;
     using Samp = GreenSampler<R>;
     using S2 = typename Samp::S2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    CT *Gs = reinterpret_cast<CT *>(smem_raw);
-    CT *P11s = Gs + EPB * NO * 16;
+    double2 *Gs = reinterpret_cast<double2 *>(smem_raw);
+    double2 *P11s = Gs + EPB * NO * 16;
     R *dcts = reinterpret_cast<R *>(P11s + EPB * NO * 4);
     S2 *s2s = reinterpret_cast<S2 *>(dcts + JC * NO);
-    R *wts = reinterpret_cast<R *>(s2s + JC);
+    double *wts = reinterpret_cast<double *>(s2s + JC);
 
     const int P = 4 * N;
     const int fgroups = (N + EPB - 1) / EPB;
@@ -153,7 +170,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     for (int i = tid; i < (EPB + 1) * 24; i += TPB) {
         const int slot = i / 24, r = i % 24;
         const int el = (slot == EPB) ? e : min(f0 + slot, N - 1);
-        wts[i] = (R)geo[(size_t)(3 + r / 4) * P + 4 * el + (r % 4)];
+        wts[i] = geo[(size_t)(3 + r / 4) * P + 4 * el + (r % 4)];
     }
 
     Samp smp;
@@ -166,9 +183,10 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
     }
 
-    CT acc[NO];
+    CT acc[NO];          // running sums
+    CT cmp[NO];          // Kahan compensation (FP32 path only)
 #pragma unroll
-    for (int n = 0; n < NO; ++n) acc[n] = mk<R>(R(0), R(0));
+    for (int n = 0; n < NO; ++n) { acc[n] = mk<R>(R(0), R(0)); cmp[n] = mk<R>(R(0), R(0)); }
 
     for (int j0 = 0; j0 <= h; j0 += JC) {
         __syncthreads();
@@ -184,23 +202,45 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         __syncthreads();
         if (active) {
             const int jn = min(JC, h + 1 - j0);
-            for (int jj = 0; jj < jn; ++jj) {
-                const CT gv = smp(s2s[jj]);
-                if constexpr (sizeof(R) == 4) {
-                    const float4 *row = reinterpret_cast<const float4 *>(dcts + jj * NO);
+            if constexpr (sizeof(R) == 4) {
+                // FP32: sums over blocks of 8 samples, each folded into the
+                // running sum with Kahan compensation.  The node-level EFIE
+                // entries are double differences of these orders, so their
+                // rounding error must stay well below one FP32 ulp.
+                for (int jb = 0; jb < jn; jb += 8) {
+                    CT cacc[NO];
 #pragma unroll
-                    for (int n4 = 0; n4 < NO / 4; ++n4) {
-                        const float4 c = row[n4];
-                        acc[4 * n4 + 0].x = fmaf(gv.x, c.x, acc[4 * n4 + 0].x);
-                        acc[4 * n4 + 0].y = fmaf(gv.y, c.x, acc[4 * n4 + 0].y);
-                        acc[4 * n4 + 1].x = fmaf(gv.x, c.y, acc[4 * n4 + 1].x);
-                        acc[4 * n4 + 1].y = fmaf(gv.y, c.y, acc[4 * n4 + 1].y);
-                        acc[4 * n4 + 2].x = fmaf(gv.x, c.z, acc[4 * n4 + 2].x);
-                        acc[4 * n4 + 2].y = fmaf(gv.y, c.z, acc[4 * n4 + 2].y);
-                        acc[4 * n4 + 3].x = fmaf(gv.x, c.w, acc[4 * n4 + 3].x);
-                        acc[4 * n4 + 3].y = fmaf(gv.y, c.w, acc[4 * n4 + 3].y);
+                    for (int n = 0; n < NO; ++n) cacc[n] = mk<R>(R(0), R(0));
+                    const int je = min(jb + 8, jn);
+                    for (int jj = jb; jj < je; ++jj) {
+                        const CT gv = smp(s2s[jj]);
+                        const float4 *row = reinterpret_cast<const float4 *>(dcts + jj * NO);
+#pragma unroll
+                        for (int n4 = 0; n4 < NO / 4; ++n4) {
+                            const float4 c = row[n4];
+                            cacc[4 * n4 + 0].x = fmaf(gv.x, c.x, cacc[4 * n4 + 0].x);
+                            cacc[4 * n4 + 0].y = fmaf(gv.y, c.x, cacc[4 * n4 + 0].y);
+                            cacc[4 * n4 + 1].x = fmaf(gv.x, c.y, cacc[4 * n4 + 1].x);
+                            cacc[4 * n4 + 1].y = fmaf(gv.y, c.y, cacc[4 * n4 + 1].y);
+                            cacc[4 * n4 + 2].x = fmaf(gv.x, c.z, cacc[4 * n4 + 2].x);
+                            cacc[4 * n4 + 2].y = fmaf(gv.y, c.z, cacc[4 * n4 + 2].y);
+                            cacc[4 * n4 + 3].x = fmaf(gv.x, c.w, cacc[4 * n4 + 3].x);
+                            cacc[4 * n4 + 3].y = fmaf(gv.y, c.w, cacc[4 * n4 + 3].y);
+                        }
                     }
-                } else {
+#pragma unroll
+                    for (int n = 0; n < NO; ++n) {
+                        const float yx = cacc[n].x - cmp[n].x, yy = cacc[n].y - cmp[n].y;
+                        const float tx = acc[n].x + yx, ty = acc[n].y + yy;
+                        cmp[n].x = (tx - acc[n].x) - yx;
+                        cmp[n].y = (ty - acc[n].y) - yy;
+                        acc[n].x = tx;
+                        acc[n].y = ty;
+                    }
+                }
+            } else {
+                for (int jj = 0; jj < jn; ++jj) {
+                    const CT gv = smp(s2s[jj]);
                     const double2 *row = reinterpret_cast<const double2 *>(dcts + jj * NO);
 #pragma unroll
                     for (int n2 = 0; n2 < NO / 2; ++n2) {
@@ -215,33 +255,35 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         }
     }
 
-    // spill per-pair orders to smem: Gs[ep][n][gh]
+    // per-pair orders to smem in FP64: Gs[ep][n][gh] = acc - cmp
 #pragma unroll
-    for (int n = 0; n < NO; ++n) Gs[(ep * NO + n) * 16 + gh] = acc[n];
+    for (int n = 0; n < NO; ++n)
+        Gs[(ep * NO + n) * 16 + gh] = make_double2((double)acc[n].x - (double)cmp[n].x,
+                                                   (double)acc[n].y - (double)cmp[n].y);
     __syncthreads();
 
-    const R ik2 = R(1.0 / (k * k));
+    const double ik2 = 1.0 / (k * k);
     // contraction jobs (ep, n): five primitives per order
     for (int job = tid; job < EPB * nord; job += TPB) {
         const int jep = job / nord, n = job % nord;
         const int ff = f0 + jep;
         if (ff >= N || abs(e - ff) < 2) continue;
-        CT G[16];
+        double2 G[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) G[i] = Gs[(jep * NO + n) * 16 + i];
-        const R *wt = wts + EPB * 24;      // test element weights
-        const R *ws = wts + jep * 24;      // source element weights
+        const double *wt = wts + EPB * 24;      // test element weights
+        const double *ws = wts + jep * 24;      // source element weights
         // right contraction: GR_x[g][b] = sum_h G[g][h] Rx[b][h]
-        CT GR1[8], GRs[8], GRd[8];
+        double2 GR1[8], GRs[8], GRd[8];
 #pragma unroll
         for (int g = 0; g < 4; ++g)
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
-                CT a1 = mk<R>(0, 0), as = mk<R>(0, 0), ad = mk<R>(0, 0);
+                double2 a1 = make_double2(0, 0), as = make_double2(0, 0), ad = make_double2(0, 0);
 #pragma unroll
                 for (int hq = 0; hq < 4; ++hq) {
-                    const CT gv = G[g * 4 + hq];
-                    const R w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq], wd = ws[(4 + b) * 4 + hq];
+                    const double2 gv = G[g * 4 + hq];
+                    const double w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq], wd = ws[(4 + b) * 4 + hq];
                     a1.x = fma(gv.x, w1, a1.x); a1.y = fma(gv.y, w1, a1.y);
                     as.x = fma(gv.x, wsv, as.x); as.y = fma(gv.y, wsv, as.y);
                     ad.x = fma(gv.x, wd, ad.x); ad.y = fma(gv.y, wd, ad.y);
@@ -249,19 +291,19 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
                 GR1[g * 2 + b] = a1; GRs[g * 2 + b] = as; GRd[g * 2 + b] = ad;
             }
         const int o = o0 + n;
-        const R tze = (R)geo[(size_t)10 * P + 4 * e], tzf = (R)geo[(size_t)10 * P + 4 * ff];
-        const R fm = R(o) * ik2;          // jm/k^2 magnitude
-        const R fm2 = R(o) * R(o) * ik2;  // m^2/k^2
-        CT *zl = Gs + (jep * NO + n) * 16;
+        const double tze = geo[(size_t)10 * P + 4 * e], tzf = geo[(size_t)10 * P + 4 * ff];
+        const double fm = o * ik2;          // jm/k^2 magnitude
+        const double fm2 = (double)o * o * ik2;  // m^2/k^2
+        double2 *zl = Gs + (jep * NO + n) * 16;
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
-                CT p11 = mk<R>(0, 0), pdd = mk<R>(0, 0), pds = mk<R>(0, 0), psd = mk<R>(0, 0), pss = mk<R>(0, 0);
+                double2 p11 = make_double2(0, 0), pdd = make_double2(0, 0), pds = make_double2(0, 0), psd = make_double2(0, 0), pss = make_double2(0, 0);
 #pragma unroll
                 for (int g = 0; g < 4; ++g) {
-                    const R l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
-                    const CT r1 = GR1[g * 2 + b], rsv = GRs[g * 2 + b], rd = GRd[g * 2 + b];
+                    const double l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
+                    const double2 r1 = GR1[g * 2 + b], rsv = GRs[g * 2 + b], rd = GRd[g * 2 + b];
                     p11.x = fma(l1, r1.x, p11.x); p11.y = fma(l1, r1.y, p11.y);
                     pdd.x = fma(ld, rd.x, pdd.x); pdd.y = fma(ld, rd.y, pdd.y);
                     pds.x = fma(ld, rsv.x, pds.x); pds.y = fma(ld, rsv.y, pds.y);
@@ -271,43 +313,43 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
                 const int ab = a * 2 + b;
                 P11s[(jep * NO + n) * 4 + ab] = p11;
                 // mode-local parts (mode m = o)
-                const R tt = tze * tzf;
-                zl[0 * 4 + ab] = mk<R>(tt * p11.x - ik2 * pdd.x, tt * p11.y - ik2 * pdd.y);
-                zl[1 * 4 + ab] = mk<R>(fm * pds.y, -fm * pds.x);       // -(j o/k^2) pds
-                zl[2 * 4 + ab] = mk<R>(-fm * psd.y, fm * psd.x);       // +(j o/k^2) psd
-                zl[3 * 4 + ab] = mk<R>(-fm2 * pss.x, -fm2 * pss.y);
+                const double tt = tze * tzf;
+                zl[0 * 4 + ab] = make_double2(tt * p11.x - ik2 * pdd.x, tt * p11.y - ik2 * pdd.y);
+                zl[1 * 4 + ab] = make_double2(fm * pds.y, -fm * pds.x);       // -(j o/k^2) pds
+                zl[2 * 4 + ab] = make_double2(-fm * psd.y, fm * psd.x);       // +(j o/k^2) psd
+                zl[3 * 4 + ab] = make_double2(-fm2 * pss.x, -fm2 * pss.y);
             }
     }
     __syncthreads();
 
     // mode combination + accumulation into Z[m]
     const int nmodes = m1 - m0 + 1;
-    const R sre = (R)sc_re, sim = (R)sc_im;
+    const double sre = sc_re, sim = sc_im;
     for (int job = tid; job < EPB * nmodes; job += TPB) {
         const int jep = job / nmodes, m = m0 + job % nmodes;
         const int ff = f0 + jep;
         if (ff >= N || abs(e - ff) < 2) continue;
         const int nl = abs(m - 1) - o0, nm = m - o0, nh = m + 1 - o0;
-        const CT *zl = Gs + (jep * NO + nm) * 16;
-        const R tre = (R)geo[(size_t)9 * P + 4 * e], trf = (R)geo[(size_t)9 * P + 4 * ff];
-        CT *Zm = Z + (size_t)m * mode_stride;
+        const double2 *zl = Gs + (jep * NO + nm) * 16;
+        const double tre = geo[(size_t)9 * P + 4 * e], trf = geo[(size_t)9 * P + 4 * ff];
+        double2 *Zm = Z + (size_t)m * mode_stride;
 #pragma unroll
         for (int ab = 0; ab < 4; ++ab) {
             const int a = ab >> 1, b = ab & 1;
-            const CT lo = P11s[(jep * NO + nl) * 4 + ab];
-            const CT hi = P11s[(jep * NO + nh) * 4 + ab];
-            const CT S = cadd(lo, hi), D = csub(lo, hi);
-            CT blk[4];
-            const R half = R(0.5);
-            blk[0] = cadd(mk<R>(half * tre * trf * S.x, half * tre * trf * S.y), zl[0 * 4 + ab]);
-            blk[1] = cadd(mk<R>(half * tre * D.y, -half * tre * D.x), zl[1 * 4 + ab]);   // t_rho(e) D/(2j)
-            blk[2] = cadd(mk<R>(-half * trf * D.y, half * trf * D.x), zl[2 * 4 + ab]);   // -t_rho(f) D/(2j)
-            blk[3] = cadd(mk<R>(half * S.x, half * S.y), zl[3 * 4 + ab]);
+            const double2 lo = P11s[(jep * NO + nl) * 4 + ab];
+            const double2 hi = P11s[(jep * NO + nh) * 4 + ab];
+            const double2 S = cadd(lo, hi), D = csub(lo, hi);
+            double2 blk[4];
+            const double half = 0.5;
+            blk[0] = cadd(make_double2(half * tre * trf * S.x, half * tre * trf * S.y), zl[0 * 4 + ab]);
+            blk[1] = cadd(make_double2(half * tre * D.y, -half * tre * D.x), zl[1 * 4 + ab]);   // t_rho(e) D/(2j)
+            blk[2] = cadd(make_double2(-half * trf * D.y, half * trf * D.x), zl[2 * 4 + ab]);   // -t_rho(f) D/(2j)
+            blk[3] = cadd(make_double2(half * S.x, half * S.y), zl[3 * 4 + ab]);
             const long long r0 = e + a, c0 = ff + b;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const long long row = r0 + (q >> 1) * Nn, col = c0 + (q & 1) * Nn;
-                const CT v = mk<R>(sre * blk[q].x - sim * blk[q].y, sre * blk[q].y + sim * blk[q].x);
+                const double2 v = make_double2(sre * blk[q].x - sim * blk[q].y, sre * blk[q].y + sim * blk[q].x);
                 catomic_add(Zm + row * ldz + col, v);
             }
         }
@@ -327,7 +369,7 @@ int launch_far(int N, int M, int nxi, double k, double sre, double sim, const do
     const int nchunks = (M + 1 + (NO - 2) - 1) / (NO - 2);
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, TPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, dct, sin2,
-                                  reinterpret_cast<C<R> *>(Z), ldz, ms);
+                                  reinterpret_cast<double2 *>(Z), ldz, ms);
     return check_launch("far_efie");
 }
 
@@ -345,8 +387,8 @@ extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, doub
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (prec == GHOST_BOR_F32) {
-        if (m_max + 1 <= 30) return launch_far<float, 32>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
-        return launch_far<float, 64>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        if (m_max + 1 <= 14) return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        return launch_far<float, 32>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
     }
     if (prec == GHOST_BOR_F64) {
         if (m_max + 1 <= 14) return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);

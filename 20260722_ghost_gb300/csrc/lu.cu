@@ -363,38 +363,60 @@ __device__ __forceinline__ bool is_masked(const int *mr, int r)
     return mr[0] == r || mr[1] == r || mr[2] == r || mr[3] == r;
 }
 
-// R = B - Zf X - band X ;  Zf float, X / B / R double.  64 x 64 tiles over
-// (rows, rhs), K in chunks of 32 accumulated in FP32 then added in FP64.
-constexpr int RK = 32;
+// R = B - Zf X - band X, all operands complex double.  64 x 64 tiles over
+// (rows, rhs).  Zf and X are split into two FP32 words each (hi + lo, ~48
+// bits); the hi*hi products are summed in FP32 over 16-term chunks and the
+// chunk sums folded into a double-float (TwoSum) accumulator; the small
+// hi*lo + lo*hi products are summed in FP32.  The FP64 band (near/self
+// blocks) is applied in FP64.
+constexpr int RK = 16;
+
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float v)
+{
+    const float s = hi + v;
+    const float bb = s - hi;
+    lo += (hi - (s - bb)) + (v - bb);
+    hi = s;
+}
+
+__device__ __forceinline__ void split2(double2 v, float2 &h, float2 &l)
+{
+    h = make_float2((float)v.x, (float)v.y);
+    l = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
+}
+
 __global__ void __launch_bounds__(256)
-residual_mixed_kernel(int n, int nrhs, int Nn, const float2 *__restrict__ Zf, long long ldz, long long sz,
+residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, long long ldz, long long sz,
                       const double2 *__restrict__ band, const int *__restrict__ mask_rows,
                       const double2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
                       double2 *__restrict__ R, float2 *__restrict__ Rlo, double *__restrict__ norms)
 {
-    __shared__ float2 Zs[GT][RK + 1];
-    __shared__ float2 Xs[RK][GT];
-    __shared__ double red[2][8];
+    __shared__ float2 Zh[RK][GT];       // transposed tiles: Z*[k][row]
+    __shared__ float2 Zl[RK][GT];
+    __shared__ float2 Xh[RK][GT];
+    __shared__ float2 Xl[RK][GT];
+    double (*red)[8] = reinterpret_cast<double (*)[8]>(&Zh[0][0]);   // reused after the K loop
     const int b = blockIdx.z;
     const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
-    const float2 *Zb = Zf + (size_t)b * sz;
+    const double2 *Zb = Zf + (size_t)b * sz;
     const double2 *Xb = X + (size_t)b * sbb;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
-    double2 acc[4][4];
+    float2 hi[4][4], lo[4][4], sm[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0, 0);
+        for (int j = 0; j < 4; ++j) { hi[i][j] = make_float2(0, 0); lo[i][j] = make_float2(0, 0); sm[i][j] = make_float2(0, 0); }
     for (int k0 = 0; k0 < n; k0 += RK) {
         __syncthreads();
         for (int i = tid; i < GT * RK; i += 256) {
             const int r = i / RK, kk = i % RK;
-            Zs[r][kk] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_float2(0, 0);
+            const double2 v = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
+            split2(v, Zh[kk][r], Zl[kk][r]);
         }
         for (int i = tid; i < RK * GT; i += 256) {
             const int kk = i / GT, c = i % GT;
-            double2 v = (k0 + kk < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kk) * ldb + c0 + c] : make_double2(0, 0);
-            Xs[kk][c] = make_float2((float)v.x, (float)v.y);
+            const double2 v = (k0 + kk < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kk) * ldb + c0 + c] : make_double2(0, 0);
+            split2(v, Xh[kk][c], Xl[kk][c]);
         }
         __syncthreads();
         float2 ac[4][4];
@@ -402,23 +424,31 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const float2 *__restrict__ Zf, lo
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j) ac[i][j] = make_float2(0, 0);
-#pragma unroll 8
+#pragma unroll 4
         for (int kk = 0; kk < RK; ++kk) {
-            float2 a[4], x[4];
+            float2 ah[4], al[4], xh[4], xl[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = Zs[ty + 16 * i][kk];
+            for (int i = 0; i < 4; ++i) { ah[i] = Zh[kk][ty + 16 * i]; al[i] = Zl[kk][ty + 16 * i]; }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) x[j] = Xs[kk][tx + 16 * j];
+            for (int j = 0; j < 4; ++j) { xh[j] = Xh[kk][tx + 16 * j]; xl[j] = Xl[kk][tx + 16 * j]; }
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) ac[i][j] = cfma(a[i], x[j], ac[i][j]);
+                for (int j = 0; j < 4; ++j) {
+                    ac[i][j] = cfma(ah[i], xh[j], ac[i][j]);
+                    sm[i][j] = cfma(ah[i], xl[j], sm[i][j]);
+                    sm[i][j] = cfma(al[i], xh[j], sm[i][j]);
+                }
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { acc[i][j].x += ac[i][j].x; acc[i][j].y += ac[i][j].y; }
+            for (int j = 0; j < 4; ++j) {
+                two_sum_acc(hi[i][j].x, lo[i][j].x, ac[i][j].x);
+                two_sum_acc(hi[i][j].y, lo[i][j].y, ac[i][j].y);
+            }
     }
+    __syncthreads();                     // Zh is reused for the norm reduction below
     const int *mr = mask_rows + 4 * b;
     const double2 *Bb = B + (size_t)b * sbb;
     double rn = 0.0, bn = 0.0;
@@ -433,7 +463,9 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const float2 *__restrict__ Zf, lo
             const int c = c0 + tx + 16 * j;
             if (c >= nrhs) continue;
             const double2 bv = Bb[(size_t)r * ldb + c];
-            double2 rv = make_double2(bv.x - acc[i][j].x, bv.y - acc[i][j].y);
+            const double zx = (double)hi[i][j].x + (double)lo[i][j].x + (double)sm[i][j].x;
+            const double zy = (double)hi[i][j].y + (double)lo[i][j].y + (double)sm[i][j].y;
+            double2 rv = make_double2(bv.x - zx, bv.y - zy);
             if (band) {
                 for (int ch = 0; ch < 2; ++ch) {
                     const double2 *bd = band + (((size_t)b * 4 + 2 * half + ch) * Nn + node) * 5;
@@ -541,7 +573,7 @@ residual64_kernel(int n, int nrhs, const double2 *__restrict__ Z, long long ldz,
 // ---------------------------------------------------------------------------
 // compose / mask / convert
 // ---------------------------------------------------------------------------
-__global__ void compose_kernel(int n, int Nn, const float2 *__restrict__ Zf, long long ldz, long long sz,
+__global__ void compose_kernel(int n, int Nn, const double2 *__restrict__ Zf, long long ldz, long long sz,
                                const double2 *__restrict__ band, const int *__restrict__ mask_rows,
                                float2 *__restrict__ A, long long lda, long long sa)
 {
@@ -554,8 +586,7 @@ __global__ void compose_kernel(int n, int Nn, const float2 *__restrict__ Zf, lon
     if (is_masked(mr, i) || is_masked(mr, j)) {
         out = make_float2(i == j ? 1.f : 0.f, 0.f);
     } else {
-        const float2 z = Zf[(size_t)b * sz + (size_t)i * ldz + j];
-        double2 v = make_double2((double)z.x, (double)z.y);
+        double2 v = Zf[(size_t)b * sz + (size_t)i * ldz + j];
         if (band) {
             const int a = i >= Nn, ch = j >= Nn;
             const int ii = i - a * Nn, jj = j - ch * Nn;
@@ -646,7 +677,7 @@ extern "C" int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual: memset");
     dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
-    residual_mixed_kernel<<<grid, 256, 0, st>>>(n, nrhs, Nn, reinterpret_cast<const float2 *>(Zf), ldz, stride_z,
+    residual_mixed_kernel<<<grid, 256, 0, st>>>(n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
                                                 reinterpret_cast<const double2 *>(band), mask_rows,
                                                 reinterpret_cast<const double2 *>(X), reinterpret_cast<const double2 *>(B),
                                                 ldb, stride_b, reinterpret_cast<double2 *>(R),
@@ -677,7 +708,7 @@ extern "C" int ghost_bor_compose(int batch, int n, int Nn, const void *Zf, long 
     if (batch < 1 || n < 1 || n != 2 * Nn || !Zf || !mask_rows || !A || ldz < n || lda < n) return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     dim3 grid((n + 255) / 256, n, batch);
-    compose_kernel<<<grid, 256, 0, st>>>(n, Nn, reinterpret_cast<const float2 *>(Zf), ldz, stride_z,
+    compose_kernel<<<grid, 256, 0, st>>>(n, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
                                          reinterpret_cast<const double2 *>(band), mask_rows,
                                          reinterpret_cast<float2 *>(A), lda, stride_a);
     return check_launch("compose");

@@ -2,7 +2,8 @@
 
 Stages (each a C-ABI call on one CUDA stream):
 
-  far fill      ghost_bor_far_efie   Z_far[m], m = 0..M (FP32 or FP64)
+  far fill      ghost_bor_far_efie   Z_far[m], m = 0..M (FP32 or FP64 sampling + DCT,
+                                     FP64 contraction and storage)
   near fill     ghost_bor_near_efie  FP64 near/self blocks (band store or dense)
   compose       ghost_bor_compose    A32 = fl32(Z_far + Z_near), masked
   excitation    ghost_bor_rhs        B[m][row][2*it + pol] (FP64)
@@ -16,9 +17,10 @@ excitation obeys V(-m) = +-D V(m), so each -m system has the solution
 +-D x(m) and contributes exactly the same far field; the mode sum weights
 m > 0 by two (checked against the per-mode reference in the tests).
 
-Precisions: "fp64" is the plain FP64 path (the comparator); "fp32ir" fills
-the far part and factors in FP32, keeps near/self blocks, the residual and the
-mode sum in FP64, and refines up to three times.
+Precisions: "fp64" is the plain FP64 path (the comparator); "fp32ir" samples
+and transforms the far kernel and factors in FP32, keeps the near/self blocks,
+the far-block contraction, the residual and the mode sum in FP64, and refines
+up to three times.
 """
 
 from __future__ import annotations
@@ -81,7 +83,8 @@ class BorGpuProblem:
         self.T = len(self.thetas)
         self.nrhs = 2 * self.T
         self.n_xi = n_xi_efie(self.k, self.rho_max, self.m_max)
-        dct, sin2 = dct_tables(self.n_xi, self.m_max + 2)
+        # the far kernels sample exp(-jkR)/R; the table carries the 1/(4 pi)
+        dct, sin2 = dct_tables(self.n_xi, self.m_max + 2, scale=1.0 / (4.0 * math.pi))
         self.near = near_tables(self.gen, self.k, self.m_max)
         self.masks = mask_rows(self.gen, self.m_max)
         dev = self.device
@@ -104,6 +107,13 @@ class BorGpuProblem:
         self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
         self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
 
+    def h2d_bytes(self) -> int:
+        """Bytes of host tables copied to the device for one problem."""
+        return int(sum(t.numel() * t.element_size() for t in (
+            self.d_geo, self.d_dct, self.d_sin2, self.d_nodes, self.d_elem, self.d_pairs,
+            self.d_tails, self.d_cells, self.d_core, self.d_tail, self.d_masks, self.d_thetas,
+            self.d_mode_w)))
+
     # -- memory -----------------------------------------------------------
     def bytes_needed(self, precision: str) -> int:
         Mb = self.m_max + 1
@@ -111,7 +121,7 @@ class BorGpuProblem:
         rhs = self.n * self.nrhs
         if precision == "fp64":
             return Mb * (2 * nn * 16 + 3 * rhs * 16)
-        return Mb * (2 * nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16)
+        return Mb * (nn * 16 + nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16)
 
     # -- stages -----------------------------------------------------------
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
@@ -197,7 +207,7 @@ class BorGpuProblem:
                      nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(norms), st); mark("residual")
             del Zc
         else:
-            Zf = torch.zeros((Mb, n, n), dtype=c64, device=self.device)
+            Zf = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
             band = torch.zeros((Mb, 4, Nn, 5), dtype=c128, device=self.device)
             self.fill_far(Zf, nat.F32, self.C, st); mark("far"); abort()
             self.fill_near(self.C, st, band=band); mark("near")

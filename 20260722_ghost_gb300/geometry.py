@@ -114,14 +114,14 @@ def n_xi_bracket(k: float, rho_max: float, m_max: int) -> int:
     return int(2 ** math.ceil(math.log2(max(128, 6 * (m_max + 2), 8 * (osc + 4)))))
 
 
-def dct_tables(n_xi: int, n_orders: int) -> Tuple[np.ndarray, np.ndarray]:
+def dct_tables(n_xi: int, n_orders: int, scale: float = 1.0) -> Tuple[np.ndarray, np.ndarray]:
     """Half-grid trapezoid/DCT-I weights equivalent to the reference's
     FFT over xi_l = -pi + 2 pi l / n_xi for an even integrand:
 
         G_n = (pi/h) [g_0 + (-1)^n g_h + 2 sum_{j=1}^{h-1} g_j cos(pi n j / h)],
 
-    h = n_xi/2, g_j = g(pi j / h).  Returns dct [h+1, n_orders] and
-    sin2 [h+1] = sin^2(pi j / n_xi)."""
+    h = n_xi/2, g_j = g(pi j / h).  Returns dct [h+1, n_orders] (times
+    ``scale``) and sin2 [h+1] = sin^2(pi j / n_xi)."""
     h = n_xi // 2
     j = np.arange(h + 1)
     n = np.arange(n_orders)
@@ -130,7 +130,7 @@ def dct_tables(n_xi: int, n_orders: int) -> Tuple[np.ndarray, np.ndarray]:
     # exact integer reduction of (n j) mod 2h keeps cos accurate for large n j
     nj = np.outer(j, n) % (2 * h)
     ang = np.pi * nj / h
-    dct = (np.pi / h) * c[:, None] * np.cos(ang)
+    dct = (np.pi / h) * c[:, None] * np.cos(ang) * scale
     sin2 = np.sin(0.5 * np.pi * j / h) ** 2
     return np.ascontiguousarray(dct), np.ascontiguousarray(sin2)
 

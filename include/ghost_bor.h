@@ -83,12 +83,16 @@ int ghost_bor_sample_mfie(int nr, int np_, int nxi,
  * combine the orders into the mode-m blocks, m = 0..m_max, then ADD
  * scale * [[ztt, ztf], [zft, zff]] into Z[m] (rows 0..Nn-1 = J_t tests,
  * Nn..2Nn-1 = J_phi tests).  Z must be zeroed (or hold other terms) first.
+ * `prec` selects the precision of the sampling and the DCT; the contraction,
+ * the mode combination and the accumulation into Z are FP64 and Z is always
+ * complex double.
  *
  *   geo   [11][P] doubles, P = 4 n_elem (Gauss points, element-major):
  *         rho, z, w, T0*w*rho, T1*w*rho, T0*w, T1*w, dRT0*w, dRT1*w, t_rho, t_z
- *   dct   [nxi/2+1][m_max+2]  (pi/h) * c_j * cos(pi n j / h), c_0 = c_h = 1, else 2
+ *   dct   [nxi/2+1][m_max+2]  (pi/h) * c_j * cos(pi n j / h) / (4 pi),
+ *                             c_0 = c_h = 1, else 2 (the kernel samples exp(-jkR)/R)
  *   sin2  [nxi/2+1]           sin^2(pi j / nxi)
- *   Z     complex, precision `prec`, Z[m] at Z + m*mode_stride, row stride ldz
+ *   Z     complex double, Z[m] at Z + m*mode_stride, row stride ldz
  * Replaces StreamingFarBlocks._build_range + efie_blocks
  * (bor_streaming.py:220-268, 320-376, 388-407).
  */
@@ -157,12 +161,13 @@ int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
 
 /* ------------------------------------------------------------------------
  * Mixed-precision residual for iterative refinement, per batch b:
- *   R = B - (Zf + band) X        with Zf complex float (far part), band
+ *   R = B - (Zf + band) X        with Zf complex double (far part), band
  *   complex double [Nn blocks as in ghost_bor_near_efie] (may be NULL), X and
  *   B complex double; rows in mask_rows[b] produce R = 0.
  * If Rlo != NULL the residual is also written as complex float to Rlo.
  * norms[b][2] receives (||R||_F^2, ||B||_F^2).
- * Products accumulate in FP32 over 64-term chunks and in FP64 across chunks.
+ * Zf and X are split into two FP32 words each; the leading products are
+ * summed in FP32 over 16-term chunks and across chunks in double-float.
  */
 int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
                        const void *Zf, long long ldz, long long stride_z,
@@ -191,8 +196,9 @@ int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
 
 /* ------------------------------------------------------------------------
  * Small helpers used between stages.
- * ghost_bor_compose: A32[b] = fl32(Zf[b] + band[b]) with masked rows/columns
- *   replaced by identity rows/columns (band may be NULL).
+ * ghost_bor_compose: A32[b] = fl32(Zf[b] + band[b]) (Zf complex double, A32
+ *   complex float) with masked rows/columns replaced by identity rows/columns
+ *   (band may be NULL).
  * ghost_bor_mask64: apply the same identity masking to a complex double Z.
  * ghost_bor_convert: elementwise complex double <-> float copy of a strided
  *   batch of row blocks (dir 0: double->float, 1: float->double, 2: float

@@ -54,8 +54,12 @@ def test_c1_sphere(pkg):
         assert abs(10 * math.log10(r["sigma_vv"][0] / mie)) < 0.01
 
 
-def test_mode_truncation_matches_reference_rule(pkg):
+def test_mode_truncation_matches_reference_rule(pkg, oracle):
+    """mode_tol truncation (two quiet modes) gives the oracle's modes_used and sum."""
     D = load_golden("sphere_n24")
-    r0 = pkg.bor_solver.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], n_modes=int(D["m_max"]),
-                                  mode_tol=1e-3, table_precision="double")
-    assert r0["modes_used"] < int(D["m_max"])
+    kw = dict(n_modes=14, mode_tol=1e-6)
+    ref = oracle.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], **kw)
+    r = pkg.bor_solver.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], table_precision="double", **kw)
+    assert ref["modes_used"] < 14
+    assert r["modes_used"] == ref["modes_used"]
+    assert rel(r["amp_vv"], ref["amp_vv"]) < 1e-10
