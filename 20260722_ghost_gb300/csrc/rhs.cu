@@ -240,3 +240,92 @@ extern "C" int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, 
         return GHOST_BOR_EINVAL;
     return check_launch("farfield");
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free excitation.
+//
+// Some callers cannot allocate device memory while they solve: a service that
+// reserves all GPU memory for its own arena at start-up, or a host thread that
+// must not call cudaMalloc/cudaFree because those calls can synchronise the
+// whole device and fail once memory is fragmented.  For them the Bessel /
+// phase workspace of ghost_bor_rhs lives in one file-scope device array of
+// fixed size that every GPU loading this library keeps until the process
+// exits; the sweep is processed in blocks of angles that fit in it.
+//
+// Limits and rules: one angle needs 4*n_elem*((m_max+2)*8 + 16) bytes of the
+// array; larger problems are rejected.  The array is shared by every call and
+// keeps the previous call's contents (everything read is written first in the
+// same call, so nothing needs clearing); calls that overlap on the GPU (other
+// streams, other host threads) race on it and must be serialised by the
+// caller.  The first call on each device looks up the array's device address
+// with cudaGetSymbolAddress while that device is current; make that first call
+// before any stream capture.
+// ---------------------------------------------------------------------------
+namespace gb {
+namespace {
+
+constexpr long long kRhsScratchBytes = 64LL << 20;
+__device__ __align__(256) unsigned char g_rhs_scratch[kRhsScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void *g_rhs_scratch_ptr[kMaxDevices] = {};
+
+void *rhs_scratch_for_current_device()
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    void *p = __atomic_load_n(&g_rhs_scratch_ptr[dev], __ATOMIC_ACQUIRE);
+    if (p) return p;
+    if (cudaGetSymbolAddress(&p, g_rhs_scratch) != cudaSuccess || !p) return nullptr;
+    __atomic_store_n(&g_rhs_scratch_ptr[dev], p, __ATOMIC_RELEASE);
+    return p;
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" long long ghost_bor_rhs_noalloc_capacity(void) { return gb::kRhsScratchBytes; }
+
+extern "C" int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double k,
+                                     double coef_e, double coef_h,
+                                     const double *geo, const double *thetas_deg,
+                                     const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                                     void *stream)
+{
+    using namespace gb;
+    const int Mp = m_max + 2;
+    if (n_elem < 1 || m_max < 0 || Mp > MAX_ORD || n_theta < 1 || !geo || !thetas_deg || !mask_rows ||
+        !B || ldb < 2LL * n_theta || mode_stride < ldb * 2LL * (n_elem + 1))
+        return GHOST_BOR_EINVAL;
+    const long long P = 4LL * n_elem;
+    const long long per_angle = P * Mp * 8 + P * 16;
+    const long long usable = kRhsScratchBytes - 256;          // alignment slack for the phase table
+    if (per_angle > usable) {
+        set_last_error("ghost_bor_rhs_noalloc: one angle needs more than the 64 MiB static workspace "
+                       "(4*n_elem*((m_max+2)*8+16) bytes); use ghost_bor_rhs with a caller workspace");
+        return GHOST_BOR_EINVAL;
+    }
+    void *scratch = rhs_scratch_for_current_device();
+    if (!scratch) {
+        set_last_error("ghost_bor_rhs_noalloc: cudaGetSymbolAddress of the static workspace failed");
+        return GHOST_BOR_ECUDA;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int chunk = (int)(usable / per_angle < n_theta ? usable / per_angle : n_theta);
+    for (int it0 = 0; it0 < n_theta; it0 += chunk) {
+        const int T = (n_theta - it0 < chunk) ? n_theta - it0 : chunk;
+        double *Jtab = reinterpret_cast<double *>(scratch);
+        double2 *Ph = reinterpret_cast<double2 *>(
+            (reinterpret_cast<uintptr_t>(Jtab + (size_t)P * Mp * T) + 15) & ~uintptr_t(15));
+        dim3 g1((T + 63) / 64, (unsigned)P);
+        bessel_phase_kernel<<<g1, 64, 0, st>>>((int)P, Mp, T, k, geo, thetas_deg + it0, Jtab, Ph);
+        int rc = check_launch("rhs_noalloc: bessel");
+        if (rc) return rc;
+        dim3 g2((T + 63) / 64, n_elem + 1, m_max + 1);
+        rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, T, k, coef_e, coef_h, geo, thetas_deg + it0,
+                                      Jtab, Ph, mask_rows, reinterpret_cast<double2 *>(B) + 2 * (size_t)it0,
+                                      ldb, mode_stride);
+        if ((rc = check_launch("rhs_noalloc"))) return rc;
+    }
+    return GHOST_BOR_OK;
+}

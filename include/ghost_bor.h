@@ -144,6 +144,25 @@ int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
                   const int *mask_rows, double *B, long long ldb, long long mode_stride,
                   void *work, void *stream);
 
+/* Allocation-free variant of ghost_bor_rhs for callers that cannot allocate
+ * device memory during a solve (a service that reserves all GPU memory up front,
+ * or a thread that must not call cudaMalloc/cudaFree because they can
+ * synchronise the device).  Same arguments and output as ghost_bor_rhs minus
+ * `work`: the workspace is a 64 MiB static device array owned by the library
+ * (held on every GPU that loads it until exit), used in blocks of angles.
+ * Rejects (GHOST_BOR_EINVAL) problems where one angle needs more than the
+ * array: 4*n_elem*((m_max+2)*8 + 16) > 64 MiB - 256.  Calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and should
+ * come before any stream capture.  No counterpart in the reference.
+ * ghost_bor_rhs_noalloc_capacity() returns the array size in bytes. */
+long long ghost_bor_rhs_noalloc_capacity(void);
+int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double k,
+                          double coef_e, double coef_h,
+                          const double *geo, const double *thetas_deg,
+                          const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                          void *stream);
+
 /* ------------------------------------------------------------------------
  * Batched complex LU with partial pivoting (|re|+|im| pivot rule, as LAPACK
  * izamax) of n x n matrices A[b] = A + b*stride_a, row-major, b < batch.
