@@ -60,6 +60,51 @@ __device__ __forceinline__ void catomic_add(double2 *p, double2 v) {
 }
 
 // ----------------------------------------------------------------------------
+// double-float arithmetic: a value is hi + lo with two FP32 words (~48 bits).
+// Used where FP64-class accuracy is needed but FP64 throughput is not (the
+// FP64 pipe of a GB300 runs at ~1/60 of the FP32 pipe).  Error-free
+// transformations: TwoProd via fmaf, TwoSum (Knuth).
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_from(double x)
+{
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+__device__ __forceinline__ double df_to(float2 a) { return (double)a.x + (double)a.y; }
+
+// s += a * b   (all double-float; s.y is left unnormalised, |s.y| << |s.x|)
+__device__ __forceinline__ void df_mac(float2 &s, float2 a, float2 b)
+{
+    const float p = a.x * b.x;
+    const float pe = fmaf(a.x, b.x, -p);
+    const float t = s.x + p;
+    const float bb = t - s.x;
+    const float te = (s.x - (t - bb)) + (p - bb);
+    s.y += te + pe + fmaf(a.x, b.y, a.y * b.x);
+    s.x = t;
+}
+
+// a * b with a double-float and b double-float, renormalised result
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b)
+{
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e += fmaf(a.x, b.y, a.y * b.x);
+    const float h = p + e;
+    return make_float2(h, e - (h - p));
+}
+
+// a + b, renormalised
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    const float e = (a.x - (s - bb)) + (b.x - bb) + a.y + b.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+
+// ----------------------------------------------------------------------------
 // error reporting helpers (host)
 // ----------------------------------------------------------------------------
 void set_last_error(const char *msg);

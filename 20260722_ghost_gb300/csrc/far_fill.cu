@@ -5,14 +5,15 @@
 // contraction, :388-407 per-mode combination) and its C sampler
 // (bor_stream_kernel.c:26-48).
 //
-// One CTA = one test element e x EPB source elements f.  Each of the 16
-// threads of an element pair owns one Gauss-point pair (g, h) and
-//   1. samples g(xi_j) = exp(-j k R)/(4 pi R) on the HALF azimuth grid
+// One CTA = one test element e x EPB source elements f = 16 EPB Gauss-point
+// pairs (g, h), each served by OG threads that
+//   1. sample g(xi_j) = exp(-j k R)/(4 pi R) on the HALF azimuth grid
 //      xi_j = pi j / h, j = 0..h (h = n_xi/2; g is even in xi, so this is the
-//      reference's full-grid trapezoid rule folded in two),
-//   2. accumulates the even DCT  G_n = sum_j dct[j][n] g_j  for a chunk of
-//      NO orders in registers (the FFT of the reference restricted to the
-//      orders that are used),
+//      reference's full-grid trapezoid rule folded in two), each thread a
+//      stride-OG subset of a 32-sample chunk, into shared memory,
+//   2. accumulate the even DCT  G_n = sum_j dct[j][n] g_j, each thread for
+//      its NT orders, in registers (the FFT of the reference restricted to
+//      the orders that are used),
 // then the CTA contracts the 4x4 point pairs with the nodal Galerkin weights
 // into five order primitives (11, dd, ds, sd, ss; the rr/zz/r1/1r primitives
 // of the reference are tangent multiples of 11 because tangents are constant
@@ -34,8 +35,8 @@
 namespace gb {
 namespace {
 
-constexpr int EPB = 8;            // element pairs per CTA
-constexpr int TPB = EPB * 16;     // one thread per Gauss-point pair
+constexpr int EPB = 4;            // element pairs per CTA
+constexpr int TPB = EPB * 16 * 4; // Gauss-point pairs x order groups
 constexpr int JC = 32;            // azimuth samples staged per smem chunk
 
 constexpr double kTwoPi = 6.283185307179586476925286766559;
@@ -118,21 +119,26 @@ template <> struct GreenSampler<float> {
     }
 };
 
-template <class R> struct SmemLayout {
-    // Gs   [EPB][NO][16]  double2  per-pair orders, later the mode-local blocks
-    // P11s [EPB][NO][4]   double2
-    // dcts [JC][NO]       R
-    // s2s  [JC]           S2
-    // wts  [EPB+1][6][4]  double   (index EPB = test element)
-    static size_t bytes(int NO) {
-        return sizeof(double2) * (size_t)EPB * NO * 16 + sizeof(double2) * (size_t)EPB * NO * 4 +
-               sizeof(R) * (size_t)JC * NO + sizeof(typename GreenSampler<R>::S2) * JC +
-               sizeof(double) * (size_t)(EPB + 1) * 24;
+constexpr int OG = 4;                 // order groups: threads sharing one Gauss-point pair
+constexpr int PPB = EPB * 16;         // Gauss-point pairs per CTA
+
+template <class R, int NT> struct SmemLayout {
+    // gsm  [JC][PPB]        C<R>     samples of the current chunk
+    // dcts [JC][OG*NT]      R
+    // s2s  [JC]             S2
+    // Gs   [EPB][OG*NT][16] 16 B     per-pair orders, later the mode-local blocks
+    // P11s [EPB][OG*NT][4]  16 B
+    // wts  [EPB+1][24]      double ; wtf [EPB+1][24] float2
+    static constexpr int NOB = OG * NT;
+    static size_t bytes() {
+        return sizeof(C<R>) * (size_t)JC * PPB + sizeof(R) * (size_t)JC * NOB +
+               sizeof(typename GreenSampler<R>::S2) * JC + 16 * (size_t)EPB * NOB * 16 +
+               16 * (size_t)EPB * NOB * 4 + (sizeof(double) + sizeof(float2)) * (size_t)(EPB + 1) * 24;
     }
 };
 
-template <class R, int NO>
-__global__ void __launch_bounds__(TPB)
+template <class R, int NT>
+__global__ void __launch_bounds__(TPB, 2)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
                 const double *__restrict__ sin2, double2 *__restrict__ Z,
@@ -141,36 +147,40 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     using CT = C<R>;
     using Samp = GreenSampler<R>;
     using S2 = typename Samp::S2;
+    constexpr int NOB = OG * NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double2 *Gs = reinterpret_cast<double2 *>(smem_raw);
-    double2 *P11s = Gs + EPB * NO * 16;
-    R *dcts = reinterpret_cast<R *>(P11s + EPB * NO * 4);
-    S2 *s2s = reinterpret_cast<S2 *>(dcts + JC * NO);
-    double *wts = reinterpret_cast<double *>(s2s + JC);
+    CT *gsm = reinterpret_cast<CT *>(smem_raw);
+    R *dcts = reinterpret_cast<R *>(gsm + JC * PPB);
+    S2 *s2s = reinterpret_cast<S2 *>(dcts + JC * NOB);
+    double2 *Gs = reinterpret_cast<double2 *>(s2s + JC);
+    double2 *P11s = Gs + EPB * NOB * 16;
+    double *wts = reinterpret_cast<double *>(P11s + EPB * NOB * 4);
+    float2 *wtf = reinterpret_cast<float2 *>(wts + (EPB + 1) * 24);
 
     const int P = 4 * N;
     const int fgroups = (N + EPB - 1) / EPB;
     const int e = blockIdx.x / fgroups;
     const int f0 = (blockIdx.x % fgroups) * EPB;
-    const int chunk = blockIdx.y;
-    const int m0 = chunk * (NO - 2);
+    const int m0 = blockIdx.y * (NOB - 2);
     if (m0 > M) return;
-    const int m1 = min(M, m0 + NO - 3);
+    const int m1 = min(M, m0 + NOB - 3);
     const int o0 = max(0, m0 - 1);
     const int nord = m1 + 1 - o0 + 1;         // orders o0..m1+1
-    const int Mp = M + 2;                     // orders stored in dct rows
+    const int Mp = M + 2;
 
     const int tid = threadIdx.x;
-    const int ep = tid >> 4;
-    const int gh = tid & 15;
+    const int og = tid / PPB;                 // order group of this thread
+    const int pp = tid % PPB;                 // Gauss-point pair of this thread
+    const int ep = pp >> 4, gh = pp & 15;
     const int f = f0 + ep;
     const bool active = (f < N) && (abs(e - f) >= 2);
 
-    // Galerkin weights: rows 3..8 of geo (T0 w rho, T1 w rho, T0 w, T1 w, dRT0 w, dRT1 w)
     for (int i = tid; i < (EPB + 1) * 24; i += TPB) {
         const int slot = i / 24, r = i % 24;
         const int el = (slot == EPB) ? e : min(f0 + slot, N - 1);
-        wts[i] = geo[(size_t)(3 + r / 4) * P + 4 * el + (r % 4)];
+        const double w = geo[(size_t)(3 + r / 4) * P + 4 * el + (r % 4)];
+        wts[i] = w;
+        wtf[i] = df_from(w);
     }
 
     Samp smp;
@@ -183,190 +193,248 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
     }
 
-    CT acc[NO];          // running sums
-    CT cmp[NO];          // Kahan compensation (FP32 path only)
+    CT acc[NT];          // running sums of this thread's NT orders
+    CT cmp[NT];          // Kahan compensation (FP32 path only)
 #pragma unroll
-    for (int n = 0; n < NO; ++n) { acc[n] = mk<R>(R(0), R(0)); cmp[n] = mk<R>(R(0), R(0)); }
+    for (int n = 0; n < NT; ++n) { acc[n] = mk<R>(R(0), R(0)); cmp[n] = mk<R>(R(0), R(0)); }
 
     for (int j0 = 0; j0 <= h; j0 += JC) {
-        __syncthreads();
-        for (int i = tid; i < JC * NO; i += TPB) {
-            const int jj = i / NO, n = i % NO;
+        __syncthreads();                      // previous chunk consumed
+        for (int i = tid; i < JC * NOB; i += TPB) {
+            const int jj = i / NOB, n = i % NOB;
             const int j = j0 + jj, o = o0 + n;
             dcts[i] = (j <= h && o < Mp) ? (R)dct[(size_t)j * Mp + o] : R(0);
         }
-        for (int jj = tid; jj < JC; jj += TPB) {
-            const int j = min(j0 + jj, h);
-            s2s[jj] = Samp::load_s2(sin2, j);
-        }
+        for (int jj = tid; jj < JC; jj += TPB) s2s[jj] = Samp::load_s2(sin2, min(j0 + jj, h));
         __syncthreads();
-        if (active) {
-            const int jn = min(JC, h + 1 - j0);
-            if constexpr (sizeof(R) == 4) {
-                // FP32: sums over blocks of 8 samples, each folded into the
-                // running sum with Kahan compensation.  The node-level EFIE
-                // entries are double differences of these orders, so their
-                // rounding error must stay well below one FP32 ulp.
-                for (int jb = 0; jb < jn; jb += 8) {
-                    CT cacc[NO];
+        // sample phase: this thread evaluates its own pair at jj = og, og+OG, ...
+        const int jn = min(JC, h + 1 - j0);
+#pragma unroll 2
+        for (int jj = og; jj < JC; jj += OG)
+            gsm[jj * PPB + pp] = (active && jj < jn) ? smp(s2s[jj]) : mk<R>(R(0), R(0));
+        __syncthreads();
+        if (!active) continue;
+        const R *drow = dcts + og * NT;
+        if constexpr (sizeof(R) == 4) {
+            // FP32: 8-sample blocks folded into the running sums with Kahan
+            // compensation (the node-level entries are double differences of
+            // these orders, so their rounding must stay well below an ulp)
+            for (int jb = 0; jb < jn; jb += 8) {
+                CT cacc[NT];
 #pragma unroll
-                    for (int n = 0; n < NO; ++n) cacc[n] = mk<R>(R(0), R(0));
-                    const int je = min(jb + 8, jn);
-                    for (int jj = jb; jj < je; ++jj) {
-                        const CT gv = smp(s2s[jj]);
-                        const float4 *row = reinterpret_cast<const float4 *>(dcts + jj * NO);
+                for (int n = 0; n < NT; ++n) cacc[n] = mk<R>(R(0), R(0));
+                const int je = min(jb + 8, jn);
+                for (int jj = jb; jj < je; ++jj) {
+                    const CT gv = gsm[jj * PPB + pp];
+                    const float4 *row = reinterpret_cast<const float4 *>(drow + jj * NOB);
 #pragma unroll
-                        for (int n4 = 0; n4 < NO / 4; ++n4) {
-                            const float4 c = row[n4];
-                            cacc[4 * n4 + 0].x = fmaf(gv.x, c.x, cacc[4 * n4 + 0].x);
-                            cacc[4 * n4 + 0].y = fmaf(gv.y, c.x, cacc[4 * n4 + 0].y);
-                            cacc[4 * n4 + 1].x = fmaf(gv.x, c.y, cacc[4 * n4 + 1].x);
-                            cacc[4 * n4 + 1].y = fmaf(gv.y, c.y, cacc[4 * n4 + 1].y);
-                            cacc[4 * n4 + 2].x = fmaf(gv.x, c.z, cacc[4 * n4 + 2].x);
-                            cacc[4 * n4 + 2].y = fmaf(gv.y, c.z, cacc[4 * n4 + 2].y);
-                            cacc[4 * n4 + 3].x = fmaf(gv.x, c.w, cacc[4 * n4 + 3].x);
-                            cacc[4 * n4 + 3].y = fmaf(gv.y, c.w, cacc[4 * n4 + 3].y);
-                        }
-                    }
-#pragma unroll
-                    for (int n = 0; n < NO; ++n) {
-                        const float yx = cacc[n].x - cmp[n].x, yy = cacc[n].y - cmp[n].y;
-                        const float tx = acc[n].x + yx, ty = acc[n].y + yy;
-                        cmp[n].x = (tx - acc[n].x) - yx;
-                        cmp[n].y = (ty - acc[n].y) - yy;
-                        acc[n].x = tx;
-                        acc[n].y = ty;
+                    for (int n4 = 0; n4 < NT / 4; ++n4) {
+                        const float4 c = row[n4];
+                        cacc[4 * n4 + 0].x = fmaf(gv.x, c.x, cacc[4 * n4 + 0].x);
+                        cacc[4 * n4 + 0].y = fmaf(gv.y, c.x, cacc[4 * n4 + 0].y);
+                        cacc[4 * n4 + 1].x = fmaf(gv.x, c.y, cacc[4 * n4 + 1].x);
+                        cacc[4 * n4 + 1].y = fmaf(gv.y, c.y, cacc[4 * n4 + 1].y);
+                        cacc[4 * n4 + 2].x = fmaf(gv.x, c.z, cacc[4 * n4 + 2].x);
+                        cacc[4 * n4 + 2].y = fmaf(gv.y, c.z, cacc[4 * n4 + 2].y);
+                        cacc[4 * n4 + 3].x = fmaf(gv.x, c.w, cacc[4 * n4 + 3].x);
+                        cacc[4 * n4 + 3].y = fmaf(gv.y, c.w, cacc[4 * n4 + 3].y);
                     }
                 }
-            } else {
-                for (int jj = 0; jj < jn; ++jj) {
-                    const CT gv = smp(s2s[jj]);
-                    const double2 *row = reinterpret_cast<const double2 *>(dcts + jj * NO);
 #pragma unroll
-                    for (int n2 = 0; n2 < NO / 2; ++n2) {
-                        const double2 c = row[n2];
-                        acc[2 * n2 + 0].x = fma(gv.x, c.x, acc[2 * n2 + 0].x);
-                        acc[2 * n2 + 0].y = fma(gv.y, c.x, acc[2 * n2 + 0].y);
-                        acc[2 * n2 + 1].x = fma(gv.x, c.y, acc[2 * n2 + 1].x);
-                        acc[2 * n2 + 1].y = fma(gv.y, c.y, acc[2 * n2 + 1].y);
-                    }
+                for (int n = 0; n < NT; ++n) {
+                    const float yx = cacc[n].x - cmp[n].x, yy = cacc[n].y - cmp[n].y;
+                    const float tx = acc[n].x + yx, ty = acc[n].y + yy;
+                    cmp[n].x = (tx - acc[n].x) - yx;
+                    cmp[n].y = (ty - acc[n].y) - yy;
+                    acc[n].x = tx;
+                    acc[n].y = ty;
+                }
+            }
+        } else {
+            for (int jj = 0; jj < jn; ++jj) {
+                const CT gv = gsm[jj * PPB + pp];
+                const double2 *row = reinterpret_cast<const double2 *>(drow + jj * NOB);
+#pragma unroll
+                for (int n2 = 0; n2 < NT / 2; ++n2) {
+                    const double2 c = row[n2];
+                    acc[2 * n2 + 0].x = fma(gv.x, c.x, acc[2 * n2 + 0].x);
+                    acc[2 * n2 + 0].y = fma(gv.y, c.x, acc[2 * n2 + 0].y);
+                    acc[2 * n2 + 1].x = fma(gv.x, c.y, acc[2 * n2 + 1].x);
+                    acc[2 * n2 + 1].y = fma(gv.y, c.y, acc[2 * n2 + 1].y);
                 }
             }
         }
     }
 
-    // per-pair orders to smem in FP64: Gs[ep][n][gh] = acc - cmp
+    // per-pair orders to smem: FP32 path as double-float words (acc - cmp)
+    if constexpr (sizeof(R) == 4) {
+        float4 *Gf = reinterpret_cast<float4 *>(Gs);
 #pragma unroll
-    for (int n = 0; n < NO; ++n)
-        Gs[(ep * NO + n) * 16 + gh] = make_double2((double)acc[n].x - (double)cmp[n].x,
-                                                   (double)acc[n].y - (double)cmp[n].y);
+        for (int n = 0; n < NT; ++n)
+            Gf[(ep * NOB + og * NT + n) * 16 + gh] = make_float4(acc[n].x, -cmp[n].x, acc[n].y, -cmp[n].y);
+    } else {
+#pragma unroll
+        for (int n = 0; n < NT; ++n)
+            Gs[(ep * NOB + og * NT + n) * 16 + gh] = make_double2(acc[n].x, acc[n].y);
+    }
     __syncthreads();
 
     const double ik2 = 1.0 / (k * k);
-    // contraction jobs (ep, n): five primitives per order
-    for (int job = tid; job < EPB * nord; job += TPB) {
-        const int jep = job / nord, n = job % nord;
+    // contraction: job (ep, n, b) = five order primitives of source node b for
+    // both test nodes a.  Results replace the orders in place, so every
+    // thread reads first and writes after a barrier (uniform trip count).
+    const int njobs = EPB * nord * 2;
+    for (int base = 0; base < njobs; base += TPB) {
+        const int job = base + tid;
+        const int jep = (job >> 1) / nord, n = (job >> 1) % nord, b = job & 1;
         const int ff = f0 + jep;
-        if (ff >= N || abs(e - ff) < 2) continue;
-        double2 G[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) G[i] = Gs[(jep * NO + n) * 16 + i];
-        const double *wt = wts + EPB * 24;      // test element weights
-        const double *ws = wts + jep * 24;      // source element weights
-        // right contraction: GR_x[g][b] = sum_h G[g][h] Rx[b][h]
-        double2 GR1[8], GRs[8], GRd[8];
-#pragma unroll
-        for (int g = 0; g < 4; ++g)
-#pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                double2 a1 = make_double2(0, 0), as = make_double2(0, 0), ad = make_double2(0, 0);
-#pragma unroll
-                for (int hq = 0; hq < 4; ++hq) {
-                    const double2 gv = G[g * 4 + hq];
-                    const double w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq], wd = ws[(4 + b) * 4 + hq];
-                    a1.x = fma(gv.x, w1, a1.x); a1.y = fma(gv.y, w1, a1.y);
-                    as.x = fma(gv.x, wsv, as.x); as.y = fma(gv.y, wsv, as.y);
-                    ad.x = fma(gv.x, wd, ad.x); ad.y = fma(gv.y, wd, ad.y);
-                }
-                GR1[g * 2 + b] = a1; GRs[g * 2 + b] = as; GRd[g * 2 + b] = ad;
-            }
-        const int o = o0 + n;
-        const double tze = geo[(size_t)10 * P + 4 * e], tzf = geo[(size_t)10 * P + 4 * ff];
-        const double fm = o * ik2;          // jm/k^2 magnitude
-        const double fm2 = (double)o * o * ik2;  // m^2/k^2
-        double2 *zl = Gs + (jep * NO + n) * 16;
-#pragma unroll
-        for (int a = 0; a < 2; ++a)
-#pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                double2 p11 = make_double2(0, 0), pdd = make_double2(0, 0), pds = make_double2(0, 0), psd = make_double2(0, 0), pss = make_double2(0, 0);
+        const bool doit = job < njobs && ff < N && abs(e - ff) >= 2;
+        double2 out[5][2];    // p11, pdd, pds, psd, pss for a = 0, 1
+        if (doit) {
+            if constexpr (sizeof(R) == 4) {
+                // double-float contraction (exact well below an FP32 ulp)
+                const float4 *Gf = reinterpret_cast<const float4 *>(Gs) + (jep * NOB + n) * 16;
+                const float2 *wt = wtf + EPB * 24;      // test element weights
+                const float2 *ws = wtf + jep * 24;      // source element weights
+                float4 GR1[4], GRs[4], GRd[4];          // (re.hi, re.lo, im.hi, im.lo) per g
 #pragma unroll
                 for (int g = 0; g < 4; ++g) {
-                    const double l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
-                    const double2 r1 = GR1[g * 2 + b], rsv = GRs[g * 2 + b], rd = GRd[g * 2 + b];
-                    p11.x = fma(l1, r1.x, p11.x); p11.y = fma(l1, r1.y, p11.y);
-                    pdd.x = fma(ld, rd.x, pdd.x); pdd.y = fma(ld, rd.y, pdd.y);
-                    pds.x = fma(ld, rsv.x, pds.x); pds.y = fma(ld, rsv.y, pds.y);
-                    psd.x = fma(ls, rd.x, psd.x); psd.y = fma(ls, rd.y, psd.y);
-                    pss.x = fma(ls, rsv.x, pss.x); pss.y = fma(ls, rsv.y, pss.y);
+                    float2 r1 = make_float2(0, 0), i1 = r1, rs = r1, is = r1, rd = r1, id = r1;
+#pragma unroll
+                    for (int hq = 0; hq < 4; ++hq) {
+                        const float4 gv = Gf[g * 4 + hq];
+                        const float2 gr = make_float2(gv.x, gv.y), gi = make_float2(gv.z, gv.w);
+                        const float2 w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq], wd = ws[(4 + b) * 4 + hq];
+                        df_mac(r1, gr, w1); df_mac(i1, gi, w1);
+                        df_mac(rs, gr, wsv); df_mac(is, gi, wsv);
+                        df_mac(rd, gr, wd); df_mac(id, gi, wd);
+                    }
+                    GR1[g] = make_float4(r1.x, r1.y, i1.x, i1.y);
+                    GRs[g] = make_float4(rs.x, rs.y, is.x, is.y);
+                    GRd[g] = make_float4(rd.x, rd.y, id.x, id.y);
                 }
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    float2 acc2[5][2];
+#pragma unroll
+                    for (int c = 0; c < 5; ++c) { acc2[c][0] = make_float2(0, 0); acc2[c][1] = make_float2(0, 0); }
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        const float2 l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
+                        const float4 q1 = GR1[g], qs = GRs[g], qd = GRd[g];
+                        df_mac(acc2[0][0], l1, make_float2(q1.x, q1.y)); df_mac(acc2[0][1], l1, make_float2(q1.z, q1.w));
+                        df_mac(acc2[1][0], ld, make_float2(qd.x, qd.y)); df_mac(acc2[1][1], ld, make_float2(qd.z, qd.w));
+                        df_mac(acc2[2][0], ld, make_float2(qs.x, qs.y)); df_mac(acc2[2][1], ld, make_float2(qs.z, qs.w));
+                        df_mac(acc2[3][0], ls, make_float2(qd.x, qd.y)); df_mac(acc2[3][1], ls, make_float2(qd.z, qd.w));
+                        df_mac(acc2[4][0], ls, make_float2(qs.x, qs.y)); df_mac(acc2[4][1], ls, make_float2(qs.z, qs.w));
+                    }
+#pragma unroll
+                    for (int c = 0; c < 5; ++c) out[c][a] = make_double2(df_to(acc2[c][0]), df_to(acc2[c][1]));
+                }
+            } else {
+                const double2 *Gd = Gs + (jep * NOB + n) * 16;
+                const double *wt = wts + EPB * 24;
+                const double *ws = wts + jep * 24;
+                double2 GR1[4], GRs[4], GRd[4];
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    double2 a1 = make_double2(0, 0), as = make_double2(0, 0), ad = make_double2(0, 0);
+#pragma unroll
+                    for (int hq = 0; hq < 4; ++hq) {
+                        const double2 gv = Gd[g * 4 + hq];
+                        const double w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq], wd = ws[(4 + b) * 4 + hq];
+                        a1.x = fma(gv.x, w1, a1.x); a1.y = fma(gv.y, w1, a1.y);
+                        as.x = fma(gv.x, wsv, as.x); as.y = fma(gv.y, wsv, as.y);
+                        ad.x = fma(gv.x, wd, ad.x); ad.y = fma(gv.y, wd, ad.y);
+                    }
+                    GR1[g] = a1; GRs[g] = as; GRd[g] = ad;
+                }
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    double2 q[5];
+#pragma unroll
+                    for (int c = 0; c < 5; ++c) q[c] = make_double2(0, 0);
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        const double l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
+                        q[0].x = fma(l1, GR1[g].x, q[0].x); q[0].y = fma(l1, GR1[g].y, q[0].y);
+                        q[1].x = fma(ld, GRd[g].x, q[1].x); q[1].y = fma(ld, GRd[g].y, q[1].y);
+                        q[2].x = fma(ld, GRs[g].x, q[2].x); q[2].y = fma(ld, GRs[g].y, q[2].y);
+                        q[3].x = fma(ls, GRd[g].x, q[3].x); q[3].y = fma(ls, GRd[g].y, q[3].y);
+                        q[4].x = fma(ls, GRs[g].x, q[4].x); q[4].y = fma(ls, GRs[g].y, q[4].y);
+                    }
+#pragma unroll
+                    for (int c = 0; c < 5; ++c) out[c][a] = q[c];
+                }
+            }
+        }
+        __syncthreads();      // every job of this round has read its orders
+        if (doit) {
+            const int o = o0 + n;
+            const double tze = geo[(size_t)10 * P + 4 * e], tzf = geo[(size_t)10 * P + 4 * ff];
+            const double tt = tze * tzf;
+            const double fm = o * ik2;               // jm/k^2 magnitude
+            const double fm2 = (double)o * o * ik2;  // m^2/k^2
+            double2 *zl = Gs + (jep * NOB + n) * 16;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
                 const int ab = a * 2 + b;
-                P11s[(jep * NO + n) * 4 + ab] = p11;
+                const double2 p11 = out[0][a], pdd = out[1][a], pds = out[2][a], psd = out[3][a], pss = out[4][a];
+                P11s[(jep * NOB + n) * 4 + ab] = p11;
                 // mode-local parts (mode m = o)
-                const double tt = tze * tzf;
                 zl[0 * 4 + ab] = make_double2(tt * p11.x - ik2 * pdd.x, tt * p11.y - ik2 * pdd.y);
                 zl[1 * 4 + ab] = make_double2(fm * pds.y, -fm * pds.x);       // -(j o/k^2) pds
                 zl[2 * 4 + ab] = make_double2(-fm * psd.y, fm * psd.x);       // +(j o/k^2) psd
                 zl[3 * 4 + ab] = make_double2(-fm2 * pss.x, -fm2 * pss.y);
             }
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
     // mode combination + accumulation into Z[m]
     const int nmodes = m1 - m0 + 1;
-    const double sre = sc_re, sim = sc_im;
     for (int job = tid; job < EPB * nmodes; job += TPB) {
         const int jep = job / nmodes, m = m0 + job % nmodes;
         const int ff = f0 + jep;
         if (ff >= N || abs(e - ff) < 2) continue;
         const int nl = abs(m - 1) - o0, nm = m - o0, nh = m + 1 - o0;
-        const double2 *zl = Gs + (jep * NO + nm) * 16;
+        const double2 *zl = Gs + (jep * NOB + nm) * 16;
         const double tre = geo[(size_t)9 * P + 4 * e], trf = geo[(size_t)9 * P + 4 * ff];
         double2 *Zm = Z + (size_t)m * mode_stride;
 #pragma unroll
         for (int ab = 0; ab < 4; ++ab) {
             const int a = ab >> 1, b = ab & 1;
-            const double2 lo = P11s[(jep * NO + nl) * 4 + ab];
-            const double2 hi = P11s[(jep * NO + nh) * 4 + ab];
+            const double2 lo = P11s[(jep * NOB + nl) * 4 + ab];
+            const double2 hi = P11s[(jep * NOB + nh) * 4 + ab];
             const double2 S = cadd(lo, hi), D = csub(lo, hi);
             double2 blk[4];
-            const double half = 0.5;
-            blk[0] = cadd(make_double2(half * tre * trf * S.x, half * tre * trf * S.y), zl[0 * 4 + ab]);
-            blk[1] = cadd(make_double2(half * tre * D.y, -half * tre * D.x), zl[1 * 4 + ab]);   // t_rho(e) D/(2j)
-            blk[2] = cadd(make_double2(-half * trf * D.y, half * trf * D.x), zl[2 * 4 + ab]);   // -t_rho(f) D/(2j)
-            blk[3] = cadd(make_double2(half * S.x, half * S.y), zl[3 * 4 + ab]);
+            blk[0] = cadd(make_double2(0.5 * tre * trf * S.x, 0.5 * tre * trf * S.y), zl[0 * 4 + ab]);
+            blk[1] = cadd(make_double2(0.5 * tre * D.y, -0.5 * tre * D.x), zl[1 * 4 + ab]);   // t_rho(e) D/(2j)
+            blk[2] = cadd(make_double2(-0.5 * trf * D.y, 0.5 * trf * D.x), zl[2 * 4 + ab]);   // -t_rho(f) D/(2j)
+            blk[3] = cadd(make_double2(0.5 * S.x, 0.5 * S.y), zl[3 * 4 + ab]);
             const long long r0 = e + a, c0 = ff + b;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const long long row = r0 + (q >> 1) * Nn, col = c0 + (q & 1) * Nn;
-                const double2 v = make_double2(sre * blk[q].x - sim * blk[q].y, sre * blk[q].y + sim * blk[q].x);
+                const double2 v = make_double2(sc_re * blk[q].x - sc_im * blk[q].y, sc_re * blk[q].y + sc_im * blk[q].x);
                 catomic_add(Zm + row * ldz + col, v);
             }
         }
     }
 }
 
-template <class R, int NO>
+template <class R, int NT>
 int launch_far(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                const double *dct, const double *sin2, void *Z, long long ldz, long long ms,
                cudaStream_t st)
 {
-    const size_t smem = SmemLayout<R>::bytes(NO);
-    auto kern = far_efie_kernel<R, NO>;
+    const size_t smem = SmemLayout<R, NT>::bytes();
+    auto kern = far_efie_kernel<R, NT>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("far_efie: smem attribute");
+    constexpr int NOB = OG * NT;
     const int fgroups = (N + EPB - 1) / EPB;
-    const int nchunks = (M + 1 + (NO - 2) - 1) / (NO - 2);
+    const int nchunks = (M + 1 + (NOB - 2) - 1) / (NOB - 2);
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, TPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, dct, sin2,
                                   reinterpret_cast<double2 *>(Z), ldz, ms);
@@ -386,13 +454,15 @@ extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, doub
         ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k > 0.0))
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // 4 order groups x NT orders per thread: NT = 8 covers |m| <= 29 in one
+    // launch row, NT = 16 covers |m| <= 61 per row
     if (prec == GHOST_BOR_F32) {
-        if (m_max + 1 <= 14) return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
-        return launch_far<float, 32>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
     }
     if (prec == GHOST_BOR_F64) {
-        if (m_max + 1 <= 14) return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
-        return launch_far<double, 32>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
     }
     return GHOST_BOR_EINVAL;
 }

@@ -91,18 +91,23 @@ panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long lo
             // reciprocal of the pivot (LAPACK scales by 1/pivot)
             const R den = pv.x * pv.x + pv.y * pv.y;
             const CT inv = mk<R>(pv.x / den, -pv.y / den);
-            // warps over rows, lanes over trailing columns (nb <= 64: two passes)
-            for (int i = col + 1 + warp; i < n; i += NW) {
-                CT l;
-                if (lane == 0) {
-                    l = cmul(Ab[(size_t)i * lda + col], inv);
-                    Ab[(size_t)i * lda + col] = l;
+            // warps over rows, lanes over the trailing panel columns; each warp
+            // loads the multipliers of 32 rows at once (one per lane) so the
+            // row updates do not wait on one load at a time
+            for (int i0 = col + 1 + 32 * warp; i0 < n; i0 += 32 * NW) {
+                const int ir = i0 + lane;
+                CT lmine = mk<R>(0, 0);
+                if (ir < n) {
+                    lmine = cmul(Ab[(size_t)ir * lda + col], inv);
+                    Ab[(size_t)ir * lda + col] = lmine;
                 }
-                l.x = __shfl_sync(0xffffffffu, l.x, 0);
-                l.y = __shfl_sync(0xffffffffu, l.y, 0);
-                for (int c = lane; c < ncol; c += 32) {
-                    CT *dst = Ab + (size_t)i * lda + col + 1 + c;
-                    *dst = cfms(l, s_prow[c], *dst);
+                const int rows = min(32, n - i0);
+                for (int q = 0; q < rows; ++q) {
+                    CT l;
+                    l.x = __shfl_sync(0xffffffffu, lmine.x, q);
+                    l.y = __shfl_sync(0xffffffffu, lmine.y, q);
+                    CT *rowp = Ab + (size_t)(i0 + q) * lda + col + 1;
+                    for (int c = lane; c < ncol; c += 32) rowp[c] = cfms(l, s_prow[c], rowp[c]);
                 }
             }
         }
@@ -365,9 +370,9 @@ __device__ __forceinline__ bool is_masked(const int *mr, int r)
 
 // R = B - Zf X - band X, all operands complex double.  64 x 64 tiles over
 // (rows, rhs).  Zf and X are split into two FP32 words each (hi + lo, ~48
-// bits); the hi*hi products are summed in FP32 over 16-term chunks and the
+// bits); the hi*hi products are summed in FP32 over 4-term chunks and the
 // chunk sums folded into a double-float (TwoSum) accumulator; the small
-// hi*lo + lo*hi products are summed in FP32.  The FP64 band (near/self
+// hi*lo + lo*hi products and the TwoSum errors share one FP32 sum.  The FP64 band (near/self
 // blocks) is applied in FP64.
 constexpr int RK = 16;
 
@@ -391,64 +396,89 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
                       const double2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
                       double2 *__restrict__ R, float2 *__restrict__ Rlo, double *__restrict__ norms)
 {
-    __shared__ float2 Zh[RK][GT];       // transposed tiles: Z*[k][row]
-    __shared__ float2 Zl[RK][GT];
-    __shared__ float2 Xh[RK][GT];
-    __shared__ float2 Xl[RK][GT];
-    double (*red)[8] = reinterpret_cast<double (*)[8]>(&Zh[0][0]);   // reused after the K loop
+    // tiles hold both FP32 words of each complex value: (hi.re, hi.im, lo.re, lo.im)
+    __shared__ float4 Zs[RK][GT];       // transposed: Zs[k][row]
+    __shared__ float4 Xs[RK][GT];
+    double (*red)[8] = reinterpret_cast<double (*)[8]>(&Zs[0][0]);   // reused after the K loop
     const int b = blockIdx.z;
     const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
     const double2 *Zb = Zf + (size_t)b * sz;
     const double2 *Xb = X + (size_t)b * sbb;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
-    float2 hi[4][4], lo[4][4], sm[4][4];
+    // hi: leading sum of the hi*hi products; sm: low-order part (hi*lo + lo*hi
+    // products and the rounding errors of the hi sums, captured by TwoSum)
+    float2 hi[4][4], sm[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) { hi[i][j] = make_float2(0, 0); lo[i][j] = make_float2(0, 0); sm[i][j] = make_float2(0, 0); }
-    for (int k0 = 0; k0 < n; k0 += RK) {
-        __syncthreads();
-        for (int i = tid; i < GT * RK; i += 256) {
+        for (int j = 0; j < 4; ++j) { hi[i][j] = make_float2(0, 0); sm[i][j] = make_float2(0, 0); }
+
+    // each thread stages 4 Z and 4 X elements per tile (GT * RK = 1024 each)
+    double2 zp[4], xp[4];
+    auto fetch = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = tid + 256 * q;
             const int r = i / RK, kk = i % RK;
-            const double2 v = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
-            split2(v, Zh[kk][r], Zl[kk][r]);
+            zp[q] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
+            const int kx = i / GT, c = i % GT;
+            xp[q] = (k0 + kx < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kx) * ldb + c0 + c] : make_double2(0, 0);
         }
-        for (int i = tid; i < RK * GT; i += 256) {
-            const int kk = i / GT, c = i % GT;
-            const double2 v = (k0 + kk < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kk) * ldb + c0 + c] : make_double2(0, 0);
-            split2(v, Xh[kk][c], Xl[kk][c]);
+    };
+    auto stage = [&]() {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = tid + 256 * q;
+            float2 h, l;
+            split2(zp[q], h, l);
+            Zs[i % RK][i / RK] = make_float4(h.x, h.y, l.x, l.y);
+            split2(xp[q], h, l);
+            Xs[i / GT][i % GT] = make_float4(h.x, h.y, l.x, l.y);
         }
+    };
+    fetch(0);
+    for (int k0 = 0; k0 < n; k0 += RK) {
+        __syncthreads();                 // previous tile fully consumed
+        stage();
         __syncthreads();
-        float2 ac[4][4];
+        if (k0 + RK < n) fetch(k0 + RK); // global loads overlap the math below
+#pragma unroll 1
+        for (int k4 = 0; k4 < RK; k4 += 4) {
+            // FP32 partial sums over 4 k-steps, folded into (hi, sm) by TwoSum
+            float2 ac[4][4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) ac[i][j] = make_float2(0, 0);
-#pragma unroll 4
-        for (int kk = 0; kk < RK; ++kk) {
-            float2 ah[4], al[4], xh[4], xl[4];
+                for (int j = 0; j < 4; ++j) ac[i][j] = make_float2(0, 0);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) { ah[i] = Zh[kk][ty + 16 * i]; al[i] = Zl[kk][ty + 16 * i]; }
+            for (int kk = k4; kk < k4 + 4; ++kk) {
+                float4 a[4], x[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { xh[j] = Xh[kk][tx + 16 * j]; xl[j] = Xl[kk][tx + 16 * j]; }
+                for (int i = 0; i < 4; ++i) a[i] = Zs[kk][ty + 16 * i];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) x[j] = Xs[kk][tx + 16 * j];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float2 ah = make_float2(a[i].x, a[i].y), al = make_float2(a[i].z, a[i].w);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float2 xh = make_float2(x[j].x, x[j].y), xl = make_float2(x[j].z, x[j].w);
+                        ac[i][j] = cfma(ah, xh, ac[i][j]);
+                        sm[i][j] = cfma(ah, xl, sm[i][j]);
+                        sm[i][j] = cfma(al, xh, sm[i][j]);
+                    }
+                }
+            }
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    ac[i][j] = cfma(ah[i], xh[j], ac[i][j]);
-                    sm[i][j] = cfma(ah[i], xl[j], sm[i][j]);
-                    sm[i][j] = cfma(al[i], xh[j], sm[i][j]);
+                    two_sum_acc(hi[i][j].x, sm[i][j].x, ac[i][j].x);
+                    two_sum_acc(hi[i][j].y, sm[i][j].y, ac[i][j].y);
                 }
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                two_sum_acc(hi[i][j].x, lo[i][j].x, ac[i][j].x);
-                two_sum_acc(hi[i][j].y, lo[i][j].y, ac[i][j].y);
-            }
     }
-    __syncthreads();                     // Zh is reused for the norm reduction below
+    __syncthreads();                     // Zs is reused for the norm reduction below
     const int *mr = mask_rows + 4 * b;
     const double2 *Bb = B + (size_t)b * sbb;
     double rn = 0.0, bn = 0.0;
@@ -463,8 +493,8 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
             const int c = c0 + tx + 16 * j;
             if (c >= nrhs) continue;
             const double2 bv = Bb[(size_t)r * ldb + c];
-            const double zx = (double)hi[i][j].x + (double)lo[i][j].x + (double)sm[i][j].x;
-            const double zy = (double)hi[i][j].y + (double)lo[i][j].y + (double)sm[i][j].y;
+            const double zx = (double)hi[i][j].x + (double)sm[i][j].x;
+            const double zy = (double)hi[i][j].y + (double)sm[i][j].y;
             double2 rv = make_double2(bv.x - zx, bv.y - zy);
             if (band) {
                 for (int ch = 0; ch < 2; ++ch) {

@@ -19,19 +19,60 @@ namespace gb {
 namespace {
 
 constexpr int TPBN = 128;      // point pairs per batch = threads
-constexpr int NC = 32;         // orders per chunk
 constexpr int NCORE = 48;      // sinh-core Gauss order (bor_kernels.py:170)
+constexpr int kNc64 = 32;      // orders per chunk, FP64 projection
+constexpr int kNcDf = 24;      // orders per chunk, double-float projection
 
 struct NearSmem {
     // Gb   [TPBN][NC] double2 : per-pair orders of the current batch/chunk
     // W    [TPBN][20] double  : Galerkin weights of the batch
     // Prim [20][Mp]   double2 : contracted primitives, all orders
-    static size_t bytes(int Mp) {
+    static size_t bytes(int Mp, int NC) {
         return sizeof(double2) * (size_t)TPBN * NC + sizeof(double) * (size_t)TPBN * 20 +
                sizeof(double2) * 20 * (size_t)Mp;
     }
 };
 
+// acc[n] += (gre + j gim) cos((n0 + n) xi), n < NC, cos by the Chebyshev
+// recurrence cos((n+1) xi) = 2 cos(xi) cos(n xi) - cos((n-1) xi).
+template <bool DF, int NC>
+__device__ __forceinline__ void project(double2 (&acc)[DF ? 1 : NC], float4 (&dacc)[DF ? NC : 1],
+                                        double gre, double gim, double c1, int n0)
+{
+    if constexpr (!DF) {
+        double cm1 = c1, c0 = 1.0;                  // cos(-xi), cos(0)
+        for (int n = 0; n < n0; ++n) { const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn; }
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            acc[n].x = fma(gre, c0, acc[n].x);
+            acc[n].y = fma(gim, c0, acc[n].y);
+            const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
+        }
+    } else {
+        const float2 gr = df_from(gre), gi = df_from(gim);
+        const float2 cf = df_from(c1);
+        const float2 tc = make_float2(2.f * cf.x, 2.f * cf.y);   // exact doubling
+        float2 cm1 = cf, c0 = make_float2(1.f, 0.f);
+        for (int n = 0; n < n0; ++n) {
+            const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
+            cm1 = c0; c0 = cn;
+        }
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
+            df_mac(ar, gr, c0);
+            df_mac(ai, gi, c0);
+            dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
+            const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
+            cm1 = c0; c0 = cn;
+        }
+    }
+}
+
+// DF = true: the cos(n xi) recurrence and the projection run in double-float
+// (two FP32 words, ~48 bits) instead of FP64; the transcendental functions of
+// each azimuth point stay FP64.
+template <bool DF, int NC>
 __global__ void __launch_bounds__(TPBN)
 near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
@@ -71,10 +112,14 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
 
         for (int bt = 0; bt < nbatch; ++bt) {
             const int c = bt * TPBN + tid;
-            double2 acc[NC];
+            double2 acc[DF ? 1 : NC];   // FP64 projection
+            float4 dacc[DF ? NC : 1];   // double-float projection: (re.hi, re.lo, im.hi, im.lo)
+            double2 axis0 = make_double2(0.0, 0.0);   // order-0 term of an on-axis pair
             double wl[20];
 #pragma unroll
-            for (int n = 0; n < NC; ++n) acc[n] = make_double2(0.0, 0.0);
+            for (int n = 0; n < (DF ? 1 : NC); ++n) acc[n] = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int n = 0; n < (DF ? NC : 1); ++n) dacc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
             for (int i = 0; i < 20; ++i) wl[i] = 0.0;
             if (c < ncell) {
@@ -85,21 +130,6 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                 const double rp = rho_e0 + s * drho_e, zp = z_e0 + s * dz_e;
                 const double rq = rho_f0 + sp * drho_f, zq = z_f0 + sp * dz_f;
                 const double w = wc * Le * Lf;
-                const double Tp[2] = {1.0 - s, s}, Tq[2] = {1.0 - sp, sp};
-                const double Dp[2] = {(drho_e * (1.0 - s) - rp) / Le, (drho_e * s + rp) / Le};
-                const double Dq[2] = {(drho_f * (1.0 - sp) - rq) / Lf, (drho_f * sp + rq) / Lf};
-                const double rr = rp * rq * w;
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int b = 0; b < 2; ++b) {
-                        const int ab = a * 2 + b;
-                        wl[0 * 4 + ab] = Tp[a] * Tq[b] * rr;   // A1
-                        wl[1 * 4 + ab] = Dp[a] * Dq[b] * w;    // Add
-                        wl[2 * 4 + ab] = Dp[a] * Tq[b] * w;    // Ads
-                        wl[3 * 4 + ab] = Tp[a] * Dq[b] * w;    // Asd
-                        wl[4 * 4 + ab] = Tp[a] * Tq[b] * w;    // Ass
-                    }
                 // near modal kernel (bor_kernels.py:185-257)
                 const double dr = rp - rq, dz = zp - zq;
                 const double d2 = dr * dr + dz * dz;
@@ -110,7 +140,7 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         double sn, cs;
                         sincos(kk * R0, &sn, &cs);
                         const double amp = 2.0 * GB_PI / (4.0 * GB_PI * fmax(R0, 1e-300));
-                        acc[0] = make_double2(amp * cs, -amp * sn);
+                        axis0 = make_double2(amp * cs, -amp * sn);
                     }
                 } else {
                     const double d = sqrt(fmax(d2, 1e-300));
@@ -131,14 +161,7 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         const double gw = 2.0 * wv * dxi / (4.0 * GB_PI * R);
                         const double gre = gw * cs, gim = -gw * sn;
                         const double c1 = 1.0 - 2.0 * sv * sv;     // cos(xi)
-                        double cm1 = c1, c0 = 1.0;                  // cos(-xi), cos(0)
-                        for (int n = 0; n < n0; ++n) { const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn; }
-#pragma unroll
-                        for (int n = 0; n < NC; ++n) {
-                            acc[n].x = fma(gre, c0, acc[n].x);
-                            acc[n].y = fma(gim, c0, acc[n].y);
-                            const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
-                        }
+                        project<DF, NC>(acc, dacc, gre, gim, c1, n0);
                     }
                     // -- Gauss tail on [xi0, pi]
                     const double xi0 = 2.0 * asin(s0);
@@ -154,20 +177,40 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         const double gw = 2.0 * wt / (4.0 * GB_PI * R);
                         const double gre = gw * cs, gim = -gw * sn;
                         const double c1 = 1.0 - 2.0 * st * st;
-                        double cm1 = c1, c0 = 1.0;
-                        for (int n = 0; n < n0; ++n) { const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn; }
-#pragma unroll
-                        for (int n = 0; n < NC; ++n) {
-                            acc[n].x = fma(gre, c0, acc[n].x);
-                            acc[n].y = fma(gim, c0, acc[n].y);
-                            const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
-                        }
+                        project<DF, NC>(acc, dacc, gre, gim, c1, n0);
                     }
+                }
+                {
+                    // Galerkin weights of this point pair (computed after the
+                    // quadrature to keep them out of the registers it needs)
+                    const double Tp[2] = {1.0 - s, s}, Tq[2] = {1.0 - sp, sp};
+                    const double Dp[2] = {(drho_e * (1.0 - s) - rp) / Le, (drho_e * s + rp) / Le};
+                    const double Dq[2] = {(drho_f * (1.0 - sp) - rq) / Lf, (drho_f * sp + rq) / Lf};
+                    const double rr = rp * rq * w;
+#pragma unroll
+                    for (int a = 0; a < 2; ++a)
+#pragma unroll
+                        for (int b = 0; b < 2; ++b) {
+                            const int ab = a * 2 + b;
+                            wl[0 * 4 + ab] = Tp[a] * Tq[b] * rr;   // A1
+                            wl[1 * 4 + ab] = Dp[a] * Dq[b] * w;    // Add
+                            wl[2 * 4 + ab] = Dp[a] * Tq[b] * w;    // Ads
+                            wl[3 * 4 + ab] = Tp[a] * Dq[b] * w;    // Asd
+                            wl[4 * 4 + ab] = Tp[a] * Tq[b] * w;    // Ass
+                        }
                 }
             }
             __syncthreads();        // the previous batch's GEMM has finished reading W and Gb
+            if constexpr (DF) {
 #pragma unroll
-            for (int n = 0; n < NC; ++n) Gb[tid * NC + n] = acc[n];
+                for (int n = 0; n < NC; ++n)
+                    Gb[tid * NC + n] = make_double2((double)dacc[n].x + (double)dacc[n].y,
+                                                    (double)dacc[n].z + (double)dacc[n].w);
+            } else {
+#pragma unroll
+                for (int n = 0; n < NC; ++n) Gb[tid * NC + n] = acc[n];
+            }
+            if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
 #pragma unroll
             for (int i = 0; i < 20; ++i) W[tid * 20 + i] = wl[i];
             __syncthreads();
@@ -258,14 +301,16 @@ extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
     if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !pairs || !tails || !cells ||
         !core_gl || !tail_gl || !(k > 0.0))
         return GHOST_BOR_EINVAL;
-    if (!band && (!Z || prec != GHOST_BOR_F64 || ldz < 2LL * (n_elem + 1)))
-        return band ? GHOST_BOR_EINVAL : (prec != GHOST_BOR_F64 ? GHOST_BOR_EUNSUPPORTED : GHOST_BOR_EINVAL);
-    const size_t smem = NearSmem::bytes(m_max + 2);
+    if (prec != GHOST_BOR_F32 && prec != GHOST_BOR_F64) return GHOST_BOR_EINVAL;
+    if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
+    const bool df = prec == GHOST_BOR_F32;
+    const size_t smem = NearSmem::bytes(m_max + 2, df ? kNcDf : kNc64);
     if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
-    if (cudaFuncSetAttribute(near_efie_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("near_efie: smem attribute");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    near_efie_kernel<<<n_pairs, TPBN, smem, st>>>(
+    auto kern = df ? near_efie_kernel<true, kNcDf> : near_efie_kernel<false, kNc64>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("near_efie: smem attribute");
+    kern<<<n_pairs, TPBN, smem, st>>>(
         n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, pairs, tails, cells,
         n_cells_total, core_gl, tail_gl, n_tail_total, reinterpret_cast<double2 *>(band),
         reinterpret_cast<double2 *>(Z), ldz, mode_stride);

@@ -52,6 +52,7 @@ class SweepResult:
     timings: Dict[str, float] = field(default_factory=dict)
     info: Optional[np.ndarray] = None
     gpu_launches: int = 0
+    res_history: List[float] = field(default_factory=list)
 
 
 class BorGpuProblem:
@@ -106,6 +107,7 @@ class BorGpuProblem:
         w[0] = 1.0
         self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
         self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
+        self.refine_floor = 1e-6     # residuals below this are at the FP32-product floor
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
@@ -130,10 +132,10 @@ class BorGpuProblem:
                  scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_dct),
                  nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), stream)
 
-    def fill_near(self, scale: complex, stream: int, band=None, Z=None):
+    def fill_near(self, scale: complex, stream: int, band=None, Z=None, precision: int = nat.F64):
         ld = 0 if Z is None else Z.shape[-1]
         ms = 0 if Z is None else Z.stride(0)
-        nat.call("ghost_bor_near_efie", nat.F64, self.N, self.m_max, self.k, scale.real, scale.imag,
+        nat.call("ghost_bor_near_efie", precision, self.N, self.m_max, self.k, scale.real, scale.imag,
                  nat.ptr(self.d_nodes), nat.ptr(self.d_elem), len(self.near.pairs),
                  nat.ptr(self.d_pairs), nat.ptr(self.d_tails), nat.ptr(self.d_cells),
                  self.near.cells.shape[1], nat.ptr(self.d_core), nat.ptr(self.d_tail),
@@ -190,6 +192,7 @@ class BorGpuProblem:
         info = torch.empty((Mb,), dtype=torch.int32, device=self.device)
         norms = torch.empty((Mb, 2), dtype=torch.float64, device=self.device)
         iters = 0
+        history: List[float] = []
         if precision == "fp64":
             Z = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
             self.fill_far(Z, nat.F64, self.C, st); mark("far"); abort()
@@ -210,7 +213,7 @@ class BorGpuProblem:
             Zf = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
             band = torch.zeros((Mb, 4, Nn, 5), dtype=c128, device=self.device)
             self.fill_far(Zf, nat.F32, self.C, st); mark("far"); abort()
-            self.fill_near(self.C, st, band=band); mark("near")
+            self.fill_near(self.C, st, band=band, precision=nat.F32); mark("near")
             A = torch.empty((Mb, n, n), dtype=c64, device=self.device)
             nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
                      nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st); mark("compose"); abort()
@@ -227,12 +230,16 @@ class BorGpuProblem:
                      nrhs, X.stride(0), st); mark("solve")
             R = torch.empty_like(B)
             prev = None
+            history = []
             for it in range(max_refine + 1):
                 nat.call("ghost_bor_residual", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
                          nat.ptr(self.d_masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0), nat.ptr(R),
                          nat.ptr(X32), nat.ptr(norms), st)
                 rel = float(torch.sqrt(torch.max(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300))))
-                if it == max_refine or rel < 1e-14 or (prev is not None and rel > 0.5 * prev):
+                history.append(rel)
+                # stop at the FP32-product floor of the residual (~1e-7 of ||B||),
+                # on stagnation, or after max_refine corrections
+                if it == max_refine or rel < self.refine_floor or (prev is not None and rel > 0.5 * prev):
                     break
                 prev = rel
                 nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
@@ -257,7 +264,7 @@ class BorGpuProblem:
         tm["gpu_total_s"] = ev[names[0]].elapsed_time(ev[names[-1]]) / 1e3
         dF_h = dF_h.reshape(Mb, self.T, 2).transpose(0, 2, 1)
         out = SweepResult(dF=np.ascontiguousarray(dF_h), residual=res, refine_iters=iters, timings=tm,
-                          info=info_h)
+                          info=info_h, res_history=history if precision == "fp32ir" else [])
         if keep:
             out.X = X
             out.B = B

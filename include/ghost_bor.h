@@ -112,7 +112,9 @@ int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
  *   core_gl   [2][48] (u01, w01);  tail_gl [2][n_tail_total] (u01, w01)
  * Output: if band != NULL, ADD scale * block into band[m][blk][Nn][5]
  * (complex double, blk = tt, tf, ft, ff; column offset -2..2); else into the
- * dense Z[m] (precision prec, like ghost_bor_far_efie).
+ * dense complex double Z[m].  `prec` selects the arithmetic of the cos(m xi)
+ * projection: GHOST_BOR_F64 = FP64, GHOST_BOR_F32 = double-float (two FP32
+ * words, ~48-bit); the azimuth-point transcendentals are FP64 in both.
  * Replaces _near_pair_data + modal_kernels_near + the near loop of
  * assemble_mode (bor_solver.py:270-336, bor_kernels.py:170-257).
  */
@@ -186,7 +188,7 @@ int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
  * If Rlo != NULL the residual is also written as complex float to Rlo.
  * norms[b][2] receives (||R||_F^2, ||B||_F^2).
  * Zf and X are split into two FP32 words each; the leading products are
- * summed in FP32 over 16-term chunks and across chunks in double-float.
+ * summed in FP32 over 4-term chunks and across chunks in double-float.
  */
 int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
                        const void *Zf, long long ldz, long long stride_z,
