@@ -13,6 +13,12 @@
 #include "common.cuh"
 
 namespace gb {
+
+long long tc_update_workspace(int batch, int M, int N, int K);
+int tc_update(int batch, int M, int N, int K, const float2 *A, long long lda, long long sa,
+              const float2 *B, long long ldb, long long sb, float2 *C, long long ldc, long long sc,
+              void *work, cudaStream_t st);
+
 namespace {
 
 template <class R> struct LuCfg;
@@ -259,17 +265,24 @@ gemm_update_kernel(int rows, int cols, int K,
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = cfma(a[i], bv[j], acc[i][j]);
     }
+    // all loads of C first, then the stores (keeps 16 loads in flight)
+    CT cv[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int r = r0 + ty + 16 * i;
-        if (r >= rows) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int c = c0 + tx + 16 * j;
-            if (c < cols) {
-                CT *dst = Cb + (size_t)r * ldc + c;
-                *dst = csub(*dst, acc[i][j]);
-            }
+            cv[i][j] = (r < rows && c < cols) ? Cb[(size_t)r * ldc + c] : mk<R>(0, 0);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty + 16 * i;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = c0 + tx + 16 * j;
+            if (r < rows && c < cols) Cb[(size_t)r * ldc + c] = csub(cv[i][j], acc[i][j]);
         }
     }
 }
@@ -294,8 +307,22 @@ int gemm_update(int batch, int rows, int cols, int K, const C<R> *A, long long l
     return check_launch("gemm_update");
 }
 
+// C -= A B: tensor cores (3xTF32) for FP32 when a workspace is given, SIMT otherwise
 template <class R>
-int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv, int *info, cudaStream_t st)
+int update(int batch, int rows, int cols, int K, const C<R> *A, long long lda, long long sa,
+           const C<R> *B, long long ldb, long long sb, C<R> *Cm, long long ldc, long long sc,
+           void *work, cudaStream_t st)
+{
+    if constexpr (sizeof(R) == 4) {
+        if (work)
+            return tc_update(batch, rows, cols, K, A, lda, sa, B, ldb, sb, Cm, ldc, sc, work, st);
+    }
+    return gemm_update<R>(batch, rows, cols, K, A, lda, sa, B, ldb, sb, Cm, ldc, sc, st);
+}
+
+template <class R>
+int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv, int *info, void *work,
+               cudaStream_t st)
 {
     constexpr int NB = LuCfg<R>::NB;
     if (cudaMemsetAsync(info, 0, sizeof(int) * batch, st) != cudaSuccess) return check_launch("getrf: memset");
@@ -315,9 +342,9 @@ int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv
             trsm_kernel<R, NB, false><<<g, 128, 0, st>>>(nb, rest, A + (size_t)k0 * lda + k0, lda, sa,
                                                           A + (size_t)k0 * lda + k0 + nb, lda, sa);
             if ((rc = check_launch("getrf: trsm"))) return rc;
-            rc = gemm_update<R>(batch, rest, rest, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
-                                A + (size_t)k0 * lda + k0 + nb, lda, sa,
-                                A + (size_t)(k0 + nb) * lda + k0 + nb, lda, sa, st);
+            rc = update<R>(batch, rest, rest, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
+                           A + (size_t)k0 * lda + k0 + nb, lda, sa,
+                           A + (size_t)(k0 + nb) * lda + k0 + nb, lda, sa, work, st);
             if (rc) return rc;
         }
     }
@@ -326,7 +353,7 @@ int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv
 
 template <class R>
 int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long long sa, const int *ipiv,
-               C<R> *B, long long ldb, long long sb, cudaStream_t st)
+               C<R> *B, long long ldb, long long sb, void *work, cudaStream_t st)
 {
     constexpr int NB = LuCfg<R>::NB;
     {
@@ -342,8 +369,8 @@ int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long lo
                                                        B + (size_t)k0 * ldb, ldb, sb);
         int rc = check_launch("getrs: trsm L");
         if (rc) return rc;
-        rc = gemm_update<R>(batch, n - k0 - nb, nrhs, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
-                            B + (size_t)k0 * ldb, ldb, sb, B + (size_t)(k0 + nb) * ldb, ldb, sb, st);
+        rc = update<R>(batch, n - k0 - nb, nrhs, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
+                       B + (size_t)k0 * ldb, ldb, sb, B + (size_t)(k0 + nb) * ldb, ldb, sb, work, st);
         if (rc) return rc;
     }
     const int last = ((n - 1) / NB) * NB;
@@ -353,8 +380,8 @@ int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long lo
                                                       B + (size_t)k0 * ldb, ldb, sb);
         int rc = check_launch("getrs: trsm U");
         if (rc) return rc;
-        rc = gemm_update<R>(batch, k0, nrhs, nb, A + k0, lda, sa, B + (size_t)k0 * ldb, ldb, sb,
-                            B, ldb, sb, st);
+        rc = update<R>(batch, k0, nrhs, nb, A + k0, lda, sa, B + (size_t)k0 * ldb, ldb, sb,
+                       B, ldb, sb, work, st);
         if (rc) return rc;
     }
     return GHOST_BOR_OK;
@@ -668,30 +695,54 @@ __global__ void convert_kernel(int dir, int rows, int cols, const void *__restri
 
 using namespace gb;
 
-extern "C" int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long long stride_a,
-                               int *ipiv, int *info, void *stream)
+extern "C" long long ghost_bor_getrf_workspace(int prec, int batch, int n)
 {
-    if (batch < 1 || n < 1 || !A || !ipiv || !info || lda < n || stride_a < lda * n) return GHOST_BOR_EINVAL;
+    if (prec != GHOST_BOR_F32 || batch < 1 || n < 1) return 0;
+    return tc_update_workspace(batch, n, n, LuCfg<float>::NB);
+}
+
+extern "C" long long ghost_bor_getrs_workspace(int prec, int batch, int n, int nrhs)
+{
+    if (prec != GHOST_BOR_F32 || batch < 1 || n < 1 || nrhs < 1) return 0;
+    return tc_update_workspace(batch, n, nrhs, LuCfg<float>::NB);
+}
+
+static bool tc_work_ok(const void *work)
+{
+    return !work || (reinterpret_cast<uintptr_t>(work) & 255) == 0;
+}
+
+extern "C" int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long long stride_a,
+                               int *ipiv, int *info, void *work, void *stream)
+{
+    if (batch < 1 || n < 1 || !A || !ipiv || !info || lda < n || stride_a < lda * n || !tc_work_ok(work))
+        return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (prec == GHOST_BOR_F32) return getrf_impl<float>(batch, n, reinterpret_cast<float2 *>(A), lda, stride_a, ipiv, info, st);
-    if (prec == GHOST_BOR_F64) return getrf_impl<double>(batch, n, reinterpret_cast<double2 *>(A), lda, stride_a, ipiv, info, st);
+    if (prec == GHOST_BOR_F32) {
+        if (work && cudaMemsetAsync(work, 0, sizeof(int), st) != cudaSuccess) return check_launch("getrf: memset");
+        return getrf_impl<float>(batch, n, reinterpret_cast<float2 *>(A), lda, stride_a, ipiv, info, work, st);
+    }
+    if (prec == GHOST_BOR_F64)
+        return getrf_impl<double>(batch, n, reinterpret_cast<double2 *>(A), lda, stride_a, ipiv, info, nullptr, st);
     return GHOST_BOR_EINVAL;
 }
 
 extern "C" int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
                                const void *A, long long lda, long long stride_a, const int *ipiv,
-                               void *B, long long ldb, long long stride_b, void *stream)
+                               void *B, long long ldb, long long stride_b, void *work, void *stream)
 {
     if (batch < 1 || n < 1 || nrhs < 1 || !A || !ipiv || !B || lda < n || ldb < nrhs ||
-        stride_a < lda * n || stride_b < ldb * n)
+        stride_a < lda * n || stride_b < ldb * n || !tc_work_ok(work))
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (prec == GHOST_BOR_F32)
+    if (prec == GHOST_BOR_F32) {
+        if (work && cudaMemsetAsync(work, 0, sizeof(int), st) != cudaSuccess) return check_launch("getrs: memset");
         return getrs_impl<float>(batch, n, nrhs, reinterpret_cast<const float2 *>(A), lda, stride_a, ipiv,
-                                 reinterpret_cast<float2 *>(B), ldb, stride_b, st);
+                                 reinterpret_cast<float2 *>(B), ldb, stride_b, work, st);
+    }
     if (prec == GHOST_BOR_F64)
         return getrs_impl<double>(batch, n, nrhs, reinterpret_cast<const double2 *>(A), lda, stride_a, ipiv,
-                                  reinterpret_cast<double2 *>(B), ldb, stride_b, st);
+                                  reinterpret_cast<double2 *>(B), ldb, stride_b, nullptr, st);
     return GHOST_BOR_EINVAL;
 }
 

@@ -1,0 +1,419 @@
+// tc_gemm.cu -- complex FP32 GEMM update C -= A B on the 5th-generation tensor
+// cores (tcgen05, kind::tf32, accumulator in TMEM, operands staged by TMA).
+//
+// Used for the trailing updates of the batched LU and the block updates of the
+// triangular solves (bor_solver.py:753 replaced by ghost_bor_getrf/getrs).
+//
+// Precision: 3xTF32.  Each FP32 operand x is split into hi = tf32(x) and
+// lo = x - hi; the product is hi*hi + hi*lo + lo*hi accumulated in FP32 (the
+// lo*lo term is below FP32 rounding).  This keeps the LU accurate to FP32
+// level, which the FP64 refinement of the solution needs.
+//
+// Complex arithmetic as one real GEMM: the FP32 storage of a complex row-major
+// matrix A [M][K] is the real matrix A_r [M][2K] (re, im interleaved).  With
+// B expanded into 2x2 real blocks B''[2k+c][2n+r] = [[Br, Bi], [-Bi, Br]][c][r]
+// the real product A_r B'' is the interleaved storage of A B.  The GEMM runs
+// D[M][2N] = A_r [M][2K] x Bt [2N][2K]^T with both operands K-major.
+//
+// Tiles: 128 x 128 output (M x 2N real), K in stages of 32 (one 128-byte
+// swizzle row), 2 stages double-buffered.  Thread 0 issues the TMA loads and
+// the MMAs; the four warps read the accumulator with tcgen05.ld.
+#include "common.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+namespace gb {
+namespace {
+
+constexpr int BM = 128, BNR = 128, BK = 32;       // tile rows, tile real columns, K per stage
+constexpr int STAGES = 2;
+constexpr int TILE_FLOATS = BM * BK;               // 16 KB per operand tile
+constexpr int TC_THREADS = 128;
+constexpr uint32_t TMEM_COLS = 256;                // allocated (128 used)
+constexpr long long WAIT_LIMIT = 1LL << 24;        // bounded mbarrier waits
+
+struct __align__(1024) TcSmem {
+    float a_hi[STAGES][TILE_FLOATS];
+    float a_lo[STAGES][TILE_FLOATS];
+    float b_hi[STAGES][TILE_FLOATS];
+    float b_lo[STAGES][TILE_FLOATS];
+    unsigned long long full[STAGES];
+    unsigned long long mma[STAGES];
+    uint32_t tmem_base;
+    int failed;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *b, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+// bounded wait on the phase with parity `parity`; false on timeout
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity)
+{
+    const uint32_t a = smem_u32(b);
+    for (long long it = 0; it < WAIT_LIMIT; ++it) {
+        uint32_t done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4}], [%5];"
+                 ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2),
+                   "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (SBO), version 1.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);             // start address      [0,14)
+    d |= (uint64_t)1u << 16;                              // LBO (unused here)  [16,30)
+    d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;        // SBO = 1024 B       [32,46)
+    d |= (uint64_t)1u << 46;                              // descriptor version [46,48)
+    d |= (uint64_t)2u << 61;                              // SWIZZLE_128B       [61,64)
+    return d;
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, M = 128, N = 128
+constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BNR >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescTf32), "r"(accumulate));
+}
+
+__device__ __forceinline__ void umma_commit(unsigned long long *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32"
+                 " {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15,"
+                 " %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_round(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// A_r split: hi/lo [batch][M][Kp], real view of the complex block A [M][K];
+// grid-stride over output pairs (one complex element -> two floats)
+__global__ void split_a_kernel(int batch, int M, int K, int Kp, const float2 *__restrict__ A, long long lda,
+                               long long sa, float2 *__restrict__ hi, float2 *__restrict__ lo)
+{
+    const int kh = Kp / 2;                              // complex columns incl. padding
+    const long long total = (long long)batch * M * kh;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % kh);
+        const long long bm = i / kh;
+        const int m = (int)(bm % M), b = (int)(bm / M);
+        const float2 a = (k < K) ? A[(size_t)b * sa + (size_t)m * lda + k] : make_float2(0.f, 0.f);
+        const float2 h = make_float2(tf32_round(a.x), tf32_round(a.y));
+        hi[i] = h;
+        lo[i] = make_float2(a.x - h.x, a.y - h.y);
+    }
+}
+
+// Bt split: hi/lo [batch][2N][Kp], Bt[2n+r][2k+c] = [[Br, -Bi], [Bi, Br]][r][c];
+// 32 x 32 complex tiles transposed through shared memory (coalesced both ways)
+__global__ void __launch_bounds__(256)
+split_b_kernel(int K, int N, int Kp, const float2 *__restrict__ B, long long ldb, long long sb,
+               float *__restrict__ hi, float *__restrict__ lo)
+{
+    __shared__ float2 t[32][33];
+    const int n0 = blockIdx.x * 32, k0 = blockIdx.y * 32, b = blockIdx.z;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;          // 32 x 8
+    for (int r = ty; r < 32; r += 8) {
+        const int k = k0 + r, n = n0 + tx;
+        t[r][tx] = (k < K && n < N) ? B[(size_t)b * sb + (size_t)k * ldb + n] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    // output rows 2n + rr (64 per tile), columns 2k + c (64 per tile)
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) {
+        const int orow = q / 64, ocol = q % 64;
+        const int n = n0 + orow / 2, rr = orow & 1;
+        const int kc = k0 * 2 + ocol;
+        if (n >= N || kc >= Kp) continue;
+        const float2 x = t[ocol / 2][orow / 2];
+        const int c = ocol & 1;
+        const float v = (rr == 0) ? (c == 0 ? x.x : -x.y) : (c == 0 ? x.y : x.x);
+        const float h = tf32_round(v);
+        const size_t o = ((size_t)b * 2 * N + 2 * n + rr) * Kp + kc;
+        hi[o] = h;
+        lo[o] = v - h;
+    }
+}
+
+__global__ void __launch_bounds__(TC_THREADS)
+tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
+                 const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
+                 int M, int Nr, int Kp, float *__restrict__ C, long long ldc_r, long long sc_r,
+                 int *__restrict__ err)
+{
+    extern __shared__ unsigned char smem_raw[];
+    TcSmem &s = *reinterpret_cast<TcSmem *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.x * BNR, m0 = blockIdx.y * BM, b = blockIdx.z;
+    const int nst = Kp / BK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(&s.tmem_base)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < STAGES; ++i) { mbar_init(&s.full[i], 1); mbar_init(&s.mma[i], 1); }
+        s.failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s.tmem_base;
+
+    if (tid == 0) {
+        const uint32_t bytes = 4u * TILE_FLOATS * 4u;
+        uint32_t full_phase[STAGES] = {0, 0}, mma_phase[STAGES] = {0, 0};
+        bool ok = true;
+        for (int st = 0; st < STAGES && st < nst; ++st) {
+            mbar_expect_tx(&s.full[st], bytes);
+            tma_load_3d(s.a_hi[st], &map_ahi, st * BK, m0, b, &s.full[st]);
+            tma_load_3d(s.a_lo[st], &map_alo, st * BK, m0, b, &s.full[st]);
+            tma_load_3d(s.b_hi[st], &map_bhi, st * BK, n0, b, &s.full[st]);
+            tma_load_3d(s.b_lo[st], &map_blo, st * BK, n0, b, &s.full[st]);
+        }
+        for (int ks = 0; ks < nst && ok; ++ks) {
+            const int st = ks % STAGES;
+            ok = mbar_wait(&s.full[st], full_phase[st]);
+            full_phase[st] ^= 1u;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah = smem_u32(s.a_hi[st]), al = smem_u32(s.a_lo[st]);
+            const uint32_t bh = smem_u32(s.b_hi[st]), bl = smem_u32(s.b_lo[st]);
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk) {          // 8 tf32 = 32 bytes per MMA
+                const uint32_t off = kk * 32;
+                const uint32_t acc0 = (ks > 0 || kk > 0) ? 1u : 0u;
+                umma_tf32(tmem, umma_desc_sw128(ah + off), umma_desc_sw128(bh + off), acc0);
+                umma_tf32(tmem, umma_desc_sw128(ah + off), umma_desc_sw128(bl + off), 1u);
+                umma_tf32(tmem, umma_desc_sw128(al + off), umma_desc_sw128(bh + off), 1u);
+            }
+            umma_commit(&s.mma[st]);
+            if (ks + STAGES < nst) {
+                // this buffer is refilled only after its MMAs have read it
+                ok = mbar_wait(&s.mma[st], mma_phase[st]);
+                mma_phase[st] ^= 1u;
+                if (!ok) break;
+                mbar_expect_tx(&s.full[st], bytes);
+                const int kn = (ks + STAGES) * BK;
+                tma_load_3d(s.a_hi[st], &map_ahi, kn, m0, b, &s.full[st]);
+                tma_load_3d(s.a_lo[st], &map_alo, kn, m0, b, &s.full[st]);
+                tma_load_3d(s.b_hi[st], &map_bhi, kn, n0, b, &s.full[st]);
+                tma_load_3d(s.b_lo[st], &map_blo, kn, n0, b, &s.full[st]);
+            }
+        }
+        // wait for the MMAs still in flight (the last STAGES commits)
+        if (ok) {
+            for (int ks = (nst > STAGES ? nst - STAGES : 0); ks < nst; ++ks) {
+                const int st = ks % STAGES;
+                if (!mbar_wait(&s.mma[st], mma_phase[st])) { ok = false; break; }
+                mma_phase[st] ^= 1u;
+            }
+        }
+        if (!ok) {
+            s.failed = 1;
+            atomicExch(err, 1);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (!s.failed) {
+        // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31.  Each
+        // 32-column slice goes through shared memory (the operand buffers
+        // are free: every MMA has completed) so the warp's read-modify-write
+        // of C covers one contiguous 128-byte row segment per instruction.
+        float (*tr)[33] = reinterpret_cast<float (*)[33]>(&s.a_hi[0][0]) + warp * 32;
+#pragma unroll 1
+        for (int c32 = 0; c32 < BNR / 32; ++c32) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c32 * 32), v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) tr[lane][i] = v[i];
+            __syncwarp();
+            const int col = n0 + c32 * 32 + lane;
+            float *cb = C + (size_t)b * sc_r + (size_t)(m0 + warp * 32) * ldc_r + col;
+            const int rows = min(32, M - (m0 + warp * 32));
+            if (col < Nr) {
+                // all loads first (the compiler cannot reorder C loads past C stores)
+                float cv[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) cv[i] = (i < rows) ? cb[(size_t)i * ldc_r] : 0.f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (i < rows) cb[(size_t)i * ldc_r] = cv[i] - tr[i][lane];
+            }
+            __syncwarp();
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 get_encode()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// K-major [batch][rows][Kp] FP32 operand, box 32 x 128, 128-byte swizzle
+bool make_map(CUtensorMap *map, const float *base, int rows, int Kp, int batch)
+{
+    auto enc = get_encode();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)Kp * 4, (cuuint64_t)rows * Kp * 4};
+    const cuuint32_t box[3] = {BK, BM, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Workspace layout: [0, 256) error flag (int, sticky: set to 1 by any call
+// whose bounded in-kernel wait gave up; the caller clears it), then the split
+// operands at a 256-byte boundary.
+long long tc_update_workspace(int batch, int M, int N, int K)
+{
+    const long long Kp = ((2LL * K + BK - 1) / BK) * BK;
+    return 4LL * Kp * batch * (2LL * M + 2LL * 2 * N) + 512;
+}
+
+// C[b] (M x N complex float) -= A[b] (M x K) B[b] (K x N) on the tensor cores.
+// The sticky error flag at the start of the workspace is set if a bounded wait
+// inside the kernel gave up (that tile is then left unchanged).
+int tc_update(int batch, int M, int N, int K, const float2 *A, long long lda, long long sa,
+              const float2 *B, long long ldb, long long sb, float2 *C, long long ldc, long long sc,
+              void *work, cudaStream_t st)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return GHOST_BOR_OK;
+    const int Kp = ((2 * K + BK - 1) / BK) * BK;
+    int *err = reinterpret_cast<int *>(work);
+    float *w = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(work) + 256);
+    float *ahi = w, *alo = ahi + (size_t)batch * M * Kp;
+    float *bhi = alo + (size_t)batch * M * Kp, *blo = bhi + (size_t)batch * 2 * N * Kp;
+    {
+        const long long pairs = (long long)batch * M * (Kp / 2);
+        const int blocks = (int)((pairs + 255) / 256 < 152 * 16 ? (pairs + 255) / 256 : 152 * 16);
+        split_a_kernel<<<blocks, 256, 0, st>>>(batch, M, K, Kp, A, lda, sa, reinterpret_cast<float2 *>(ahi),
+                                               reinterpret_cast<float2 *>(alo));
+        int rc = check_launch("tc_update: split A");
+        if (rc) return rc;
+        dim3 g2((N + 31) / 32, (Kp / 2 + 31) / 32, batch);
+        split_b_kernel<<<g2, 256, 0, st>>>(K, N, Kp, B, ldb, sb, bhi, blo);
+        if ((rc = check_launch("tc_update: split B"))) return rc;
+    }
+    CUtensorMap mah, mal, mbh, mbl;
+    if (!make_map(&mah, ahi, M, Kp, batch) || !make_map(&mal, alo, M, Kp, batch) ||
+        !make_map(&mbh, bhi, 2 * N, Kp, batch) || !make_map(&mbl, blo, 2 * N, Kp, batch)) {
+        set_last_error("tc_update: cuTensorMapEncodeTiled failed");
+        return GHOST_BOR_ECUDA;
+    }
+    const size_t smem = sizeof(TcSmem) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return check_launch("tc_update: smem attribute");
+        attr = true;
+    }
+    dim3 grid((2 * N + BNR - 1) / BNR, (M + BM - 1) / BM, batch);
+    tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, M, 2 * N, Kp,
+                                                     reinterpret_cast<float *>(C), 2 * ldc, 2 * sc, err);
+    return check_launch("tc_update");
+}
+
+}  // namespace gb
+
+extern "C" long long ghost_bor_cgemm_tc_workspace(int batch, int M, int N, int K)
+{
+    return gb::tc_update_workspace(batch, M, N, K);
+}
+
+extern "C" int ghost_bor_cgemm_tc(int batch, int M, int N, int K,
+                                  const void *A, long long lda, long long stride_a,
+                                  const void *B, long long ldb, long long stride_b,
+                                  void *C, long long ldc, long long stride_c,
+                                  void *work, int *status, void *stream)
+{
+    if (batch < 1 || M < 0 || N < 0 || K < 0 || !A || !B || !C || !work || lda < K || ldb < N || ldc < N ||
+        (reinterpret_cast<uintptr_t>(work) & 255))
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(work, 0, sizeof(int), st) != cudaSuccess) return gb::check_launch("cgemm_tc: memset");
+    const int rc = gb::tc_update(batch, M, N, K, reinterpret_cast<const float2 *>(A), lda, stride_a,
+                                 reinterpret_cast<const float2 *>(B), ldb, stride_b,
+                                 reinterpret_cast<float2 *>(C), ldc, stride_c, work, st);
+    if (rc == GHOST_BOR_OK && status) {
+        if (cudaMemcpyAsync(status, work, sizeof(int), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            return gb::check_launch("cgemm_tc: status copy");
+    }
+    return rc;
+}

@@ -108,6 +108,7 @@ class BorGpuProblem:
         self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
         self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
         self.refine_floor = 1e-6     # residuals below this are at the FP32-product floor
+        self.tensor_cores = True     # FP32 LU / solve updates on tcgen05 (3xTF32)
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
@@ -123,7 +124,8 @@ class BorGpuProblem:
         rhs = self.n * self.nrhs
         if precision == "fp64":
             return Mb * (2 * nn * 16 + 3 * rhs * 16)
-        return Mb * (nn * 16 + nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16)
+        tc = 4 * 128 * Mb * (2 * self.n + 4 * max(self.n, self.nrhs)) * 2
+        return Mb * (nn * 16 + nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16) + tc
 
     # -- stages -----------------------------------------------------------
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
@@ -203,9 +205,9 @@ class BorGpuProblem:
             work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
             X = B.clone()
             nat.call("ghost_bor_getrf", nat.F64, Mb, n, nat.ptr(Z), n, Z.stride(0), nat.ptr(ipiv),
-                     nat.ptr(info), st); mark("lu"); abort()
+                     nat.ptr(info), 0, st); mark("lu"); abort()
             nat.call("ghost_bor_getrs", nat.F64, Mb, n, nrhs, nat.ptr(Z), n, Z.stride(0), nat.ptr(ipiv),
-                     nat.ptr(X), nrhs, X.stride(0), st); mark("solve")
+                     nat.ptr(X), nrhs, X.stride(0), 0, st); mark("solve")
             nat.call("ghost_bor_residual64", Mb, n, nrhs, nat.ptr(Zc), n, Zc.stride(0), nat.ptr(X),
                      nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(norms), st); mark("residual")
             del Zc
@@ -219,12 +221,20 @@ class BorGpuProblem:
                      nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st); mark("compose"); abort()
             work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
             X32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
+            lib = nat.load()
+            if self.tensor_cores:
+                lu_ws = torch.empty(int(lib.ghost_bor_getrf_workspace(nat.F32, Mb, n)), dtype=torch.uint8,
+                                    device=self.device)
+                rs_ws = torch.empty(int(lib.ghost_bor_getrs_workspace(nat.F32, Mb, n, nrhs)),
+                                    dtype=torch.uint8, device=self.device)
+            else:
+                lu_ws = rs_ws = None
             nat.call("ghost_bor_convert", 0, Mb, n, nrhs, nat.ptr(B), nrhs, B.stride(0), nat.ptr(X32),
                      nrhs, X32.stride(0), st)
             nat.call("ghost_bor_getrf", nat.F32, Mb, n, nat.ptr(A), n, A.stride(0), nat.ptr(ipiv),
-                     nat.ptr(info), st); mark("lu"); abort()
+                     nat.ptr(info), nat.ptr(lu_ws), st); mark("lu"); abort()
             nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0), nat.ptr(ipiv),
-                     nat.ptr(X32), nrhs, X32.stride(0), st)
+                     nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(rs_ws), st)
             X = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
             nat.call("ghost_bor_convert", 1, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(X),
                      nrhs, X.stride(0), st); mark("solve")
@@ -243,12 +253,16 @@ class BorGpuProblem:
                     break
                 prev = rel
                 nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
-                         nat.ptr(ipiv), nat.ptr(X32), nrhs, X32.stride(0), st)
+                         nat.ptr(ipiv), nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(rs_ws), st)
                 nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
                          nat.ptr(X), nrhs, X.stride(0), st)
                 iters += 1
                 abort()
             mark("residual")
+            if lu_ws is not None:
+                flags = torch.stack([lu_ws[:4].view(torch.int32)[0], rs_ws[:4].view(torch.int32)[0]])
+                if int(flags.max()) != 0:
+                    raise RuntimeError("a bounded tensor-core wait gave up in the LU / solve kernels")
             if not keep:
                 del Zf, A, R, X32, band
         dF = torch.empty((Mb, nrhs), dtype=c128, device=self.device)

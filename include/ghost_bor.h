@@ -169,16 +169,37 @@ int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double k,
  * Batched complex LU with partial pivoting (|re|+|im| pivot rule, as LAPACK
  * izamax) of n x n matrices A[b] = A + b*stride_a, row-major, b < batch.
  * ipiv[b][n] receives 0-based pivot rows; info[b] = 0 or (first zero pivot
- * column + 1).  In place.
+ * column + 1).  In place.  For GHOST_BOR_F32 with a workspace of
+ * ghost_bor_getrf_workspace() bytes (256-byte aligned) the trailing updates
+ * run on the tensor cores (ghost_bor_cgemm_tc); the first int of the
+ * workspace is then a sticky status (1 = a bounded in-kernel wait gave up).
+ * work = NULL selects the SIMT updates (always for FP64).
  */
+long long ghost_bor_getrf_workspace(int prec, int batch, int n);
 int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long long stride_a,
-                    int *ipiv, int *info, void *stream);
+                    int *ipiv, int *info, void *work, void *stream);
+
+/* Complex FP32 update C[b] -= A[b] B[b] on the tensor cores (tcgen05
+ * kind::tf32, 3xTF32 split, TMA-staged operands, TMEM accumulator):
+ * A [M][K], B [K][N], C [M][N] row-major complex float with leading
+ * dimensions lda/ldb/ldc and batch strides (complex elements).
+ * work: ghost_bor_cgemm_tc_workspace() bytes of device scratch.  status
+ * (device int, may be NULL) receives 1 if a bounded in-kernel wait gave up.
+ * Building block of the LU trailing updates and the triangular solves. */
+long long ghost_bor_cgemm_tc_workspace(int batch, int M, int N, int K);
+int ghost_bor_cgemm_tc(int batch, int M, int N, int K,
+                       const void *A, long long lda, long long stride_a,
+                       const void *B, long long ldb, long long stride_b,
+                       void *C, long long ldc, long long stride_c,
+                       void *work, int *status, void *stream);
 
 /* Solve A X = B with the factors of ghost_bor_getrf for nrhs columns
- * (B row-major n x nrhs, in place).  precisions of A and B are equal. */
+ * (B row-major n x nrhs, in place).  Precisions of A and B are equal; work as
+ * for ghost_bor_getrf (ghost_bor_getrs_workspace() bytes, or NULL). */
+long long ghost_bor_getrs_workspace(int prec, int batch, int n, int nrhs);
 int ghost_bor_getrs(int prec, int batch, int n, int nrhs,
                     const void *A, long long lda, long long stride_a, const int *ipiv,
-                    void *B, long long ldb, long long stride_b, void *stream);
+                    void *B, long long ldb, long long stride_b, void *work, void *stream);
 
 /* ------------------------------------------------------------------------
  * Mixed-precision residual for iterative refinement, per batch b:

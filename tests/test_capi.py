@@ -35,6 +35,6 @@ def test_library_exports_all(pkg):
 def test_bad_arguments_rejected(pkg):
     nat = pkg._native
     with pytest.raises(ValueError):
-        nat.call("ghost_bor_getrf", nat.F32, 0, 10, 0, 10, 100, 0, 0, 0)
+        nat.call("ghost_bor_getrf", nat.F32, 0, 10, 0, 10, 100, 0, 0, 0, 0)
     with pytest.raises(ValueError):
         nat.call("ghost_bor_far_efie", 7, 10, 3, 64, 1.0, 1.0, 0.0, 0, 0, 0, 0, 22, 484, 0)

@@ -93,8 +93,8 @@ def test_full_operator_and_excitation(pkg, name):
         assert rel(ff, D[f"ff_{m}"][::4]) < 1e-12
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", 1e-11), ("f32", 5e-4)])
-def test_batched_lu(pkg, torch, prec, tol):
+@pytest.mark.parametrize("prec,tol,tc", [("f64", 1e-11, False), ("f32", 5e-4, False), ("f32", 5e-4, True)])
+def test_batched_lu(pkg, torch, prec, tol, tc):
     """ghost_bor_getrf / getrs vs numpy on random complex systems, including a
     size that is not a multiple of the panel width and pivoting-heavy rows."""
     nat = pkg._native
@@ -111,9 +111,16 @@ def test_batched_lu(pkg, torch, prec, tol):
     ipiv = torch.empty((batch, n), dtype=torch.int32, device="cuda")
     info = torch.empty((batch,), dtype=torch.int32, device="cuda")
     st = nat.stream_handle()
-    nat.call("ghost_bor_getrf", p, batch, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info), st)
+    lib = nat.load()
+    wf = torch.empty(max(1, int(lib.ghost_bor_getrf_workspace(p, batch, n))), dtype=torch.uint8, device="cuda")
+    ws = torch.empty(max(1, int(lib.ghost_bor_getrs_workspace(p, batch, n, nrhs))), dtype=torch.uint8,
+                     device="cuda")
+    nat.call("ghost_bor_getrf", p, batch, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info),
+             nat.ptr(wf) if tc else 0, st)
     nat.call("ghost_bor_getrs", p, batch, n, nrhs, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(dB),
-             nrhs, n * nrhs, st)
+             nrhs, n * nrhs, nat.ptr(ws) if tc else 0, st)
+    if tc:
+        assert int(wf[:4].view(torch.int32)[0].cpu()) == 0 and int(ws[:4].view(torch.int32)[0].cpu()) == 0
     X = dB.cpu().numpy()
     assert np.all(info.cpu().numpy() == 0)
     assert rel(X, X_ref) < tol
@@ -131,7 +138,7 @@ def test_singular_pivot_reported(pkg, torch):
     dA = torch.as_tensor(A[None], device="cuda").contiguous()
     ipiv = torch.empty((1, n), dtype=torch.int32, device="cuda")
     info = torch.empty((1,), dtype=torch.int32, device="cuda")
-    nat.call("ghost_bor_getrf", nat.F64, 1, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info),
+    nat.call("ghost_bor_getrf", nat.F64, 1, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info), 0,
              nat.stream_handle())
     assert int(info.cpu()[0]) == 41
 
