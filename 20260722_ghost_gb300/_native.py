@@ -31,6 +31,9 @@ SIGNATURES = {
     "ghost_bor_far_efie": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_near_efie": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _i,
                                  _vp, _vp, _i, _vp, _vp, _ll, _ll, _vp]),
+    "ghost_bor_far_mfie": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
+    "ghost_bor_near_mfie": (_i, [_i, _i, _d, _d, _d, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i,
+                                 _vp, _vp, _i, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_rhs_workspace": (_ll, [_i, _i, _i]),
     "ghost_bor_rhs": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_rhs_noalloc_capacity": (_ll, []),
@@ -43,6 +46,8 @@ SIGNATURES = {
     "ghost_bor_getrs": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_residual": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
                                 _vp, _vp, _vp, _vp]),
+    "ghost_bor_residual_x32": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
+                                    _vp, _vp, _vp, _vp]),
     "ghost_bor_residual64": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp, _vp, _ll, _ll, _vp, _vp, _vp]),
     "ghost_bor_farfield": (_i, [_i, _i, _i, _i, _i, _d, _vp, _vp, _ll, _ll, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_compose": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _ll, _ll, _vp]),

@@ -76,12 +76,11 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
     precision = _precision_of(table_precision)
     if zs is not None and np.any(np.abs(np.asarray(zs, dtype=complex)) > 0.0):
         raise NotImplementedError("surface impedance (IBC-EFIE) is not on the GPU path yet")
-    if form != "efie":
-        raise NotImplementedError(f"formulation '{form}' is not on the GPU path yet")
     if check_abort is not None:
         check_abort()
     thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
-    prob = BorGpuProblem(points, freq_hz, thetas, m_max=n_modes, gauss_order=gauss_order)
+    prob = BorGpuProblem(points, freq_hz, thetas, m_max=n_modes, gauss_order=gauss_order,
+                         formulation=form, cfie_alpha=cfie_alpha)
     t_setup = time.perf_counter()
     res = prob.sweep(precision=precision, check_abort=check_abort)
     F, modes_used = replay_truncation(res.dF, mode_tol)
@@ -129,8 +128,8 @@ class BorPecSolver:
 
     Operators are built on the GPU for all modes 0..m_max at once (FP64) and
     returned per mode as complex128 NumPy arrays for compatibility; mode -m is
-    D Z(m) D.  Only the EFIE operators and the plane-wave excitation/far field
-    are provided.
+    D Z(m) D for both operators.  The EFIE and MFIE operators and the
+    plane-wave excitations / far field are provided (no IBC / PMCHWT).
     """
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,
@@ -160,12 +159,13 @@ class BorPecSolver:
         self._points = np.asarray(points, dtype=float)
         self._stream = None
         self._ops: Optional[Tuple[int, object]] = None
+        self._mops: Optional[Tuple[int, object]] = None
         self._single = bool(single_tables)
 
     # -- operator cache ----------------------------------------------------
-    def _problem(self, m_max: int, thetas=(0.0,)):
+    def _problem(self, m_max: int, thetas=(0.0,), formulation: str = "efie"):
         return BorGpuProblem(self._points, self.freq_hz, thetas, m_max=m_max,
-                             gauss_order=self.gauss_order)
+                             gauss_order=self.gauss_order, formulation=formulation)
 
     def enable_streaming(self, m_max: int, efie: bool = True, mfie: bool = False,
                          ibc_zs_pt: Optional[np.ndarray] = None, single_blocks: bool = False,
@@ -179,20 +179,34 @@ class BorPecSolver:
 
     def prepare_operators(self, m_max: int, efie: bool = True, mfie: bool = False,
                           ibc: bool = False, workers: int = 1) -> None:
-        if mfie or ibc:
-            raise NotImplementedError("MFIE / IBC operators are not on the GPU path yet")
-        if self._ops is None or self._ops[0] < m_max:
+        """Build the FP64 operators of every mode 0..m_max on the GPU
+        (bor_solver.py:578-608); modes -m follow by symmetry."""
+        if ibc:
+            raise NotImplementedError("IBC operators are not on the GPU path yet")
+        if efie and (self._ops is None or self._ops[0] < m_max):
             prob = self._problem(m_max)
             self._ops = (m_max, prob.assemble_modes_fp64())
+        if mfie and (self._mops is None or self._mops[0] < m_max):
+            prob = self._problem(m_max, formulation="mfie")
+            self._mops = (m_max, prob.assemble_mfie_modes_fp64())
 
-    def assemble_mode(self, m: int, m_max: int) -> np.ndarray:
-        self.prepare_operators(max(m_max, abs(m)))
-        Z = self._ops[1][abs(m)].cpu().numpy()
+    def _mode(self, ops, m: int) -> np.ndarray:
+        Z = ops[1][abs(m)].cpu().numpy()
         if m < 0:
             Nn = self.Nn
             Z[:Nn, Nn:] *= -1.0
             Z[Nn:, :Nn] *= -1.0
         return Z
+
+    def assemble_mode(self, m: int, m_max: int) -> np.ndarray:
+        """EFIE operator C [[ztt, ztf], [zft, zff]] of mode m (bor_solver.py:293-345)."""
+        self.prepare_operators(max(m_max, abs(m)))
+        return self._mode(self._ops, m)
+
+    def assemble_mfie_mode(self, m: int, m_max: int) -> np.ndarray:
+        """MFIE operator M/2 - K of mode m (bor_solver.py:399-435)."""
+        self.prepare_operators(max(m_max, abs(m)), efie=False, mfie=True)
+        return self._mode(self._mops, m)
 
     def basis_mask(self, m: int) -> np.ndarray:
         return _basis_mask(self.gen, m)
@@ -216,6 +230,12 @@ class BorPecSolver:
     def rhs_mode(self, m: int, theta_inc_deg: float, pol: str) -> np.ndarray:
         """<W, E_inc> for one mode, angle and polarisation (bor_solver.py:625-645)."""
         V = self._excitation(m, theta_inc_deg, 1.0, 0.0)
+        return V[:, 0 if pol.upper() in ("VV", "THETA", "TM") else 1].copy()
+
+    def rhs_mfie_mode(self, m: int, theta_inc_deg: float, pol: str) -> np.ndarray:
+        """<W, n x H_inc> rotated, for one mode, angle and polarisation
+        (bor_solver.py:437-461)."""
+        V = self._excitation(m, theta_inc_deg, 0.0, 1.0)
         return V[:, 0 if pol.upper() in ("VV", "THETA", "TM") else 1].copy()
 
     def farfield_mode(self, m: int, sol: np.ndarray, theta_s_deg: float,

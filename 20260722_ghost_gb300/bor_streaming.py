@@ -2,9 +2,11 @@
 
 ``StreamingFarBlocks`` keeps its constructor signature and per-mode accessors
 (bor_streaming.py:119-421) but the far blocks of every mode are produced in one
-GPU sweep by the fused far-fill kernel (ghost_bor_far_efie) instead of
-tile-by-tile CPU sampling + FFT + einsum.  ``efie_blocks(m)`` returns the four
-nodal EFIE blocks WITHOUT the C = j k eta 2 pi factor, exactly as the
+GPU sweep by the fused far-fill kernels (ghost_bor_far_efie,
+ghost_bor_far_mfie) instead of tile-by-tile CPU sampling + FFT + einsum.
+``efie_blocks(m)`` returns the four nodal EFIE blocks WITHOUT the
+C = j k eta 2 pi factor and ``bracket_blocks("mfie", m)`` the four MFIE
+bracket blocks K (2 pi Galerkin factor included, no mass term), exactly as the
 reference (same/adjacent element pairs contribute zero; the near path adds
 them).  Blocks are held on the device; accessors copy one mode to the host.
 """
@@ -40,8 +42,8 @@ class StreamingFarBlocks:
                  ibc_zs_pt: Optional[np.ndarray] = None, dtype=np.complex128,
                  tile_budget_gb: float = 1.0, workers: int = 1,
                  mode_block: Optional[int] = None):
-        if mfie or ibc_zs_pt is not None:
-            raise NotImplementedError("MFIE / IBC bracket blocks are not on the GPU path yet")
+        if ibc_zs_pt is not None:
+            raise NotImplementedError("IBC bracket blocks are not on the GPU path yet")
         import torch
         self.solver = solver
         self.m_max = int(m_max)
@@ -51,20 +53,26 @@ class StreamingFarBlocks:
         self.n_sweeps = 1
         self.lo, self.hi = 0, self.m_max
         prob = BorGpuProblem(solver._points, solver.freq_hz, (0.0,), m_max=self.m_max,
-                             gauss_order=solver.gauss_order)
+                             gauss_order=solver.gauss_order, formulation="mfie" if mfie else "efie")
         single = np.dtype(dtype) == np.complex64
-        Z = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
-        prob.fill_far(Z, nat.F32 if single else nat.F64, 1.0 + 0.0j, nat.stream_handle())
-        self.Z = Z
-        self.K = None
-        self.B = None
+        prec = nat.F32 if single else nat.F64
+        self.Z = self.K = self.B = None
+        if efie:
+            Z = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
+            prob.fill_far(Z, prec, 1.0 + 0.0j, nat.stream_handle())
+            self.Z = Z
+        if mfie:
+            # the kernel adds -scale * K (the far part of M/2 - K): scale -1 stores K
+            K = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
+            prob.fill_far_mfie(K, prec, -1.0 + 0.0j, nat.stream_handle())
+            self.K = K
 
-    def efie_blocks(self, m: int):
+    def _blocks(self, store, m: int):
         am = abs(m)
         if am > self.m_max:
             raise ValueError(f"mode {m} outside the built range 0..{self.m_max}")
         Nn = self.Nn
-        Zm = self.Z[am].cpu().numpy()
+        Zm = store[am].cpu().numpy()
         if np.dtype(self.dtype) == np.complex64:
             Zm = Zm.astype(np.complex64).astype(np.complex128)
         ztt, ztf = Zm[:Nn, :Nn].copy(), Zm[:Nn, Nn:].copy()
@@ -73,8 +81,20 @@ class StreamingFarBlocks:
             ztf, zft = -ztf, -zft
         return ztt, ztf, zft, zff
 
+    def efie_blocks(self, m: int):
+        """Far EFIE blocks of mode m (bor_streaming.py:388-407)."""
+        if self.Z is None:
+            raise ValueError("EFIE blocks were not built")
+        return self._blocks(self.Z, m)
+
     def bracket_blocks(self, which: str, m: int):
-        raise NotImplementedError("MFIE / IBC bracket blocks are not on the GPU path yet")
+        """Far MFIE bracket blocks K_tt, K_tf, K_ft, K_ff of mode m
+        (bor_streaming.py:409-414); K(-m) = D K(m) D."""
+        if which != "mfie":
+            raise NotImplementedError("IBC bracket blocks are not on the GPU path yet")
+        if self.K is None:
+            raise ValueError("MFIE bracket blocks were not built")
+        return self._blocks(self.K, m)
 
     def memory_gb(self) -> float:
-        return float(self.Z.numel() * self.Z.element_size()) / 1e9
+        return float(sum(t.numel() * t.element_size() for t in (self.Z, self.K) if t is not None)) / 1e9

@@ -31,6 +31,7 @@
 // to ~1e-7 rad before an accurate sincosf, and the DCT is summed in blocks
 // of 8 samples folded in with Kahan compensation.
 #include "common.cuh"
+#include "samplers.cuh"
 
 namespace gb {
 namespace {
@@ -38,86 +39,6 @@ namespace {
 constexpr int EPB = 4;            // element pairs per CTA
 constexpr int TPB = EPB * 16 * 4; // Gauss-point pairs x order groups
 constexpr int JC = 32;            // azimuth samples staged per smem chunk
-
-constexpr double kTwoPi = 6.283185307179586476925286766559;
-// 2 pi = A + B + C; A (8 bits) and B (12 bits) are short enough that q*A and
-// q*B are exact in FP32 for every reduction count q < 2^11 (k R < 12800).
-constexpr float kTwoPiA = 6.28125f;
-constexpr float kTwoPiB = 4059.0f / 2097152.0f;
-constexpr float kTwoPiC = (float)(kTwoPi - 6.28125 - 4059.0 / 2097152.0);
-constexpr float kInvTwoPi = (float)(1.0 / kTwoPi);
-
-// ---------------------------------------------------------------------------
-// per-pair samplers
-// ---------------------------------------------------------------------------
-template <class R> struct GreenSampler;
-
-template <> struct GreenSampler<double> {
-    using S2 = double;          // sin^2 table entry type
-    double d2, a2, k;
-    __device__ void init(double d2_, double a2_, double k_) { d2 = d2_; a2 = a2_; k = k_; }
-    static __device__ __forceinline__ double load_s2(const double *t, int j) { return t[j]; }
-    __device__ __forceinline__ double2 operator()(double s2) const {
-        double R = sqrt(fma(a2, s2, d2));
-        R = fmax(R, 1e-30);
-        double sn, cs;
-        sincos(k * R, &sn, &cs);
-        const double amp = 1.0 / R;                  // 1/(4 pi) is folded into the DCT table
-        return make_double2(amp * cs, -amp * sn);
-    }
-};
-
-template <> struct GreenSampler<float> {
-    using S2 = float2;          // (hi, lo) split of sin^2
-    float d2h, d2l, a2h, a2l, kh, kl;
-    __device__ void init(double d2, double a2, double k) {
-        d2h = (float)d2; d2l = (float)(d2 - (double)d2h);
-        a2h = (float)a2; a2l = (float)(a2 - (double)a2h);
-        kh = (float)k;   kl = (float)(k - (double)kh);
-    }
-    static __device__ __forceinline__ float2 load_s2(const double *t, int j) {
-        const double v = t[j];
-        const float hi = (float)v;
-        return make_float2(hi, (float)(v - (double)hi));
-    }
-    __device__ __forceinline__ float2 operator()(float2 s2) const {
-        // R^2 = d^2 + a^2 s2 in double-float
-        const float p = a2h * s2.x;
-        const float pe = fmaf(a2h, s2.x, -p);
-        const float t = d2h + p;
-        const float bb = t - d2h;
-        const float te = (d2h - (t - bb)) + (p - bb);
-        const float lo = te + pe + fmaf(a2h, s2.y, a2l * s2.x) + d2l;
-        const float R2 = t + lo;
-        const float R2l = lo - (R2 - t);
-        // R = r + rl from one rsqrt and one Newton-style correction
-        const float rs = rsqrtf(R2);
-        const float r = R2 * rs;
-        const float e = fmaf(-r, r, R2) + R2l;
-        const float rl = 0.5f * e * rs;
-        // phase k R in double-float (ph + phl), reduced mod 2 pi: ph - q A is
-        // exact, the subtraction of q B is made exact with a two-sum, and the
-        // remaining small terms form a first-order correction dt.
-        const float ph = kh * r;
-        const float phe = fmaf(kh, r, -ph);
-        const float phl = phe + fmaf(kh, rl, kl * r);
-        const float q = rintf(ph * kInvTwoPi);
-        const float t1 = fmaf(-q, kTwoPiA, ph);
-        const float qb = -q * kTwoPiB;
-        const float t2 = t1 + qb;
-        const float tb = t2 - t1;
-        const float t2e = (t1 - (t2 - tb)) + (qb - tb);
-        const float dt = fmaf(-q, kTwoPiC, phl) + t2e;
-        float sn, cs;
-        sincosf(t2, &sn, &cs);
-        const float s1 = fmaf(dt, cs, sn);            // sin(t2 + dt)
-        const float c1 = fmaf(-dt, sn, cs);           // cos(t2 + dt)
-        // 1/R = 1/(r + rl) from an IEEE reciprocal and a first-order correction
-        const float ir = __frcp_rn(r);
-        const float amp = ir * fmaf(-rl, ir, 1.0f);  // 1/(4 pi) is folded into the DCT table
-        return make_float2(amp * c1, -amp * s1);
-    }
-};
 
 constexpr int OG = 4;                 // order groups: threads sharing one Gauss-point pair
 constexpr int PPB = EPB * 16;         // Gauss-point pairs per CTA

@@ -417,20 +417,30 @@ __device__ __forceinline__ void split2(double2 v, float2 &h, float2 &l)
     l = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
 }
 
+__device__ __forceinline__ double2 ld_x(const double2 *p) { return *p; }
+__device__ __forceinline__ double2 ld_x(const float2 *p) { const float2 v = *p; return make_double2(v.x, v.y); }
+
+// XT = double2: X in FP64, split into two FP32 words like Z.
+// XT = float2:  X is an FP32 solution, its low word is zero and the Z_hi X_lo
+//               products are skipped.
+template <class XT>
 __global__ void __launch_bounds__(256)
 residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, long long ldz, long long sz,
                       const double2 *__restrict__ band, const int *__restrict__ mask_rows,
-                      const double2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
+                      const XT *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
                       double2 *__restrict__ R, float2 *__restrict__ Rlo, double *__restrict__ norms)
 {
+    constexpr bool kXlo = sizeof(XT) == sizeof(double2);
     // tiles hold both FP32 words of each complex value: (hi.re, hi.im, lo.re, lo.im)
-    __shared__ float4 Zs[RK][GT];       // transposed: Zs[k][row]
+    // Zs is transposed (Zs[k][row]) and padded by one float4 per k so that the
+    // staging stores (consecutive threads -> consecutive k) hit distinct banks
+    __shared__ float4 Zs[RK][GT + 1];
     __shared__ float4 Xs[RK][GT];
     double (*red)[8] = reinterpret_cast<double (*)[8]>(&Zs[0][0]);   // reused after the K loop
     const int b = blockIdx.z;
     const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
     const double2 *Zb = Zf + (size_t)b * sz;
-    const double2 *Xb = X + (size_t)b * sbb;
+    const XT *Xb = X + (size_t)b * sbb;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     // hi: leading sum of the hi*hi products; sm: low-order part (hi*lo + lo*hi
     // products and the rounding errors of the hi sums, captured by TwoSum)
@@ -449,7 +459,7 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
             const int r = i / RK, kk = i % RK;
             zp[q] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
             const int kx = i / GT, c = i % GT;
-            xp[q] = (k0 + kx < n && c0 + c < nrhs) ? Xb[(size_t)(k0 + kx) * ldb + c0 + c] : make_double2(0, 0);
+            xp[q] = (k0 + kx < n && c0 + c < nrhs) ? ld_x(Xb + (size_t)(k0 + kx) * ldb + c0 + c) : make_double2(0, 0);
         }
     };
     auto stage = [&]() {
@@ -491,7 +501,7 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
                     for (int j = 0; j < 4; ++j) {
                         const float2 xh = make_float2(x[j].x, x[j].y), xl = make_float2(x[j].z, x[j].w);
                         ac[i][j] = cfma(ah, xh, ac[i][j]);
-                        sm[i][j] = cfma(ah, xl, sm[i][j]);
+                        if constexpr (kXlo) sm[i][j] = cfma(ah, xl, sm[i][j]);
                         sm[i][j] = cfma(al, xh, sm[i][j]);
                     }
                 }
@@ -529,12 +539,12 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
                     for (int d = 0; d < 5; ++d) {
                         const int jn = node + d - 2;
                         if (jn < 0 || jn >= Nn) continue;
-                        rv = cfms(bd[d], Xb[(size_t)(ch * Nn + jn) * ldb + c], rv);
+                        rv = cfms(bd[d], ld_x(Xb + (size_t)(ch * Nn + jn) * ldb + c), rv);
                     }
                 }
             }
             if (masked) rv = make_double2(0, 0);
-            R[(size_t)b * sbb + (size_t)r * ldb + c] = rv;
+            if (R) R[(size_t)b * sbb + (size_t)r * ldb + c] = rv;
             if (Rlo) Rlo[(size_t)b * sbb + (size_t)r * ldb + c] = make_float2((float)rv.x, (float)rv.y);
             rn += rv.x * rv.x + rv.y * rv.y;
             bn += bv.x * bv.x + bv.y * bv.y;
@@ -682,6 +692,9 @@ __global__ void convert_kernel(int dir, int rows, int cols, const void *__restri
     if (dir == 0) {
         const double2 v = reinterpret_cast<const double2 *>(src)[(size_t)b * ss + (size_t)r * lds + c];
         reinterpret_cast<float2 *>(dst)[(size_t)b * sd + (size_t)r * ldd + c] = make_float2((float)v.x, (float)v.y);
+    } else if (dir == 3) {
+        reinterpret_cast<float2 *>(dst)[(size_t)b * sd + (size_t)r * ldd + c] =
+            reinterpret_cast<const float2 *>(src)[(size_t)b * ss + (size_t)r * lds + c];
     } else {
         const float2 v = reinterpret_cast<const float2 *>(src)[(size_t)b * ss + (size_t)r * lds + c];
         double2 *o = reinterpret_cast<double2 *>(dst) + (size_t)b * sd + (size_t)r * ldd + c;
@@ -758,12 +771,32 @@ extern "C" int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual: memset");
     dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
-    residual_mixed_kernel<<<grid, 256, 0, st>>>(n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
-                                                reinterpret_cast<const double2 *>(band), mask_rows,
-                                                reinterpret_cast<const double2 *>(X), reinterpret_cast<const double2 *>(B),
-                                                ldb, stride_b, reinterpret_cast<double2 *>(R),
-                                                reinterpret_cast<float2 *>(Rlo), norms);
+    residual_mixed_kernel<double2><<<grid, 256, 0, st>>>(
+        n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
+        reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const double2 *>(X),
+        reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
+        reinterpret_cast<float2 *>(Rlo), norms);
     return check_launch("residual");
+}
+
+extern "C" int ghost_bor_residual_x32(int batch, int n, int nrhs, int Nn,
+                                      const void *Zf, long long ldz, long long stride_z,
+                                      const double *band, const int *mask_rows,
+                                      const float *X32, const double *B, long long ldb, long long stride_b,
+                                      double *R, float *R32, double *norms, void *stream)
+{
+    if (batch < 1 || n < 1 || nrhs < 1 || !Zf || !mask_rows || !X32 || !B || (!R && !R32) || !norms ||
+        ldz < n || ldb < nrhs || n != 2 * Nn)
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual_x32: memset");
+    dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
+    residual_mixed_kernel<float2><<<grid, 256, 0, st>>>(
+        n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
+        reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const float2 *>(X32),
+        reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
+        reinterpret_cast<float2 *>(R32), norms);
+    return check_launch("residual_x32");
 }
 
 extern "C" int ghost_bor_residual64(int batch, int n, int nrhs,
@@ -809,7 +842,7 @@ extern "C" int ghost_bor_convert(int dir, int batch, int rows, int cols,
                                  const void *src, long long lds, long long stride_s,
                                  void *dst, long long ldd, long long stride_d, void *stream)
 {
-    if (dir < 0 || dir > 2 || batch < 1 || rows < 1 || cols < 1 || !src || !dst || lds < cols || ldd < cols)
+    if (dir < 0 || dir > 3 || batch < 1 || rows < 1 || cols < 1 || !src || !dst || lds < cols || ldd < cols)
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     dim3 grid((cols + 255) / 256, rows, batch);

@@ -2,25 +2,31 @@
 
 Stages (each a C-ABI call on one CUDA stream):
 
-  far fill      ghost_bor_far_efie   Z_far[m], m = 0..M (FP32 or FP64 sampling + DCT,
-                                     FP64 contraction and storage)
-  near fill     ghost_bor_near_efie  FP64 near/self blocks (band store or dense)
+  far fill      ghost_bor_far_efie   alpha C Z_E far blocks, m = 0..M (FP32 or FP64
+                ghost_bor_far_mfie   sampling + transforms, FP64 contraction and storage)
+                                     and (1 - alpha) eta0 (-K) MFIE far brackets
+  near fill     ghost_bor_near_efie  FP64 near/self blocks (band store or dense),
+                ghost_bor_near_mfie  MFIE near brackets and the mass term M/2
   compose       ghost_bor_compose    A32 = fl32(Z_far + Z_near), masked
-  excitation    ghost_bor_rhs        B[m][row][2*it + pol] (FP64)
-  LU + solve    ghost_bor_getrf/getrs
-  refinement    ghost_bor_residual   R = B - (Z_far + Z_near) X in FP64 (FP32 products,
-                                     FP64 accumulation) then A32^-1 R, <= 3 passes
+  excitation    ghost_bor_rhs        B = alpha V_E + (1 - alpha) eta0 V_H (FP64); for
+                                     CFIE / MFIE also V_E alone for the far field
+  LU + solve    ghost_bor_getrf/getrs  (FP32, trailing updates on tcgen05)
+  refinement    ghost_bor_residual_x32  R0 = B - (Z_far + Z_near) X0 with Z in FP64
+                                     (split FP32 words, FP32 products, compensated
+                                     sums), then per correction D = A32^-1 R:
+                                     X += D, R -= fl32(Z) D (ghost_bor_cgemm_tc)
   far field     ghost_bor_farfield   dF[m][col] by reciprocity
 
-Only modes m >= 0 are factored: Z(-m) = D Z(m) D with D = diag(I, -I) and the
-excitation obeys V(-m) = +-D V(m), so each -m system has the solution
-+-D x(m) and contributes exactly the same far field; the mode sum weights
-m > 0 by two (checked against the per-mode reference in the tests).
+Only modes m >= 0 are factored: Z(-m) = D Z(m) D with D = diag(I, -I) for the
+EFIE and the MFIE operator, and the excitation obeys V(-m) = +-D V(m), so each
+-m system has the solution +-D x(m) and contributes exactly the same far field;
+the mode sum weights m > 0 by two (checked against the per-mode reference in
+the tests).
 
 Precisions: "fp64" is the plain FP64 path (the comparator); "fp32ir" samples
-and transforms the far kernel and factors in FP32, keeps the near/self blocks,
-the far-block contraction, the residual and the mode sum in FP64, and refines
-up to three times.
+and transforms the far kernels and factors in FP32, keeps the near/self blocks,
+the far-block contraction, the first residual and the mode sum in FP64-class
+arithmetic, and refines up to three times.
 """
 
 from __future__ import annotations
@@ -33,8 +39,9 @@ from typing import Callable, Dict, List, Optional
 import numpy as np
 
 from . import _native as nat
-from .geometry import (C0, ETA0, Generatrix, dct_tables, default_n_modes, gauss_on_generatrix,
-                       mask_rows, n_xi_efie, near_tables, pack_geo)
+from .geometry import (C0, ETA0, Generatrix, bracket_tables, dct_tables, default_n_modes,
+                       element_mass, gauss_on_generatrix, mask_rows, n_xi_bracket, n_xi_efie,
+                       near_tables, pack_geo)
 
 
 def _torch():
@@ -53,13 +60,16 @@ class SweepResult:
     info: Optional[np.ndarray] = None
     gpu_launches: int = 0
     res_history: List[float] = field(default_factory=list)
+    # device seconds of single launches, bracketed by CUDA events on the launch stream
+    kernel_s: Dict[str, List[float]] = field(default_factory=dict)
 
 
 class BorGpuProblem:
     """Host tables (FP64) and their device copies for one body at one frequency."""
 
     def __init__(self, points, freq_hz: float, thetas_deg, m_max: Optional[int] = None,
-                 gauss_order: int = 4, device=None):
+                 gauss_order: int = 4, device=None, formulation: str = "efie",
+                 cfie_alpha: float = 0.5):
         if gauss_order != 4:
             raise NotImplementedError("the GPU kernels are specialised for gauss_order=4")
         torch = _torch()
@@ -107,25 +117,44 @@ class BorGpuProblem:
         w[0] = 1.0
         self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
         self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
+        # A = alpha Z_EFIE + (1 - alpha) eta0 Z_MFIE (bor_solver.py:929-938)
+        form = formulation.strip().lower()
+        if form not in ("efie", "cfie", "mfie"):
+            raise ValueError(f"unknown formulation {formulation!r}")
+        self.formulation = form
+        self.alpha = float(cfie_alpha) if form == "cfie" else (1.0 if form == "efie" else 0.0)
+        self.d_btab = self.d_bsin2 = self.d_emass = None
+        self.n_xi_b = 0
+        if self.alpha < 1.0:
+            self.n_xi_b = n_xi_bracket(self.k, self.rho_max, self.m_max)
+            btab, bs2 = bracket_tables(self.n_xi_b, self.m_max)
+            self.d_btab = torch.as_tensor(btab, dtype=f64, device=dev)
+            self.d_bsin2 = torch.as_tensor(bs2, dtype=f64, device=dev)
+            self.d_emass = torch.as_tensor(element_mass(self.g, self.N), dtype=f64, device=dev)
         self.refine_floor = 1e-6     # residuals below this are at the FP32-product floor
-        self.tensor_cores = True     # FP32 LU / solve updates on tcgen05 (3xTF32)
+        self.tensor_cores = True     # FP32 LU / solve / residual updates on tcgen05 (3xTF32)
+        self.update_ws_bytes = 4 << 30   # scratch bound of one residual-update GEMM launch
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
         return int(sum(t.numel() * t.element_size() for t in (
             self.d_geo, self.d_dct, self.d_sin2, self.d_nodes, self.d_elem, self.d_pairs,
             self.d_tails, self.d_cells, self.d_core, self.d_tail, self.d_masks, self.d_thetas,
-            self.d_mode_w)))
+            self.d_mode_w) + tuple(t for t in (self.d_btab, self.d_bsin2, self.d_emass) if t is not None)))
 
     # -- memory -----------------------------------------------------------
     def bytes_needed(self, precision: str) -> int:
         Mb = self.m_max + 1
         nn = self.n * self.n
         rhs = self.n * self.nrhs
+        ve = Mb * rhs * 16 if self.alpha < 1.0 else 0       # separate V_E for the far field
         if precision == "fp64":
-            return Mb * (2 * nn * 16 + 3 * rhs * 16)
+            return Mb * (2 * nn * 16 + 3 * rhs * 16) + ve
         tc = 4 * 128 * Mb * (2 * self.n + 4 * max(self.n, self.nrhs)) * 2
-        return Mb * (nn * 16 + nn * 8 + 3 * rhs * 16 + rhs * 8 + 4 * self.Nn * 5 * 16) + tc
+        # Zf (c128), A and its unfactored copy (c64), B and X (c128), X32 and R32
+        # (c64), the near band, LU / solve scratch and the residual-update scratch
+        return (Mb * (nn * 16 + 2 * nn * 8 + 2 * rhs * 16 + 2 * rhs * 8 + 4 * self.Nn * 5 * 16) + tc + ve
+                + self.update_ws_bytes)
 
     # -- stages -----------------------------------------------------------
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
@@ -143,6 +172,36 @@ class BorGpuProblem:
                  self.near.cells.shape[1], nat.ptr(self.d_core), nat.ptr(self.d_tail),
                  self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms, stream)
 
+    def fill_far_mfie(self, Z, precision: int, scale: complex, stream: int):
+        ld = Z.shape[-1]
+        nat.call("ghost_bor_far_mfie", precision, self.N, self.m_max, self.n_xi_b, self.k,
+                 scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_btab),
+                 nat.ptr(self.d_bsin2), nat.ptr(Z), ld, Z.stride(0), stream)
+
+    def fill_near_mfie(self, scale: complex, stream: int, band=None, Z=None):
+        ld = 0 if Z is None else Z.shape[-1]
+        ms = 0 if Z is None else Z.stride(0)
+        nat.call("ghost_bor_near_mfie", self.N, self.m_max, self.k, scale.real, scale.imag,
+                 nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(self.d_emass),
+                 len(self.near.pairs), nat.ptr(self.d_pairs), nat.ptr(self.d_tails),
+                 nat.ptr(self.d_cells), self.near.cells.shape[1], nat.ptr(self.d_core),
+                 nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
+                 stream)
+
+    def fill_operator_far(self, Z, precision: int, stream: int):
+        """Far parts of A = alpha C Z_E + (1 - alpha) eta0 Z_M into Z."""
+        if self.alpha > 0.0:
+            self.fill_far(Z, precision, self.alpha * self.C, stream)
+        if self.alpha < 1.0:
+            self.fill_far_mfie(Z, precision, complex((1.0 - self.alpha) * ETA0), stream)
+
+    def fill_operator_near(self, stream: int, band=None, Z=None, precision: int = nat.F64):
+        """Near/self parts (and the MFIE mass term) of A into the band or Z."""
+        if self.alpha > 0.0:
+            self.fill_near(self.alpha * self.C, stream, band=band, Z=Z, precision=precision)
+        if self.alpha < 1.0:
+            self.fill_near_mfie(complex((1.0 - self.alpha) * ETA0), stream, band=band, Z=Z)
+
     def excitation(self, B, coef_e: float, coef_h: float, stream: int):
         torch = self.torch
         lib = nat.load()
@@ -153,14 +212,40 @@ class BorGpuProblem:
                  nat.ptr(B), B.shape[-1], B.stride(0), nat.ptr(work), stream)
         return work
 
+    def excitation_coefs(self):
+        """(coef_e, coef_h) of the solve's right-hand side (bor_solver.py:939-947)."""
+        return (self.alpha if self.alpha > 0.0 else 0.0,
+                (1.0 - self.alpha) * ETA0 if self.alpha < 1.0 else 0.0)
+
+    def _far_excitation(self, B, stream: int):
+        """The EFIE excitation V_E that the reciprocity far field needs: B itself
+        for EFIE, a second excitation for CFIE / MFIE (whose B mixes in n x H)."""
+        if self.alpha >= 1.0:
+            return B
+        Ve = self.torch.empty_like(B)
+        self._ve_work = self.excitation(Ve, 1.0, 0.0, stream)
+        return Ve
+
+    def assemble_mfie_modes_fp64(self, stream: Optional[int] = None):
+        """Dense FP64 Z_MFIE(m) = M/2 - K(m), m = 0..M, unmasked: the
+        assemble_mfie_mode operator of the reference for every m >= 0."""
+        torch = self.torch
+        if self.d_btab is None:
+            raise ValueError("this problem was built without the MFIE tables")
+        st = nat.stream_handle() if stream is None else stream
+        Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
+        self.fill_far_mfie(Z, nat.F64, 1.0 + 0.0j, st)
+        self.fill_near_mfie(1.0 + 0.0j, st, Z=Z)
+        return Z
+
     def assemble_modes_fp64(self, stream: Optional[int] = None):
         """Dense FP64 Z(m), m = 0..M, unmasked, C factor applied: the
         assemble_mode operator of the reference for every m >= 0."""
         torch = self.torch
         st = nat.stream_handle() if stream is None else stream
         Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
-        self.fill_far(Z, nat.F64, self.C, st)
-        self.fill_near(self.C, st, Z=Z)
+        self.fill_operator_far(Z, nat.F64, st)
+        self.fill_operator_near(st, Z=Z)
         return Z
 
     # -- the sweep ---------------------------------------------------------
@@ -187,6 +272,18 @@ class BorGpuProblem:
             if check_abort is not None:
                 check_abort()
 
+        kev: Dict[str, list] = {}
+
+        def kstart():
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            return e
+
+        def kend(name, e0):
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record()
+            kev.setdefault(name, []).append((e0, e1))
+
         mark("start")
         c128, c64 = torch.complex128, torch.complex64
         B = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
@@ -197,12 +294,13 @@ class BorGpuProblem:
         history: List[float] = []
         if precision == "fp64":
             Z = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
-            self.fill_far(Z, nat.F64, self.C, st); mark("far"); abort()
-            self.fill_near(self.C, st, Z=Z); mark("near")
+            self.fill_operator_far(Z, nat.F64, st); mark("far"); abort()
+            self.fill_operator_near(st, Z=Z); mark("near")
             nat.call("ghost_bor_mask64", Mb, n, nat.ptr(self.d_masks), nat.ptr(Z), n, Z.stride(0), st)
             Zc = Z.clone()
             mark("compose"); abort()
-            work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
+            work = self.excitation(B, *self.excitation_coefs(), st)
+            Ve = self._far_excitation(B, st); mark("rhs")
             X = B.clone()
             nat.call("ghost_bor_getrf", nat.F64, Mb, n, nat.ptr(Z), n, Z.stride(0), nat.ptr(ipiv),
                      nat.ptr(info), 0, st); mark("lu"); abort()
@@ -214,12 +312,15 @@ class BorGpuProblem:
         else:
             Zf = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
             band = torch.zeros((Mb, 4, Nn, 5), dtype=c128, device=self.device)
-            self.fill_far(Zf, nat.F32, self.C, st); mark("far"); abort()
-            self.fill_near(self.C, st, band=band, precision=nat.F32); mark("near")
+            k0 = kstart(); self.fill_operator_far(Zf, nat.F32, st); kend("far_fill", k0)
+            mark("far"); abort()
+            k0 = kstart(); self.fill_operator_near(st, band=band, precision=nat.F32); kend("near_fill", k0)
+            mark("near")
             A = torch.empty((Mb, n, n), dtype=c64, device=self.device)
             nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
                      nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st); mark("compose"); abort()
-            work = self.excitation(B, 1.0, 0.0, st); mark("rhs")
+            work = self.excitation(B, *self.excitation_coefs(), st)
+            Ve = self._far_excitation(B, st); mark("rhs")
             X32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
             lib = nat.load()
             if self.tensor_cores:
@@ -238,36 +339,78 @@ class BorGpuProblem:
             X = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
             nat.call("ghost_bor_convert", 1, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(X),
                      nrhs, X.stride(0), st); mark("solve")
-            R = torch.empty_like(B)
+            # refinement: R0 = B - Z X0 once with the split-word kernel (Z in FP64,
+            # X0 the FP32 solution); for each correction D = A^-1 R the next
+            # residual is R - Z D, and since |D| ~ 1e-5 |X| a tensor-core GEMM
+            # on fl32(Z) is accurate enough for that product
+            R32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
+            k0 = kstart()
+            nat.call("ghost_bor_residual_x32", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
+                     nat.ptr(self.d_masks), nat.ptr(X32), nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(R32),
+                     nat.ptr(norms), st)
+            kend("residual", k0)
+            bn2 = torch.clamp(norms[:, 1], min=1e-300)
+            rel = float(torch.sqrt(torch.max(norms[:, 0] / bn2)))
+            history = [rel]
             prev = None
-            history = []
-            for it in range(max_refine + 1):
-                nat.call("ghost_bor_residual", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
-                         nat.ptr(self.d_masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0), nat.ptr(R),
-                         nat.ptr(X32), nat.ptr(norms), st)
-                rel = float(torch.sqrt(torch.max(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300))))
-                history.append(rel)
-                # stop at the FP32-product floor of the residual (~1e-7 of ||B||),
-                # on stagnation, or after max_refine corrections
-                if it == max_refine or rel < self.refine_floor or (prev is not None and rel > 0.5 * prev):
+            Ac = up_ws = status = None
+            for it in range(max_refine):
+                # stop at the floor of the split-word residual (~1e-7 of ||B||)
+                # or on stagnation
+                if rel < self.refine_floor or (prev is not None and rel > 0.5 * prev):
                     break
                 prev = rel
+                if Ac is None:
+                    # fl32(Z), masked like A, kept for the residual updates
+                    Ac = torch.empty((Mb, n, n), dtype=c64, device=self.device)
+                    nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
+                             nat.ptr(self.d_masks), nat.ptr(Ac), n, Ac.stride(0), st)
+                nat.call("ghost_bor_convert", 3, Mb, n, nrhs, nat.ptr(R32), nrhs, R32.stride(0),
+                         nat.ptr(X32), nrhs, X32.stride(0), st)
                 nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
                          nat.ptr(ipiv), nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(rs_ws), st)
                 nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
                          nat.ptr(X), nrhs, X.stride(0), st)
+                k0 = kstart()
+                if self.tensor_cores:
+                    if up_ws is None:
+                        per = int(lib.ghost_bor_cgemm_tc_workspace(1, n, nrhs, n))
+                        chunk = max(1, min(Mb, int(self.update_ws_bytes // max(per, 1))))
+                        up_ws = torch.empty(int(lib.ghost_bor_cgemm_tc_workspace(chunk, n, nrhs, n)),
+                                            dtype=torch.uint8, device=self.device)
+                        status = torch.zeros(((Mb + chunk - 1) // chunk) * max_refine, dtype=torch.int32,
+                                             device=self.device)
+                    for ci, b0 in enumerate(range(0, Mb, chunk)):
+                        nb = min(chunk, Mb - b0)
+                        nat.call("ghost_bor_cgemm_tc", nb, n, nrhs, n, nat.ptr(Ac[b0]), n, Ac.stride(0),
+                                 nat.ptr(X32[b0]), nrhs, X32.stride(0), nat.ptr(R32[b0]), nrhs, R32.stride(0),
+                                 nat.ptr(up_ws), nat.ptr(status[it * ((Mb + chunk - 1) // chunk) + ci]), st)
+                else:
+                    # SIMT path: the split-word residual of the updated solution
+                    Rd = torch.empty_like(B)
+                    nat.call("ghost_bor_residual", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0),
+                             nat.ptr(band), nat.ptr(self.d_masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0),
+                             nat.ptr(Rd), nat.ptr(R32), nat.ptr(norms), st)
+                    del Rd
+                kend("residual_update", k0)
+                rn = torch.linalg.vector_norm(R32, dim=(1, 2)).double() ** 2
+                norms[:, 0].copy_(rn)
+                rel = float(torch.sqrt(torch.max(rn / bn2)))
+                history.append(rel)
                 iters += 1
                 abort()
+            if status is not None and int(status.max()) != 0:
+                raise RuntimeError("a bounded tensor-core wait gave up in the residual update")
             mark("residual")
             if lu_ws is not None:
                 flags = torch.stack([lu_ws[:4].view(torch.int32)[0], rs_ws[:4].view(torch.int32)[0]])
                 if int(flags.max()) != 0:
                     raise RuntimeError("a bounded tensor-core wait gave up in the LU / solve kernels")
             if not keep:
-                del Zf, A, R, X32, band
+                del Zf, A, Ac, R32, X32, band
         dF = torch.empty((Mb, nrhs), dtype=c128, device=self.device)
         nat.call("ghost_bor_farfield", nat.F64, Mb, n, nrhs, Nn, self.k, nat.ptr(self.d_mode_w),
-                 nat.ptr(B), nrhs, B.stride(0), nat.ptr(X), nrhs, X.stride(0), nat.ptr(dF), st)
+                 nat.ptr(Ve), nrhs, Ve.stride(0), nat.ptr(X), nrhs, X.stride(0), nat.ptr(dF), st)
         mark("farfield")
         dF_h = dF.cpu().numpy()
         res = torch.sqrt(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300)).cpu().numpy()
@@ -276,9 +419,10 @@ class BorGpuProblem:
         names = list(ev)
         tm = {f"{b}_s": ev[a].elapsed_time(ev[b]) / 1e3 for a, b in zip(names[:-1], names[1:])}
         tm["gpu_total_s"] = ev[names[0]].elapsed_time(ev[names[-1]]) / 1e3
+        ks = {k: [a.elapsed_time(b) / 1e3 for a, b in v] for k, v in kev.items()}
         dF_h = dF_h.reshape(Mb, self.T, 2).transpose(0, 2, 1)
         out = SweepResult(dF=np.ascontiguousarray(dF_h), residual=res, refine_iters=iters, timings=tm,
-                          info=info_h, res_history=history if precision == "fp32ir" else [])
+                          info=info_h, res_history=history if precision == "fp32ir" else [], kernel_s=ks)
         if keep:
             out.X = X
             out.B = B

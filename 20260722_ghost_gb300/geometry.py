@@ -135,6 +135,55 @@ def dct_tables(n_xi: int, n_orders: int, scale: float = 1.0) -> Tuple[np.ndarray
     return np.ascontiguousarray(dct), np.ascontiguousarray(sin2)
 
 
+def bracket_tables(n_xi: int, m_max: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Half-grid tables of the MFIE bracket transforms, m = 0..m_max.
+
+    The reference takes the FFT of each of its four brackets over
+    xi_l = -pi + 2 pi l / n_xi, keeps bins m (phase e^{j pi m} 2 pi / n_xi)
+    and multiplies by the Galerkin 2 pi (bor_streaming.py:241-246, 378-385):
+    K(m) = (4 pi^2 / n_xi) sum_l F(xi_l) e^{-j m xi_l}.  With
+    s2 = sin^2(xi/2) and p = (1 + j k R) e^{-j k R} / R^3 every bracket is
+    p (u + v s2) or sin(xi) p (u + v s2) with per-point-pair constants u, v,
+    so three half-grid transforms of p cover all four (the 1/(4 pi) of the
+    kernel is folded in):
+
+        tab[0][j][m] = (pi/n) c_j cos(m xi_j)          c_j = 1, 2, ..., 2, 1
+        tab[1][j][m] = (pi/n) c_j s2_j cos(m xi_j)
+        tab[2][j][m] = (pi/n) 2 sin(xi_j) sin(m xi_j)  (zero at j = 0, h)
+
+    xi_j = pi j / h, h = n_xi / 2.  Returns (tab [3, h+1, m_max+1], sin2 [h+1])."""
+    h = n_xi // 2
+    j = np.arange(h + 1)
+    m = np.arange(m_max + 1)
+    c = np.full(h + 1, 2.0)
+    c[0] = c[h] = 1.0
+    mj = np.outer(j, m) % (2 * h)
+    ang = np.pi * mj / h
+    xi = np.pi * j / h
+    s2 = np.sin(0.5 * xi) ** 2
+    sx = np.sin(np.pi * (j % (2 * h)) / h)
+    sx[0] = sx[h] = 0.0
+    f = np.pi / n_xi
+    tab = np.empty((3, h + 1, m_max + 1))
+    tab[0] = f * c[:, None] * np.cos(ang)
+    tab[1] = tab[0] * s2[:, None]
+    tab[2] = f * 2.0 * sx[:, None] * np.sin(ang)
+    return np.ascontiguousarray(tab), np.ascontiguousarray(s2)
+
+
+def element_mass(g: "GaussData", n_elem: int) -> np.ndarray:
+    """Element contributions of the MFIE mass matrix 2 pi B_T diag(w rho) B_T^T
+    (bor_solver.py:389-397): [n_elem, 4] = (a, b) in (0,0), (0,1), (1,0), (1,1)
+    for nodes (e + a, e + b)."""
+    wr = (g.w * g.rho).reshape(n_elem, -1)
+    T = (g.T0.reshape(n_elem, -1), g.T1.reshape(n_elem, -1))
+    out = np.empty((n_elem, 4))
+    for a in range(2):
+        for b in range(2):
+            out[:, 2 * a + b] = 2.0 * np.pi * np.sum(T[a] * T[b] * wr, axis=1)
+    return np.ascontiguousarray(out)
+
+
 # ---------------------------------------------------------------------------
 # graded near cells (bor_solver.py:54-110)
 # ---------------------------------------------------------------------------

@@ -128,6 +128,50 @@ int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
                         void *stream);
 
 /* ------------------------------------------------------------------------
+ * Fused MFIE far fill: for every far element pair (|e - f| >= 2) sample
+ * p(R) = (1 + j k R) e^{-j k R} / R^3 on the half bracket grid
+ * xi_j = pi j / (nxi/2), take the three transforms in `tab`, form the four
+ * bracket blocks K_tt, K_tf, K_ft, K_ff of the reference (exact
+ * rearrangement: every bracket is p (u + v s2) or sin(xi) p (u + v s2) with
+ * per-point-pair constants), contract with the weights T w rho on both sides
+ * and ADD -scale * [[K_tt, K_tf], [K_ft, K_ff]] into Z[m], m = 0..m_max
+ * (the far part of Z_MFIE = M/2 - K; K(-m) = D K(m) D with D = diag(I, -I)).
+ * `prec` selects the sampling / transform arithmetic; the contraction and
+ * the accumulation into Z are FP64.
+ *   geo   as in ghost_bor_far_efie
+ *   tab   [3][nxi/2+1][m_max+1]: (pi/nxi) c_j cos(m xi_j),
+ *         (pi/nxi) c_j sin^2(xi_j/2) cos(m xi_j), (pi/nxi) 2 sin(xi_j) sin(m xi_j)
+ *   sin2  [nxi/2+1] sin^2(xi_j / 2);  nxi = the bracket rule
+ *         (bor_streaming.py:114-116)
+ * Replaces sample_mfie + the bracket FFT and contraction of
+ * StreamingFarBlocks (bor_stream_kernel.c:65-106, bor_streaming.py:241-246,
+ * 378-385, 409-421).
+ */
+int ghost_bor_far_mfie(int prec, int n_elem, int m_max, int nxi, double k,
+                       double scale_re, double scale_im,
+                       const double *geo, const double *tab, const double *sin2,
+                       void *Z, long long ldz, long long mode_stride, void *stream);
+
+/* ------------------------------------------------------------------------
+ * FP64 near MFIE blocks (|e - f| <= 1) on the graded cells of
+ * ghost_bor_near_efie, with the bracket grid of the reference (sinh core
+ * with s0 = 1 for on-axis points + Gauss tail, +xi and -xi folded), plus the
+ * mass term: ADD scale * (M/2 - K) for m = 0..m_max into the band or the
+ * dense Z (layouts as in ghost_bor_near_efie).
+ *   emass [n_elem][4] element mass contributions 2 pi sum_g T_a T_b w rho
+ *         for (a, b) = (0,0), (0,1), (1,0), (1,1)
+ * Replaces mfie_kernels_near, _near_mfie_data, mass_blocks and the near loop
+ * of assemble_mfie_mode (bor_kernels.py:334-431, bor_solver.py:372-435).
+ */
+int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale_re, double scale_im,
+                        const double *nodes, const double *elem, const double *emass,
+                        int n_pairs, const int *pairs, const int *tails,
+                        const double *cells, int n_cells_total,
+                        const double *core_gl, const double *tail_gl, int n_tail_total,
+                        double *band, void *Z, long long ldz, long long mode_stride,
+                        void *stream);
+
+/* ------------------------------------------------------------------------
  * Excitation for all modes 0..m_max, angles and both polarisations:
  *   B[m][row][2*it + pol] (complex double, row stride ldb, mode stride),
  *   pol 0 = VV (theta), 1 = HH (phi).  Rows flagged in mask_rows[m][4]
@@ -217,6 +261,19 @@ int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
                        const double *X, const double *B, long long ldb, long long stride_b,
                        double *R, float *Rlo, double *norms, void *stream);
 
+/* Residual of an FP32 solution X32 (complex float, same ldb / stride_b as B):
+ *   R = B - (Zf + band) X32, with the arithmetic of ghost_bor_residual (the
+ *   low FP32 word of X is zero, so the Z_hi X_lo products drop out).
+ * R (complex double) and R32 (complex float) are each optional, not both.
+ * The first residual of the refinement; later residuals follow from it by
+ * R -= fl32(Z) D for each correction D (ghost_bor_cgemm_tc).  No counterpart in
+ * the reference (its solve is FP64 LAPACK, bor_solver.py:753-756). */
+int ghost_bor_residual_x32(int batch, int n, int nrhs, int Nn,
+                           const void *Zf, long long ldz, long long stride_z,
+                           const double *band, const int *mask_rows,
+                           const float *X32, const double *B, long long ldb, long long stride_b,
+                           double *R, float *R32, double *norms, void *stream);
+
 /* FP64 residual R = B - Z X (all complex double); norms as above. */
 int ghost_bor_residual64(int batch, int n, int nrhs,
                          const double *Z, long long ldz, long long stride_z,
@@ -242,9 +299,9 @@ int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
  *   complex float) with masked rows/columns replaced by identity rows/columns
  *   (band may be NULL).
  * ghost_bor_mask64: apply the same identity masking to a complex double Z.
- * ghost_bor_convert: elementwise complex double <-> float copy of a strided
- *   batch of row blocks (dir 0: double->float, 1: float->double, 2: float
- *   added into double).
+ * ghost_bor_convert: elementwise complex copy of a strided batch of row
+ *   blocks (dir 0: double->float, 1: float->double, 2: float added into
+ *   double, 3: float->float).
  */
 int ghost_bor_compose(int batch, int n, int Nn, const void *Zf, long long ldz, long long stride_z,
                       const double *band, const int *mask_rows,

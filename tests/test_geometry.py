@@ -89,3 +89,57 @@ def test_bodies(pkg):
     assert all(200 <= x["n"] <= 1600 for x in bodies)
     s = b.sphere_generatrix(1.0, 8)
     np.testing.assert_allclose(np.hypot(s[:, 0], s[:, 1]), 1.0)
+
+
+def test_bracket_tables_reproduce_reference_brackets(pkg, oracle):
+    """Three half-grid transforms of p with the per-pair constants used by the
+    MFIE far kernel give the reference's four bracket transforms (full-grid
+    FFT of each bracket, bins m >= 0, 2 pi Galerkin factor)."""
+    D = load_golden("conesphere_n40")
+    geo = pkg.geometry
+    gen = geo.Generatrix(D["points"])
+    g = geo.gauss_on_generatrix(gen, 4)
+    k = 2 * math.pi * float(D["freq_hz"]) / geo.C0
+    M = int(D["m_max"])
+    nb = geo.n_xi_bracket(k, float(np.max(gen.nodes[:, 0])), M)
+    tab, s2 = geo.bracket_tables(nb, M)
+    xi = 2 * np.pi * np.arange(nb) / nb - np.pi
+    m = np.arange(M + 1)
+    rng = np.random.default_rng(3)
+    for _ in range(40):
+        e = int(rng.integers(0, gen.n_elems))
+        f = int(np.clip(e + rng.choice([-9, -3, -2, 2, 3, 9]), 0, gen.n_elems - 1))
+        p, q = 4 * e + int(rng.integers(0, 4)), 4 * f + int(rng.integers(0, 4))
+        args = [np.array([v]) for v in (g.rho[p], g.z[p], g.trho[p], g.tz[p],
+                                        g.rho[q], g.z[q], g.trho[q], g.tz[q])]
+        F = oracle._mfie_bracket_grid(*args, k, xi[None, :])
+        want = [(np.fft.fft(Fi[0])[m] * np.exp(1j * np.pi * m) * 2 * np.pi / nb) * 2 * np.pi for Fi in F]
+        rp, zp, trp, tzp, rq, zq, trq, tzq = (float(a[0]) for a in args)
+        dr, dz = rp - rq, zp - zq
+        R = np.sqrt(dr * dr + dz * dz + 4 * rp * rq * s2)
+        pt = (1 + 1j * k * R) * np.exp(-1j * k * R) / R ** 3
+        Cp, Cs, S = tab[0].T @ pt, tab[1].T @ pt, tab[2].T @ pt
+        X0 = trp * tzq - tzp * trq
+        N0 = trp * dz - tzp * dr
+        A0 = trp * dr + tzp * dz
+        D0 = trp * trq + tzp * tzq
+        c0 = dr * tzq - dz * trq
+        c1 = 2 * (A0 * tzp * trq + trp * rq * X0 + D0 * tzp * rq + trp * trq * N0)
+        e0 = rq * X0 + trq * N0
+        got = [-c0 * Cp - c1 * Cs, -1j * dz * S, 1j * e0 * S, N0 * Cp - 2 * (N0 - rq * tzp) * Cs]
+        scale = max(np.max(np.abs(w)) for w in want)
+        for gv, wv in zip(got, want):
+            assert np.max(np.abs(gv - wv)) < 1e-11 * scale
+
+
+def test_element_mass(pkg, oracle):
+    D = load_golden("conesphere_n40")
+    geo = pkg.geometry
+    gen = geo.Generatrix(D["points"])
+    em = geo.element_mass(geo.gauss_on_generatrix(gen, 4), gen.n_elems)
+    Mm = np.zeros((gen.n_nodes, gen.n_nodes))
+    for e in range(gen.n_elems):
+        for ab in range(4):
+            Mm[e + ab // 2, e + ab % 2] += em[e, ab]
+    ref = oracle.OracleSolver(D["points"], float(D["freq_hz"])).mass()
+    assert np.max(np.abs(Mm - ref)) < 1e-14 * np.max(np.abs(ref))
