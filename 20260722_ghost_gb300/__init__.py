@@ -4,6 +4,7 @@ Drop-in modules mirroring the reference project's entry points:
 
     bor_solver     solve_bor, solve_bor_pec, BorPecSolver, sphere_generatrix, ...
     bor_streaming  StreamingFarBlocks, estimate_streaming_gb
+    adjoint        bspline_rcs (torch.autograd.Function), ShapeGradient
 
 All numerics run on one GPU through libghost_bor.so (C ABI in include/ghost_bor.h).
 """
@@ -11,12 +12,12 @@ All numerics run on one GPU through libghost_bor.so (C ABI in include/ghost_bor.
 from . import bodies, geometry  # noqa: F401
 from .build import build  # noqa: F401
 
-__all__ = ["bodies", "geometry", "build", "bor_solver", "bor_streaming", "engine"]
+__all__ = ["bodies", "geometry", "build", "bor_solver", "bor_streaming", "engine", "adjoint"]
 
 
 def __getattr__(name):
     # the GPU modules import torch lazily so that a CPU-only import stays cheap
-    if name in ("bor_solver", "bor_streaming", "engine", "_native"):
+    if name in ("bor_solver", "bor_streaming", "engine", "_native", "adjoint"):
         import importlib
         return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)

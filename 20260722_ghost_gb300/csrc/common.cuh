@@ -109,5 +109,7 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b)
 // ----------------------------------------------------------------------------
 void set_last_error(const char *msg);
 int check_launch(const char *where);
+// persistent grid size of the near-field kernels (CTAs) on the current device
+int near_grid();
 
 }  // namespace gb

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(TPB, 2)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
                 const double *__restrict__ sin2, double2 *__restrict__ Z,
-                long long ldz, long long mode_stride)
+                long long ldz, long long mode_stride, const unsigned char *__restrict__ emask)
 {
     using CT = C<R>;
     using Samp = GreenSampler<R>;
@@ -84,6 +84,13 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     const int f0 = (blockIdx.x % fgroups) * EPB;
     const int m0 = blockIdx.y * (NOB - 2);
     if (m0 > M) return;
+    // element mask: only pairs with a flagged test or source element (used for
+    // the shape-derivative fills of the adjoint gradient)
+    if (emask && !emask[e]) {
+        bool any = false;
+        for (int j = 0; j < EPB; ++j) any |= (f0 + j < N) && emask[f0 + j];
+        if (!any) return;
+    }
     const int m1 = min(M, m0 + NOB - 3);
     const int o0 = max(0, m0 - 1);
     const int nord = m1 + 1 - o0 + 1;         // orders o0..m1+1
@@ -94,7 +101,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     const int pp = tid % PPB;                 // Gauss-point pair of this thread
     const int ep = pp >> 4, gh = pp & 15;
     const int f = f0 + ep;
-    const bool active = (f < N) && (abs(e - f) >= 2);
+    const bool active = (f < N) && (abs(e - f) >= 2) && (!emask || emask[e] || emask[f]);
 
     for (int i = tid; i < (EPB + 1) * 24; i += TPB) {
         const int slot = i / 24, r = i % 24;
@@ -209,7 +216,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         const int job = base + tid;
         const int jep = (job >> 1) / nord, n = (job >> 1) % nord, b = job & 1;
         const int ff = f0 + jep;
-        const bool doit = job < njobs && ff < N && abs(e - ff) >= 2;
+        const bool doit = job < njobs && ff < N && abs(e - ff) >= 2 && (!emask || emask[e] || emask[ff]);
         double2 out[5][2];    // p11, pdd, pds, psd, pss for a = 0, 1
         if (doit) {
             if constexpr (sizeof(R) == 4) {
@@ -317,7 +324,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     for (int job = tid; job < EPB * nmodes; job += TPB) {
         const int jep = job / nmodes, m = m0 + job % nmodes;
         const int ff = f0 + jep;
-        if (ff >= N || abs(e - ff) < 2) continue;
+        if (ff >= N || abs(e - ff) < 2 || (emask && !emask[e] && !emask[ff])) continue;
         const int nl = abs(m - 1) - o0, nm = m - o0, nh = m + 1 - o0;
         const double2 *zl = Gs + (jep * NOB + nm) * 16;
         const double tre = geo[(size_t)9 * P + 4 * e], trf = geo[(size_t)9 * P + 4 * ff];
@@ -347,7 +354,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
 template <class R, int NT>
 int launch_far(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                const double *dct, const double *sin2, void *Z, long long ldz, long long ms,
-               cudaStream_t st)
+               const unsigned char *emask, cudaStream_t st)
 {
     const size_t smem = SmemLayout<R, NT>::bytes();
     auto kern = far_efie_kernel<R, NT>;
@@ -358,17 +365,18 @@ int launch_far(int N, int M, int nxi, double k, double sre, double sim, const do
     const int nchunks = (M + 1 + (NOB - 2) - 1) / (NOB - 2);
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, TPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, dct, sin2,
-                                  reinterpret_cast<double2 *>(Z), ldz, ms);
+                                  reinterpret_cast<double2 *>(Z), ldz, ms, emask);
     return check_launch("far_efie");
 }
 
 }  // namespace
 }  // namespace gb
 
-extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
-                                  double scale_re, double scale_im,
-                                  const double *geo, const double *dct, const double *sin2,
-                                  void *Z, long long ldz, long long mode_stride, void *stream)
+extern "C" int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k,
+                                         double scale_re, double scale_im,
+                                         const double *geo, const double *dct, const double *sin2,
+                                         void *Z, long long ldz, long long mode_stride,
+                                         const unsigned char *elem_mask, void *stream)
 {
     using namespace gb;
     if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !dct || !sin2 || !Z ||
@@ -378,12 +386,21 @@ extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, doub
     // 4 order groups x NT orders per thread: NT = 8 covers |m| <= 29 in one
     // launch row, NT = 16 covers |m| <= 61 per row
     if (prec == GHOST_BOR_F32) {
-        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
-        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
+        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
     }
     if (prec == GHOST_BOR_F64) {
-        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
-        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, st);
+        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
+        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
     }
     return GHOST_BOR_EINVAL;
+}
+
+extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
+                                  double scale_re, double scale_im,
+                                  const double *geo, const double *dct, const double *sin2,
+                                  void *Z, long long ldz, long long mode_stride, void *stream)
+{
+    return ghost_bor_far_efie_masked(prec, n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z,
+                                     ldz, mode_stride, nullptr, stream);
 }

@@ -216,11 +216,15 @@ far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
 }
 
 // ---------------------------------------------------------------------------
-// near pairs |e - f| <= 1 (graded cells, sinh core + Gauss tail) and mass
+// near pairs |e - f| <= 1 (graded cells, sinh core + Gauss tail) and mass.
+// Persistent grid; per batch of 128 point pairs each thread evaluates its
+// azimuth nodes once (FP64 transcendentals) into a per-CTA scratch, then each
+// chunk of NCM orders projects from it (see near_fill.cu).
 // ---------------------------------------------------------------------------
 constexpr int NTPB = 128;
 constexpr int NCORE_M = 48;
 constexpr int NCM = 8;                  // orders per chunk
+constexpr size_t kMNodeBytes = 64;      // p w (16), s2, sin xi, and the cos / sin recurrence state (4 x 8)
 
 struct NearMfieSmem {
     // Gb [NTPB][3][NCM] double2, W [NTPB][24] double, Prim [24][M+1] double2
@@ -230,21 +234,17 @@ struct NearMfieSmem {
     }
 };
 
-// accumulate p w {cos(n xi), s2 cos(n xi), sin(xi) sin(n xi)}, n = n0..n0+NCM-1
-__device__ __forceinline__ void project3(double2 (&acc)[3][NCM], double pre, double pim,
-                                         double s2, double sx, double c1, double s1, int n0)
+// accumulate p w {cos(n xi), s2 cos(n xi), sin(xi) sin(n xi)}, n = n0..n0+NCM-1,
+// from the recurrence state (cos, sin of (n0-1) xi and n0 xi), which is advanced
+__device__ __forceinline__ void project3(double2 (&acc)[3][NCM], double2 p, double s2, double sx,
+                                         double &cm1, double &c0, double &sm1, double &s0)
 {
-    // cos / sin of n xi by the Chebyshev recurrences
-    double cm1 = c1, c0 = 1.0, sm1 = -s1, s0 = 0.0;
-    for (int n = 0; n < n0; ++n) {
-        const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
-        const double sn = 2.0 * c1 * s0 - sm1; sm1 = s0; s0 = sn;
-    }
-    const double qre = pre * s2, qim = pim * s2;
-    const double ure = pre * sx, uim = pim * sx;
+    const double c1 = 1.0 - 2.0 * s2;            // cos(xi)
+    const double qre = p.x * s2, qim = p.y * s2;
+    const double ure = p.x * sx, uim = p.y * sx;
 #pragma unroll
     for (int n = 0; n < NCM; ++n) {
-        acc[0][n].x = fma(pre, c0, acc[0][n].x); acc[0][n].y = fma(pim, c0, acc[0][n].y);
+        acc[0][n].x = fma(p.x, c0, acc[0][n].x); acc[0][n].y = fma(p.y, c0, acc[0][n].y);
         acc[1][n].x = fma(qre, c0, acc[1][n].x); acc[1][n].y = fma(qim, c0, acc[1][n].y);
         acc[2][n].x = fma(ure, s0, acc[2][n].x); acc[2][n].y = fma(uim, s0, acc[2][n].y);
         const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
@@ -252,57 +252,64 @@ __device__ __forceinline__ void project3(double2 (&acc)[3][NCM], double pre, dou
     }
 }
 
-__global__ void __launch_bounds__(NTPB)
+__global__ void __launch_bounds__(NTPB, 2)
 near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
-                 const double *__restrict__ emass,
+                 const double *__restrict__ emass, int n_pairs,
                  const int *__restrict__ pairs, const int *__restrict__ tails,
                  const double *__restrict__ cells, int ncells_total,
                  const double *__restrict__ core_gl, const double *__restrict__ tail_gl, int ntail_total,
-                 double2 *__restrict__ band, double2 *__restrict__ Z, long long ldz, long long mode_stride)
+                 int nmax, double2 *__restrict__ band, double2 *__restrict__ Z, long long ldz,
+                 long long mode_stride, unsigned char *__restrict__ scratch, int *__restrict__ status)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Mo = M + 1;
     double2 *Gb = reinterpret_cast<double2 *>(smem_raw);
     double *W = reinterpret_cast<double *>(Gb + NTPB * 3 * NCM);
     double2 *Prim = reinterpret_cast<double2 *>(W + NTPB * 24);
-
-    const int pi = blockIdx.x;
-    const int e = pairs[4 * pi + 0], f = pairs[4 * pi + 1];
-    const int coff = pairs[4 * pi + 2], ncell = pairs[4 * pi + 3];
-    const int toff = tails[2 * pi + 0], ntail = tails[2 * pi + 1];
     const int tid = threadIdx.x;
 
-    const double rho_e0 = nodes[2 * e], z_e0 = nodes[2 * e + 1];
-    const double drho_e = nodes[2 * e + 2] - rho_e0, dz_e = nodes[2 * e + 3] - z_e0;
-    const double rho_f0 = nodes[2 * f], z_f0 = nodes[2 * f + 1];
-    const double drho_f = nodes[2 * f + 2] - rho_f0, dz_f = nodes[2 * f + 3] - z_f0;
-    const double Le = elem[e], Lf = elem[f];
-    const double tre = elem[N + e], tze = elem[2 * N + e];
-    const double trf = elem[N + f], tzf = elem[2 * N + f];
-
-    for (int i = tid; i < 24 * Mo; i += NTPB) Prim[i] = make_double2(0.0, 0.0);
+    const size_t plane = (size_t)nmax * NTPB;
+    double2 *gP = reinterpret_cast<double2 *>(scratch + (size_t)blockIdx.x * plane * kMNodeBytes);
+    double *gS2 = reinterpret_cast<double *>(gP + plane);
+    double *gSx = gS2 + plane;
+    double *gCm = gSx + plane;
+    double *gC0 = gCm + plane;
+    double *gSm = gC0 + plane;
+    double *gS0 = gSm + plane;
 
     constexpr int NOUT = (24 * NCM + NTPB - 1) / NTPB;
-    const int nbatch = (ncell + NTPB - 1) / NTPB;
     const int nchunk = (Mo + NCM - 1) / NCM;
-    for (int ch = 0; ch < nchunk; ++ch) {
-        const int n0 = ch * NCM;
-        double2 out[NOUT];
-#pragma unroll
-        for (int r = 0; r < NOUT; ++r) out[r] = make_double2(0.0, 0.0);
+    const double ik4pi = 1.0 / (4.0 * GB_PI);
 
+    for (int pi = blockIdx.x; pi < n_pairs; pi += gridDim.x) {
+        const int e = pairs[4 * pi + 0], f = pairs[4 * pi + 1];
+        const int coff = pairs[4 * pi + 2], ncell = pairs[4 * pi + 3];
+        const int toff = tails[2 * pi + 0], ntail = tails[2 * pi + 1];
+        const int nn = NCORE_M + ntail;
+        if (nn > nmax) {
+            if (tid == 0) atomicExch(status, 1);
+            continue;
+        }
+        const double rho_e0 = nodes[2 * e], z_e0 = nodes[2 * e + 1];
+        const double drho_e = nodes[2 * e + 2] - rho_e0, dz_e = nodes[2 * e + 3] - z_e0;
+        const double rho_f0 = nodes[2 * f], z_f0 = nodes[2 * f + 1];
+        const double drho_f = nodes[2 * f + 2] - rho_f0, dz_f = nodes[2 * f + 3] - z_f0;
+        const double Le = elem[e], Lf = elem[f];
+        const double tre = elem[N + e], tze = elem[2 * N + e];
+        const double trf = elem[N + f], tzf = elem[2 * N + f];
+
+        __syncthreads();                     // the previous pair has finished reading Prim
+        for (int i = tid; i < 24 * Mo; i += NTPB) Prim[i] = make_double2(0.0, 0.0);
+
+        const int nbatch = (ncell + NTPB - 1) / NTPB;
         for (int bt = 0; bt < nbatch; ++bt) {
             const int c = bt * NTPB + tid;
-            double2 acc[3][NCM];
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-#pragma unroll
-                for (int n = 0; n < NCM; ++n) acc[t][n] = make_double2(0.0, 0.0);
+            const bool valid = c < ncell;
             double wl[24];
 #pragma unroll
             for (int i = 0; i < 24; ++i) wl[i] = 0.0;
-            if (c < ncell) {
+            if (valid) {
                 const double s = cells[coff + c];
                 const double sp = cells[ncells_total + coff + c];
                 const double wc = cells[2 * ncells_total + coff + c];
@@ -318,7 +325,6 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                 const double da = d / a;
                 const double s0 = (rr4 <= 1e-30) ? 1.0 : fmin(0.25, 20.0 * da);
                 const double vmax = asinh(s0 / da);
-                const double ik4pi = 1.0 / (4.0 * GB_PI);
                 for (int i = 0; i < NCORE_M; ++i) {
                     const double v = core_gl[i] * vmax;
                     const double wv = core_gl[NCORE_M + i] * vmax;
@@ -332,9 +338,13 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     sincos(kr, &sn, &cs);
                     const double ir = 1.0 / R;
                     const double amp = 2.0 * wv * dxi * ik4pi * ir * ir * ir;   // x2: +xi and -xi
-                    const double s2 = sv * sv;
-                    project3(acc, fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp, s2, 2.0 * sv * cv,
-                             1.0 - 2.0 * s2, 2.0 * sv * cv, n0);
+                    const size_t q = (size_t)i * NTPB + tid;
+                    const double sx = 2.0 * sv * cv;
+                    gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    gS2[q] = sv * sv;
+                    gSx[q] = sx;
+                    gCm[q] = 1.0 - 2.0 * sv * sv; gC0[q] = 1.0;    // cos(-xi), cos(0)
+                    gSm[q] = -sx; gS0[q] = 0.0;                    // sin(-xi), sin(0)
                 }
                 const double xi0 = 2.0 * asin(fmin(s0, 1.0));
                 const double span = GB_PI - xi0;
@@ -349,9 +359,13 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     sincos(kr, &sn, &cs);
                     const double ir = 1.0 / R;
                     const double amp = 2.0 * wt * ik4pi * ir * ir * ir;
-                    const double s2 = st * st;
-                    project3(acc, fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp, s2, 2.0 * st * ct,
-                             1.0 - 2.0 * s2, 2.0 * st * ct, n0);
+                    const size_t q = (size_t)(NCORE_M + i) * NTPB + tid;
+                    const double sx = 2.0 * st * ct;
+                    gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    gS2[q] = st * st;
+                    gSx[q] = sx;
+                    gCm[q] = 1.0 - 2.0 * st * st; gC0[q] = 1.0;
+                    gSm[q] = -sx; gS0[q] = 0.0;
                 }
                 double cf[6];
                 bracket_coefs(rp, zp, tre, tze, rq, zq, trf, tzf, cf);
@@ -364,70 +378,83 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     for (int kk = 0; kk < 6; ++kk) wl[kk * 4 + ab] = wab * cf[kk];
                 }
             }
-            __syncthreads();        // the previous batch's GEMM has finished reading W and Gb
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-#pragma unroll
-                for (int n = 0; n < NCM; ++n) Gb[(tid * 3 + t) * NCM + n] = acc[t][n];
+            __syncthreads();                 // the previous batch's GEMM has finished reading W
 #pragma unroll
             for (int i = 0; i < 24; ++i) W[tid * 24 + i] = wl[i];
-            __syncthreads();
-            // GEMM: out(kind, ab, n) += sum_t W[t][kind, ab] Gb[t][src(kind)][n],
-            // src = C[p] for kinds 0, 2; C[p s2] for 1, 3; S for 4, 5
             const int cnt = min(NTPB, ncell - bt * NTPB);
+
+            for (int ch = 0; ch < nchunk; ++ch) {
+                const int n0 = ch * NCM;
+                double2 acc[3][NCM];
 #pragma unroll
-            for (int r = 0; r < NOUT; ++r) {
-                const int o = tid + r * NTPB;
-                if (o < 24 * NCM) {
-                    const int c24 = o / NCM, n = o % NCM;
-                    const int kind = c24 >> 2;
-                    const int src = kind >= 4 ? 2 : (kind & 1);
-                    double2 sacc = out[r];
-                    for (int t = 0; t < cnt; ++t) {
-                        const double wv = W[t * 24 + c24];
-                        const double2 gv = Gb[(t * 3 + src) * NCM + n];
-                        sacc.x = fma(wv, gv.x, sacc.x);
-                        sacc.y = fma(wv, gv.y, sacc.y);
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int n = 0; n < NCM; ++n) acc[t][n] = make_double2(0.0, 0.0);
+                if (valid) {
+                    for (int v = 0; v < nn; ++v) {
+                        const size_t q = (size_t)v * NTPB + tid;
+                        double cm1 = gCm[q], c0 = gC0[q], sm1 = gSm[q], s0 = gS0[q];
+                        project3(acc, gP[q], gS2[q], gSx[q], cm1, c0, sm1, s0);
+                        if (ch + 1 < nchunk) { gCm[q] = cm1; gC0[q] = c0; gSm[q] = sm1; gS0[q] = s0; }
                     }
-                    out[r] = sacc;
+                }
+                __syncthreads();             // the previous chunk's GEMM has finished reading Gb
+#pragma unroll
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int n = 0; n < NCM; ++n) Gb[(tid * 3 + t) * NCM + n] = acc[t][n];
+                __syncthreads();
+                // GEMM: Prim(kind, ab, n0 + n) += sum_t W[t][kind, ab] Gb[t][src(kind)][n],
+                // src = C[p] for kinds 0, 2; C[p s2] for 1, 3; S for 4, 5
+#pragma unroll
+                for (int r = 0; r < NOUT; ++r) {
+                    const int o = tid + r * NTPB;
+                    if (o < 24 * NCM) {
+                        const int c24 = o / NCM, n = o % NCM;
+                        const int kind = c24 >> 2;
+                        const int src = kind >= 4 ? 2 : (kind & 1);
+                        double2 sacc = make_double2(0.0, 0.0);
+                        for (int t = 0; t < cnt; ++t) {
+                            const double wv = W[t * 24 + c24];
+                            const double2 gv = Gb[(t * 3 + src) * NCM + n];
+                            sacc.x = fma(wv, gv.x, sacc.x);
+                            sacc.y = fma(wv, gv.y, sacc.y);
+                        }
+                        if (n0 + n < Mo) {
+                            double2 &pr = Prim[c24 * Mo + n0 + n];
+                            pr.x += sacc.x;
+                            pr.y += sacc.y;
+                        }
+                    }
                 }
             }
         }
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < NOUT; ++r) {
-            const int o = tid + r * NTPB;
-            if (o < 24 * NCM) {
-                const int c24 = o / NCM, n = n0 + o % NCM;
-                if (n < Mo) Prim[c24 * Mo + n] = out[r];
-            }
-        }
-        __syncthreads();
-    }
 
-    // blocks: Z_M = M/2 - K; K_tt = O0 + O1, K_ff = O2 + O3, K_tf = -j O4, K_ft = -j O5
-    for (int job = tid; job < Mo * 16; job += NTPB) {
-        const int m = job / 16, blk = (job / 4) % 4, ab = job % 4;
-        const int a = ab >> 1, b = ab & 1;
-        double2 K;
-        if (blk == 0 || blk == 3) {
-            const int k0 = blk == 0 ? 0 : 2;
-            const double2 u = Prim[(k0 * 4 + ab) * Mo + m], v = Prim[((k0 + 1) * 4 + ab) * Mo + m];
-            K = make_double2(u.x + v.x, u.y + v.y);
-        } else {
-            const double2 u = Prim[((blk == 1 ? 4 : 5) * 4 + ab) * Mo + m];
-            K = make_double2(u.y, -u.x);
-        }
-        double2 v = make_double2(-K.x, -K.y);
-        if (e == f && (blk == 0 || blk == 3)) v.x += 0.5 * emass[4 * e + ab];
-        const double2 sv = make_double2(sc_re * v.x - sc_im * v.y, sc_re * v.y + sc_im * v.x);
-        const int i = e + a, j = f + b;
-        if (band) {
-            double2 *dst = band + (((size_t)m * 4 + blk) * Nn + i) * 5 + (j - i + 2);
-            catomic_add(dst, sv);
-        } else {
-            const long long row = i + (blk >> 1) * Nn, col = j + (blk & 1) * Nn;
-            catomic_add(Z + (size_t)m * mode_stride + row * ldz + col, sv);
+        // blocks: Z_M = M/2 - K; K_tt = O0 + O1, K_ff = O2 + O3, K_tf = -j O4, K_ft = -j O5
+        for (int job = tid; job < Mo * 16; job += NTPB) {
+            const int m = job / 16, blk = (job / 4) % 4, ab = job % 4;
+            const int a = ab >> 1, b = ab & 1;
+            double2 K;
+            if (blk == 0 || blk == 3) {
+                const int k0 = blk == 0 ? 0 : 2;
+                const double2 u = Prim[(k0 * 4 + ab) * Mo + m], v = Prim[((k0 + 1) * 4 + ab) * Mo + m];
+                K = make_double2(u.x + v.x, u.y + v.y);
+            } else {
+                const double2 u = Prim[((blk == 1 ? 4 : 5) * 4 + ab) * Mo + m];
+                K = make_double2(u.y, -u.x);
+            }
+            double2 v = make_double2(-K.x, -K.y);
+            if (e == f && (blk == 0 || blk == 3)) v.x += 0.5 * emass[4 * e + ab];
+            const double2 sv = make_double2(sc_re * v.x - sc_im * v.y, sc_re * v.y + sc_im * v.x);
+            const int i = e + a, j = f + b;
+            if (band) {
+                double2 *dst = band + (((size_t)m * 4 + blk) * Nn + i) * 5 + (j - i + 2);
+                catomic_add(dst, sv);
+            } else {
+                const long long row = i + (blk >> 1) * Nn, col = j + (blk & 1) * Nn;
+                catomic_add(Z + (size_t)m * mode_stride + row * ldz + col, sv);
+            }
         }
     }
 }
@@ -469,17 +496,24 @@ extern "C" int ghost_bor_far_mfie(int prec, int n_elem, int m_max, int nxi, doub
     return GHOST_BOR_EINVAL;
 }
 
+extern "C" long long ghost_bor_near_mfie_workspace(int n_tail_max)
+{
+    if (n_tail_max < 0) return -1;
+    return 256 + (long long)gb::near_grid() * gb::NTPB * (gb::NCORE_M + n_tail_max) * (long long)gb::kMNodeBytes;
+}
+
 extern "C" int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale_re, double scale_im,
                                    const double *nodes, const double *elem, const double *emass,
                                    int n_pairs, const int *pairs, const int *tails,
                                    const double *cells, int n_cells_total,
                                    const double *core_gl, const double *tail_gl, int n_tail_total,
                                    double *band, void *Z, long long ldz, long long mode_stride,
-                                   void *stream)
+                                   int n_tail_max, void *work, long long work_bytes, void *stream)
 {
     using namespace gb;
     if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !emass || !pairs || !tails ||
-        !cells || !core_gl || !tail_gl || !(k > 0.0))
+        !cells || !core_gl || !tail_gl || !(k > 0.0) || n_tail_max < 0 || !work ||
+        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_near_mfie_workspace(n_tail_max))
         return GHOST_BOR_EINVAL;
     if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
     const size_t smem = NearMfieSmem::bytes(m_max + 1);
@@ -488,9 +522,13 @@ extern "C" int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale
     if (cudaFuncSetAttribute(near_mfie_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return check_launch("near_mfie: smem attribute");
-    near_mfie_kernel<<<n_pairs, NTPB, smem, st>>>(
-        n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, emass, pairs, tails, cells,
-        n_cells_total, core_gl, tail_gl, n_tail_total, reinterpret_cast<double2 *>(band),
-        reinterpret_cast<double2 *>(Z), ldz, mode_stride);
+    int *status = reinterpret_cast<int *>(work);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_mfie: memset");
+    const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
+    near_mfie_kernel<<<grid, NTPB, smem, st>>>(
+        n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, emass, n_pairs, pairs, tails, cells,
+        n_cells_total, core_gl, tail_gl, n_tail_total, NCORE_M + n_tail_max,
+        reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, mode_stride,
+        reinterpret_cast<unsigned char *>(work) + 256, status);
     return check_launch("near_mfie");
 }

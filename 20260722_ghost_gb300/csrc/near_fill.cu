@@ -1,18 +1,23 @@
-// near_fill.cu -- FP64 near/self EFIE element-pair blocks for all modes.
+// near_fill.cu -- FP64-class near/self EFIE element-pair blocks for all modes.
 //
 // Replaces the reference's refined near-pair path: graded cells
 // (bor_solver.py:54-110), the near modal kernel (bor_kernels.py:170-257:
 // sinh-graded core s in [0, s0] + Gauss tail xi in [xi0, pi]), and the near
 // loop of assemble_mode (bor_solver.py:309-336).
 //
-// One CTA per element pair (e, f), |e - f| <= 1.  Threads own Gauss-point
-// pairs of the graded cells; each evaluates G_n, n in a chunk of NC orders,
-// by the two-piece azimuth quadrature with cos(n xi) from the Chebyshev
-// recurrence (cos xi obtained from sin(xi/2) without an arcsine).  The CTA
-// then contracts the pairs with the 20 Galerkin weights (5 primitives x 2x2
-// nodes) as a small GEMM through shared memory, combines orders
-// |m-1|, m, m+1 into the four mode-m blocks and adds scale * block into the
-// output (FP64 band store or dense Z).
+// A persistent grid of CTAs walks the element pairs (e, f), |e - f| <= 1.
+// Per batch of 128 Gauss-point pairs of the graded cells, each thread first
+// evaluates its pair's azimuth nodes once -- g(xi) times the quadrature weight
+// and cos(xi), all transcendental functions in FP64 -- into a per-CTA global
+// scratch (node-major, so every access is coalesced); then, for each chunk of
+// NC orders, it projects the nodes onto cos(n xi) by the Chebyshev recurrence
+// and the CTA contracts the pairs with the 20 Galerkin weights (5 primitives x
+// 2x2 nodes) as a small GEMM through shared memory.  The FP64 transcendental
+// work is therefore done once per node instead of once per order chunk.
+// Finally the CTA combines orders |m-1|, m, m+1 into the four mode-m blocks and
+// adds scale * block into the output (FP64 band store or dense Z).
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace gb {
@@ -33,96 +38,122 @@ struct NearSmem {
     }
 };
 
-// acc[n] += (gre + j gim) cos((n0 + n) xi), n < NC, cos by the Chebyshev
-// recurrence cos((n+1) xi) = 2 cos(xi) cos(n xi) - cos((n-1) xi).
-template <bool DF, int NC>
-__device__ __forceinline__ void project(double2 (&acc)[DF ? 1 : NC], float4 (&dacc)[DF ? NC : 1],
-                                        double gre, double gim, double c1, int n0)
+// Per-node scratch of one CTA (node-major, [v][TPBN]): the weighted kernel
+// value g w, cos(xi) and the Chebyshev state (cos((n-1) xi), cos(n xi)) at the
+// start of the next order chunk.  DF: double-float words; FP64: doubles.
+template <bool DF> struct NodeT;
+template <> struct NodeT<true> { using A = float4; using B = float2; };
+template <> struct NodeT<false> { using A = double2; using B = double; };
+constexpr size_t kNodeBytes = 40;      // 16 + 3 * 8 per node and thread
+
+__device__ __forceinline__ void put_node(float4 *A, float2 *Bc, float2 *S0, float2 *S1, size_t i,
+                                         double gre, double gim, double c1)
 {
-    if constexpr (!DF) {
-        double cm1 = c1, c0 = 1.0;                  // cos(-xi), cos(0)
-        for (int n = 0; n < n0; ++n) { const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn; }
+    const float2 r = df_from(gre), m = df_from(gim), cf = df_from(c1);
+    A[i] = make_float4(r.x, r.y, m.x, m.y);
+    Bc[i] = cf;
+    S0[i] = cf;                          // cos(-xi)
+    S1[i] = make_float2(1.f, 0.f);       // cos(0)
+}
+__device__ __forceinline__ void put_node(double2 *A, double *Bc, double *S0, double *S1, size_t i,
+                                         double gre, double gim, double c1)
+{
+    A[i] = make_double2(gre, gim);
+    Bc[i] = c1;
+    S0[i] = c1;
+    S1[i] = 1.0;
+}
+
+// acc[n] += g cos((n0 + n) xi), n < NC, from the state (cm1, c0) =
+// (cos((n0-1) xi), cos(n0 xi)) by the Chebyshev recurrence
+// cos((n+1) xi) = 2 cos(xi) cos(n xi) - cos((n-1) xi); the state is advanced.
+template <int NC>
+__device__ __forceinline__ void project(double2 (&acc)[NC], double2 g, double c1, double &cm1, double &c0)
+{
 #pragma unroll
-        for (int n = 0; n < NC; ++n) {
-            acc[n].x = fma(gre, c0, acc[n].x);
-            acc[n].y = fma(gim, c0, acc[n].y);
-            const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
-        }
-    } else {
-        const float2 gr = df_from(gre), gi = df_from(gim);
-        const float2 cf = df_from(c1);
-        const float2 tc = make_float2(2.f * cf.x, 2.f * cf.y);   // exact doubling
-        float2 cm1 = cf, c0 = make_float2(1.f, 0.f);
-        for (int n = 0; n < n0; ++n) {
-            const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
-            cm1 = c0; c0 = cn;
-        }
+    for (int n = 0; n < NC; ++n) {
+        acc[n].x = fma(g.x, c0, acc[n].x);
+        acc[n].y = fma(g.y, c0, acc[n].y);
+        const double cn = 2.0 * c1 * c0 - cm1; cm1 = c0; c0 = cn;
+    }
+}
+template <int NC>
+__device__ __forceinline__ void project(float4 (&dacc)[NC], float4 g, float2 cf, float2 &cm1, float2 &c0)
+{
+    const float2 gr = make_float2(g.x, g.y), gi = make_float2(g.z, g.w);
+    const float2 tc = make_float2(2.f * cf.x, 2.f * cf.y);   // exact doubling
 #pragma unroll
-        for (int n = 0; n < NC; ++n) {
-            float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
-            df_mac(ar, gr, c0);
-            df_mac(ai, gi, c0);
-            dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
-            const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
-            cm1 = c0; c0 = cn;
-        }
+    for (int n = 0; n < NC; ++n) {
+        float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
+        df_mac(ar, gr, c0);
+        df_mac(ai, gi, c0);
+        dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
+        const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
+        cm1 = c0; c0 = cn;
     }
 }
 
-// DF = true: the cos(n xi) recurrence and the projection run in double-float
+// DF = true: the cos(m xi) recurrence and the projection run in double-float
 // (two FP32 words, ~48 bits) instead of FP64; the transcendental functions of
-// each azimuth point stay FP64.
+// each azimuth node are FP64 in both.
 template <bool DF, int NC>
-__global__ void __launch_bounds__(TPBN)
+__global__ void __launch_bounds__(TPBN, 2)
 near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
-                 const int *__restrict__ pairs, const int *__restrict__ tails,
+                 int n_pairs, const int *__restrict__ pairs, const int *__restrict__ tails,
                  const double *__restrict__ cells, int ncells_total,
                  const double *__restrict__ core_gl, const double *__restrict__ tail_gl, int ntail_total,
-                 double2 *__restrict__ band, double2 *__restrict__ Z, long long ldz, long long mode_stride)
+                 int nmax, double2 *__restrict__ band, double2 *__restrict__ Z, long long ldz,
+                 long long mode_stride, unsigned char *__restrict__ scratch, int *__restrict__ status)
 {
+    using NA = typename NodeT<DF>::A;
+    using NB = typename NodeT<DF>::B;
+    using Acc = typename std::conditional<DF, float4, double2>::type;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Mp = M + 2;
     double2 *Gb = reinterpret_cast<double2 *>(smem_raw);
     double *W = reinterpret_cast<double *>(Gb + TPBN * NC);
     double2 *Prim = reinterpret_cast<double2 *>(W + TPBN * 20);
-
-    const int pi = blockIdx.x;
-    const int e = pairs[4 * pi + 0], f = pairs[4 * pi + 1];
-    const int coff = pairs[4 * pi + 2], ncell = pairs[4 * pi + 3];
-    const int toff = tails[2 * pi + 0], ntail = tails[2 * pi + 1];
     const int tid = threadIdx.x;
 
-    const double rho_e0 = nodes[2 * e], z_e0 = nodes[2 * e + 1];
-    const double drho_e = nodes[2 * e + 2] - rho_e0, dz_e = nodes[2 * e + 3] - z_e0;
-    const double rho_f0 = nodes[2 * f], z_f0 = nodes[2 * f + 1];
-    const double drho_f = nodes[2 * f + 2] - rho_f0, dz_f = nodes[2 * f + 3] - z_f0;
-    const double Le = elem[e], Lf = elem[f];
+    const size_t plane = (size_t)nmax * TPBN;
+    NA *gA = reinterpret_cast<NA *>(scratch + (size_t)blockIdx.x * plane * kNodeBytes);
+    NB *gC = reinterpret_cast<NB *>(gA + plane);
+    NB *gS0 = gC + plane;
+    NB *gS1 = gS0 + plane;
+
+    constexpr int NOUT = (20 * NC + TPBN - 1) / TPBN;
+    const int nchunk = (Mp + NC - 1) / NC;
     const double kk = k;
 
-    for (int i = tid; i < 20 * Mp; i += TPBN) Prim[i] = make_double2(0.0, 0.0);
+    for (int pi = blockIdx.x; pi < n_pairs; pi += gridDim.x) {
+        const int e = pairs[4 * pi + 0], f = pairs[4 * pi + 1];
+        const int coff = pairs[4 * pi + 2], ncell = pairs[4 * pi + 3];
+        const int toff = tails[2 * pi + 0], ntail = tails[2 * pi + 1];
+        const int nn = NCORE + ntail;
+        if (nn > nmax) {                     // scratch sized for a smaller tail order
+            if (tid == 0) atomicExch(status, 1);
+            continue;
+        }
+        const double rho_e0 = nodes[2 * e], z_e0 = nodes[2 * e + 1];
+        const double drho_e = nodes[2 * e + 2] - rho_e0, dz_e = nodes[2 * e + 3] - z_e0;
+        const double rho_f0 = nodes[2 * f], z_f0 = nodes[2 * f + 1];
+        const double drho_f = nodes[2 * f + 2] - rho_f0, dz_f = nodes[2 * f + 3] - z_f0;
+        const double Le = elem[e], Lf = elem[f];
 
-    const int nbatch = (ncell + TPBN - 1) / TPBN;
-    const int nchunk = (Mp + NC - 1) / NC;
-    for (int ch = 0; ch < nchunk; ++ch) {
-        const int n0 = ch * NC;
-        double2 out[(20 * NC + TPBN - 1) / TPBN];
-#pragma unroll
-        for (int r = 0; r < (20 * NC + TPBN - 1) / TPBN; ++r) out[r] = make_double2(0.0, 0.0);
+        __syncthreads();                     // the previous pair has finished reading Prim
+        for (int i = tid; i < 20 * Mp; i += TPBN) Prim[i] = make_double2(0.0, 0.0);
 
+        const int nbatch = (ncell + TPBN - 1) / TPBN;
         for (int bt = 0; bt < nbatch; ++bt) {
             const int c = bt * TPBN + tid;
-            double2 acc[DF ? 1 : NC];   // FP64 projection
-            float4 dacc[DF ? NC : 1];   // double-float projection: (re.hi, re.lo, im.hi, im.lo)
+            const bool valid = c < ncell;
+            bool on_axis = false;
             double2 axis0 = make_double2(0.0, 0.0);   // order-0 term of an on-axis pair
             double wl[20];
 #pragma unroll
-            for (int n = 0; n < (DF ? 1 : NC); ++n) acc[n] = make_double2(0.0, 0.0);
-#pragma unroll
-            for (int n = 0; n < (DF ? NC : 1); ++n) dacc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
             for (int i = 0; i < 20; ++i) wl[i] = 0.0;
-            if (c < ncell) {
+            if (valid) {
                 const double s = cells[coff + c];
                 const double sp = cells[ncells_total + coff + c];
                 const double wc = cells[2 * ncells_total + coff + c];
@@ -135,13 +166,12 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                 const double d2 = dr * dr + dz * dz;
                 const double rr4 = 4.0 * rp * rq;
                 if (rr4 <= 1e-30) {
-                    if (n0 == 0) {
-                        const double R0 = sqrt(d2);
-                        double sn, cs;
-                        sincos(kk * R0, &sn, &cs);
-                        const double amp = 2.0 * GB_PI / (4.0 * GB_PI * fmax(R0, 1e-300));
-                        axis0 = make_double2(amp * cs, -amp * sn);
-                    }
+                    on_axis = true;
+                    const double R0 = sqrt(d2);
+                    double sn, cs;
+                    sincos(kk * R0, &sn, &cs);
+                    const double amp = 2.0 * GB_PI / (4.0 * GB_PI * fmax(R0, 1e-300));
+                    axis0 = make_double2(amp * cs, -amp * sn);
                 } else {
                     const double d = sqrt(fmax(d2, 1e-300));
                     const double a = sqrt(rr4);
@@ -159,9 +189,8 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
                         const double gw = 2.0 * wv * dxi / (4.0 * GB_PI * R);
-                        const double gre = gw * cs, gim = -gw * sn;
-                        const double c1 = 1.0 - 2.0 * sv * sv;     // cos(xi)
-                        project<DF, NC>(acc, dacc, gre, gim, c1, n0);
+                        put_node(gA, gC, gS0, gS1, (size_t)i * TPBN + tid, gw * cs, -gw * sn,
+                                 1.0 - 2.0 * sv * sv);
                     }
                     // -- Gauss tail on [xi0, pi]
                     const double xi0 = 2.0 * asin(s0);
@@ -175,118 +204,146 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
                         const double gw = 2.0 * wt / (4.0 * GB_PI * R);
-                        const double gre = gw * cs, gim = -gw * sn;
-                        const double c1 = 1.0 - 2.0 * st * st;
-                        project<DF, NC>(acc, dacc, gre, gim, c1, n0);
+                        put_node(gA, gC, gS0, gS1, (size_t)(NCORE + i) * TPBN + tid, gw * cs, -gw * sn,
+                                 1.0 - 2.0 * st * st);
                     }
                 }
-                {
-                    // Galerkin weights of this point pair (computed after the
-                    // quadrature to keep them out of the registers it needs)
-                    const double Tp[2] = {1.0 - s, s}, Tq[2] = {1.0 - sp, sp};
-                    const double Dp[2] = {(drho_e * (1.0 - s) - rp) / Le, (drho_e * s + rp) / Le};
-                    const double Dq[2] = {(drho_f * (1.0 - sp) - rq) / Lf, (drho_f * sp + rq) / Lf};
-                    const double rr = rp * rq * w;
+                // Galerkin weights of this point pair
+                const double Tp[2] = {1.0 - s, s}, Tq[2] = {1.0 - sp, sp};
+                const double Dp[2] = {(drho_e * (1.0 - s) - rp) / Le, (drho_e * s + rp) / Le};
+                const double Dq[2] = {(drho_f * (1.0 - sp) - rq) / Lf, (drho_f * sp + rq) / Lf};
+                const double rr = rp * rq * w;
 #pragma unroll
-                    for (int a = 0; a < 2; ++a)
+                for (int a = 0; a < 2; ++a)
 #pragma unroll
-                        for (int b = 0; b < 2; ++b) {
-                            const int ab = a * 2 + b;
-                            wl[0 * 4 + ab] = Tp[a] * Tq[b] * rr;   // A1
-                            wl[1 * 4 + ab] = Dp[a] * Dq[b] * w;    // Add
-                            wl[2 * 4 + ab] = Dp[a] * Tq[b] * w;    // Ads
-                            wl[3 * 4 + ab] = Tp[a] * Dq[b] * w;    // Asd
-                            wl[4 * 4 + ab] = Tp[a] * Tq[b] * w;    // Ass
-                        }
-                }
+                    for (int b = 0; b < 2; ++b) {
+                        const int ab = a * 2 + b;
+                        wl[0 * 4 + ab] = Tp[a] * Tq[b] * rr;   // A1
+                        wl[1 * 4 + ab] = Dp[a] * Dq[b] * w;    // Add
+                        wl[2 * 4 + ab] = Dp[a] * Tq[b] * w;    // Ads
+                        wl[3 * 4 + ab] = Tp[a] * Dq[b] * w;    // Asd
+                        wl[4 * 4 + ab] = Tp[a] * Tq[b] * w;    // Ass
+                    }
             }
-            __syncthreads();        // the previous batch's GEMM has finished reading W and Gb
-            if constexpr (DF) {
-#pragma unroll
-                for (int n = 0; n < NC; ++n)
-                    Gb[tid * NC + n] = make_double2((double)dacc[n].x + (double)dacc[n].y,
-                                                    (double)dacc[n].z + (double)dacc[n].w);
-            } else {
-#pragma unroll
-                for (int n = 0; n < NC; ++n) Gb[tid * NC + n] = acc[n];
-            }
-            if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
+            __syncthreads();                 // the previous batch's GEMM has finished reading W
 #pragma unroll
             for (int i = 0; i < 20; ++i) W[tid * 20 + i] = wl[i];
-            __syncthreads();
-            // GEMM: out(c20, n) += sum_t W[t][c20] Gb[t][n]
             const int cnt = min(TPBN, ncell - bt * TPBN);
+
+            for (int ch = 0; ch < nchunk; ++ch) {
+                const int n0 = ch * NC;
+                Acc acc[NC];
 #pragma unroll
-            for (int r = 0; r < (20 * NC + TPBN - 1) / TPBN; ++r) {
-                const int o = tid + r * TPBN;
-                if (o < 20 * NC) {
-                    const int c20 = o / NC, n = o % NC;
-                    double2 sacc = out[r];
-                    for (int t = 0; t < cnt; ++t) {
-                        const double wv = W[t * 20 + c20];
-                        const double2 gv = Gb[t * NC + n];
-                        sacc.x = fma(wv, gv.x, sacc.x);
-                        sacc.y = fma(wv, gv.y, sacc.y);
+                for (int n = 0; n < NC; ++n) {
+                    if constexpr (DF) acc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    else acc[n] = make_double2(0.0, 0.0);
+                }
+                if (valid && !on_axis) {
+                    for (int v = 0; v < nn; ++v) {
+                        const size_t i = (size_t)v * TPBN + tid;
+                        NB cm1 = gS0[i], c0 = gS1[i];
+                        project<NC>(acc, gA[i], gC[i], cm1, c0);
+                        if (ch + 1 < nchunk) { gS0[i] = cm1; gS1[i] = c0; }
                     }
-                    out[r] = sacc;
+                }
+                __syncthreads();             // the previous chunk's GEMM has finished reading Gb
+#pragma unroll
+                for (int n = 0; n < NC; ++n) {
+                    if constexpr (DF)
+                        Gb[tid * NC + n] = make_double2((double)acc[n].x + (double)acc[n].y,
+                                                        (double)acc[n].z + (double)acc[n].w);
+                    else
+                        Gb[tid * NC + n] = acc[n];
+                }
+                if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
+                __syncthreads();
+                // GEMM: Prim(c20, n0 + n) += sum_t W[t][c20] Gb[t][n]; each (c20, n)
+                // belongs to one thread, so the accumulation needs no atomics
+#pragma unroll
+                for (int r = 0; r < NOUT; ++r) {
+                    const int o = tid + r * TPBN;
+                    if (o < 20 * NC) {
+                        const int c20 = o / NC, n = o % NC;
+                        double2 sacc = make_double2(0.0, 0.0);
+                        for (int t = 0; t < cnt; ++t) {
+                            const double wv = W[t * 20 + c20];
+                            const double2 gv = Gb[t * NC + n];
+                            sacc.x = fma(wv, gv.x, sacc.x);
+                            sacc.y = fma(wv, gv.y, sacc.y);
+                        }
+                        if (n0 + n < Mp) {
+                            double2 &pr = Prim[c20 * Mp + n0 + n];
+                            pr.x += sacc.x;
+                            pr.y += sacc.y;
+                        }
+                    }
                 }
             }
         }
         __syncthreads();
-#pragma unroll
-        for (int r = 0; r < (20 * NC + TPBN - 1) / TPBN; ++r) {
-            const int o = tid + r * TPBN;
-            if (o < 20 * NC) {
-                const int c20 = o / NC, n = n0 + o % NC;
-                if (n < Mp) Prim[c20 * Mp + n] = out[r];
-            }
-        }
-        __syncthreads();
-    }
 
-    // mode combination: job = (m, blk, ab)
-    const double ik2 = 1.0 / (kk * kk);
-    const double tre = elem[N + e], tze = elem[2 * N + e];
-    const double trf = elem[N + f], tzf = elem[2 * N + f];
-    for (int job = tid; job < (M + 1) * 16; job += TPBN) {
-        const int m = job / 16, blk = (job / 4) % 4, ab = job % 4;
-        const int a = ab >> 1, b = ab & 1;
-        const int ml = abs(m - 1), mh = m + 1;
-        const double2 lo = Prim[(0 * 4 + ab) * Mp + ml], hi = Prim[(0 * 4 + ab) * Mp + mh];
-        const double2 A1 = Prim[(0 * 4 + ab) * Mp + m];
-        const double2 S = make_double2(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y));          // A1(Gc)
-        const double2 Dh = make_double2(0.5 * (lo.x - hi.x), 0.5 * (lo.y - hi.y));         // (A1lo - A1hi)/2
-        const double2 Gs = make_double2(Dh.y, -Dh.x);                                       // A1(Gs) = Dh / j
-        const double fm = m * ik2, fm2 = (double)m * m * ik2;
-        double2 v;
-        if (blk == 0) {
-            const double2 Add = Prim[(1 * 4 + ab) * Mp + m];
-            v = make_double2(tre * trf * S.x + tze * tzf * A1.x - ik2 * Add.x,
-                             tre * trf * S.y + tze * tzf * A1.y - ik2 * Add.y);
-        } else if (blk == 1) {
-            const double2 Ads = Prim[(2 * 4 + ab) * Mp + m];
-            v = make_double2(tre * Gs.x + fm * Ads.y, tre * Gs.y - fm * Ads.x);
-        } else if (blk == 2) {
-            const double2 Asd = Prim[(3 * 4 + ab) * Mp + m];
-            v = make_double2(-trf * Gs.x - fm * Asd.y, -trf * Gs.y + fm * Asd.x);
-        } else {
-            const double2 Ass = Prim[(4 * 4 + ab) * Mp + m];
-            v = make_double2(S.x - fm2 * Ass.x, S.y - fm2 * Ass.y);
-        }
-        const double2 sv = make_double2(sc_re * v.x - sc_im * v.y, sc_re * v.y + sc_im * v.x);
-        const int i = e + a, j = f + b;
-        if (band) {
-            double2 *dst = band + (((size_t)m * 4 + blk) * Nn + i) * 5 + (j - i + 2);
-            catomic_add(dst, sv);
-        } else {
-            const long long row = i + (blk >> 1) * Nn, col = j + (blk & 1) * Nn;
-            catomic_add(Z + (size_t)m * mode_stride + row * ldz + col, sv);
+        // mode combination: job = (m, blk, ab)
+        const double ik2 = 1.0 / (kk * kk);
+        const double tre = elem[N + e], tze = elem[2 * N + e];
+        const double trf = elem[N + f], tzf = elem[2 * N + f];
+        for (int job = tid; job < (M + 1) * 16; job += TPBN) {
+            const int m = job / 16, blk = (job / 4) % 4, ab = job % 4;
+            const int a = ab >> 1, b = ab & 1;
+            const int ml = abs(m - 1), mh = m + 1;
+            const double2 lo = Prim[(0 * 4 + ab) * Mp + ml], hi = Prim[(0 * 4 + ab) * Mp + mh];
+            const double2 A1 = Prim[(0 * 4 + ab) * Mp + m];
+            const double2 S = make_double2(0.5 * (lo.x + hi.x), 0.5 * (lo.y + hi.y));          // A1(Gc)
+            const double2 Dh = make_double2(0.5 * (lo.x - hi.x), 0.5 * (lo.y - hi.y));         // (A1lo - A1hi)/2
+            const double2 Gs = make_double2(Dh.y, -Dh.x);                                       // A1(Gs) = Dh / j
+            const double fm = m * ik2, fm2 = (double)m * m * ik2;
+            double2 v;
+            if (blk == 0) {
+                const double2 Add = Prim[(1 * 4 + ab) * Mp + m];
+                v = make_double2(tre * trf * S.x + tze * tzf * A1.x - ik2 * Add.x,
+                                 tre * trf * S.y + tze * tzf * A1.y - ik2 * Add.y);
+            } else if (blk == 1) {
+                const double2 Ads = Prim[(2 * 4 + ab) * Mp + m];
+                v = make_double2(tre * Gs.x + fm * Ads.y, tre * Gs.y - fm * Ads.x);
+            } else if (blk == 2) {
+                const double2 Asd = Prim[(3 * 4 + ab) * Mp + m];
+                v = make_double2(-trf * Gs.x - fm * Asd.y, -trf * Gs.y + fm * Asd.x);
+            } else {
+                const double2 Ass = Prim[(4 * 4 + ab) * Mp + m];
+                v = make_double2(S.x - fm2 * Ass.x, S.y - fm2 * Ass.y);
+            }
+            const double2 sv = make_double2(sc_re * v.x - sc_im * v.y, sc_re * v.y + sc_im * v.x);
+            const int i = e + a, j = f + b;
+            if (band) {
+                double2 *dst = band + (((size_t)m * 4 + blk) * Nn + i) * 5 + (j - i + 2);
+                catomic_add(dst, sv);
+            } else {
+                const long long row = i + (blk >> 1) * Nn, col = j + (blk & 1) * Nn;
+                catomic_add(Z + (size_t)m * mode_stride + row * ldz + col, sv);
+            }
         }
     }
 }
 
 }  // namespace
 }  // namespace gb
+
+namespace gb {
+// persistent grid of the near kernels: two CTAs per SM
+int near_grid()
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 1;
+    return 2 * sms;
+}
+}  // namespace gb
+
+extern "C" long long ghost_bor_near_workspace(int n_tail_max)
+{
+    if (n_tail_max < 0) return -1;
+    return 256 + (long long)gb::near_grid() * gb::TPBN * (gb::NCORE + n_tail_max) * (long long)gb::kNodeBytes;
+}
 
 extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
                                    double scale_re, double scale_im,
@@ -295,11 +352,12 @@ extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
                                    const double *cells, int n_cells_total,
                                    const double *core_gl, const double *tail_gl, int n_tail_total,
                                    double *band, void *Z, long long ldz, long long mode_stride,
-                                   void *stream)
+                                   int n_tail_max, void *work, long long work_bytes, void *stream)
 {
     using namespace gb;
     if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !pairs || !tails || !cells ||
-        !core_gl || !tail_gl || !(k > 0.0))
+        !core_gl || !tail_gl || !(k > 0.0) || n_tail_max < 0 || !work ||
+        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_near_workspace(n_tail_max))
         return GHOST_BOR_EINVAL;
     if (prec != GHOST_BOR_F32 && prec != GHOST_BOR_F64) return GHOST_BOR_EINVAL;
     if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
@@ -310,9 +368,13 @@ extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
     auto kern = df ? near_efie_kernel<true, kNcDf> : near_efie_kernel<false, kNc64>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("near_efie: smem attribute");
-    kern<<<n_pairs, TPBN, smem, st>>>(
-        n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, pairs, tails, cells,
-        n_cells_total, core_gl, tail_gl, n_tail_total, reinterpret_cast<double2 *>(band),
-        reinterpret_cast<double2 *>(Z), ldz, mode_stride);
+    int *status = reinterpret_cast<int *>(work);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_efie: memset");
+    const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
+    kern<<<grid, TPBN, smem, st>>>(
+        n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, n_pairs, pairs, tails, cells,
+        n_cells_total, core_gl, tail_gl, n_tail_total, NCORE + n_tail_max,
+        reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, mode_stride,
+        reinterpret_cast<unsigned char *>(work) + 256, status);
     return check_launch("near_efie");
 }

@@ -97,6 +97,8 @@ class BorGpuProblem:
         # the far kernels sample exp(-jkR)/R; the table carries the 1/(4 pi)
         dct, sin2 = dct_tables(self.n_xi, self.m_max + 2, scale=1.0 / (4.0 * math.pi))
         self.near = near_tables(self.gen, self.k, self.m_max)
+        self.n_tail_max = int(np.max(self.near.tails[:, 1]))
+        self._near_ws: Dict[str, object] = {}
         self.masks = mask_rows(self.gen, self.m_max)
         dev = self.device
         f64 = torch.float64
@@ -163,14 +165,32 @@ class BorGpuProblem:
                  scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_dct),
                  nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), stream)
 
+    def _near_work(self, name: str):
+        """Scratch of a near kernel (azimuth nodes of every resident CTA) and
+        its status word; kept on the problem so its lifetime covers the launch."""
+        lib = nat.load()
+        nbytes = int(getattr(lib, name)(self.n_tail_max))
+        work = self._near_ws.get(name)
+        if work is None or work.numel() < nbytes:
+            work = self.torch.empty(nbytes, dtype=self.torch.uint8, device=self.device)
+            self._near_ws[name] = work
+        return work, nbytes
+
+    def check_near_status(self):
+        for name, work in self._near_ws.items():
+            if int(work[:4].view(self.torch.int32)[0]) != 0:
+                raise RuntimeError(f"near kernel scratch too small ({name})")
+
     def fill_near(self, scale: complex, stream: int, band=None, Z=None, precision: int = nat.F64):
         ld = 0 if Z is None else Z.shape[-1]
         ms = 0 if Z is None else Z.stride(0)
+        work, nbytes = self._near_work("ghost_bor_near_workspace")
         nat.call("ghost_bor_near_efie", precision, self.N, self.m_max, self.k, scale.real, scale.imag,
                  nat.ptr(self.d_nodes), nat.ptr(self.d_elem), len(self.near.pairs),
                  nat.ptr(self.d_pairs), nat.ptr(self.d_tails), nat.ptr(self.d_cells),
                  self.near.cells.shape[1], nat.ptr(self.d_core), nat.ptr(self.d_tail),
-                 self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms, stream)
+                 self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
+                 self.n_tail_max, nat.ptr(work), nbytes, stream)
 
     def fill_far_mfie(self, Z, precision: int, scale: complex, stream: int):
         ld = Z.shape[-1]
@@ -181,12 +201,13 @@ class BorGpuProblem:
     def fill_near_mfie(self, scale: complex, stream: int, band=None, Z=None):
         ld = 0 if Z is None else Z.shape[-1]
         ms = 0 if Z is None else Z.stride(0)
+        work, nbytes = self._near_work("ghost_bor_near_mfie_workspace")
         nat.call("ghost_bor_near_mfie", self.N, self.m_max, self.k, scale.real, scale.imag,
                  nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(self.d_emass),
                  len(self.near.pairs), nat.ptr(self.d_pairs), nat.ptr(self.d_tails),
                  nat.ptr(self.d_cells), self.near.cells.shape[1], nat.ptr(self.d_core),
                  nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
-                 stream)
+                 self.n_tail_max, nat.ptr(work), nbytes, stream)
 
     def fill_operator_far(self, Z, precision: int, stream: int):
         """Far parts of A = alpha C Z_E + (1 - alpha) eta0 Z_M into Z."""
@@ -236,6 +257,7 @@ class BorGpuProblem:
         Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
         self.fill_far_mfie(Z, nat.F64, 1.0 + 0.0j, st)
         self.fill_near_mfie(1.0 + 0.0j, st, Z=Z)
+        self.check_near_status()
         return Z
 
     def assemble_modes_fp64(self, stream: Optional[int] = None):
@@ -246,6 +268,7 @@ class BorGpuProblem:
         Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
         self.fill_operator_far(Z, nat.F64, st)
         self.fill_operator_near(st, Z=Z)
+        self.check_near_status()
         return Z
 
     # -- the sweep ---------------------------------------------------------
@@ -416,6 +439,7 @@ class BorGpuProblem:
         res = torch.sqrt(norms[:, 0] / torch.clamp(norms[:, 1], min=1e-300)).cpu().numpy()
         info_h = info.cpu().numpy()
         torch.cuda.synchronize()
+        self.check_near_status()
         names = list(ev)
         tm = {f"{b}_s": ev[a].elapsed_time(ev[b]) / 1e3 for a, b in zip(names[:-1], names[1:])}
         tm["gpu_total_s"] = ev[names[0]].elapsed_time(ev[names[-1]]) / 1e3

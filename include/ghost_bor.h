@@ -102,6 +102,16 @@ int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
                        void *Z, long long ldz, long long mode_stride,
                        void *stream);
 
+/* ghost_bor_far_efie restricted to the far pairs (e, f) with elem_mask[e] or
+ * elem_mask[f] nonzero (elem_mask: n_elem bytes on the device; NULL = all
+ * pairs).  Used by the adjoint gradient to fill the operator change of a
+ * local shape perturbation.  No counterpart in the reference. */
+int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k,
+                              double scale_re, double scale_im,
+                              const double *geo, const double *dct, const double *sin2,
+                              void *Z, long long ldz, long long mode_stride,
+                              const unsigned char *elem_mask, void *stream);
+
 /* ------------------------------------------------------------------------
  * FP64 near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
  * the graded-cell + sinh-core + Gauss-tail quadrature of the reference.
@@ -115,9 +125,15 @@ int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
  * dense complex double Z[m].  `prec` selects the arithmetic of the cos(m xi)
  * projection: GHOST_BOR_F64 = FP64, GHOST_BOR_F32 = double-float (two FP32
  * words, ~48-bit); the azimuth-point transcendentals are FP64 in both.
+ * work: ghost_bor_near_workspace(n_tail_max) bytes, 256-byte aligned, where
+ * n_tail_max >= every n_tail of `tails`; its first int is a status word set to
+ * 1 if a pair had a larger n_tail (that pair is then skipped).  Each CTA of the
+ * persistent grid keeps the azimuth nodes of its 128 point pairs there, so
+ * the FP64 transcendental functions run once per node.
  * Replaces _near_pair_data + modal_kernels_near + the near loop of
  * assemble_mode (bor_solver.py:270-336, bor_kernels.py:170-257).
  */
+long long ghost_bor_near_workspace(int n_tail_max);
 int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
                         double scale_re, double scale_im,
                         const double *nodes, const double *elem,
@@ -125,7 +141,7 @@ int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
                         const double *cells, int n_cells_total,
                         const double *core_gl, const double *tail_gl, int n_tail_total,
                         double *band, void *Z, long long ldz, long long mode_stride,
-                        void *stream);
+                        int n_tail_max, void *work, long long work_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
  * Fused MFIE far fill: for every far element pair (|e - f| >= 2) sample
@@ -160,16 +176,19 @@ int ghost_bor_far_mfie(int prec, int n_elem, int m_max, int nxi, double k,
  * dense Z (layouts as in ghost_bor_near_efie).
  *   emass [n_elem][4] element mass contributions 2 pi sum_g T_a T_b w rho
  *         for (a, b) = (0,0), (0,1), (1,0), (1,1)
+ *   work  ghost_bor_near_mfie_workspace(n_tail_max) bytes, as in
+ *         ghost_bor_near_efie
  * Replaces mfie_kernels_near, _near_mfie_data, mass_blocks and the near loop
  * of assemble_mfie_mode (bor_kernels.py:334-431, bor_solver.py:372-435).
  */
+long long ghost_bor_near_mfie_workspace(int n_tail_max);
 int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale_re, double scale_im,
                         const double *nodes, const double *elem, const double *emass,
                         int n_pairs, const int *pairs, const int *tails,
                         const double *cells, int n_cells_total,
                         const double *core_gl, const double *tail_gl, int n_tail_total,
                         double *band, void *Z, long long ldz, long long mode_stride,
-                        void *stream);
+                        int n_tail_max, void *work, long long work_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
  * Excitation for all modes 0..m_max, angles and both polarisations:

@@ -163,3 +163,21 @@ def test_bessel_rhs_against_scipy(pkg, torch):
             P = np.exp(1j * k * math.cos(t) * g.z)
             want = np.concatenate([s.B_T @ (g.w * g.rho * P * g.trho * Is), s.B_T @ (g.w * g.rho * P * Ic)])
             assert rel(v, want) < 1e-12, (m, th)
+
+
+@pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40"])
+def test_near_band_double_float_matches_fp64(pkg, torch, name):
+    """The double-float near projection (FP32 path) reproduces the FP64 near band."""
+    D = load_golden(name)
+    eng = pkg.engine
+    nat = pkg._native
+    prob = eng.BorGpuProblem(D["points"], float(D["freq_hz"]), D["thetas"], m_max=int(D["m_max"]))
+    Mb = prob.m_max + 1
+    b64 = torch.zeros((Mb, 4, prob.Nn, 5), dtype=torch.complex128, device="cuda")
+    b32 = torch.zeros_like(b64)
+    st = nat.stream_handle()
+    prob.fill_near(prob.C, st, band=b64, precision=nat.F64)
+    prob.fill_near(prob.C, st, band=b32, precision=nat.F32)
+    torch.cuda.synchronize()
+    prob.check_near_status()
+    assert (b32 - b64).abs().max().item() < 1e-12 * b64.abs().max().item()

@@ -49,3 +49,48 @@ def test_truncation_replay(pkg, oracle):
             else:
                 quiet = 0
         assert used == used_r and np.array_equal(F, Fr)
+
+
+def test_adjoint_identity_on_oracle(pkg, oracle):
+    """The gradient formula of the adjoint module, dF = s c [2 (Dx)^T dV -
+    (Dx)^T dZ x] (reciprocity adjoint y = D x), against a central difference
+    of the oracle's far field for a B-spline body; and Z^T = D Z D up to the
+    quadrature's symmetry."""
+    O = oracle
+    bodies = pkg.bodies
+    radii = np.random.default_rng(0).uniform(0.3, 0.6, 6)
+    N, k, M, m = 30, 6.0, 3, 2
+    f = k * O.C0 / (2 * np.pi)
+    th = np.array([35.0, 50.0])
+
+    def build(r):
+        s = O.OracleSolver(bodies.bspline_body(r, N)[0], f)
+        s.build_far(M, efie=True)
+        return s
+
+    s0 = build(radii)
+    Nn = s0.geo.Nn
+    D = np.concatenate([np.ones(Nn), -np.ones(Nn)])
+    Z = s0.assemble_efie(m, M)
+    assert np.max(np.abs(Z.T - D[:, None] * Z * D[None, :])) < 1e-4 * np.max(np.abs(Z))
+    mask = s0.basis_mask(m)
+    c = -1j * k * O.ETA0 / (4 * np.pi)
+
+    def field(s):
+        A = s.assemble_efie(m, M)[np.ix_(mask, mask)]
+        V = s.rhs_efie(m, th, "HH")[:, mask].T
+        x = np.linalg.solve(A, V)
+        return -c * np.sum(D[mask][:, None] * V * x, axis=0), A, V, x
+
+    _, A0, V0, x0 = field(s0)
+    h, j = 1e-5, 2
+    rp, rm = radii.copy(), radii.copy()
+    rp[j] += h
+    rm[j] -= h
+    Fp, Ap, Vp, _ = field(build(rp))
+    Fm, Am, Vm, _ = field(build(rm))
+    dZ, dV = (Ap - Am) / (2 * h), (Vp - Vm) / (2 * h)
+    Dx = D[mask][:, None] * x0
+    adj = -c * (2 * np.sum(Dx * dV, axis=0) - np.sum(Dx * (dZ @ x0), axis=0))
+    fd = (Fp - Fm) / (2 * h)
+    assert np.max(np.abs(adj - fd)) < 1e-5 * np.max(np.abs(fd))
