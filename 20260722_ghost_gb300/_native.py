@@ -49,8 +49,12 @@ SIGNATURES = {
     "ghost_bor_getrs": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_residual": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
                                 _vp, _vp, _vp, _vp]),
-    "ghost_bor_residual_x32": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
+    "ghost_bor_residual_x32": (_i, [_i, _i, _i, _i, _vp, _i, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
                                     _vp, _vp, _vp, _vp]),
+    "ghost_bor_split_words": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp]),
+    "ghost_bor_residual_exact_workspace": (_ll, [_i, _i, _i]),
+    "ghost_bor_residual_exact": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp, _ll, _ll,
+                                      _vp, _vp, _vp, _vp, _ll, _vp]),
     "ghost_bor_residual64": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp, _vp, _ll, _ll, _vp, _vp, _vp]),
     "ghost_bor_farfield": (_i, [_i, _i, _i, _i, _i, _d, _vp, _vp, _ll, _ll, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_compose": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _ll, _ll, _vp]),

@@ -6,12 +6,16 @@ reciprocity (the farfield kernel of this package),
 
     F = s c (D V)^T x,    Z x = V,    c = -j k eta0 / (4 pi),
 
-s = +1 for VV (F_theta), -1 for HH (F_phi), D = diag(I, -I).  The Galerkin
-BoR EFIE operator satisfies Z^T = D Z D (to the symmetry of its quadrature,
-~1e-5 relative: the near cells use a source order one above the test order),
-so the adjoint solution of D V is D x and no extra solve is needed:
+s = +1 for VV (F_theta), -1 for HH (F_phi), D = diag(I, -I), so
 
-    dF = s c [ 2 (D x)^T dV - (D x)^T dZ x ].
+    dF = s c [ (D x)^T dV + y^T dV - y^T dZ x ],    Z^T y = D V.
+
+The Galerkin BoR EFIE operator satisfies Z^T = D Z D up to the symmetry of
+its quadrature (~1e-5 relative: the near cells use a source order one above
+the test order), so y = D x + delta with Z^T delta = s := D V - Z^T D x, a
+small right-hand side; delta = D Z^-1 D s to first order in the asymmetry,
+one solve with the factors of the sweep.  s uses the unfactored fl32(Z)
+(its error, 6e-8, is far below the asymmetry it resolves).
 
 For J = mean over angles of sigma = 4 pi |F|^2 (F summed over m with the mode
 weights 1, 2, 2, ...), dJ/dp = mean 8 pi Re(conj(F) dF/dp).
@@ -62,27 +66,44 @@ class ShapeGradient:
     """dJ/dp for J = mean_theta sigma_pol(theta) of one body, given the
     converged solution of its sweep (EFIE, PEC)."""
 
-    def __init__(self, prob: BorGpuProblem, X, F: np.ndarray, pol: str, h: float = 1e-5):
+    def __init__(self, prob: BorGpuProblem, res, F: np.ndarray, pol: str, h: float = 1e-5):
         if prob.alpha != 1.0:
             raise NotImplementedError("the adjoint gradient covers the EFIE formulation")
         self.prob = prob
         self.torch = prob.torch
-        self.X = X                               # [Mb, n, nrhs] complex128, device
         self.pol = _POLS[pol.upper()]
         self.F = F                               # [2, T] complex128, host
         self.h = float(h)
         t = self.torch
-        Mb, n = prob.m_max + 1, prob.n
-        self.cols = t.arange(prob.T, device=prob.device) * 2 + self.pol
-        Xp = X[:, :, self.cols]                  # [Mb, n, T]
+        Mb, n, T = prob.m_max + 1, prob.n, prob.T
+        self.cols = t.arange(T, device=prob.device) * 2 + self.pol
         d = t.ones(n, dtype=t.float64, device=prob.device)
         d[prob.Nn:] = -1.0
-        self.Xp = Xp.contiguous()
-        self.DX = (d[None, :, None] * Xp).contiguous()
+        self.Xp = res.X[:, :, self.cols].contiguous()          # [Mb, n, T]
+        self.DX = (d[None, :, None] * self.Xp).contiguous()
+        self.Y = self._adjoint(res, d)
+        self.Xp32 = self.Xp.to(t.complex64)
         self.mode_w = prob.d_mode_w.to(t.complex128)
         self.dZ = t.empty((Mb, n, n), dtype=t.complex128, device=prob.device)
         self.V2 = t.empty((2, Mb, n, prob.nrhs), dtype=t.complex128, device=prob.device)
         self.rhs_work = None
+
+    def _adjoint(self, res, d):
+        """y = Z^-T D V = D x + D Z^-1 D s, s = D V - Z^T D x (see the module docstring)."""
+        t = self.torch
+        p = self.prob
+        lu = res.lu
+        Mb, n, T = p.m_max + 1, p.n, p.T
+        V = res.Ve[:, :, self.cols]
+        DV = d[None, :, None] * V
+        op = lu["op"]
+        ZtDx = t.bmm(op.transpose(1, 2), self.DX.to(op.dtype)).to(t.complex128)
+        Ds = d[None, :, None] * (DV - ZtDx)
+        rdt = t.complex64 if lu["prec"] == nat.F32 else t.complex128
+        w = Ds.to(rdt).contiguous()
+        nat.call("ghost_bor_getrs", lu["prec"], Mb, n, T, nat.ptr(lu["A"]), n, lu["A"].stride(0),
+                 nat.ptr(lu["ipiv"]), nat.ptr(w), T, w.stride(0), nat.ptr(lu["work"]), nat.stream_handle())
+        return (self.DX + d[None, :, None] * w.to(t.complex128)).contiguous()
 
     def _fill(self, tabs: _Tables, scale: complex, emask, pairs, tails, st):
         p = self.prob
@@ -132,8 +153,9 @@ class ShapeGradient:
         self._excite(plus, self.V2[0], st)
         self._excite(minus, self.V2[1], st)
         dV = (self.V2[0][:, :, self.cols] - self.V2[1][:, :, self.cols]) / (2.0 * h)
-        Y = t.bmm(self.dZ, self.Xp)                                   # dZ x
-        g = t.sum(self.DX * (2.0 * dV - Y), dim=1)                    # [Mb, T]
+        # dZ x in complex64: the central difference is accurate to ~1e-9 only
+        dZx = t.bmm(self.dZ.to(t.complex64), self.Xp32).to(t.complex128)
+        g = t.sum(self.DX * dV + self.Y * (dV - dZx), dim=1)       # [Mb, T]
         c = -1j * p.k * ETA0 / (4.0 * math.pi)
         s = 1.0 if self.pol == 0 else -1.0
         dF = s * c * t.sum(self.mode_w[:, None] * g, dim=0)          # [T]
@@ -156,8 +178,8 @@ def _bspline_forward(radii, n_seg, freq_hz, thetas_deg, pol, m_max, precision, h
     return prob, res, F, Bsp
 
 
-def _bspline_gradient(prob, X, F, Bsp, n_radii: int, pol: str, h: float) -> np.ndarray:
-    sg = ShapeGradient(prob, X, F, pol, h=h)
+def _bspline_gradient(prob, res, F, Bsp, n_radii: int, pol: str, h: float) -> np.ndarray:
+    sg = ShapeGradient(prob, res, F, pol, h=h)
     grad = np.empty(n_radii)
     for j in range(n_radii):
         dn = np.zeros((prob.Nn, 2))
@@ -180,7 +202,7 @@ def bspline_rcs_and_gradient(radii: Sequence[float], n_seg: int, freq_hz: float,
     J = objective(F, pol)
     prob.torch.cuda.synchronize()
     t1 = time.perf_counter()
-    grad = _bspline_gradient(prob, res.X, F, Bsp, len(radii), pol, h)
+    grad = _bspline_gradient(prob, res, F, Bsp, len(radii), pol, h)
     if timings is not None:
         timings["forward_s"] = t1 - t0
         timings["gradient_s"] = time.perf_counter() - t1
@@ -200,13 +222,13 @@ def _rcs_function():
             r = radii.detach().cpu().double().numpy()
             prob, res, F, Bsp = _bspline_forward(r, int(n_seg), float(freq_hz), thetas, pol, m_max,
                                                  precision, 1.0)
-            ctx.state = (prob, res.X, F, Bsp, len(r), pol)
+            ctx.state = (prob, res, F, Bsp, len(r), pol)
             return radii.new_tensor(objective(F, pol))
 
         @staticmethod
         def backward(ctx, gJ):
-            prob, X, F, Bsp, nr, pol = ctx.state
-            grad = _bspline_gradient(prob, X, F, Bsp, nr, pol, 1e-5)
+            prob, res, F, Bsp, nr, pol = ctx.state
+            grad = _bspline_gradient(prob, res, F, Bsp, nr, pol, 1e-5)
             ctx.state = None
             g = torch.as_tensor(grad, dtype=gJ.dtype, device=gJ.device)
             return gJ * g, None, None, None, None, None, None

@@ -83,6 +83,12 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
                          formulation=form, cfie_alpha=cfie_alpha)
     t_setup = time.perf_counter()
     res = prob.sweep(precision=precision, check_abort=check_abort)
+    return _result(prob, res, thetas, form, precision, mode_tol, progress, t_wall, t_setup)
+
+
+def _result(prob: BorGpuProblem, res, thetas, form: str, precision: str, mode_tol: float,
+            progress: Optional[Callable], t_wall: float, t_setup: float) -> Dict:
+    """The reference's result dict of one sweep (bor_solver.py:987-1004)."""
     F, modes_used = replay_truncation(res.dF, mode_tol)
     if progress is not None:
         progress(modes_used, prob.m_max)
@@ -114,6 +120,45 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
         "refine_residual": lin_res,
         "timings": timings,
     }
+
+
+def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: float = 0.5,
+                    mode_tol: float = 1e-6, table_precision: str = "auto",
+                    progress: Optional[Callable] = None) -> List[Dict]:
+    """Monostatic RCS of many bodies of revolution on one GPU.
+
+    ``bodies``: iterable of dicts with ``points``, ``freq_hz`` and optionally
+    ``n_modes`` (or ``m_max``).  The host set-up of the next body (geometry,
+    near tables, device upload) runs on a worker thread while the GPU sweeps
+    the current one; each sweep batches every mode of its body.  Returns one
+    ``solve_bor`` result dict per body, in order.  No counterpart in the
+    reference (its callers loop over bodies).
+    """
+    from concurrent.futures import ThreadPoolExecutor
+    form = formulation.strip().lower()
+    precision = _precision_of(table_precision)
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    items = list(bodies)
+
+    def setup(b):
+        t0 = time.perf_counter()
+        m = b.get("n_modes", b.get("m_max"))
+        prob = BorGpuProblem(b["points"], float(b["freq_hz"]), thetas, m_max=m,
+                             formulation=form, cfie_alpha=cfie_alpha)
+        return prob, t0, time.perf_counter()
+
+    out: List[Dict] = []
+    with ThreadPoolExecutor(max_workers=1) as ex:
+        nxt = ex.submit(setup, items[0]) if items else None
+        for i in range(len(items)):
+            prob, t0, t1 = nxt.result()
+            nxt = ex.submit(setup, items[i + 1]) if i + 1 < len(items) else None
+            res = prob.sweep(precision=precision)
+            out.append(_result(prob, res, thetas, form, precision, mode_tol, None, t0, t1))
+            if progress is not None:
+                progress(i + 1, len(items))
+            del prob, res
+    return out
 
 
 def solve_bor_pec(points, freq_hz: float, thetas_deg, n_modes: Optional[int] = None,

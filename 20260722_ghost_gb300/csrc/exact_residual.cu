@@ -1,0 +1,480 @@
+// exact_residual.cu -- refinement residual R = B - (Z_far + Z_near) X with
+// exact products on the bf16 tensor cores (Ozaki splitting).
+//
+// Z_far (complex double) is viewed as the real matrix A [n][2n] (re, im
+// interleaved) and X (the FP32 solution) through the 2x2 real expansion
+// Bt[2j+r][2k+c] = [[Xr, -Xi], [Xi, Xr]][r][c] (as in tc_gemm.cu), so that
+// A Bt^T is the interleaved storage of Z_far X.
+//
+// Splitting: every row i of A gets a power-of-two scale 2^e_i >= its largest
+// magnitude, every complex column j of X a scale 2^f_j; each scaled value u
+// (|u| < 1) is written as q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31 with
+// integers |q_s| <= 128 (balanced base-256 digits), which bf16 holds exactly.
+// A product q_s q_t (|.| <= 2^14) is exact in the FP32 accumulator, and so is
+// any sum of them below 2^24: the slice pairs with the same s + t share one
+// TMEM accumulator ("level" L = s + t - 2, scale 2^(-14 - 8 L)), at most four
+// pairs per level, accumulated over K chunks of 192 real columns
+// (192 * 4 * 2^14 < 2^24).  After each chunk the five levels are folded into
+// double-float (hi, lo) register accumulators; pairs with s + t > 6 are
+// dropped (below 2^-40 of the row and column scales).  The result carries
+// ~2^-32 of the row / column scales (the truncation of the fourth digit) --
+// far below the FP32-product floor (~2^-24) of a split-word SIMT residual --
+// and runs at tensor-core rate.
+//
+// The near band and the masks are applied in FP64 in the epilogue.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "tcgen05.cuh"
+
+namespace gb {
+namespace {
+
+constexpr int XS = 4;                    // slices per operand
+constexpr int XBM = 128;                 // tile rows
+constexpr int XBN = 64;                  // tile real columns (32 complex rhs)
+constexpr int XBK = 64;                  // real K per stage (64 bf16 = one 128-byte swizzle row)
+constexpr int XCHUNK = 3;                // stages per exact accumulation (K = 192)
+constexpr int XLEV = 5;                  // levels s + t = 2..6
+constexpr uint32_t XTMEM_COLS = 512;     // power of two >= XLEV * XBN
+constexpr int XTHREADS = 128;
+constexpr int XA_TILE = XBM * XBK;       // bf16 elements
+constexpr int XB_TILE = XBN * XBK;
+
+struct __align__(1024) XSmem {
+    __nv_bfloat16 a[2][XS][XA_TILE];     // 2 stages x 4 slices x 16 KB
+    __nv_bfloat16 b[2][XS][XB_TILE];     // 2 stages x 4 slices x 8 KB
+    unsigned long long full[2];
+    unsigned long long mma[2];
+    uint32_t tmem_base;
+    int failed;
+};
+
+// instruction descriptor: D f32, A/B bf16 (kind::f16), both K-major, M = 128, N = 64
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XBN >> 3) << 17) |
+                                ((uint32_t)(XBM >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescBf16), "r"(accumulate));
+}
+
+// exponent e with |v| < 2^e for every |v| <= m (m > 0); 0 for m = 0
+__device__ __forceinline__ int scale_exp(double m)
+{
+    if (!(m > 0.0)) return 0;
+    int e;
+    frexp(m, &e);                        // m = f 2^e, f in [0.5, 1)
+    return e;
+}
+
+// four balanced base-256 digits of u (|u| < 1): u ~ q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31
+__device__ __forceinline__ void digits(double u, float (&q)[XS])
+{
+    double t = u * 128.0;
+#pragma unroll
+    for (int s = 0; s < XS; ++s) {
+        const double d = rint(t);
+        q[s] = (float)d;
+        t = (t - d) * 256.0;
+    }
+}
+
+// row exponents of A: one warp per row of Z_far (2n reals)
+__global__ void row_exp_kernel(int batch, int n, const double2 *__restrict__ Z, long long ldz, long long sz,
+                               int *__restrict__ ex)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= batch * n) return;
+    const int b = warp / n, i = warp % n;
+    const double2 *row = Z + (size_t)b * sz + (size_t)i * ldz;
+    double m = 0.0;
+    for (int k = lane; k < n; k += 32) {
+        const double2 v = row[k];
+        m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (lane == 0) ex[warp] = scale_exp(m);
+}
+
+// A slices: As[s][b][i][kr], kr < Kp (zero beyond 2n)
+__global__ void slice_a_kernel(int batch, int n, int Kp, const double2 *__restrict__ Z, long long ldz, long long sz,
+                               const int *__restrict__ ex, __nv_bfloat16 *__restrict__ As)
+{
+    const int kh = Kp / 2;
+    const long long total = (long long)batch * n * kh;
+    const size_t plane = (size_t)batch * n * Kp;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % kh);
+        const long long bi = idx / kh;
+        const int i = (int)(bi % n), b = (int)(bi / n);
+        const double2 v = (k < n) ? Z[(size_t)b * sz + (size_t)i * ldz + k] : make_double2(0.0, 0.0);
+        const int e = ex[bi];
+        float qr[XS], qi[XS];
+        digits(ldexp(v.x, -e), qr);
+        digits(ldexp(v.y, -e), qi);
+        const size_t o = (size_t)bi * Kp + 2 * (size_t)k;
+#pragma unroll
+        for (int s = 0; s < XS; ++s) {
+            __nv_bfloat162 w;
+            w.x = __float2bfloat16_rn(qr[s]);
+            w.y = __float2bfloat16_rn(qi[s]);
+            *reinterpret_cast<__nv_bfloat162 *>(As + s * plane + o) = w;
+        }
+    }
+}
+
+// column exponents of X (FP32 solution [b][k][j], k < n, j < nrhs)
+__global__ void col_exp_kernel(int n, int nrhs, const float2 *__restrict__ X, long long ldx, long long sx,
+                               int *__restrict__ fx)
+{
+    __shared__ float red[8][33];
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31), ty = threadIdx.x >> 5, b = blockIdx.y;
+    float m = 0.f;
+    if (j < nrhs)
+        for (int k = ty; k < n; k += 8) {
+            const float2 v = X[(size_t)b * sx + (size_t)k * ldx + j];
+            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+        }
+    red[ty][threadIdx.x & 31] = m;
+    __syncthreads();
+    if (ty == 0 && j < nrhs) {
+        for (int r = 1; r < 8; ++r) m = fmaxf(m, red[r][threadIdx.x]);
+        fx[(size_t)b * nrhs + j] = scale_exp((double)m);
+    }
+}
+
+// Bt slices: Bs[s][b][2j + r][kr] with Bt[2j+r][2k+c] = [[Xr, -Xi], [Xi, Xr]][r][c];
+// 32 x 32 complex tiles transposed through shared memory
+__global__ void __launch_bounds__(256)
+slice_b_kernel(int batch, int n, int nrhs, int Kp, const float2 *__restrict__ X, long long ldx, long long sx,
+               const int *__restrict__ fx, __nv_bfloat16 *__restrict__ Bs)
+{
+    __shared__ float2 t[32][33];
+    const int j0 = blockIdx.x * 32, k0 = blockIdx.y * 32, b = blockIdx.z;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const int k = k0 + r, j = j0 + tx;
+        t[r][tx] = (k < n && j < nrhs) ? X[(size_t)b * sx + (size_t)k * ldx + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const size_t plane = (size_t)batch * 2 * nrhs * Kp;
+    for (int q = threadIdx.x; q < 64 * 64; q += 256) {
+        const int orow = q / 64, ocol = q % 64;
+        const int j = j0 + orow / 2, rr = orow & 1;
+        const int kc = k0 * 2 + ocol;
+        if (j >= nrhs || kc >= Kp) continue;
+        const float2 x = t[ocol / 2][orow / 2];
+        const int c = ocol & 1;
+        const float v = (rr == 0) ? (c == 0 ? x.x : -x.y) : (c == 0 ? x.y : x.x);
+        float qd[XS];
+        digits(ldexp((double)v, -fx[(size_t)b * nrhs + j]), qd);
+        const size_t o = ((size_t)b * 2 * nrhs + 2 * j + rr) * Kp + kc;
+#pragma unroll
+        for (int s = 0; s < XS; ++s) Bs[s * plane + o] = __float2bfloat16_rn(qd[s]);
+    }
+}
+
+__device__ __forceinline__ bool row_masked(const int *mr, int r)
+{
+    return mr[0] == r || mr[1] == r || mr[2] == r || mr[3] == r;
+}
+
+struct XMaps {
+    CUtensorMap a[XS];
+    CUtensorMap b[XS];
+};
+
+__global__ void __launch_bounds__(XTHREADS)
+exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int Nn, int Kp,
+                      const int *__restrict__ ex, const int *__restrict__ fx,
+                      const double2 *__restrict__ band, const int *__restrict__ mask_rows,
+                      const float2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
+                      double2 *__restrict__ R, float2 *__restrict__ R32, double *__restrict__ norms,
+                      int *__restrict__ err)
+{
+    extern __shared__ unsigned char smem_raw[];
+    XSmem &s = *reinterpret_cast<XSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n0 = blockIdx.x * XBN, m0 = blockIdx.y * XBM, b = blockIdx.z;
+    const int nst = Kp / XBK;
+    const int nch = (nst + XCHUNK - 1) / XCHUNK;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(&s.tmem_base)), "r"(XTMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) { mbar_init(&s.full[i], 1); mbar_init(&s.mma[i], 1); }
+        s.failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = s.tmem_base;
+    const uint32_t stage_bytes = (uint32_t)(XS * (XA_TILE + XB_TILE) * 2);
+
+    // producer state (thread 0 only)
+    uint32_t full_phase[2] = {0, 0}, mma_phase[2] = {0, 0};
+    bool pending[2] = {false, false};
+    bool ok = true;
+    auto load_stage = [&](int ks) {
+        const int st = ks & 1;
+        mbar_expect_tx(&s.full[st], stage_bytes);
+#pragma unroll
+        for (int q = 0; q < XS; ++q) {
+            tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
+            tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
+        }
+    };
+    auto wait_mma = [&](int st) {
+        if (!pending[st]) return;
+        if (!mbar_wait(&s.mma[st], mma_phase[st])) ok = false;
+        mma_phase[st] ^= 1u;
+        pending[st] = false;
+    };
+    if (tid == 0) {
+        load_stage(0);
+        if (nst > 1) load_stage(1);
+    }
+
+    // double-float accumulators of this thread's row, 64 real columns
+    float hi[XBN], lo[XBN];
+#pragma unroll
+    for (int c = 0; c < XBN; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
+
+    for (int ch = 0; ch < nch; ++ch) {
+        if (tid == 0 && ok) {
+            const int k_lo = ch * XCHUNK, k_hi = min(nst, k_lo + XCHUNK);
+            for (int ks = k_lo; ks < k_hi && ok; ++ks) {
+                const int st = ks & 1;
+                if (!mbar_wait(&s.full[st], full_phase[st])) { ok = false; break; }
+                full_phase[st] ^= 1u;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                for (int L = 0; L < XLEV; ++L) {
+                    const int lev = L + 2;
+                    const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XS ? lev - 1 : XS;
+                    for (int sa = s_lo; sa <= s_hi; ++sa) {
+                        const int sb = lev - sa;
+                        const uint32_t ab = smem_u32(s.a[st][sa - 1]), bb = smem_u32(s.b[st][sb - 1]);
+#pragma unroll
+                        for (int kk = 0; kk < XBK / 16; ++kk) {    // 16 bf16 = 32 bytes per MMA
+                            const uint32_t acc = (ks > k_lo || sa > s_lo || kk > 0) ? 1u : 0u;
+                            umma_bf16(tmem + (uint32_t)(L * XBN), umma_desc_sw128(ab + kk * 32),
+                                      umma_desc_sw128(bb + kk * 32), acc);
+                        }
+                    }
+                }
+                umma_commit(&s.mma[st]);
+                pending[st] = true;
+                if (ks + 2 < nst) {
+                    wait_mma(st);                 // the buffer is refilled after its MMAs read it
+                    if (!ok) break;
+                    load_stage(ks + 2);
+                }
+            }
+            // every MMA of this chunk must be complete before its accumulators are read
+            if (ok) wait_mma(0);
+            if (ok) wait_mma(1);
+            if (!ok) {
+                s.failed = 1;
+                atomicExch(err, 1);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!s.failed) {
+            const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+            for (int L = 0; L < XLEV; ++L) {
+                const float sc = ldexpf(1.0f, -14 - 8 * L);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    float v[32];
+                    tmem_ld32(row_addr + (uint32_t)(L * XBN + h * 32), v);
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) {
+                        // x is exact (an integer times a power of two); a two-sum
+                        // keeps every level exact in (hi, lo), so lo only collects
+                        // rounding errors of hi (~2^-24 |hi|) and stays precise
+                        const float x = v[c] * sc;
+                        const float t = hi[h * 32 + c] + x;
+                        const float bb2 = t - hi[h * 32 + c];
+                        lo[h * 32 + c] += (hi[h * 32 + c] - (t - bb2)) + (x - bb2);
+                        hi[h * 32 + c] = t;
+                    }
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();                         // accumulators consumed: the next chunk may overwrite them
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+
+    // P = 2^(e_i + f_j) (hi + lo) through shared memory (the operand buffers are free)
+    double (*Ps)[XBN + 1] = reinterpret_cast<double (*)[XBN + 1]>(&s.a[0][0][0]);
+    if (!s.failed) {
+        const int r = warp * 32 + lane;
+        const int i = m0 + r;
+        const int e = (i < n) ? ex[(size_t)b * n + i] : 0;
+#pragma unroll
+        for (int c = 0; c < XBN; ++c) {
+            const int j = (n0 + c) >> 1;
+            const int f = (j < nrhs) ? fx[(size_t)b * nrhs + j] : 0;
+            Ps[r][c] = ldexp((double)hi[c] + (double)lo[c], e + f);
+        }
+    }
+    __syncthreads();
+    double rn = 0.0, bn = 0.0;
+    if (!s.failed) {
+        const int *mr = mask_rows + 4 * b;
+        const double2 *Bb = B + (size_t)b * sbb;
+        const float2 *Xb = X + (size_t)b * sbb;
+        const int j = (n0 >> 1) + lane;          // complex column of this lane
+        for (int rr = 0; rr < 32; ++rr) {
+            const int r = warp * 32 + rr;
+            const int i = m0 + r;
+            if (i >= n || j >= nrhs) continue;
+            const double2 bv = Bb[(size_t)i * ldb + j];
+            double2 rv = make_double2(bv.x - Ps[r][2 * lane], bv.y - Ps[r][2 * lane + 1]);
+            if (band) {
+                const int half = i >= Nn ? 1 : 0, node = i - half * Nn;
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    const double2 *bd = band + (((size_t)b * 4 + 2 * half + c2) * Nn + node) * 5;
+                    for (int d = 0; d < 5; ++d) {
+                        const int jn = node + d - 2;
+                        if (jn < 0 || jn >= Nn) continue;
+                        const float2 xv = Xb[(size_t)(c2 * Nn + jn) * ldb + j];
+                        rv = cfms(bd[d], make_double2(xv.x, xv.y), rv);
+                    }
+                }
+            }
+            if (row_masked(mr, i)) rv = make_double2(0.0, 0.0);
+            if (R) R[(size_t)b * sbb + (size_t)i * ldb + j] = rv;
+            if (R32) R32[(size_t)b * sbb + (size_t)i * ldb + j] = make_float2((float)rv.x, (float)rv.y);
+            rn += rv.x * rv.x + rv.y * rv.y;
+            bn += bv.x * bv.x + bv.y * bv.y;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        rn += __shfl_xor_sync(0xffffffffu, rn, off);
+        bn += __shfl_xor_sync(0xffffffffu, bn, off);
+    }
+    if (lane == 0 && !s.failed) {
+        atomicAdd(norms + 2 * b, rn);
+        atomicAdd(norms + 2 * b + 1, bn);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(XTMEM_COLS));
+}
+
+// K-major [batch][rows][Kp] bf16 operand, box 64 x box_rows, 128-byte swizzle
+bool make_map_bf16(CUtensorMap *map, const __nv_bfloat16 *base, int rows, int Kp, int batch, int box_rows)
+{
+    auto enc = get_encode();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+    const cuuint32_t box[3] = {XBK, (cuuint32_t)box_rows, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims, strides, box,
+               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+long long kp_of(int n) { return ((2LL * n + XBK - 1) / XBK) * XBK; }
+
+}  // namespace
+}  // namespace gb
+
+// Workspace: [0, 256) status int (1 = a bounded wait gave up), then row and
+// column exponents, then the A and Bt slices (256-byte aligned blocks).
+extern "C" long long ghost_bor_residual_exact_workspace(int batch, int n, int nrhs)
+{
+    if (batch < 1 || n < 1 || nrhs < 1) return -1;
+    using namespace gb;
+    const long long Kp = kp_of(n);
+    auto up = [](long long x) { return (x + 255) / 256 * 256; };
+    return 256 + up(4LL * batch * n) + up(4LL * batch * nrhs) + up(2LL * XS * batch * n * Kp) +
+           up(2LL * XS * batch * 2 * nrhs * Kp);
+}
+
+extern "C" int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
+                                        const double *Zf, long long ldz, long long stride_z,
+                                        const double *band, const int *mask_rows,
+                                        const float *X32, const double *B, long long ldb, long long stride_b,
+                                        double *R, float *R32, double *norms,
+                                        void *work, long long work_bytes, void *stream)
+{
+    using namespace gb;
+    if (batch < 1 || n < 1 || nrhs < 1 || !Zf || !mask_rows || !X32 || !B || (!R && !R32) || !norms ||
+        ldz < n || ldb < nrhs || n != 2 * Nn || !work || (reinterpret_cast<uintptr_t>(work) & 255) ||
+        work_bytes < ghost_bor_residual_exact_workspace(batch, n, nrhs))
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int Kp = (int)kp_of(n);
+    auto up = [](long long x) { return (x + 255) / 256 * 256; };
+    unsigned char *w = reinterpret_cast<unsigned char *>(work);
+    int *errp = reinterpret_cast<int *>(w);
+    int *ex = reinterpret_cast<int *>(w + 256);
+    int *fx = reinterpret_cast<int *>(w + 256 + up(4LL * batch * n));
+    __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(w + 256 + up(4LL * batch * n) + up(4LL * batch * nrhs));
+    __nv_bfloat16 *Bs = As + up(2LL * XS * batch * n * Kp) / 2;
+    const size_t aplane = (size_t)batch * n * Kp, bplane = (size_t)batch * 2 * nrhs * Kp;
+
+    if (cudaMemsetAsync(errp, 0, sizeof(int), st) != cudaSuccess ||
+        cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess)
+        return check_launch("residual_exact: memset");
+    const double2 *Z = reinterpret_cast<const double2 *>(Zf);
+    const float2 *X = reinterpret_cast<const float2 *>(X32);
+    {
+        const long long rows = (long long)batch * n;
+        row_exp_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(batch, n, Z, ldz, stride_z, ex);
+        int rc = check_launch("residual_exact: row exponents");
+        if (rc) return rc;
+        const long long pairs = (long long)batch * n * (Kp / 2);
+        const int blocks = (int)((pairs + 255) / 256 < 152 * 32 ? (pairs + 255) / 256 : 152 * 32);
+        slice_a_kernel<<<blocks, 256, 0, st>>>(batch, n, Kp, Z, ldz, stride_z, ex, As);
+        if ((rc = check_launch("residual_exact: slice A"))) return rc;
+        dim3 gc((nrhs + 31) / 32, batch);
+        col_exp_kernel<<<gc, 256, 0, st>>>(n, nrhs, X, ldb, stride_b, fx);
+        if ((rc = check_launch("residual_exact: column exponents"))) return rc;
+        dim3 gb2((nrhs + 31) / 32, (Kp / 2 + 31) / 32, batch);
+        slice_b_kernel<<<gb2, 256, 0, st>>>(batch, n, nrhs, Kp, X, ldb, stride_b, fx, Bs);
+        if ((rc = check_launch("residual_exact: slice B"))) return rc;
+    }
+    XMaps maps;
+    for (int q = 0; q < XS; ++q) {
+        if (!make_map_bf16(&maps.a[q], As + q * aplane, n, Kp, batch, XBM) ||
+            !make_map_bf16(&maps.b[q], Bs + q * bplane, 2 * nrhs, Kp, batch, XBN)) {
+            set_last_error("residual_exact: cuTensorMapEncodeTiled failed");
+            return GHOST_BOR_ECUDA;
+        }
+    }
+    const size_t smem = sizeof(XSmem) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(exact_residual_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return check_launch("residual_exact: smem attribute");
+        attr = true;
+    }
+    dim3 grid((2 * nrhs + XBN - 1) / XBN, (n + XBM - 1) / XBM, batch);
+    exact_residual_kernel<<<grid, XTHREADS, smem, st>>>(maps, n, nrhs, Nn, Kp, ex, fx,
+                                                         reinterpret_cast<const double2 *>(band), mask_rows, X,
+                                                         reinterpret_cast<const double2 *>(B), ldb, stride_b,
+                                                         reinterpret_cast<double2 *>(R),
+                                                         reinterpret_cast<float2 *>(R32), norms, errp);
+    return check_launch("residual_exact");
+}

@@ -417,15 +417,31 @@ __device__ __forceinline__ void split2(double2 v, float2 &h, float2 &l)
     l = make_float2((float)(v.x - (double)h.x), (float)(v.y - (double)h.y));
 }
 
+// tile element loaders: Z as complex double (split on the fly) or as its
+// pre-split FP32 words (hi.re, hi.im, lo.re, lo.im); X as complex double or as
+// an FP32 solution (low word zero)
+__device__ __forceinline__ float4 split_words(double2 v)
+{
+    float2 h, l;
+    split2(v, h, l);
+    return make_float4(h.x, h.y, l.x, l.y);
+}
+__device__ __forceinline__ float4 z_words(const double2 *p) { return split_words(*p); }
+__device__ __forceinline__ float4 z_words(const float4 *p) { return *p; }
+__device__ __forceinline__ float4 x_words(const double2 *p) { return split_words(*p); }
+__device__ __forceinline__ float4 x_words(const float2 *p) { const float2 v = *p; return make_float4(v.x, v.y, 0.f, 0.f); }
 __device__ __forceinline__ double2 ld_x(const double2 *p) { return *p; }
 __device__ __forceinline__ double2 ld_x(const float2 *p) { const float2 v = *p; return make_double2(v.x, v.y); }
 
 // XT = double2: X in FP64, split into two FP32 words like Z.
 // XT = float2:  X is an FP32 solution, its low word is zero and the Z_hi X_lo
 //               products are skipped.
-template <class XT>
+// ZT = double2: Z_far in complex double, split while staging the tiles;
+// ZT = float4:  Z_far already split in place (ghost_bor_split_words), so the
+//               staging does no FP64 work.
+template <class XT, class ZT>
 __global__ void __launch_bounds__(256)
-residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, long long ldz, long long sz,
+residual_mixed_kernel(int n, int nrhs, int Nn, const ZT *__restrict__ Zf, long long ldz, long long sz,
                       const double2 *__restrict__ band, const int *__restrict__ mask_rows,
                       const XT *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
                       double2 *__restrict__ R, float2 *__restrict__ Rlo, double *__restrict__ norms)
@@ -439,7 +455,7 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
     double (*red)[8] = reinterpret_cast<double (*)[8]>(&Zs[0][0]);   // reused after the K loop
     const int b = blockIdx.z;
     const int r0 = blockIdx.y * GT, c0 = blockIdx.x * GT;
-    const double2 *Zb = Zf + (size_t)b * sz;
+    const ZT *Zb = Zf + (size_t)b * sz;
     const XT *Xb = X + (size_t)b * sbb;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     // hi: leading sum of the hi*hi products; sm: low-order part (hi*lo + lo*hi
@@ -451,26 +467,25 @@ residual_mixed_kernel(int n, int nrhs, int Nn, const double2 *__restrict__ Zf, l
         for (int j = 0; j < 4; ++j) { hi[i][j] = make_float2(0, 0); sm[i][j] = make_float2(0, 0); }
 
     // each thread stages 4 Z and 4 X elements per tile (GT * RK = 1024 each)
-    double2 zp[4], xp[4];
+    float4 zp[4], xp[4];
     auto fetch = [&](int k0) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = tid + 256 * q;
             const int r = i / RK, kk = i % RK;
-            zp[q] = (r0 + r < n && k0 + kk < n) ? Zb[(size_t)(r0 + r) * ldz + k0 + kk] : make_double2(0, 0);
+            zp[q] = (r0 + r < n && k0 + kk < n) ? z_words(Zb + (size_t)(r0 + r) * ldz + k0 + kk)
+                                                : make_float4(0.f, 0.f, 0.f, 0.f);
             const int kx = i / GT, c = i % GT;
-            xp[q] = (k0 + kx < n && c0 + c < nrhs) ? ld_x(Xb + (size_t)(k0 + kx) * ldb + c0 + c) : make_double2(0, 0);
+            xp[q] = (k0 + kx < n && c0 + c < nrhs) ? x_words(Xb + (size_t)(k0 + kx) * ldb + c0 + c)
+                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
         }
     };
     auto stage = [&]() {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = tid + 256 * q;
-            float2 h, l;
-            split2(zp[q], h, l);
-            Zs[i % RK][i / RK] = make_float4(h.x, h.y, l.x, l.y);
-            split2(xp[q], h, l);
-            Xs[i / GT][i % GT] = make_float4(h.x, h.y, l.x, l.y);
+            Zs[i % RK][i / RK] = zp[q];
+            Xs[i / GT][i % GT] = xp[q];
         }
     };
     fetch(0);
@@ -771,7 +786,7 @@ extern "C" int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual: memset");
     dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
-    residual_mixed_kernel<double2><<<grid, 256, 0, st>>>(
+    residual_mixed_kernel<double2, double2><<<grid, 256, 0, st>>>(
         n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
         reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const double2 *>(X),
         reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
@@ -780,7 +795,7 @@ extern "C" int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
 }
 
 extern "C" int ghost_bor_residual_x32(int batch, int n, int nrhs, int Nn,
-                                      const void *Zf, long long ldz, long long stride_z,
+                                      const void *Zf, int z_split, long long ldz, long long stride_z,
                                       const double *band, const int *mask_rows,
                                       const float *X32, const double *B, long long ldb, long long stride_b,
                                       double *R, float *R32, double *norms, void *stream)
@@ -791,12 +806,39 @@ extern "C" int ghost_bor_residual_x32(int batch, int n, int nrhs, int Nn,
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(norms, 0, sizeof(double) * 2 * batch, st) != cudaSuccess) return check_launch("residual_x32: memset");
     dim3 grid((nrhs + GT - 1) / GT, (n + GT - 1) / GT, batch);
-    residual_mixed_kernel<float2><<<grid, 256, 0, st>>>(
-        n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
-        reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const float2 *>(X32),
-        reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
-        reinterpret_cast<float2 *>(R32), norms);
+    if (z_split)
+        residual_mixed_kernel<float2, float4><<<grid, 256, 0, st>>>(
+            n, nrhs, Nn, reinterpret_cast<const float4 *>(Zf), ldz, stride_z,
+            reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const float2 *>(X32),
+            reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
+            reinterpret_cast<float2 *>(R32), norms);
+    else
+        residual_mixed_kernel<float2, double2><<<grid, 256, 0, st>>>(
+            n, nrhs, Nn, reinterpret_cast<const double2 *>(Zf), ldz, stride_z,
+            reinterpret_cast<const double2 *>(band), mask_rows, reinterpret_cast<const float2 *>(X32),
+            reinterpret_cast<const double2 *>(B), ldb, stride_b, reinterpret_cast<double2 *>(R),
+            reinterpret_cast<float2 *>(R32), norms);
     return check_launch("residual_x32");
+}
+
+// in-place split of complex double into FP32 words (hi.re, hi.im, lo.re, lo.im)
+__global__ void split_words_kernel(int rows, int cols, double2 *__restrict__ Z, long long ldz, long long sz)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    double2 *p = Z + (size_t)blockIdx.z * sz + (size_t)blockIdx.y * ldz + c;
+    const float4 w = split_words(*p);
+    *reinterpret_cast<float4 *>(p) = w;
+}
+
+extern "C" int ghost_bor_split_words(int batch, int rows, int cols, void *Z, long long ldz, long long stride_z,
+                                     void *stream)
+{
+    if (batch < 1 || rows < 1 || cols < 1 || !Z || ldz < cols) return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    dim3 grid((cols + 255) / 256, rows, batch);
+    split_words_kernel<<<grid, 256, 0, st>>>(rows, cols, reinterpret_cast<double2 *>(Z), ldz, stride_z);
+    return check_launch("split_words");
 }
 
 extern "C" int ghost_bor_residual64(int batch, int n, int nrhs,

@@ -19,9 +19,7 @@
 // swizzle row), 2 stages double-buffered.  Thread 0 issues the TMA loads and
 // the MMAs; the four warps read the accumulator with tcgen05.ld.
 #include "common.cuh"
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
+#include "tcgen05.cuh"
 
 namespace gb {
 namespace {
@@ -31,7 +29,6 @@ constexpr int STAGES = 2;
 constexpr int TILE_FLOATS = BM * BK;               // 16 KB per operand tile
 constexpr int TC_THREADS = 128;
 constexpr uint32_t TMEM_COLS = 256;                // allocated (128 used)
-constexpr long long WAIT_LIMIT = 1LL << 24;        // bounded mbarrier waits
 
 struct __align__(1024) TcSmem {
     float a_hi[STAGES][TILE_FLOATS];
@@ -44,58 +41,6 @@ struct __align__(1024) TcSmem {
     int failed;
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *b, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-
-// bounded wait on the phase with parity `parity`; false on timeout
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity)
-{
-    const uint32_t a = smem_u32(b);
-    for (long long it = 0; it < WAIT_LIMIT; ++it) {
-        uint32_t done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                     " selp.u32 %0, 1, 0, p;\n}\n"
-                     : "=r"(done) : "r"(a), "r"(parity) : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                            unsigned long long *bar)
-{
-    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%2, %3, %4}], [%5];"
-                 ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2),
-                   "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// UMMA shared-memory descriptor: K-major operand, 128-byte swizzle, 8-row
-// groups 1024 bytes apart (SBO), version 1.
-__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);             // start address      [0,14)
-    d |= (uint64_t)1u << 16;                              // LBO (unused here)  [16,30)
-    d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;        // SBO = 1024 B       [32,46)
-    d |= (uint64_t)1u << 46;                              // descriptor version [46,48)
-    d |= (uint64_t)2u << 61;                              // SWIZZLE_128B       [61,64)
-    return d;
-}
-
 // instruction descriptor: D f32, A/B tf32, both K-major, M = 128, N = 128
 constexpr uint32_t kIdescTf32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BNR >> 3) << 17) |
                                 ((uint32_t)(BM >> 4) << 24);
@@ -105,28 +50,6 @@ __device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint6
     asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                  " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n"
                  ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kIdescTf32), "r"(accumulate));
-}
-
-__device__ __forceinline__ void umma_commit(unsigned long long *bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                 ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
-{
-    uint32_t r[32];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32"
-                 " {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15,"
-                 " %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-                   "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-                   "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                 : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ float tf32_round(float x)
@@ -308,19 +231,6 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-PFN_cuTensorMapEncodeTiled_v12000 get_encode()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
 // K-major [batch][rows][Kp] FP32 operand, box 32 x 128, 128-byte swizzle
 bool make_map(CUtensorMap *map, const float *base, int rows, int Kp, int batch)
 {

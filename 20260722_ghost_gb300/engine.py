@@ -11,9 +11,9 @@ Stages (each a C-ABI call on one CUDA stream):
   excitation    ghost_bor_rhs        B = alpha V_E + (1 - alpha) eta0 V_H (FP64); for
                                      CFIE / MFIE also V_E alone for the far field
   LU + solve    ghost_bor_getrf/getrs  (FP32, trailing updates on tcgen05)
-  refinement    ghost_bor_residual_x32  R0 = B - (Z_far + Z_near) X0 with Z in FP64
-                                     (split FP32 words, FP32 products, compensated
-                                     sums), then per correction D = A32^-1 R:
+  refinement    ghost_bor_residual_exact  R0 = B - (Z_far + Z_near) X0 with exact
+                                     products of 8-bit slices on the bf16 tensor
+                                     cores, then per correction D = A32^-1 R:
                                      X += D, R -= fl32(Z) D (ghost_bor_cgemm_tc)
   far field     ghost_bor_farfield   dF[m][col] by reciprocity
 
@@ -42,6 +42,9 @@ from . import _native as nat
 from .geometry import (C0, ETA0, Generatrix, bracket_tables, dct_tables, default_n_modes,
                        element_mass, gauss_on_generatrix, mask_rows, n_xi_bracket, n_xi_efie,
                        near_tables, pack_geo)
+
+
+_NEAR_SCRATCH: Dict[tuple, object] = {}
 
 
 def _torch():
@@ -133,9 +136,14 @@ class BorGpuProblem:
             self.d_btab = torch.as_tensor(btab, dtype=f64, device=dev)
             self.d_bsin2 = torch.as_tensor(bs2, dtype=f64, device=dev)
             self.d_emass = torch.as_tensor(element_mass(self.g, self.N), dtype=f64, device=dev)
-        self.refine_floor = 1e-6     # residuals below this are at the FP32-product floor
+        # residual norm (relative to ||B||) where the refinement stops.  The exact
+        # first residual and the tensor-core updates resolve ~1e-11, but the
+        # FP32 far fill already perturbs the operator by ~4e-8 of its largest
+        # entries, so corrections below that change nothing measurable
+        self.refine_floor = 2e-8
         self.tensor_cores = True     # FP32 LU / solve / residual updates on tcgen05 (3xTF32)
         self.update_ws_bytes = 4 << 30   # scratch bound of one residual-update GEMM launch
+        self.exact_residual = True       # first residual with exact products (bf16 Ozaki slices)
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
@@ -167,13 +175,17 @@ class BorGpuProblem:
 
     def _near_work(self, name: str):
         """Scratch of a near kernel (azimuth nodes of every resident CTA) and
-        its status word; kept on the problem so its lifetime covers the launch."""
+        its status word.  One buffer per device and kernel, shared by every
+        problem (all launches go to one stream) and grown on demand; the
+        problem keeps a reference so the buffer outlives its launches."""
         lib = nat.load()
         nbytes = int(getattr(lib, name)(self.n_tail_max))
-        work = self._near_ws.get(name)
+        key = (str(self.device), name)
+        work = _NEAR_SCRATCH.get(key)
         if work is None or work.numel() < nbytes:
             work = self.torch.empty(nbytes, dtype=self.torch.uint8, device=self.device)
-            self._near_ws[name] = work
+            _NEAR_SCRATCH[key] = work
+        self._near_ws[name] = work
         return work, nbytes
 
     def check_near_status(self):
@@ -278,6 +290,8 @@ class BorGpuProblem:
         if precision not in ("fp64", "fp32ir"):
             raise ValueError("precision must be 'fp64' or 'fp32ir'")
         free, _ = torch.cuda.mem_get_info(self.device)
+        # blocks cached by torch's allocator are free for this sweep too
+        free += torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
         need = self.bytes_needed(precision)
         if need > 0.92 * free:
             raise MemoryError(f"GPU sweep needs {need / 1e9:.1f} GB, {free / 1e9:.1f} GB free")
@@ -331,6 +345,7 @@ class BorGpuProblem:
                      nat.ptr(X), nrhs, X.stride(0), 0, st); mark("solve")
             nat.call("ghost_bor_residual64", Mb, n, nrhs, nat.ptr(Zc), n, Zc.stride(0), nat.ptr(X),
                      nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(norms), st); mark("residual")
+            lu = dict(prec=nat.F64, A=Z, ipiv=ipiv, op=Zc, work=None)
             del Zc
         else:
             Zf = torch.zeros((Mb, n, n), dtype=c128, device=self.device)
@@ -367,27 +382,54 @@ class BorGpuProblem:
             # residual is R - Z D, and since |D| ~ 1e-5 |X| a tensor-core GEMM
             # on fl32(Z) is accurate enough for that product
             R32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
+            Ac = None
+            z_split = 0
+            if (self.tensor_cores and max_refine > 0) or keep:
+                # fl32(Z), masked like A, for the residual updates (and the adjoint);
+                # composed before Z_far is overwritten by its FP32 words
+                Ac = torch.empty((Mb, n, n), dtype=c64, device=self.device)
+                nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
+                         nat.ptr(self.d_masks), nat.ptr(Ac), n, Ac.stride(0), st)
             k0 = kstart()
-            nat.call("ghost_bor_residual_x32", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
-                     nat.ptr(self.d_masks), nat.ptr(X32), nat.ptr(B), nrhs, B.stride(0), 0, nat.ptr(R32),
-                     nat.ptr(norms), st)
+            if self.tensor_cores and self.exact_residual:
+                # exact products on the bf16 tensor cores, modes in chunks that
+                # bound the slice workspace
+                per = int(lib.ghost_bor_residual_exact_workspace(1, n, nrhs))
+                chunk = max(1, min(Mb, int(self.update_ws_bytes // max(per, 1))))
+                ex_ws = torch.empty(int(lib.ghost_bor_residual_exact_workspace(chunk, n, nrhs)),
+                                    dtype=torch.uint8, device=self.device)
+                ex_flags = torch.zeros((Mb + chunk - 1) // chunk, dtype=torch.int32, device=self.device)
+                for ci, b0 in enumerate(range(0, Mb, chunk)):
+                    nb = min(chunk, Mb - b0)
+                    nat.call("ghost_bor_residual_exact", nb, n, nrhs, Nn, nat.ptr(Zf[b0]), n, Zf.stride(0),
+                             nat.ptr(band[b0]), nat.ptr(self.d_masks[b0]), nat.ptr(X32[b0]), nat.ptr(B[b0]),
+                             nrhs, B.stride(0), 0, nat.ptr(R32[b0]), nat.ptr(norms[b0]), nat.ptr(ex_ws),
+                             ex_ws.numel(), st)
+                    ex_flags[ci:ci + 1].copy_(ex_ws[:4].view(torch.int32))
+                del ex_ws
+            else:
+                if self.tensor_cores:
+                    # Z_far is read only by the first residual from here on: split it in
+                    # place into FP32 words so that kernel does no FP64 work per tile
+                    nat.call("ghost_bor_split_words", Mb, n, n, nat.ptr(Zf), n, Zf.stride(0), st)
+                    z_split = 1
+                ex_flags = None
+                nat.call("ghost_bor_residual_x32", Mb, n, nrhs, Nn, nat.ptr(Zf), z_split, n, Zf.stride(0),
+                         nat.ptr(band), nat.ptr(self.d_masks), nat.ptr(X32), nat.ptr(B), nrhs, B.stride(0), 0,
+                         nat.ptr(R32), nat.ptr(norms), st)
             kend("residual", k0)
+            if ex_flags is not None and int(ex_flags.max()) != 0:
+                raise RuntimeError("a bounded tensor-core wait gave up in the exact residual")
             bn2 = torch.clamp(norms[:, 1], min=1e-300)
             rel = float(torch.sqrt(torch.max(norms[:, 0] / bn2)))
             history = [rel]
             prev = None
-            Ac = up_ws = status = None
+            up_ws = status = None
             for it in range(max_refine):
-                # stop at the floor of the split-word residual (~1e-7 of ||B||)
-                # or on stagnation
+                # stop at the residual floor or on stagnation
                 if rel < self.refine_floor or (prev is not None and rel > 0.5 * prev):
                     break
                 prev = rel
-                if Ac is None:
-                    # fl32(Z), masked like A, kept for the residual updates
-                    Ac = torch.empty((Mb, n, n), dtype=c64, device=self.device)
-                    nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
-                             nat.ptr(self.d_masks), nat.ptr(Ac), n, Ac.stride(0), st)
                 nat.call("ghost_bor_convert", 3, Mb, n, nrhs, nat.ptr(R32), nrhs, R32.stride(0),
                          nat.ptr(X32), nrhs, X32.stride(0), st)
                 nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
@@ -429,6 +471,7 @@ class BorGpuProblem:
                 flags = torch.stack([lu_ws[:4].view(torch.int32)[0], rs_ws[:4].view(torch.int32)[0]])
                 if int(flags.max()) != 0:
                     raise RuntimeError("a bounded tensor-core wait gave up in the LU / solve kernels")
+            lu = dict(prec=nat.F32, A=A, ipiv=ipiv, op=Ac, work=rs_ws)
             if not keep:
                 del Zf, A, Ac, R32, X32, band
         dF = torch.empty((Mb, nrhs), dtype=c128, device=self.device)
@@ -450,6 +493,8 @@ class BorGpuProblem:
         if keep:
             out.X = X
             out.B = B
+            out.Ve = Ve
+            out.lu = lu          # factors, pivots and the unfactored (masked) operator
         return out
 
 

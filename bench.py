@@ -48,6 +48,14 @@ WORKLOADS = {
                              dtheta=0.5),
     "cone_sphere_ka100": dict(body="cone_sphere", a=0.5, half_angle=15.0, N=3000, k=200.0, M=120,
                               dtheta=0.25),
+    # clamped cubic B-spline body, 64 control radii r_j ~ U(0.3, 0.6) (numpy seed 0)
+    # on a 2 m axis, ka = 20 at r = 0.5; objective mean sigma_HH over 30..60 deg;
+    # the line adds the adjoint gradient leg
+    # 64 seeded random bodies (bodies.random_bodies, seed 0): N ~ U{200..1600},
+    # 12 segments per wavelength, |m| <= ceil(k rho_max) + 10, 181 angles x 2 pols
+    "random64": dict(body="random", n_bodies=64, N=0, k=0.0, M=0, dtheta=1.0),
+    "bspline_ka20": dict(body="bspline", n_radii=64, N=600, k=40.0, M=30, theta0=30.0, theta1=60.0,
+                         dtheta=0.5, pol="HH"),
 }
 METRIC = "monostatic RCS angle·pol/s on 1 GB300: FP32+IR batched vs FP64 plain, ≤0.01 dB err"
 
@@ -56,12 +64,71 @@ def workload_inputs(name):
     import numpy as np
     w = WORKLOADS[name]
     bodies = importlib.import_module(PKG + ".bodies")
+    if w["body"] == "random":
+        # the CPU baseline of the batch samples its first body
+        b = bodies.random_bodies(w["n_bodies"], 0)[0]
+        return b["points"], b["freq_hz"], np.arange(0.0, 180.0 + 1e-9, w["dtheta"]), b["m_max"]
     if w["body"] == "sphere":
         pts = bodies.sphere_generatrix(w["a"], w["N"])
+    elif w["body"] == "bspline":
+        pts = bodies.bspline_body(bspline_radii(w), w["N"])[0]
     else:
         pts = bodies.cone_sphere_generatrix(w["a"], w["half_angle"], w["N"])
-    thetas = np.arange(0.0, 180.0 + 1e-9, w["dtheta"])
+    thetas = np.arange(w.get("theta0", 0.0), w.get("theta1", 180.0) + 1e-9, w["dtheta"])
     return pts, w["k"] * C0 / (2 * math.pi), thetas, w["M"]
+
+
+def bspline_radii(w):
+    import numpy as np
+    return np.random.default_rng(0).uniform(0.3, 0.6, w["n_radii"])
+
+
+def adjoint_leg(w, f, thetas):
+    """Adjoint gradient of mean sigma_pol w.r.t. the control radii: timing of
+    the forward sweep and the backward pass, FP32+IR vs FP64 gradient, and
+    central differences (h = 1e-4 m, FP64 solves) on four radii."""
+    import numpy as np
+    import torch
+    adj = importlib.import_module(PKG + ".adjoint")
+    r = bspline_radii(w)
+    pol = w["pol"]
+    adj.bspline_rcs_and_gradient(r, w["N"], f, thetas, pol, w["M"], "fp32ir")        # warm-up
+    tm = {}
+    J32, g32 = adj.bspline_rcs_and_gradient(r, w["N"], f, thetas, pol, w["M"], "fp32ir", timings=tm)
+    tm64 = {}
+    J64, g64 = adj.bspline_rcs_and_gradient(r, w["N"], f, thetas, pol, w["M"], "fp64", timings=tm64)
+    h = 1e-4
+    checks = []
+
+    def central(j, hh):
+        Js = []
+        for sgn in (1.0, -1.0):
+            rr = r.copy()
+            rr[j] += sgn * hh
+            Js.append(adj.objective(adj._bspline_forward(rr, w["N"], f, thetas, pol, w["M"], "fp64", 1.0)[2],
+                                    pol))
+        return (Js[0] - Js[1]) / (2 * hh)
+
+    for j in (0, len(r) // 3, 2 * len(r) // 3, len(r) - 1):
+        fd = central(j, h)
+        # Richardson extrapolation of the central difference (h, h/2) removes
+        # its O(h^2) truncation error, which is large for this objective
+        fd_r = (4.0 * central(j, h / 2) - fd) / 3.0
+        den = max(abs(fd_r), 1e-3 * float(np.max(np.abs(g64))))
+        checks.append({"param": j, "fd": fd, "fd_richardson": fd_r, "adjoint_fp32ir": float(g32[j]),
+                       "adjoint_fp64": float(g64[j]), "rel_err_fp32ir": abs(g32[j] - fd_r) / den,
+                       "rel_err_fp64": abs(g64[j] - fd_r) / den, "rel_err_fp32ir_plain_fd": abs(g32[j] - fd) / den})
+    torch.cuda.synchronize()
+    return {"objective": f"mean sigma_{pol} over {thetas[0]:g}..{thetas[-1]:g} deg (m^2)", "J_fp32ir": J32,
+            "J_fp64": J64, "n_params": len(r), "forward_s": tm["forward_s"], "gradient_s": tm["gradient_s"],
+            "forward_fp64_s": tm64["forward_s"], "gradient_fp64_s": tm64["gradient_s"],
+            "grad_fp32ir_vs_fp64_rel": float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))),
+            "fd_check": {"h": h, "method": "central differences of FP64 solves at h and h/2, Richardson-"
+                                            "extrapolated; rel_err_*_plain_fd: against the plain h = 1e-4 value",
+                         "max_rel_err_fp32ir": max(c["rel_err_fp32ir"] for c in checks),
+                         "max_rel_err_fp64": max(c["rel_err_fp64"] for c in checks),
+                         "max_rel_err_fp32ir_plain_fd": max(c["rel_err_fp32ir_plain_fd"] for c in checks),
+                         "params": checks}}
 
 
 class ClockSampler:
@@ -116,6 +183,27 @@ def load_peaks():
         d = json.load(open(p))
         return {"hbm_gbs": d.get("hbm_gbs"), "bf16_tflops": d.get("bf16_tflops"), "source": "measured"}
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def max_over_ranks(x: float) -> float:
+    """Maximum of a per-rank time over the process group (one value per rank);
+    works on the nccl (CUDA tensor) and gloo (CPU tensor) backends."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput of independent replicas: every rank processes
+    units_per_rank; the job takes the slowest rank's time."""
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    return units_per_rank * world / max_over_ranks(seconds)
 
 
 # ---------------------------------------------------------------------------
@@ -201,7 +289,7 @@ def run_gpu(args, rank, world):
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
         results = []
-        kernel_s = {}
+        kernel_s, kernel_w = {}, {}
         for _ in range(args.steps):
             r = prob.sweep("fp32ir")
             results.append(r)
@@ -209,21 +297,20 @@ def run_gpu(args, rank, world):
                 stages[kk] = stages.get(kk, 0.0) + v / args.steps
             for kk, v in r.kernel_s.items():
                 kernel_s.setdefault(kk, []).extend(v)
+                kernel_w.setdefault(kk, []).extend([kernel_work(prob, kk)] * len(v))
         e1.record()
         torch.cuda.synchronize()
         barrier()
     launches = nat.launch_count() - l0
-    dev_s = e0.elapsed_time(e1) / 1e3 / args.steps
-    if dist:
-        t = torch.tensor([dev_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t)
-    value = angle_pol * world / dev_s
+    dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps)
+    value = replica_throughput(angle_pol, dev_s)
     clocks = clk.summary()
 
-    # FP64 plain comparator (same sweep, FP64 fill/LU/solve/residual)
-    r64 = prob.sweep("fp64")
-    torch.cuda.synchronize()
+    # FP64 plain comparator (same sweep, FP64 fill/LU/solve/residual); its
+    # warm-up sweep is skipped when one FP32+IR sweep already takes > 5 s
+    if dev_s < 5.0:
+        r64 = prob.sweep("fp64")
+        torch.cuda.synchronize()
     f64_steps = max(1, args.steps // 3)
     e0.record()
     for _ in range(f64_steps):
@@ -245,66 +332,139 @@ def run_gpu(args, rank, world):
     for _ in range(e2e_steps):
         out = bs.solve_bor(pts, f, thetas, n_modes=M, mode_tol=0.0, table_precision="auto")
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps)
     h2d = prob.h2d_bytes()
     d2h = (M + 1) * angle_pol * 16 + (M + 1) * (2 * 8 + 4)
-    return dict(value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s, clocks=clocks, launches=launches,
+    adjoint = adjoint_leg(WORKLOADS[args.workload], f, thetas) if WORKLOADS[args.workload]["body"] == "bspline" \
+        else None
+    return dict(adjoint=adjoint, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s,
+                kernel_work=kernel_w, steps=args.steps, clocks=clocks, launches=launches,
                 f64_s=f64_s, f64_steps=f64_steps, db=db, rel=rel, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
                 refine_iters=results[-1].refine_iters, residual=float(np.max(results[-1].residual)),
                 prob=prob, angle_pol=angle_pol, M=M, thetas=thetas)
 
 
-def roofline(res, peaks):
+def kernel_work(prob, name):
+    """Algorithmic work of one launch: flops for the residual (complex MAC = 8
+    real flops), bytes of the complex128 operator written for the fills."""
+    n, M1, nrhs = prob.n, prob.m_max + 1, prob.nrhs
+    if name in ("residual", "residual_update"):
+        return 8.0 * n * n * nrhs * M1
+    if name == "far_fill":
+        return 16.0 * M1 * n * n
+    return 16.0 * M1 * 4 * prob.Nn * 5
+
+
+def run_batch(args, rank, world):
+    """Batch workload: every body's sweep back to back (value), the public
+    solve_bor_batch with host inputs (e2e), FP64 plain on every 8th body."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    eng = importlib.import_module(PKG + ".engine")
+    bs = importlib.import_module(PKG + ".bor_solver")
+    nat = importlib.import_module(PKG + "._native")
+    w = WORKLOADS[args.workload]
+    bodies = importlib.import_module(PKG + ".bodies").random_bodies(w["n_bodies"], 0)
+    thetas = np.arange(0.0, 180.0 + 1e-9, w["dtheta"])
+    probs = [eng.BorGpuProblem(b["points"], b["freq_hz"], thetas, m_max=b["m_max"]) for b in bodies]
+    angle_pol = 2 * len(thetas) * len(bodies)
+
+    for _ in range(args.warmup):
+        for p in probs:
+            p.sweep("fp32ir")
+    torch.cuda.synchronize()
+    stages, kernel_s, kernel_w = {}, {}, {}
+    l0 = nat.launch_count()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        last = []
+        for _ in range(args.steps):
+            last = []
+            for p in probs:
+                r = p.sweep("fp32ir")
+                last.append(r)
+                for kk, v in r.timings.items():
+                    stages[kk] = stages.get(kk, 0.0) + v / args.steps
+                for kk, v in r.kernel_s.items():
+                    kernel_s.setdefault(kk, []).extend(v)
+                    kernel_w.setdefault(kk, []).extend([kernel_work(p, kk)] * len(v))
+        e1.record()
+        torch.cuda.synchronize()
+    launches = nat.launch_count() - l0
+    dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps)
+    value = replica_throughput(angle_pol, dev_s)
+    clocks = clk.summary()
+    # FP64 plain on every 8th body; the speed-up is taken on the same bodies
+    sample = list(range(0, len(probs), 8))
+    t32 = sum(last[i].timings["gpu_total_s"] for i in sample)
+    e0.record()
+    r64 = {i: probs[i].sweep("fp64") for i in sample}
+    e1.record()
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3
+    db, rel = 0.0, 0.0
+    for i in sample:
+        F32, F64 = last[i].dF.sum(0), r64[i].dF.sum(0)
+        db = max(db, float(np.max(np.abs(20 * np.log10(np.abs(F32) / np.abs(F64))))))
+        rel = max(rel, float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64))))
+    # end to end through the public batch API with host inputs
+    t0 = time.perf_counter()
+    bs.solve_bor_batch(bodies, thetas, mode_tol=0.0, table_precision="auto")
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    h2d = sum(p.h2d_bytes() for p in probs)
+    d2h = sum((p.m_max + 1) * 2 * len(thetas) * 16 + (p.m_max + 1) * 20 for p in probs)
+    return dict(adjoint=None, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s, kernel_work=kernel_w,
+                steps=args.steps, clocks=clocks, launches=launches, f64_s=t64 * dev_s / max(t32, 1e-12),
+                f64_steps=1, f64_note=f"FP64 plain on bodies {sample}: {t64:.2f} s vs FP32+IR {t32:.2f} s, "
+                                      "scaled to the batch by that ratio",
+                db=db, rel=rel, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
+                refine_iters=max(r.refine_iters for r in last), residual=float(max(np.max(r.residual) for r in last)),
+                angle_pol=angle_pol / world * world, M=max(p.m_max for p in probs), thetas=thetas)
+
+
+def roofline(res, peaks, workload):
     """Roofline of the kernel with the largest device time per step.
 
     Launch durations come from CUDA events recorded on the launch stream
-    around single launches inside the timed steps.  Algorithmic work per
-    launch:
-      residual  R = B - (Z_far + Z_near) X over every mode: 8 n^2 nrhs (M+1)
-                real flops (complex MAC = 8); a GEMM, so the tensor peak is
-                the ceiling even though the kernel runs split-word FP32 on
-                the CUDA cores
-      fills     far_fill / near_fill: the bytes of the operator they write
-                (complex128 Z(m) for m = 0..M, resp. the near band); both
-                are arithmetic-bound, so this fraction is small by nature
+    around single launches inside the timed steps; achieved = algorithmic work
+    of those launches / their time.  The residual R = B - (Z_far + Z_near) X is
+    GEMM-shaped, so the tensor peak is its ceiling even though it runs
+    split-word FP32 on the CUDA cores; the fills are arithmetic-bound and are
+    reported against HBM with the operator bytes they write (small by nature).
     """
-    prob = res["prob"]
-    ks = res["kernel_s"]
-    steps = max(1, len(ks.get("far_fill", [1])))
-    per_step = {k: sum(v) / steps for k, v in ks.items()}
+    ks, kw = res["kernel_s"], res["kernel_work"]
+    per_step = {k: sum(v) / res["steps"] for k, v in ks.items()}
     name = max(per_step, key=per_step.get)
-    dur = statistics.mean(ks[name])
-    n, M1, nrhs = prob.n, prob.m_max + 1, prob.nrhs
+    t_sum, w_sum = sum(ks[name]), sum(kw[name])
     shares = {k: round(v / res["dev_s"], 4) for k, v in per_step.items()}
-    if name == "residual":
-        work = 8.0 * n * n * nrhs * M1
-        ach = work / dur / 1e12
+    if name.startswith("residual"):
+        ach = w_sum / t_sum / 1e12
         peak = peaks["bf16_tflops"]
         out = {"bound": "tensor", "achieved": round(ach, 3), "peak": peak, "unit": "TFLOP/s",
                "frac": round(ach / peak, 5) if peak else None,
                "note": "residual B - Z X of all modes, 8 n^2 nrhs (M+1) flops per launch; "
                        "split-word FP32 on CUDA cores, so the bf16 tensor peak is a loose ceiling"}
     else:
-        work = 16.0 * M1 * (n * n if name == "far_fill" else 4 * prob.Nn * 5)
-        ach = work / dur / 1e9
+        ach = w_sum / t_sum / 1e9
         peak = peaks["hbm_gbs"]
         out = {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                "frac": round(ach / peak, 4) if peak else None,
                "note": f"{name}: complex128 operator bytes written per launch"}
-    out.update({"kernel": name, "launch_ms": round(dur * 1e3, 3), "launches_per_step":
-                len(ks[name]) / steps, "share_of_step": shares, "traffic": TRAFFIC.get(name),
-                "peak_source": peaks["source"]})
+    out.update({"kernel": name, "launch_ms": round(t_sum / len(ks[name]) * 1e3, 3),
+                "launches_per_step": len(ks[name]) / res["steps"], "share_of_step": shares,
+                "traffic": TRAFFIC.get((name, workload)), "peak_source": peaks["source"]})
     return out
 
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 1200-segment
 # cone-sphere; None until captured.
-TRAFFIC = {}
+TRAFFIC = {}     # (kernel, workload) -> bytes
 
 
 def main():
@@ -319,8 +479,12 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     w = WORKLOADS[args.workload]
+    n_theta = int(round((w.get("theta1", 180.0) - w.get("theta0", 0.0)) / w["dtheta"])) + 1
     config = {"workload": args.workload, "body": w["body"], "N": w["N"], "k": w["k"], "m_max": w["M"],
-              "n_theta": int(round(180 / w["dtheta"])) + 1, "pols": 2,
+              "n_theta": n_theta, "pols": 2,
+              **({"n_bodies": w["n_bodies"], "seed": 0, "N": "200..1600", "k": "12 seg/wavelength",
+                  "m_max": "ceil(k rho_max) + 10", "cpu_baseline_sample": "first body"}
+                 if w["body"] == "random" else {}),
               "l2": "per-step working set of several GB (>> 129 MB L2)",
               "parallelism": f"replicas x{world}"}
     cores = os.cpu_count() or 1
@@ -336,7 +500,7 @@ def main():
                 vals.append(v)
         v = statistics.median(vals)
         line = {"metric": METRIC, "value": v, "unit": "angle·pol/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2 * config["n_theta"] / v * 1e3,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2 * n_theta / v * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
                 "data": "synthetic (seeded geometry)", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "angle·pol/s", "cores": cores, "kind": "port",
@@ -348,7 +512,7 @@ def main():
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
-    res = run_gpu(args, rank, world)
+    res = run_batch(args, rank, world) if w["body"] == "random" else run_gpu(args, rank, world)
     if rank != 0:
         return
     cpu = None
@@ -365,15 +529,17 @@ def main():
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
-        "roofline": roofline(res, peaks),
+        "roofline": roofline(res, peaks, args.workload),
         "cpu_baseline": cpu,
         "fp64_plain": {"value": res["angle_pol"] / res["f64_s"], "ms_per_step": res["f64_s"] * 1e3,
-                       "steps": res["f64_steps"]},
+                       "steps": res["f64_steps"], **({"note": res["f64_note"]} if "f64_note" in res else {})},
         "speedup_fp32ir_vs_fp64": res["f64_s"] / res["dev_s"],
         "accuracy_vs_fp64": {"max_db_err": res["db"], "max_rel_amp_err": res["rel"]},
         "refine": {"iters": res["refine_iters"], "max_residual": res["residual"]},
         "stages_s": {k: round(v, 5) for k, v in res["stages"].items()},
     }
+    if res["adjoint"] is not None:
+        line["adjoint"] = res["adjoint"]
     print(json.dumps(line))
 
 

@@ -284,11 +284,14 @@ int ghost_bor_residual(int batch, int n, int nrhs, int Nn,
  *   R = B - (Zf + band) X32, with the arithmetic of ghost_bor_residual (the
  *   low FP32 word of X is zero, so the Z_hi X_lo products drop out).
  * R (complex double) and R32 (complex float) are each optional, not both.
+ * z_split = 1: Zf holds the FP32 words (hi.re, hi.im, lo.re, lo.im) written by
+ * ghost_bor_split_words instead of complex double (same 16 bytes per element),
+ * which takes the FP64 splitting out of the tile staging.
  * The first residual of the refinement; later residuals follow from it by
  * R -= fl32(Z) D for each correction D (ghost_bor_cgemm_tc).  No counterpart in
  * the reference (its solve is FP64 LAPACK, bor_solver.py:753-756). */
 int ghost_bor_residual_x32(int batch, int n, int nrhs, int Nn,
-                           const void *Zf, long long ldz, long long stride_z,
+                           const void *Zf, int z_split, long long ldz, long long stride_z,
                            const double *band, const int *mask_rows,
                            const float *X32, const double *B, long long ldb, long long stride_b,
                            double *R, float *R32, double *norms, void *stream);
@@ -322,6 +325,29 @@ int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
  *   blocks (dir 0: double->float, 1: float->double, 2: float added into
  *   double, 3: float->float).
  */
+/* Refinement residual with exact products on the bf16 tensor cores (Ozaki
+ * splitting): R = B - (Zf + band) X32 with Zf complex double, X32 the FP32
+ * solution (same ldb / stride_b as B).  Rows of Zf and columns of X32 are
+ * scaled by powers of two and split into four 8-bit integer slices (exact in
+ * bf16); slice products are accumulated exactly in FP32 TMEM over K chunks of
+ * 192 and folded into double-float accumulators, so the residual carries
+ * ~2^-31 of the row / column scales instead of the ~2^-24 of FP32 products.
+ * R and R32 optional (not both NULL); norms as in ghost_bor_residual.
+ * work: ghost_bor_residual_exact_workspace(batch, n, nrhs) bytes, 256-byte
+ * aligned; its first int is set to 1 if a bounded in-kernel wait gave up.
+ * No counterpart in the reference (its solve is FP64 LAPACK). */
+long long ghost_bor_residual_exact_workspace(int batch, int n, int nrhs);
+int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
+                             const double *Zf, long long ldz, long long stride_z,
+                             const double *band, const int *mask_rows,
+                             const float *X32, const double *B, long long ldb, long long stride_b,
+                             double *R, float *R32, double *norms,
+                             void *work, long long work_bytes, void *stream);
+
+/* In place: complex double Z -> its two FP32 words (hi.re, hi.im, lo.re, lo.im),
+ * hi = fl32(z), lo = fl32(z - hi). */
+int ghost_bor_split_words(int batch, int rows, int cols, void *Z, long long ldz, long long stride_z,
+                          void *stream);
 int ghost_bor_compose(int batch, int n, int Nn, const void *Zf, long long ldz, long long stride_z,
                       const double *band, const int *mask_rows,
                       void *A, long long lda, long long stride_a, void *stream);

@@ -181,3 +181,88 @@ def test_near_band_double_float_matches_fp64(pkg, torch, name):
     torch.cuda.synchronize()
     prob.check_near_status()
     assert (b32 - b64).abs().max().item() < 1e-12 * b64.abs().max().item()
+
+
+def test_residual_x32_presplit_matches(pkg, torch):
+    """ghost_bor_residual_x32 on Z_far split in place into FP32 words gives the
+    residual of the on-the-fly split bit for bit, and matches an FP64 residual."""
+    nat = pkg._native
+    rng = np.random.default_rng(5)
+    Mb, Nn, nrhs = 3, 70, 33
+    n = 2 * Nn
+    Zh = (rng.standard_normal((Mb, n, n)) + 1j * rng.standard_normal((Mb, n, n)))
+    Xh = (rng.standard_normal((Mb, n, nrhs)) + 1j * rng.standard_normal((Mb, n, nrhs))).astype(np.complex64)
+    Bh = Zh @ Xh.astype(np.complex128) + 1e-3 * (rng.standard_normal((Mb, n, nrhs)) + 0j)
+    Z = torch.as_tensor(Zh, device="cuda")
+    X = torch.as_tensor(Xh, device="cuda")
+    B = torch.as_tensor(Bh, device="cuda")
+    masks = torch.full((Mb, 4), -1, dtype=torch.int32, device="cuda")
+    out = []
+    for split in (0, 1):
+        R32 = torch.empty((Mb, n, nrhs), dtype=torch.complex64, device="cuda")
+        R = torch.empty((Mb, n, nrhs), dtype=torch.complex128, device="cuda")
+        norms = torch.empty((Mb, 2), dtype=torch.float64, device="cuda")
+        if split:
+            nat.call("ghost_bor_split_words", Mb, n, n, nat.ptr(Z), n, Z.stride(0), nat.stream_handle())
+        nat.call("ghost_bor_residual_x32", Mb, n, nrhs, Nn, nat.ptr(Z), split, n, Z.stride(0), 0,
+                 nat.ptr(masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0), nat.ptr(R), nat.ptr(R32),
+                 nat.ptr(norms), nat.stream_handle())
+        torch.cuda.synchronize()
+        out.append((R.cpu().numpy(), R32.cpu().numpy()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    ref = Bh - Zh @ Xh.astype(np.complex128)
+    assert np.max(np.abs(out[1][0] - ref)) < 1e-6 * np.max(np.abs(Bh))
+
+
+@pytest.mark.parametrize("Mb,Nn,nrhs", [(2, 70, 33), (3, 161, 97)])
+def test_residual_exact_bf16_slices(pkg, torch, Mb, Nn, nrhs):
+    """ghost_bor_residual_exact (Ozaki bf16 slices on tcgen05) against an FP64
+    reference, with a near band and masked rows: far below the FP32-product
+    floor of the split-word residual."""
+    nat = pkg._native
+    lib = nat.load()
+    rng = np.random.default_rng(11)
+    n = 2 * Nn
+    Zh = rng.standard_normal((Mb, n, n)) + 1j * rng.standard_normal((Mb, n, n))
+    Zh *= np.exp(rng.uniform(-3, 3, (Mb, n, 1)))            # rows of different magnitude
+    Xh = (rng.standard_normal((Mb, n, nrhs)) + 1j * rng.standard_normal((Mb, n, nrhs))).astype(np.complex64)
+    Xh *= np.exp(rng.uniform(-2, 2, (Mb, 1, nrhs))).astype(np.float32)
+    band_h = rng.standard_normal((Mb, 4, Nn, 5)) + 1j * rng.standard_normal((Mb, 4, Nn, 5))
+    Bh = Zh @ Xh.astype(np.complex128) * (1 + 1e-6 * rng.standard_normal((Mb, n, nrhs)))
+    masks_h = np.full((Mb, 4), -1, dtype=np.int32)
+    masks_h[:, 0] = 0
+    masks_h[:, 1] = Nn
+    # FP64 reference with the band (block (row half, col half) diagonals -2..2)
+    ref = Bh - Zh @ Xh.astype(np.complex128)
+    X64 = Xh.astype(np.complex128)
+    for b in range(Mb):
+        for half in range(2):
+            for ch in range(2):
+                for d in range(5):
+                    for node in range(Nn):
+                        jn = node + d - 2
+                        if 0 <= jn < Nn:
+                            ref[b, half * Nn + node] -= band_h[b, 2 * half + ch, node, d] * X64[b, ch * Nn + jn]
+        ref[b, masks_h[b][masks_h[b] >= 0]] = 0
+    Z = torch.as_tensor(Zh, device="cuda")
+    X = torch.as_tensor(Xh, device="cuda")
+    B = torch.as_tensor(Bh, device="cuda")
+    band = torch.as_tensor(band_h, device="cuda")
+    masks = torch.as_tensor(masks_h, device="cuda")
+    R = torch.empty((Mb, n, nrhs), dtype=torch.complex128, device="cuda")
+    R32 = torch.empty((Mb, n, nrhs), dtype=torch.complex64, device="cuda")
+    norms = torch.empty((Mb, 2), dtype=torch.float64, device="cuda")
+    nbytes = int(lib.ghost_bor_residual_exact_workspace(Mb, n, nrhs))
+    work = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    nat.call("ghost_bor_residual_exact", Mb, n, nrhs, Nn, nat.ptr(Z), n, Z.stride(0), nat.ptr(band),
+             nat.ptr(masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0), nat.ptr(R), nat.ptr(R32),
+             nat.ptr(norms), nat.ptr(work), nbytes, nat.stream_handle())
+    torch.cuda.synchronize()
+    assert int(work[:4].view(torch.int32)[0]) == 0
+    got = R.cpu().numpy()
+    scale = np.max(np.abs(Bh))
+    assert np.max(np.abs(got - ref)) < 2e-9 * scale, np.max(np.abs(got - ref)) / scale
+    nr = norms.cpu().numpy()
+    np.testing.assert_allclose(nr[:, 0], np.sum(np.abs(got) ** 2, axis=(1, 2)), rtol=1e-10)
+    np.testing.assert_allclose(nr[:, 1], np.sum(np.abs(Bh) ** 2, axis=(1, 2)), rtol=1e-10)

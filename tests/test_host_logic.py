@@ -90,7 +90,17 @@ def test_adjoint_identity_on_oracle(pkg, oracle):
     Fp, Ap, Vp, _ = field(build(rp))
     Fm, Am, Vm, _ = field(build(rm))
     dZ, dV = (Ap - Am) / (2 * h), (Vp - Vm) / (2 * h)
-    Dx = D[mask][:, None] * x0
-    adj = -c * (2 * np.sum(Dx * dV, axis=0) - np.sum(Dx * (dZ @ x0), axis=0))
+    Dm = D[mask][:, None]
+    Dx = Dm * x0
     fd = (Fp - Fm) / (2 * h)
-    assert np.max(np.abs(adj - fd)) < 1e-5 * np.max(np.abs(fd))
+    # reciprocity adjoint y = D x (exact only for a symmetric quadrature)
+    adj_sym = -c * (2 * np.sum(Dx * dV, axis=0) - np.sum(Dx * (dZ @ x0), axis=0))
+    assert np.max(np.abs(adj_sym - fd)) < 1e-4 * np.max(np.abs(fd))
+    # the adjoint module's y = D x + D A^-1 D s, s = D V - A^T D x, against the
+    # exact adjoint solution A^T y = D V and the central difference
+    y_exact = np.linalg.solve(A0.T, Dm * V0)
+    s_ = Dm * V0 - A0.T @ Dx
+    y = Dx + Dm * np.linalg.solve(A0, Dm * s_)
+    assert np.max(np.abs(y - y_exact)) < 1e-7 * np.max(np.abs(y_exact))
+    adj = -c * (np.sum(Dx * dV, axis=0) + np.sum(y * (dV - dZ @ x0), axis=0))
+    assert np.max(np.abs(adj - fd)) < 1e-6 * np.max(np.abs(fd))
