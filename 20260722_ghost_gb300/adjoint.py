@@ -110,7 +110,7 @@ class ShapeGradient:
         n = p.n
         nat.call("ghost_bor_far_efie_masked", nat.F64, p.N, p.m_max, p.n_xi, p.k, scale.real, scale.imag,
                  nat.ptr(tabs.geo), nat.ptr(p.d_dct), nat.ptr(p.d_sin2), nat.ptr(self.dZ), n,
-                 self.dZ.stride(0), nat.ptr(emask), st)
+                 self.dZ.stride(0), nat.ptr(emask), 0, st)
         if pairs is not None:
             work, nbytes = p._near_work("ghost_bor_near_workspace")
             nat.call("ghost_bor_near_efie", nat.F64, p.N, p.m_max, p.k, scale.real, scale.imag,

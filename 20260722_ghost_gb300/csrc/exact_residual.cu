@@ -21,7 +21,8 @@
 // far below the FP32-product floor (~2^-24) of a split-word SIMT residual --
 // and runs at tensor-core rate.
 //
-// The near band and the masks are applied in FP64 in the epilogue.
+// The near band is added to Z_far before the split (A = Z_far + band), so the
+// epilogue only forms R = B - P in FP64 and zeroes the masked rows.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -37,7 +38,8 @@ constexpr int XBK = 64;                  // real K per stage (64 bf16 = one 128-
 constexpr int XCHUNK = 3;                // stages per exact accumulation (K = 192)
 constexpr int XLEV = 5;                  // levels s + t = 2..6
 constexpr uint32_t XTMEM_COLS = 512;     // power of two >= XLEV * XBN
-constexpr int XTHREADS = 128;
+constexpr int XTHREADS = 256;            // 8 warps: warps w and w + 4 share TMEM lanes, split the columns
+constexpr int XCOLS = XBN / 2;           // real columns per thread in the fold
 constexpr int XA_TILE = XBM * XBK;       // bf16 elements
 constexpr int XB_TILE = XBN * XBK;
 
@@ -70,21 +72,57 @@ __device__ __forceinline__ int scale_exp(double m)
     return e;
 }
 
-// four balanced base-256 digits of u (|u| < 1): u ~ q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31
-__device__ __forceinline__ void digits(double u, float (&q)[XS])
+// four balanced base-256 digits of v / 2^e (|v| < 2^e):
+//   v / 2^e ~ q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31,  |q_s| <= 128,
+// by integer arithmetic on the IEEE bits: W = round(v 2^(31 - e)) (|W| <= 2^31)
+// is split into balanced base-256 digits with arithmetic shifts.
+__device__ __forceinline__ void digits(double v, int e, float (&q)[XS])
 {
-    double t = u * 128.0;
+    const long long bits = __double_as_longlong(v);
+    const int E = (int)((bits >> 52) & 0x7ff);
+    long long W = 0;
+    if (E != 0) {                                    // zero and subnormals -> 0 (below 2^-1022)
+        const long long m = (bits & 0xfffffffffffffLL) | 0x10000000000000LL;
+        const int sh = (E - 1075) + 31 - e;          // v = m 2^(E - 1075)
+        if (sh >= 0) W = m << sh;
+        else if (sh > -64) W = (m + (1LL << (-sh - 1))) >> (-sh);
+        if (bits < 0) W = -W;
+    }
+#pragma unroll
+    for (int s = XS - 1; s >= 1; --s) {
+        const long long t = (W + 128) >> 8;          // floor((W + 128) / 256)
+        q[s] = (float)(int)(W - (t << 8));
+        W = t;
+    }
+    q[0] = (float)(int)W;
+}
+
+// the same for an FP32 value (exact FP32 arithmetic)
+__device__ __forceinline__ void digits(float v, int e, float (&q)[XS])
+{
+    float t = ldexpf(v, 7 - e);
 #pragma unroll
     for (int s = 0; s < XS; ++s) {
-        const double d = rint(t);
-        q[s] = (float)d;
-        t = (t - d) * 256.0;
+        const float d = rintf(t);
+        q[s] = d;
+        t = (t - d) * 256.0f;
     }
 }
 
+// near band entry of A = Z_far + band at (row i, complex column k), or 0
+__device__ __forceinline__ double2 band_at(const double2 *band, int b, int Nn, int i, int k)
+{
+    if (!band) return make_double2(0.0, 0.0);
+    const int half = i >= Nn ? 1 : 0, node = i - half * Nn;
+    const int ch = k >= Nn ? 1 : 0, jn = k - ch * Nn;
+    const int d = jn - node + 2;
+    if (d < 0 || d > 4) return make_double2(0.0, 0.0);
+    return band[(((size_t)b * 4 + 2 * half + ch) * Nn + node) * 5 + d];
+}
+
 // row exponents of A: one warp per row of Z_far (2n reals)
-__global__ void row_exp_kernel(int batch, int n, const double2 *__restrict__ Z, long long ldz, long long sz,
-                               int *__restrict__ ex)
+__global__ void row_exp_kernel(int batch, int n, int Nn, const double2 *__restrict__ Z, long long ldz, long long sz,
+                               const double2 *__restrict__ band, int *__restrict__ ex)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= batch * n) return;
@@ -92,7 +130,7 @@ __global__ void row_exp_kernel(int batch, int n, const double2 *__restrict__ Z, 
     const double2 *row = Z + (size_t)b * sz + (size_t)i * ldz;
     double m = 0.0;
     for (int k = lane; k < n; k += 32) {
-        const double2 v = row[k];
+        const double2 v = cadd(row[k], band_at(band, b, Nn, i, k));
         m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
     }
 #pragma unroll
@@ -101,8 +139,9 @@ __global__ void row_exp_kernel(int batch, int n, const double2 *__restrict__ Z, 
 }
 
 // A slices: As[s][b][i][kr], kr < Kp (zero beyond 2n)
-__global__ void slice_a_kernel(int batch, int n, int Kp, const double2 *__restrict__ Z, long long ldz, long long sz,
-                               const int *__restrict__ ex, __nv_bfloat16 *__restrict__ As)
+__global__ void slice_a_kernel(int batch, int n, int Nn, int Kp, const double2 *__restrict__ Z, long long ldz,
+                               long long sz, const double2 *__restrict__ band, const int *__restrict__ ex,
+                               __nv_bfloat16 *__restrict__ As)
 {
     const int kh = Kp / 2;
     const long long total = (long long)batch * n * kh;
@@ -112,11 +151,12 @@ __global__ void slice_a_kernel(int batch, int n, int Kp, const double2 *__restri
         const int k = (int)(idx % kh);
         const long long bi = idx / kh;
         const int i = (int)(bi % n), b = (int)(bi / n);
-        const double2 v = (k < n) ? Z[(size_t)b * sz + (size_t)i * ldz + k] : make_double2(0.0, 0.0);
+        const double2 v = (k < n) ? cadd(Z[(size_t)b * sz + (size_t)i * ldz + k], band_at(band, b, Nn, i, k))
+                                  : make_double2(0.0, 0.0);
         const int e = ex[bi];
         float qr[XS], qi[XS];
-        digits(ldexp(v.x, -e), qr);
-        digits(ldexp(v.y, -e), qi);
+        digits(v.x, e, qr);
+        digits(v.y, e, qi);
         const size_t o = (size_t)bi * Kp + 2 * (size_t)k;
 #pragma unroll
         for (int s = 0; s < XS; ++s) {
@@ -172,11 +212,17 @@ slice_b_kernel(int batch, int n, int nrhs, int Kp, const float2 *__restrict__ X,
         const int c = ocol & 1;
         const float v = (rr == 0) ? (c == 0 ? x.x : -x.y) : (c == 0 ? x.y : x.x);
         float qd[XS];
-        digits(ldexp((double)v, -fx[(size_t)b * nrhs + j]), qd);
+        digits(v, fx[(size_t)b * nrhs + j], qd);
         const size_t o = ((size_t)b * 2 * nrhs + 2 * j + rr) * Kp + kc;
 #pragma unroll
         for (int s = 0; s < XS; ++s) Bs[s * plane + o] = __float2bfloat16_rn(qd[s]);
     }
+}
+
+// 2^k as a double (|k| < 1023), built from the exponent bits
+__device__ __forceinline__ double exp2i(int k)
+{
+    return __longlong_as_double((long long)(k + 1023) << 52);
 }
 
 __device__ __forceinline__ bool row_masked(const int *mr, int r)
@@ -190,10 +236,9 @@ struct XMaps {
 };
 
 __global__ void __launch_bounds__(XTHREADS)
-exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int Nn, int Kp,
-                      const int *__restrict__ ex, const int *__restrict__ fx,
-                      const double2 *__restrict__ band, const int *__restrict__ mask_rows,
-                      const float2 *__restrict__ X, const double2 *__restrict__ B, long long ldb, long long sbb,
+exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int Kp,
+                      const int *__restrict__ ex, const int *__restrict__ fx, const int *__restrict__ mask_rows,
+                      const double2 *__restrict__ B, long long ldb, long long sbb,
                       double2 *__restrict__ R, float2 *__restrict__ R32, double *__restrict__ norms,
                       int *__restrict__ err)
 {
@@ -244,10 +289,12 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int N
         if (nst > 1) load_stage(1);
     }
 
-    // double-float accumulators of this thread's row, 64 real columns
-    float hi[XBN], lo[XBN];
+    // double-float accumulators of this thread's row (TMEM lane 32 (warp % 4) + lane)
+    // and 32 of the tile's 64 real columns (half warp / 4)
+    const int quad = warp & 3, chalf = warp >> 2;
+    float hi[XCOLS], lo[XCOLS];
 #pragma unroll
-    for (int c = 0; c < XBN; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
+    for (int c = 0; c < XCOLS; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
 
     for (int ch = 0; ch < nch; ++ch) {
         if (tid == 0 && ok) {
@@ -292,25 +339,22 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int N
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (!s.failed) {
-            const uint32_t row_addr = tmem + ((uint32_t)(warp * 32) << 16);
+            const uint32_t row_addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(chalf * XCOLS);
 #pragma unroll
             for (int L = 0; L < XLEV; ++L) {
                 const float sc = ldexpf(1.0f, -14 - 8 * L);
+                float v[32];
+                tmem_ld32(row_addr + (uint32_t)(L * XBN), v);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    float v[32];
-                    tmem_ld32(row_addr + (uint32_t)(L * XBN + h * 32), v);
-#pragma unroll
-                    for (int c = 0; c < 32; ++c) {
-                        // x is exact (an integer times a power of two); a two-sum
-                        // keeps every level exact in (hi, lo), so lo only collects
-                        // rounding errors of hi (~2^-24 |hi|) and stays precise
-                        const float x = v[c] * sc;
-                        const float t = hi[h * 32 + c] + x;
-                        const float bb2 = t - hi[h * 32 + c];
-                        lo[h * 32 + c] += (hi[h * 32 + c] - (t - bb2)) + (x - bb2);
-                        hi[h * 32 + c] = t;
-                    }
+                for (int c = 0; c < XCOLS; ++c) {
+                    // x is exact (an integer times a power of two); a two-sum keeps
+                    // every level exact in (hi, lo), so lo only collects rounding
+                    // errors of hi (~2^-24 |hi|) and stays precise
+                    const float x = v[c] * sc;
+                    const float t = hi[c] + x;
+                    const float bb2 = t - hi[c];
+                    lo[c] += (hi[c] - (t - bb2)) + (x - bb2);
+                    hi[c] = t;
                 }
             }
         }
@@ -322,46 +366,38 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int N
     // P = 2^(e_i + f_j) (hi + lo) through shared memory (the operand buffers are free)
     double (*Ps)[XBN + 1] = reinterpret_cast<double (*)[XBN + 1]>(&s.a[0][0][0]);
     if (!s.failed) {
-        const int r = warp * 32 + lane;
+        const int r = quad * 32 + lane;
         const int i = m0 + r;
         const int e = (i < n) ? ex[(size_t)b * n + i] : 0;
 #pragma unroll
-        for (int c = 0; c < XBN; ++c) {
-            const int j = (n0 + c) >> 1;
+        for (int c = 0; c < XCOLS; ++c) {
+            const int cc = chalf * XCOLS + c;
+            const int j = (n0 + cc) >> 1;
             const int f = (j < nrhs) ? fx[(size_t)b * nrhs + j] : 0;
-            Ps[r][c] = ldexp((double)hi[c] + (double)lo[c], e + f);
+            Ps[r][cc] = ((double)hi[c] + (double)lo[c]) * exp2i(e + f);
         }
     }
     __syncthreads();
-    double rn = 0.0, bn = 0.0;
+    // R = B - P (the near band is inside the slices), masked rows zero; each warp
+    // 16 rows, lane = complex column; norms in FP32 (reported, not refined)
+    float rn = 0.f, bn = 0.f;
     if (!s.failed) {
         const int *mr = mask_rows + 4 * b;
         const double2 *Bb = B + (size_t)b * sbb;
-        const float2 *Xb = X + (size_t)b * sbb;
-        const int j = (n0 >> 1) + lane;          // complex column of this lane
-        for (int rr = 0; rr < 32; ++rr) {
-            const int r = warp * 32 + rr;
+        const int j = (n0 >> 1) + lane;
+        for (int rr = 0; rr < XBM / 8; ++rr) {
+            const int r = warp * (XBM / 8) + rr;
             const int i = m0 + r;
             if (i >= n || j >= nrhs) continue;
             const double2 bv = Bb[(size_t)i * ldb + j];
             double2 rv = make_double2(bv.x - Ps[r][2 * lane], bv.y - Ps[r][2 * lane + 1]);
-            if (band) {
-                const int half = i >= Nn ? 1 : 0, node = i - half * Nn;
-                for (int c2 = 0; c2 < 2; ++c2) {
-                    const double2 *bd = band + (((size_t)b * 4 + 2 * half + c2) * Nn + node) * 5;
-                    for (int d = 0; d < 5; ++d) {
-                        const int jn = node + d - 2;
-                        if (jn < 0 || jn >= Nn) continue;
-                        const float2 xv = Xb[(size_t)(c2 * Nn + jn) * ldb + j];
-                        rv = cfms(bd[d], make_double2(xv.x, xv.y), rv);
-                    }
-                }
-            }
             if (row_masked(mr, i)) rv = make_double2(0.0, 0.0);
             if (R) R[(size_t)b * sbb + (size_t)i * ldb + j] = rv;
-            if (R32) R32[(size_t)b * sbb + (size_t)i * ldb + j] = make_float2((float)rv.x, (float)rv.y);
-            rn += rv.x * rv.x + rv.y * rv.y;
-            bn += bv.x * bv.x + bv.y * bv.y;
+            const float2 r32 = make_float2((float)rv.x, (float)rv.y);
+            if (R32) R32[(size_t)b * sbb + (size_t)i * ldb + j] = r32;
+            const float2 b32 = make_float2((float)bv.x, (float)bv.y);
+            rn = fmaf(r32.x, r32.x, fmaf(r32.y, r32.y, rn));
+            bn = fmaf(b32.x, b32.x, fmaf(b32.y, b32.y, bn));
         }
     }
 #pragma unroll
@@ -370,8 +406,8 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int N
         bn += __shfl_xor_sync(0xffffffffu, bn, off);
     }
     if (lane == 0 && !s.failed) {
-        atomicAdd(norms + 2 * b, rn);
-        atomicAdd(norms + 2 * b + 1, bn);
+        atomicAdd(norms + 2 * b, (double)rn);
+        atomicAdd(norms + 2 * b + 1, (double)bn);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -440,12 +476,13 @@ extern "C" int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
     const float2 *X = reinterpret_cast<const float2 *>(X32);
     {
         const long long rows = (long long)batch * n;
-        row_exp_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(batch, n, Z, ldz, stride_z, ex);
+        const double2 *bd = reinterpret_cast<const double2 *>(band);
+        row_exp_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(batch, n, Nn, Z, ldz, stride_z, bd, ex);
         int rc = check_launch("residual_exact: row exponents");
         if (rc) return rc;
         const long long pairs = (long long)batch * n * (Kp / 2);
         const int blocks = (int)((pairs + 255) / 256 < 152 * 32 ? (pairs + 255) / 256 : 152 * 32);
-        slice_a_kernel<<<blocks, 256, 0, st>>>(batch, n, Kp, Z, ldz, stride_z, ex, As);
+        slice_a_kernel<<<blocks, 256, 0, st>>>(batch, n, Nn, Kp, Z, ldz, stride_z, bd, ex, As);
         if ((rc = check_launch("residual_exact: slice A"))) return rc;
         dim3 gc((nrhs + 31) / 32, batch);
         col_exp_kernel<<<gc, 256, 0, st>>>(n, nrhs, X, ldb, stride_b, fx);
@@ -471,8 +508,7 @@ extern "C" int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
         attr = true;
     }
     dim3 grid((2 * nrhs + XBN - 1) / XBN, (n + XBM - 1) / XBM, batch);
-    exact_residual_kernel<<<grid, XTHREADS, smem, st>>>(maps, n, nrhs, Nn, Kp, ex, fx,
-                                                         reinterpret_cast<const double2 *>(band), mask_rows, X,
+    exact_residual_kernel<<<grid, XTHREADS, smem, st>>>(maps, n, nrhs, Kp, ex, fx, mask_rows,
                                                          reinterpret_cast<const double2 *>(B), ldb, stride_b,
                                                          reinterpret_cast<double2 *>(R),
                                                          reinterpret_cast<float2 *>(R32), norms, errp);

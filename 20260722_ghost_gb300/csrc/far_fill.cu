@@ -41,19 +41,21 @@ constexpr int TPB = EPB * 16 * 4; // Gauss-point pairs x order groups
 constexpr int JC = 32;            // azimuth samples staged per smem chunk
 
 constexpr int OG = 4;                 // order groups: threads sharing one Gauss-point pair
+constexpr int SLAB = 17;              // 16-byte entries per (pair, order) slab of Gs: 16 used + 1 pad
+                                      // so that slabs read by neighbouring threads hit distinct banks
 constexpr int PPB = EPB * 16;         // Gauss-point pairs per CTA
 
 template <class R, int NT> struct SmemLayout {
     // gsm  [JC][PPB]        C<R>     samples of the current chunk
     // dcts [JC][OG*NT]      R
     // s2s  [JC]             S2
-    // Gs   [EPB][OG*NT][16] 16 B     per-pair orders, later the mode-local blocks
+    // Gs   [EPB][OG*NT][SLAB] 16 B   per-pair orders, later the mode-local blocks
     // P11s [EPB][OG*NT][4]  16 B
     // wts  [EPB+1][24]      double ; wtf [EPB+1][24] float2
     static constexpr int NOB = OG * NT;
     static size_t bytes() {
         return sizeof(C<R>) * (size_t)JC * PPB + sizeof(R) * (size_t)JC * NOB +
-               sizeof(typename GreenSampler<R>::S2) * JC + 16 * (size_t)EPB * NOB * 16 +
+               sizeof(typename GreenSampler<R>::S2) * JC + 16 * (size_t)EPB * NOB * SLAB +
                16 * (size_t)EPB * NOB * 4 + (sizeof(double) + sizeof(float2)) * (size_t)(EPB + 1) * 24;
     }
 };
@@ -63,7 +65,8 @@ __global__ void __launch_bounds__(TPB, 2)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
                 const double *__restrict__ sin2, double2 *__restrict__ Z,
-                long long ldz, long long mode_stride, const unsigned char *__restrict__ emask)
+                long long ldz, long long mode_stride, const unsigned char *__restrict__ emask,
+                const float *__restrict__ dct32)
 {
     using CT = C<R>;
     using Samp = GreenSampler<R>;
@@ -74,7 +77,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     R *dcts = reinterpret_cast<R *>(gsm + JC * PPB);
     S2 *s2s = reinterpret_cast<S2 *>(dcts + JC * NOB);
     double2 *Gs = reinterpret_cast<double2 *>(s2s + JC);
-    double2 *P11s = Gs + EPB * NOB * 16;
+    double2 *P11s = Gs + EPB * NOB * SLAB;
     double *wts = reinterpret_cast<double *>(P11s + EPB * NOB * 4);
     float2 *wtf = reinterpret_cast<float2 *>(wts + (EPB + 1) * 24);
 
@@ -131,7 +134,12 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         for (int i = tid; i < JC * NOB; i += TPB) {
             const int jj = i / NOB, n = i % NOB;
             const int j = j0 + jj, o = o0 + n;
-            dcts[i] = (j <= h && o < Mp) ? (R)dct[(size_t)j * Mp + o] : R(0);
+            R t = R(0);
+            if (j <= h && o < Mp) {
+                if constexpr (sizeof(R) == 4) t = dct32 ? dct32[(size_t)j * Mp + o] : (R)dct[(size_t)j * Mp + o];
+                else t = dct[(size_t)j * Mp + o];
+            }
+            dcts[i] = t;
         }
         for (int jj = tid; jj < JC; jj += TPB) s2s[jj] = Samp::load_s2(sin2, min(j0 + jj, h));
         __syncthreads();
@@ -199,11 +207,11 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         float4 *Gf = reinterpret_cast<float4 *>(Gs);
 #pragma unroll
         for (int n = 0; n < NT; ++n)
-            Gf[(ep * NOB + og * NT + n) * 16 + gh] = make_float4(acc[n].x, -cmp[n].x, acc[n].y, -cmp[n].y);
+            Gf[(ep * NOB + og * NT + n) * SLAB + gh] = make_float4(acc[n].x, -cmp[n].x, acc[n].y, -cmp[n].y);
     } else {
 #pragma unroll
         for (int n = 0; n < NT; ++n)
-            Gs[(ep * NOB + og * NT + n) * 16 + gh] = make_double2(acc[n].x, acc[n].y);
+            Gs[(ep * NOB + og * NT + n) * SLAB + gh] = make_double2(acc[n].x, acc[n].y);
     }
     __syncthreads();
 
@@ -221,7 +229,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         if (doit) {
             if constexpr (sizeof(R) == 4) {
                 // double-float contraction (exact well below an FP32 ulp)
-                const float4 *Gf = reinterpret_cast<const float4 *>(Gs) + (jep * NOB + n) * 16;
+                const float4 *Gf = reinterpret_cast<const float4 *>(Gs) + (jep * NOB + n) * SLAB;
                 const float2 *wt = wtf + EPB * 24;      // test element weights
                 const float2 *ws = wtf + jep * 24;      // source element weights
                 float4 GR1[4], GRs[4], GRd[4];          // (re.hi, re.lo, im.hi, im.lo) per g
@@ -260,7 +268,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
                     for (int c = 0; c < 5; ++c) out[c][a] = make_double2(df_to(acc2[c][0]), df_to(acc2[c][1]));
                 }
             } else {
-                const double2 *Gd = Gs + (jep * NOB + n) * 16;
+                const double2 *Gd = Gs + (jep * NOB + n) * SLAB;
                 const double *wt = wts + EPB * 24;
                 const double *ws = wts + jep * 24;
                 double2 GR1[4], GRs[4], GRd[4];
@@ -303,7 +311,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
             const double tt = tze * tzf;
             const double fm = o * ik2;               // jm/k^2 magnitude
             const double fm2 = (double)o * o * ik2;  // m^2/k^2
-            double2 *zl = Gs + (jep * NOB + n) * 16;
+            double2 *zl = Gs + (jep * NOB + n) * SLAB;
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
                 const int ab = a * 2 + b;
@@ -326,7 +334,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         const int ff = f0 + jep;
         if (ff >= N || abs(e - ff) < 2 || (emask && !emask[e] && !emask[ff])) continue;
         const int nl = abs(m - 1) - o0, nm = m - o0, nh = m + 1 - o0;
-        const double2 *zl = Gs + (jep * NOB + nm) * 16;
+        const double2 *zl = Gs + (jep * NOB + nm) * SLAB;
         const double tre = geo[(size_t)9 * P + 4 * e], trf = geo[(size_t)9 * P + 4 * ff];
         double2 *Zm = Z + (size_t)m * mode_stride;
 #pragma unroll
@@ -354,7 +362,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
 template <class R, int NT>
 int launch_far(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                const double *dct, const double *sin2, void *Z, long long ldz, long long ms,
-               const unsigned char *emask, cudaStream_t st)
+               const unsigned char *emask, const float *dct32, cudaStream_t st)
 {
     const size_t smem = SmemLayout<R, NT>::bytes();
     auto kern = far_efie_kernel<R, NT>;
@@ -365,7 +373,7 @@ int launch_far(int N, int M, int nxi, double k, double sre, double sim, const do
     const int nchunks = (M + 1 + (NOB - 2) - 1) / (NOB - 2);
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, TPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, dct, sin2,
-                                  reinterpret_cast<double2 *>(Z), ldz, ms, emask);
+                                  reinterpret_cast<double2 *>(Z), ldz, ms, emask, dct32);
     return check_launch("far_efie");
 }
 
@@ -376,7 +384,7 @@ extern "C" int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nx
                                          double scale_re, double scale_im,
                                          const double *geo, const double *dct, const double *sin2,
                                          void *Z, long long ldz, long long mode_stride,
-                                         const unsigned char *elem_mask, void *stream)
+                                         const unsigned char *elem_mask, const float *dct32, void *stream)
 {
     using namespace gb;
     if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !dct || !sin2 || !Z ||
@@ -386,12 +394,12 @@ extern "C" int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nx
     // 4 order groups x NT orders per thread: NT = 8 covers |m| <= 29 in one
     // launch row, NT = 16 covers |m| <= 61 per row
     if (prec == GHOST_BOR_F32) {
-        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
-        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
+        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
     }
     if (prec == GHOST_BOR_F64) {
-        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
-        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, st);
+        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
     }
     return GHOST_BOR_EINVAL;
 }
@@ -402,5 +410,5 @@ extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, doub
                                   void *Z, long long ldz, long long mode_stride, void *stream)
 {
     return ghost_bor_far_efie_masked(prec, n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z,
-                                     ldz, mode_stride, nullptr, stream);
+                                     ldz, mode_stride, nullptr, nullptr, stream);
 }

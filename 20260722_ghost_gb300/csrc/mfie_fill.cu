@@ -348,11 +348,16 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                 }
                 const double xi0 = 2.0 * asin(fmin(s0, 1.0));
                 const double span = GB_PI - xi0;
+                const bool std_tail = s0 == 0.25;          // tabulated half-angle nodes
                 for (int i = 0; i < ntail; ++i) {
-                    const double xi = xi0 + tail_gl[toff + i] * span;
                     const double wt = tail_gl[ntail_total + toff + i] * span;
                     double st, ct;
-                    sincos(0.5 * xi, &st, &ct);
+                    if (std_tail) {
+                        st = tail_gl[2 * ntail_total + toff + i];
+                        ct = tail_gl[3 * ntail_total + toff + i];
+                    } else {
+                        sincos(0.5 * (xi0 + tail_gl[toff + i] * span), &st, &ct);
+                    }
                     const double R = fmax(sqrt(d * d + (a * st) * (a * st)), 1e-300);
                     const double kr = k * R;
                     double sn, cs;

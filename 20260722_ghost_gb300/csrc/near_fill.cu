@@ -184,26 +184,36 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         const double wv = core_gl[NCORE + i] * vmax;
                         const double sh = sinh(v), ch2 = cosh(v);
                         const double sv = fmin(da * sh, 1.0);
-                        const double R = sqrt(d * d + (a * sv) * (a * sv));
-                        const double dxi = 2.0 * da * ch2 / sqrt(fmax(1.0 - sv * sv, 1e-15));
+                        // R and 1/R from one reciprocal square root
+                        const double R2 = d * d + (a * sv) * (a * sv);
+                        const double iR = rsqrt(R2);
+                        const double R = R2 * iR;
+                        const double dxi = 2.0 * da * ch2 * rsqrt(fmax(1.0 - sv * sv, 1e-15));
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
-                        const double gw = 2.0 * wv * dxi / (4.0 * GB_PI * R);
+                        const double gw = 2.0 * wv * dxi * (1.0 / (4.0 * GB_PI)) * iR;
                         put_node(gA, gC, gS0, gS1, (size_t)i * TPBN + tid, gw * cs, -gw * sn,
                                  1.0 - 2.0 * sv * sv);
                     }
                     // -- Gauss tail on [xi0, pi]
                     const double xi0 = 2.0 * asin(s0);
                     const double span = GB_PI - xi0;
+                    const bool std_tail = s0 == 0.25;          // tabulated half-angle nodes
                     for (int i = 0; i < ntail; ++i) {
-                        const double xi = xi0 + tail_gl[toff + i] * span;
                         const double wt = tail_gl[ntail_total + toff + i] * span;
                         double st, ct;
-                        sincos(0.5 * xi, &st, &ct);
-                        const double R = sqrt(d * d + (a * st) * (a * st));
+                        if (std_tail) {
+                            st = tail_gl[2 * ntail_total + toff + i];
+                            ct = tail_gl[3 * ntail_total + toff + i];
+                        } else {
+                            sincos(0.5 * (xi0 + tail_gl[toff + i] * span), &st, &ct);
+                        }
+                        const double R2 = d * d + (a * st) * (a * st);
+                        const double iR = rsqrt(R2);
+                        const double R = R2 * iR;
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
-                        const double gw = 2.0 * wt / (4.0 * GB_PI * R);
+                        const double gw = 2.0 * wt * (1.0 / (4.0 * GB_PI)) * iR;
                         put_node(gA, gC, gS0, gS1, (size_t)(NCORE + i) * TPBN + tid, gw * cs, -gw * sn,
                                  1.0 - 2.0 * st * st);
                     }

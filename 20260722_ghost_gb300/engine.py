@@ -108,6 +108,7 @@ class BorGpuProblem:
         elem = np.stack([self.gen.lengths, self.gen.trho, self.gen.tz])
         self.d_geo = torch.as_tensor(pack_geo(self.g), dtype=f64, device=dev)
         self.d_dct = torch.as_tensor(dct, dtype=f64, device=dev)
+        self.d_dct32 = self.d_dct.to(torch.float32)            # the FP32 fill reads fl32 of the table
         self.d_sin2 = torch.as_tensor(sin2, dtype=f64, device=dev)
         self.d_nodes = torch.as_tensor(np.ascontiguousarray(self.gen.nodes), dtype=f64, device=dev)
         self.d_elem = torch.as_tensor(np.ascontiguousarray(elem), dtype=f64, device=dev)
@@ -169,9 +170,10 @@ class BorGpuProblem:
     # -- stages -----------------------------------------------------------
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
         ld = Z.shape[-1]
-        nat.call("ghost_bor_far_efie", precision, self.N, self.m_max, self.n_xi, self.k,
+        nat.call("ghost_bor_far_efie_masked", precision, self.N, self.m_max, self.n_xi, self.k,
                  scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_dct),
-                 nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), stream)
+                 nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), 0,
+                 nat.ptr(self.d_dct32) if precision == nat.F32 else 0, stream)
 
     def _near_work(self, name: str):
         """Scratch of a near kernel (azimuth nodes of every resident CTA) and

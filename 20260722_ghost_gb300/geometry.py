@@ -240,7 +240,7 @@ class NearTables:
     tails: np.ndarray        # [n_pairs, 2] int32: tail offset, n_tail
     cells: np.ndarray        # [3, n_cells_total]
     core_gl: np.ndarray      # [2, 48]
-    tail_gl: np.ndarray      # [2, n_tail_total]
+    tail_gl: np.ndarray      # [4, n_tail_total]: u, w, and sin / cos(xi/2) of the node for s0 = 1/4
     n_tail: np.ndarray = field(default=None)
 
 
@@ -291,8 +291,17 @@ def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> 
         tab_w.append(0.5 * wt)
         offs[n] = o
         o += n
-    tail_gl = (np.ascontiguousarray(np.stack([np.concatenate(tab_u), np.concatenate(tab_w)]))
-               if uniq else np.zeros((2, 1)))
+    if uniq:
+        u = np.concatenate(tab_u)
+        # the near kernels' tail nodes xi = xi0 + u (pi - xi0); for the common
+        # core bound s0 = 1/4 (xi0 = 2 asin(1/4)) their half-angle sin / cos are
+        # the same for every point pair, so they are tabulated here
+        xi0 = 2.0 * math.asin(0.25)
+        xi = xi0 + u * (math.pi - xi0)
+        tail_gl = np.ascontiguousarray(np.stack([u, np.concatenate(tab_w), np.sin(0.5 * xi),
+                                                 np.cos(0.5 * xi)]))
+    else:
+        tail_gl = np.zeros((4, 1))
     tails = np.asarray([(offs.get(int(n), 0), int(n)) for n in ntails], dtype=np.int32)
     xc, wc = np.polynomial.legendre.leggauss(core_order)
     core_gl = np.ascontiguousarray(np.stack([0.5 * (xc + 1.0), 0.5 * wc]))

@@ -104,13 +104,15 @@ int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, double k,
 
 /* ghost_bor_far_efie restricted to the far pairs (e, f) with elem_mask[e] or
  * elem_mask[f] nonzero (elem_mask: n_elem bytes on the device; NULL = all
- * pairs).  Used by the adjoint gradient to fill the operator change of a
- * local shape perturbation.  No counterpart in the reference. */
+ * pairs; used by the adjoint gradient to fill the operator change of a local
+ * shape perturbation), and optionally reading the FP32 path's DCT table from
+ * dct32 (fl32 of `dct`, same layout; NULL = convert `dct` on the fly).  No
+ * counterpart in the reference. */
 int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k,
                               double scale_re, double scale_im,
                               const double *geo, const double *dct, const double *sin2,
                               void *Z, long long ldz, long long mode_stride,
-                              const unsigned char *elem_mask, void *stream);
+                              const unsigned char *elem_mask, const float *dct32, void *stream);
 
 /* ------------------------------------------------------------------------
  * FP64 near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
@@ -119,7 +121,9 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
  *   pairs     [n_pairs][4] ints: e, f, cell-table offset, cell count
  *   tails     [n_pairs][2] ints: tail-table offset, n_tail
  *   cells     [3][n_cells_total] (s, s', w)
- *   core_gl   [2][48] (u01, w01);  tail_gl [2][n_tail_total] (u01, w01)
+ *   core_gl   [2][48] (u01, w01);  tail_gl [4][n_tail_total] (u01, w01,
+ *             sin and cos of xi/2 at the node for the core bound s0 = 1/4,
+ *             xi = xi0 + u01 (pi - xi0), xi0 = 2 asin(1/4))
  * Output: if band != NULL, ADD scale * block into band[m][blk][Nn][5]
  * (complex double, blk = tt, tf, ft, ff; column offset -2..2); else into the
  * dense complex double Z[m].  `prec` selects the arithmetic of the cos(m xi)
@@ -332,7 +336,8 @@ int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
  * bf16); slice products are accumulated exactly in FP32 TMEM over K chunks of
  * 192 and folded into double-float accumulators, so the residual carries
  * ~2^-31 of the row / column scales instead of the ~2^-24 of FP32 products.
- * R and R32 optional (not both NULL); norms as in ghost_bor_residual.
+ * R and R32 optional (not both NULL); norms as in ghost_bor_residual, summed
+ * in FP32 per thread (relative accuracy ~1e-7, enough for a stopping test).
  * work: ghost_bor_residual_exact_workspace(batch, n, nrhs) bytes, 256-byte
  * aligned; its first int is set to 1 if a bounded in-kernel wait gave up.
  * No counterpart in the reference (its solve is FP64 LAPACK). */

@@ -263,6 +263,6 @@ def test_residual_exact_bf16_slices(pkg, torch, Mb, Nn, nrhs):
     got = R.cpu().numpy()
     scale = np.max(np.abs(Bh))
     assert np.max(np.abs(got - ref)) < 2e-9 * scale, np.max(np.abs(got - ref)) / scale
-    nr = norms.cpu().numpy()
-    np.testing.assert_allclose(nr[:, 0], np.sum(np.abs(got) ** 2, axis=(1, 2)), rtol=1e-10)
-    np.testing.assert_allclose(nr[:, 1], np.sum(np.abs(Bh) ** 2, axis=(1, 2)), rtol=1e-10)
+    nr = norms.cpu().numpy()           # accumulated in FP32 per thread (reported, not refined)
+    np.testing.assert_allclose(nr[:, 0], np.sum(np.abs(got) ** 2, axis=(1, 2)), rtol=1e-5)
+    np.testing.assert_allclose(nr[:, 1], np.sum(np.abs(Bh) ** 2, axis=(1, 2)), rtol=1e-5)
