@@ -320,17 +320,57 @@ int update(int batch, int rows, int cols, int K, const C<R> *A, long long lda, l
     return gemm_update<R>(batch, rows, cols, K, A, lda, sa, B, ldb, sb, Cm, ldc, sc, st);
 }
 
+// Side stream (higher priority for the panel on the caller's stream is not
+// needed: the panel is launched first) and events of the look-ahead LU, one
+// set per device, created on first use.
+struct LookAhead {
+    cudaStream_t side = nullptr;
+    cudaEvent_t la = nullptr, rest = nullptr;
+};
+
+bool look_ahead(LookAhead &L)
+{
+    static thread_local LookAhead cache[16];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return false;
+    LookAhead &c = cache[dev];
+    if (!c.side) {
+        if (cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (cudaEventCreateWithFlags(&c.la, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c.rest, cudaEventDisableTiming) != cudaSuccess)
+            return false;
+    }
+    L = c;
+    return true;
+}
+
+// Right-looking blocked LU with one step of look-ahead: the trailing update of
+// step k is split into the next panel's NB columns (caller's stream) and the
+// remaining columns (side stream), so the panel of step k + 1 -- a
+// latency-bound kernel with one CTA per matrix -- runs while the bulk of the
+// update of step k fills the other SMs.  The row swaps of step k + 1 touch
+// every column and wait for the side stream first; the tensor-core workspace
+// is used by one update at a time (the side update starts after the
+// look-ahead update of its step and finishes before the next one starts).
 template <class R>
 int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv, int *info, void *work,
                cudaStream_t st)
 {
     constexpr int NB = LuCfg<R>::NB;
     if (cudaMemsetAsync(info, 0, sizeof(int) * batch, st) != cudaSuccess) return check_launch("getrf: memset");
+    LookAhead L;
+    const bool la = look_ahead(L);
+    bool rest_pending = false;
+    int rc;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int nb = min(NB, n - k0);
         panel_kernel<R><<<batch, PANEL_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
-        int rc = check_launch("getrf: panel");
-        if (rc) return rc;
+        if ((rc = check_launch("getrf: panel"))) return rc;
+        if (rest_pending) {
+            // the row swaps below touch the columns the side stream is updating
+            if (cudaStreamWaitEvent(st, L.rest, 0) != cudaSuccess) return check_launch("getrf: wait");
+            rest_pending = false;
+        }
         if (n - nb > 0) {
             dim3 g((n - nb + 255) / 256, batch);
             laswp_kernel<R><<<g, 256, 0, st>>>(n, k0, nb, A, lda, sa, ipiv);
@@ -342,12 +382,27 @@ int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv
             trsm_kernel<R, NB, false><<<g, 128, 0, st>>>(nb, rest, A + (size_t)k0 * lda + k0, lda, sa,
                                                           A + (size_t)k0 * lda + k0 + nb, lda, sa);
             if ((rc = check_launch("getrf: trsm"))) return rc;
-            rc = update<R>(batch, rest, rest, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
-                           A + (size_t)k0 * lda + k0 + nb, lda, sa,
-                           A + (size_t)(k0 + nb) * lda + k0 + nb, lda, sa, work, st);
-            if (rc) return rc;
+            const C<R> *L21 = A + (size_t)(k0 + nb) * lda + k0;
+            const C<R> *U12 = A + (size_t)k0 * lda + k0 + nb;
+            C<R> *A22 = A + (size_t)(k0 + nb) * lda + k0 + nb;
+            const int ahead = min(NB, rest);                    // columns of the next panel
+            if (!la || rest <= ahead) {
+                if ((rc = update<R>(batch, rest, rest, nb, L21, lda, sa, U12, lda, sa, A22, lda, sa, work, st)))
+                    return rc;
+                continue;
+            }
+            if ((rc = update<R>(batch, rest, ahead, nb, L21, lda, sa, U12, lda, sa, A22, lda, sa, work, st)))
+                return rc;
+            if (cudaEventRecord(L.la, st) != cudaSuccess || cudaStreamWaitEvent(L.side, L.la, 0) != cudaSuccess)
+                return check_launch("getrf: look-ahead event");
+            if ((rc = update<R>(batch, rest, rest - ahead, nb, L21, lda, sa, U12 + ahead, lda, sa, A22 + ahead,
+                                lda, sa, work, L.side)))
+                return rc;
+            if (cudaEventRecord(L.rest, L.side) != cudaSuccess) return check_launch("getrf: side event");
+            rest_pending = true;
         }
     }
+    if (rest_pending && cudaStreamWaitEvent(st, L.rest, 0) != cudaSuccess) return check_launch("getrf: final wait");
     return GHOST_BOR_OK;
 }
 

@@ -15,6 +15,7 @@ problem exactly as the reference defines it:
 
 from __future__ import annotations
 
+import functools
 import math
 from dataclasses import dataclass, field
 from typing import Dict, List, Tuple
@@ -25,6 +26,17 @@ C0 = 299_792_458.0
 ETA0 = 376.730313668
 AXIS_TOL = 1e-12
 GEO_ROWS = 11      # rho, z, w, T0 w rho, T1 w rho, T0 w, T1 w, dRT0 w, dRT1 w, t_rho, t_z
+
+
+@functools.lru_cache(maxsize=None)
+def _leggauss(n: int) -> Tuple[np.ndarray, np.ndarray]:
+    """Gauss-Legendre nodes and weights on [-1, 1], cached: the rule costs an
+    O(n^3) eigenproblem and the near tail orders (up to 1024) repeat across
+    element pairs, bodies and calls."""
+    x, w = np.polynomial.legendre.leggauss(n)
+    x.flags.writeable = False
+    w.flags.writeable = False
+    return x, w
 
 
 class Generatrix:
@@ -77,7 +89,7 @@ class GaussData:
 
 
 def gauss_on_generatrix(gen: Generatrix, order: int = 4) -> GaussData:
-    xg, wg = np.polynomial.legendre.leggauss(order)
+    xg, wg = _leggauss(order)
     s = 0.5 * (xg + 1.0)
     w = 0.5 * wg
     ne = gen.n_elems
@@ -217,8 +229,8 @@ def graded_cells(kind: str, depth: int = 4) -> List[Tuple[float, float, float, f
 def cell_points(kind: str, gorder: int = 4) -> Tuple[np.ndarray, np.ndarray, np.ndarray]:
     """Test points (order ``gorder``), source points (order ``gorder + 1``, so a
     test and a source point never coincide) and weights over the cells."""
-    xs, ws = np.polynomial.legendre.leggauss(gorder)
-    xq, wq = np.polynomial.legendre.leggauss(gorder + 1)
+    xs, ws = _leggauss(gorder)
+    xq, wq = _leggauss(gorder + 1)
     us, vs = 0.5 * (xs + 1.0), 0.5 * ws
     uq, vq = 0.5 * (xq + 1.0), 0.5 * wq
     S, Q, W = [], [], []
@@ -286,7 +298,7 @@ def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> 
     tab_u, tab_w, offs = [], [], {}
     o = 0
     for n in uniq:
-        x, wt = np.polynomial.legendre.leggauss(n)
+        x, wt = _leggauss(n)
         tab_u.append(0.5 * (x + 1.0))
         tab_w.append(0.5 * wt)
         offs[n] = o
@@ -303,7 +315,7 @@ def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> 
     else:
         tail_gl = np.zeros((4, 1))
     tails = np.asarray([(offs.get(int(n), 0), int(n)) for n in ntails], dtype=np.int32)
-    xc, wc = np.polynomial.legendre.leggauss(core_order)
+    xc, wc = _leggauss(core_order)
     core_gl = np.ascontiguousarray(np.stack([0.5 * (xc + 1.0), 0.5 * wc]))
     return NearTables(pairs=np.ascontiguousarray(pairs), tails=np.ascontiguousarray(tails),
                       cells=cells, core_gl=core_gl, tail_gl=tail_gl, n_tail=ntails)

@@ -322,6 +322,7 @@ def run_gpu(args, rank, world):
     F64 = r64.dF.sum(0)
     db = float(np.max(np.abs(20 * np.log10(np.abs(F32) / np.abs(F64)))))
     rel = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
+    acc_extra = db_stats(F32, F64)
 
     # end to end through the public API with host inputs
     bs.solve_bor(pts, f, thetas, n_modes=M, mode_tol=0.0, table_precision="auto")
@@ -339,9 +340,23 @@ def run_gpu(args, rank, world):
         else None
     return dict(adjoint=adjoint, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s,
                 kernel_work=kernel_w, steps=args.steps, clocks=clocks, launches=launches,
-                f64_s=f64_s, f64_steps=f64_steps, db=db, rel=rel, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
+                f64_s=f64_s, f64_steps=f64_steps, db=db, rel=rel, acc_extra=acc_extra, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
                 refine_iters=results[-1].refine_iters, residual=float(np.max(results[-1].residual)),
                 prob=prob, angle_pol=angle_pol, M=M, thetas=thetas)
+
+
+def db_stats(F32, F64):
+    """dB error statistics of the FP32+IR far field against FP64 over every
+    angle and polarisation: percentiles, the maximum over angles within 60 dB
+    of the peak of their polarisation, and the depth of the worst angle."""
+    import numpy as np
+    a64 = np.abs(F64)
+    db = np.abs(20 * np.log10(np.abs(F32) / a64))
+    depth = 20 * np.log10(a64 / a64.max(axis=1, keepdims=True))
+    i = np.unravel_index(np.argmax(db), db.shape)
+    return {"db_err_p50": float(np.percentile(db, 50)), "db_err_p99": float(np.percentile(db, 99)),
+            "max_db_err_within_60db_of_peak": float(np.max(db[depth > -60.0])),
+            "depth_db_at_max_err": float(depth[i])}
 
 
 def kernel_work(prob, name):
@@ -364,7 +379,7 @@ def kernel_work(prob, name):
 
 def run_batch(args, rank, world):
     """Batch workload: every body's sweep back to back (value), the public
-    solve_bor_batch with host inputs (e2e), FP64 plain on every 8th body."""
+    solve_bor_batch with host inputs (e2e), FP64 plain on every 16th body."""
     import numpy as np
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
@@ -405,8 +420,8 @@ def run_batch(args, rank, world):
     dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps)
     value = replica_throughput(angle_pol, dev_s)
     clocks = clk.summary()
-    # FP64 plain on every 8th body; the speed-up is taken on the same bodies
-    sample = list(range(0, len(probs), 8))
+    # FP64 plain on every 16th body; the speed-up is taken on the same bodies
+    sample = list(range(0, len(probs), 16))
     t32 = sum(last[i].timings["gpu_total_s"] for i in sample)
     e0.record()
     r64 = {i: probs[i].sweep("fp64") for i in sample}
@@ -552,7 +567,7 @@ def main():
         "fp64_plain": {"value": res["angle_pol"] / res["f64_s"], "ms_per_step": res["f64_s"] * 1e3,
                        "steps": res["f64_steps"], **({"note": res["f64_note"]} if "f64_note" in res else {})},
         "speedup_fp32ir_vs_fp64": res["f64_s"] / res["dev_s"],
-        "accuracy_vs_fp64": {"max_db_err": res["db"], "max_rel_amp_err": res["rel"]},
+        "accuracy_vs_fp64": {"max_db_err": res["db"], "max_rel_amp_err": res["rel"], **res.get("acc_extra", {})},
         "refine": {"iters": res["refine_iters"], "max_residual": res["residual"]},
         "stages_s": {k: round(v, 5) for k, v in res["stages"].items()},
     }
