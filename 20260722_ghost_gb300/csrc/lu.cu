@@ -26,13 +26,16 @@ template <> struct LuCfg<float> { static constexpr int NB = 64; };
 template <> struct LuCfg<double> { static constexpr int NB = 32; };
 
 constexpr int PANEL_THREADS = 512;
+constexpr int kSolveBlocks = 4;      // tensor-core substitutions: outer blocks of 4 NB rows
 constexpr int GT = 64;               // gemm tile (rows and columns)
 
 // ---------------------------------------------------------------------------
 // panel factorisation (one CTA per batch matrix)
 // ---------------------------------------------------------------------------
+// (register cap of two CTAs per SM, so that the panel of the next step fits
+// beside the tensor-core update of the look-ahead LU)
 template <class R>
-__global__ void __launch_bounds__(PANEL_THREADS)
+__global__ void __launch_bounds__(PANEL_THREADS, 2)
 panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long long sa,
              int *__restrict__ ipiv, int *__restrict__ info)
 {
@@ -97,9 +100,10 @@ panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long lo
             // reciprocal of the pivot (LAPACK scales by 1/pivot)
             const R den = pv.x * pv.x + pv.y * pv.y;
             const CT inv = mk<R>(pv.x / den, -pv.y / den);
-            // warps over rows, lanes over the trailing panel columns; each warp
-            // loads the multipliers of 32 rows at once (one per lane) so the
-            // row updates do not wait on one load at a time
+            // warps over groups of 32 rows, lanes over the trailing panel
+            // columns; each warp loads the multipliers of its 32 rows at once
+            // (one per lane), then all 32 row values of its column before the
+            // first store, so a group costs one memory latency, not 32
             for (int i0 = col + 1 + 32 * warp; i0 < n; i0 += 32 * NW) {
                 const int ir = i0 + lane;
                 CT lmine = mk<R>(0, 0);
@@ -108,12 +112,26 @@ panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long lo
                     Ab[(size_t)ir * lda + col] = lmine;
                 }
                 const int rows = min(32, n - i0);
-                for (int q = 0; q < rows; ++q) {
-                    CT l;
-                    l.x = __shfl_sync(0xffffffffu, lmine.x, q);
-                    l.y = __shfl_sync(0xffffffffu, lmine.y, q);
-                    CT *rowp = Ab + (size_t)(i0 + q) * lda + col + 1;
-                    for (int c = lane; c < ncol; c += 32) rowp[c] = cfms(l, s_prow[c], rowp[c]);
+                CT *rows0 = Ab + (size_t)i0 * lda + col + 1;
+                for (int c0 = 0; c0 < ncol; c0 += 32) {
+                    const int c = c0 + lane;
+                    const bool act = c < ncol;
+                    const CT u = act ? s_prow[c] : mk<R>(0, 0);
+                    constexpr int QB = 8;                             // rows per batch of loads
+#pragma unroll 1
+                    for (int q0 = 0; q0 < 32; q0 += QB) {
+                        CT v[QB];
+#pragma unroll
+                        for (int q = 0; q < QB; ++q)
+                            if (act && q0 + q < rows) v[q] = rows0[(size_t)(q0 + q) * lda + c];
+#pragma unroll
+                        for (int q = 0; q < QB; ++q) {
+                            CT l;
+                            l.x = __shfl_sync(0xffffffffu, lmine.x, q0 + q);
+                            l.y = __shfl_sync(0xffffffffu, lmine.y, q0 + q);
+                            if (act && q0 + q < rows) rows0[(size_t)(q0 + q) * lda + c] = cfms(l, u, v[q]);
+                        }
+                    }
                 }
             }
         }
@@ -417,27 +435,44 @@ int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long lo
         int rc = check_launch("getrs: laswp");
         if (rc) return rc;
     }
+    // The substitutions run in outer blocks of NBS rows: inside a block, NB-row
+    // diagonal solves and updates of the block's remaining rows; then one
+    // update of every row below (above) the block with K = NBS.  The large
+    // updates read and write the right-hand sides once per NBS rows, so on the
+    // tensor-core path (whose updates are bound by that traffic) NBS = 4 NB.
+    const int NBS = (sizeof(R) == 4 && work) ? kSolveBlocks * NB : NB;
     dim3 gt((nrhs + 127) / 128, batch);
-    for (int k0 = 0; k0 < n; k0 += NB) {
-        const int nb = min(NB, n - k0);
-        trsm_kernel<R, NB, false><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)k0 * lda + k0, lda, sa,
-                                                       B + (size_t)k0 * ldb, ldb, sb);
-        int rc = check_launch("getrs: trsm L");
-        if (rc) return rc;
-        rc = update<R>(batch, n - k0 - nb, nrhs, nb, A + (size_t)(k0 + nb) * lda + k0, lda, sa,
-                       B + (size_t)k0 * ldb, ldb, sb, B + (size_t)(k0 + nb) * ldb, ldb, sb, work, st);
-        if (rc) return rc;
+    int rc;
+    for (int k0 = 0; k0 < n; k0 += NBS) {
+        const int kb = min(NBS, n - k0);
+        for (int j0 = k0; j0 < k0 + kb; j0 += NB) {
+            const int nb = min(NB, k0 + kb - j0);
+            trsm_kernel<R, NB, false><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
+                                                           B + (size_t)j0 * ldb, ldb, sb);
+            if ((rc = check_launch("getrs: trsm L"))) return rc;
+            if ((rc = update<R>(batch, k0 + kb - j0 - nb, nrhs, nb, A + (size_t)(j0 + nb) * lda + j0, lda, sa,
+                                B + (size_t)j0 * ldb, ldb, sb, B + (size_t)(j0 + nb) * ldb, ldb, sb, work, st)))
+                return rc;
+        }
+        if ((rc = update<R>(batch, n - k0 - kb, nrhs, kb, A + (size_t)(k0 + kb) * lda + k0, lda, sa,
+                            B + (size_t)k0 * ldb, ldb, sb, B + (size_t)(k0 + kb) * ldb, ldb, sb, work, st)))
+            return rc;
     }
-    const int last = ((n - 1) / NB) * NB;
-    for (int k0 = last; k0 >= 0; k0 -= NB) {
-        const int nb = min(NB, n - k0);
-        trsm_kernel<R, NB, true><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)k0 * lda + k0, lda, sa,
-                                                      B + (size_t)k0 * ldb, ldb, sb);
-        int rc = check_launch("getrs: trsm U");
-        if (rc) return rc;
-        rc = update<R>(batch, k0, nrhs, nb, A + k0, lda, sa, B + (size_t)k0 * ldb, ldb, sb,
-                       B, ldb, sb, work, st);
-        if (rc) return rc;
+    const int last = ((n - 1) / NBS) * NBS;
+    for (int k0 = last; k0 >= 0; k0 -= NBS) {
+        const int kb = min(NBS, n - k0);
+        for (int j0 = k0 + ((kb - 1) / NB) * NB; j0 >= k0; j0 -= NB) {
+            const int nb = min(NB, k0 + kb - j0);
+            trsm_kernel<R, NB, true><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
+                                                          B + (size_t)j0 * ldb, ldb, sb);
+            if ((rc = check_launch("getrs: trsm U"))) return rc;
+            if ((rc = update<R>(batch, j0 - k0, nrhs, nb, A + (size_t)k0 * lda + j0, lda, sa,
+                                B + (size_t)j0 * ldb, ldb, sb, B + (size_t)k0 * ldb, ldb, sb, work, st)))
+                return rc;
+        }
+        if ((rc = update<R>(batch, k0, nrhs, kb, A + k0, lda, sa, B + (size_t)k0 * ldb, ldb, sb, B, ldb, sb,
+                            work, st)))
+            return rc;
     }
     return GHOST_BOR_OK;
 }
@@ -787,7 +822,7 @@ extern "C" long long ghost_bor_getrf_workspace(int prec, int batch, int n)
 extern "C" long long ghost_bor_getrs_workspace(int prec, int batch, int n, int nrhs)
 {
     if (prec != GHOST_BOR_F32 || batch < 1 || n < 1 || nrhs < 1) return 0;
-    return tc_update_workspace(batch, n, nrhs, LuCfg<float>::NB);
+    return tc_update_workspace(batch, n, nrhs, kSolveBlocks * LuCfg<float>::NB);
 }
 
 static bool tc_work_ok(const void *work)

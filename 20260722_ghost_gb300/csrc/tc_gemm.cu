@@ -16,8 +16,11 @@
 // D[M][2N] = A_r [M][2K] x Bt [2N][2K]^T with both operands K-major.
 //
 // Tiles: 128 x 128 output (M x 2N real), K in stages of 32 (one 128-byte
-// swizzle row), 2 stages double-buffered.  Thread 0 issues the TMA loads and
-// the MMAs; the four warps read the accumulator with tcgen05.ld.
+// swizzle row), 3 stages.  The kernel is persistent (one CTA per SM walks the
+// tiles) and warp-specialised: warp 0 issues the TMA loads, warp 1 the MMAs
+// into one of two TMEM accumulators, and warps 2..5 drain the other
+// accumulator (tcgen05.ld, C -= acc), so the epilogue of one tile overlaps
+// the main loop of the next.
 #include "common.cuh"
 #include "tcgen05.cuh"
 
@@ -25,18 +28,22 @@ namespace gb {
 namespace {
 
 constexpr int BM = 128, BNR = 128, BK = 32;       // tile rows, tile real columns, K per stage
-constexpr int STAGES = 2;
+constexpr int STAGES = 3;
 constexpr int TILE_FLOATS = BM * BK;               // 16 KB per operand tile
-constexpr int TC_THREADS = 128;
-constexpr uint32_t TMEM_COLS = 256;                // allocated (128 used)
+constexpr int TC_THREADS = 192;                    // producer, MMA, 4 epilogue warps
+constexpr uint32_t TMEM_COLS = 256;                // two 128-column accumulators
 
 struct __align__(1024) TcSmem {
     float a_hi[STAGES][TILE_FLOATS];
     float a_lo[STAGES][TILE_FLOATS];
     float b_hi[STAGES][TILE_FLOATS];
     float b_lo[STAGES][TILE_FLOATS];
-    unsigned long long full[STAGES];
-    unsigned long long mma[STAGES];
+    float tr[4][32][33];                           // epilogue transposes, one per warp
+    unsigned long long full[STAGES];               // TMA -> MMA
+    unsigned long long empty[STAGES];              // MMA -> TMA (tcgen05.commit)
+    unsigned long long tfull[2];                   // MMA -> epilogue (tcgen05.commit)
+    unsigned long long tempty[2];                  // epilogue -> MMA (4 warp arrivals)
+    unsigned long long drain;                      // MMA drain on the error path
     uint32_t tmem_base;
     int failed;
 };
@@ -108,26 +115,32 @@ split_b_kernel(int K, int N, int Kp, const float2 *__restrict__ B, long long ldb
     }
 }
 
-__global__ void __launch_bounds__(TC_THREADS)
+// (register cap of two CTAs per SM: one CTA fits by shared memory, and the
+// cap leaves room for the LU panel kernel to run beside it)
+__global__ void __launch_bounds__(TC_THREADS, 2)
 tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                  const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
-                 int M, int Nr, int Kp, float *__restrict__ C, long long ldc_r, long long sc_r,
-                 int *__restrict__ err)
+                 int M, int Nr, int Kp, int tiles_n, int tiles_m, int batch, float *__restrict__ C,
+                 long long ldc_r, long long sc_r, int *__restrict__ err)
 {
     extern __shared__ unsigned char smem_raw[];
     TcSmem &s = *reinterpret_cast<TcSmem *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int n0 = blockIdx.x * BNR, m0 = blockIdx.y * BM, b = blockIdx.z;
     const int nst = Kp / BK;
+    const int per_b = tiles_n * tiles_m;
+    const int ntiles = per_b * batch;
+    volatile int *failed = &s.failed;
 
-    if (warp == 0) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      ::"r"(smem_u32(&s.tmem_base)), "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int i = 0; i < STAGES; ++i) { mbar_init(&s.full[i], 1); mbar_init(&s.mma[i], 1); }
+        for (int i = 0; i < STAGES; ++i) { mbar_init(&s.full[i], 1); mbar_init(&s.empty[i], 1); }
+        for (int i = 0; i < 2; ++i) { mbar_init(&s.tfull[i], 1); mbar_init(&s.tempty[i], 4); }
+        mbar_init(&s.drain, 1);
         s.failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -136,96 +149,118 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s.tmem_base;
 
-    if (tid == 0) {
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer: stage g % STAGES, its u-th use waits for the
+        // MMAs of use u - 1 (empty phase u - 1)
         const uint32_t bytes = 4u * TILE_FLOATS * 4u;
-        uint32_t full_phase[STAGES] = {0, 0}, mma_phase[STAGES] = {0, 0};
-        bool ok = true;
-        for (int st = 0; st < STAGES && st < nst; ++st) {
-            mbar_expect_tx(&s.full[st], bytes);
-            tma_load_3d(s.a_hi[st], &map_ahi, st * BK, m0, b, &s.full[st]);
-            tma_load_3d(s.a_lo[st], &map_alo, st * BK, m0, b, &s.full[st]);
-            tma_load_3d(s.b_hi[st], &map_bhi, st * BK, n0, b, &s.full[st]);
-            tma_load_3d(s.b_lo[st], &map_blo, st * BK, n0, b, &s.full[st]);
-        }
-        for (int ks = 0; ks < nst && ok; ++ks) {
-            const int st = ks % STAGES;
-            ok = mbar_wait(&s.full[st], full_phase[st]);
-            full_phase[st] ^= 1u;
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t ah = smem_u32(s.a_hi[st]), al = smem_u32(s.a_lo[st]);
-            const uint32_t bh = smem_u32(s.b_hi[st]), bl = smem_u32(s.b_lo[st]);
-#pragma unroll
-            for (int kk = 0; kk < BK / 8; ++kk) {          // 8 tf32 = 32 bytes per MMA
-                const uint32_t off = kk * 32;
-                const uint32_t acc0 = (ks > 0 || kk > 0) ? 1u : 0u;
-                umma_tf32(tmem, umma_desc_sw128(ah + off), umma_desc_sw128(bh + off), acc0);
-                umma_tf32(tmem, umma_desc_sw128(ah + off), umma_desc_sw128(bl + off), 1u);
-                umma_tf32(tmem, umma_desc_sw128(al + off), umma_desc_sw128(bh + off), 1u);
-            }
-            umma_commit(&s.mma[st]);
-            if (ks + STAGES < nst) {
-                // this buffer is refilled only after its MMAs have read it
-                ok = mbar_wait(&s.mma[st], mma_phase[st]);
-                mma_phase[st] ^= 1u;
-                if (!ok) break;
+        uint32_t g = 0;
+        for (int t = blockIdx.x; t < ntiles && !*failed; t += gridDim.x) {
+            const int b = t / per_b, r = t % per_b;
+            const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BNR;
+            for (int ks = 0; ks < nst; ++ks, ++g) {
+                const uint32_t st = g % STAGES, u = g / STAGES;
+                if (u > 0 && !mbar_wait(&s.empty[st], (u - 1) & 1u)) {
+                    *failed = 1;
+                    break;
+                }
                 mbar_expect_tx(&s.full[st], bytes);
-                const int kn = (ks + STAGES) * BK;
-                tma_load_3d(s.a_hi[st], &map_ahi, kn, m0, b, &s.full[st]);
-                tma_load_3d(s.a_lo[st], &map_alo, kn, m0, b, &s.full[st]);
-                tma_load_3d(s.b_hi[st], &map_bhi, kn, n0, b, &s.full[st]);
-                tma_load_3d(s.b_lo[st], &map_blo, kn, n0, b, &s.full[st]);
+                tma_load_3d(s.a_hi[st], &map_ahi, ks * BK, m0, b, &s.full[st]);
+                tma_load_3d(s.a_lo[st], &map_alo, ks * BK, m0, b, &s.full[st]);
+                tma_load_3d(s.b_hi[st], &map_bhi, ks * BK, n0, b, &s.full[st]);
+                tma_load_3d(s.b_lo[st], &map_blo, ks * BK, n0, b, &s.full[st]);
             }
         }
-        // wait for the MMAs still in flight (the last STAGES commits)
-        if (ok) {
-            for (int ks = (nst > STAGES ? nst - STAGES : 0); ks < nst; ++ks) {
-                const int st = ks % STAGES;
-                if (!mbar_wait(&s.mma[st], mma_phase[st])) { ok = false; break; }
-                mma_phase[st] ^= 1u;
+        if (*failed) {
+            // let the copies still in flight land before the CTA exits
+            const uint32_t j0 = g > STAGES ? g - STAGES : 0;
+            for (uint32_t j = j0; j < g; ++j) mbar_wait(&s.full[j % STAGES], (j / STAGES) & 1u);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer: tile i accumulates into TMEM buffer i & 1
+        uint32_t g = 0;
+        int i = 0;
+        bool issued = false;
+        for (int t = blockIdx.x; t < ntiles && !*failed; t += gridDim.x, ++i) {
+            const uint32_t ab = i & 1, ui = i >> 1;
+            if (ui > 0 && !mbar_wait(&s.tempty[ab], (ui - 1) & 1u)) { *failed = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t d = tmem + ab * BNR;
+            for (int ks = 0; ks < nst; ++ks, ++g) {
+                const uint32_t st = g % STAGES, u = g / STAGES;
+                if (!mbar_wait(&s.full[st], u & 1u)) { *failed = 1; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t ah = smem_u32(s.a_hi[st]), al = smem_u32(s.a_lo[st]);
+                const uint32_t bh = smem_u32(s.b_hi[st]), bl = smem_u32(s.b_lo[st]);
+#pragma unroll
+                for (int kk = 0; kk < BK / 8; ++kk) {          // 8 tf32 = 32 bytes per MMA
+                    const uint32_t off = kk * 32;
+                    const uint32_t acc0 = (ks > 0 || kk > 0) ? 1u : 0u;
+                    umma_tf32(d, umma_desc_sw128(ah + off), umma_desc_sw128(bh + off), acc0);
+                    umma_tf32(d, umma_desc_sw128(ah + off), umma_desc_sw128(bl + off), 1u);
+                    umma_tf32(d, umma_desc_sw128(al + off), umma_desc_sw128(bh + off), 1u);
+                }
+                issued = true;
+                umma_commit(&s.empty[st]);
             }
+            if (*failed) break;
+            umma_commit(&s.tfull[ab]);
         }
-        if (!ok) {
-            s.failed = 1;
-            atomicExch(err, 1);
+        if (*failed && issued) {
+            // the accumulators are released only after the MMAs in flight
+            umma_commit(&s.drain);
+            mbar_wait(&s.drain, 0);
         }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-    if (!s.failed) {
-        // epilogue: warp w owns accumulator lanes (rows) 32w..32w+31.  Each
-        // 32-column slice goes through shared memory (the operand buffers
-        // are free: every MMA has completed) so the warp's read-modify-write
-        // of C covers one contiguous 128-byte row segment per instruction.
-        float (*tr)[33] = reinterpret_cast<float (*)[33]>(&s.a_hi[0][0]) + warp * 32;
+    } else if (warp >= 2) {
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of
+        // the tile); each 32-column slice goes through shared memory so the
+        // read-modify-write of C covers one 128-byte row segment per instruction
+        const int q = warp & 3;
+        float(*tr)[33] = s.tr[q];
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            const int stop = __shfl_sync(0xffffffffu, *failed, 0);
+            if (stop) break;
+            const uint32_t ab = i & 1, ui = i >> 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&s.tfull[ab], ui & 1u));
+            if (!ok) {
+                if (lane == 0) *failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int b = t / per_b, r = t % per_b;
+            const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BNR;
+            const int rows = min(32, M - (m0 + q * 32));
 #pragma unroll 1
-        for (int c32 = 0; c32 < BNR / 32; ++c32) {
-            float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c32 * 32), v);
+            for (int c32 = 0; c32 < BNR / 32; ++c32) {
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BNR + (uint32_t)(c32 * 32), v);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) tr[lane][i] = v[i];
-            __syncwarp();
-            const int col = n0 + c32 * 32 + lane;
-            float *cb = C + (size_t)b * sc_r + (size_t)(m0 + warp * 32) * ldc_r + col;
-            const int rows = min(32, M - (m0 + warp * 32));
-            if (col < Nr) {
-                // all loads first (the compiler cannot reorder C loads past C stores)
-                float cv[32];
+                for (int j = 0; j < 32; ++j) tr[lane][j] = v[j];
+                __syncwarp();
+                const int col = n0 + c32 * 32 + lane;
+                float *cb = C + (size_t)b * sc_r + (size_t)(m0 + q * 32) * ldc_r + col;
+                if (col < Nr && rows > 0) {
+                    // all loads first (the compiler cannot reorder C loads past C stores)
+                    float cv[32];
 #pragma unroll
-                for (int i = 0; i < 32; ++i) cv[i] = (i < rows) ? cb[(size_t)i * ldc_r] : 0.f;
+                    for (int j = 0; j < 32; ++j) cv[j] = (j < rows) ? cb[(size_t)j * ldc_r] : 0.f;
 #pragma unroll
-                for (int i = 0; i < 32; ++i)
-                    if (i < rows) cb[(size_t)i * ldc_r] = cv[i] - tr[i][lane];
+                    for (int j = 0; j < 32; ++j)
+                        if (j < rows) cb[(size_t)j * ldc_r] = cv[j] - tr[j][lane];
+                }
+                __syncwarp();
             }
-            __syncwarp();
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            if (lane == 0) mbar_arrive(&s.tempty[ab]);          // accumulator free for tile i + 2
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    if (tid == 0 && *failed) atomicExch(err, 1);
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -294,8 +329,18 @@ int tc_update(int batch, int M, int N, int K, const float2 *A, long long lda, lo
             return check_launch("tc_update: smem attribute");
         attr = true;
     }
-    dim3 grid((2 * N + BNR - 1) / BNR, (M + BM - 1) / BM, batch);
-    tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, M, 2 * N, Kp,
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            sms = 1;
+    }
+    const int tiles_n = (2 * N + BNR - 1) / BNR, tiles_m = (M + BM - 1) / BM;
+    const long long ntiles = (long long)tiles_n * tiles_m * batch;
+    if (ntiles > 0x7fffffffLL) return GHOST_BOR_EUNSUPPORTED;
+    const int grid = (int)(ntiles < sms ? ntiles : sms);      // persistent: one CTA per SM
+    tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, M, 2 * N, Kp, tiles_n, tiles_m, batch,
                                                      reinterpret_cast<float *>(C), 2 * ldc, 2 * sc, err);
     return check_launch("tc_update");
 }

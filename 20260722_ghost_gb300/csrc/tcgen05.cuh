@@ -28,6 +28,11 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, uint32_t b
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
 // bounded wait on the phase with parity `parity`; false on timeout
 __device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity)
 {

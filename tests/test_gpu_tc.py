@@ -5,7 +5,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("batch,M,N,K", [(2, 200, 150, 64), (1, 128, 64, 8), (3, 77, 301, 37), (1, 300, 40, 200)])
+# the last two cases have more tiles than SMs (each persistent CTA walks several
+# tiles and reuses both TMEM accumulators) and many K stages
+@pytest.mark.parametrize("batch,M,N,K", [(2, 200, 150, 64), (1, 128, 64, 8), (3, 77, 301, 37), (1, 300, 40, 200),
+                                         (5, 1000, 700, 64), (2, 640, 900, 333)])
 def test_cgemm_tc_matches_numpy(pkg, batch, M, N, K):
     import torch
     nat = pkg._native
