@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "df_math.cuh"
 
 namespace gb {
 namespace {
@@ -32,9 +33,10 @@ struct NearSmem {
     // Gb   [TPBN][NC] double2 : per-pair orders of the current batch/chunk
     // W    [TPBN][20] double  : Galerkin weights of the batch
     // Prim [20][Mp]   double2 : contracted primitives, all orders
+    // Tab  [257]     float4  : double-float sin, cos of j pi/128 (FP32 path)
     static size_t bytes(int Mp, int NC) {
         return sizeof(double2) * (size_t)TPBN * NC + sizeof(double) * (size_t)TPBN * 20 +
-               sizeof(double2) * 20 * (size_t)Mp;
+               sizeof(double2) * 20 * (size_t)Mp + sizeof(float4) * kDfTabN;
     }
 };
 
@@ -45,6 +47,19 @@ template <bool DF> struct NodeT;
 template <> struct NodeT<true> { using A = float4; using B = float2; };
 template <> struct NodeT<false> { using A = double2; using B = double; };
 constexpr size_t kNodeBytes = 40;      // 16 + 3 * 8 per node and thread
+// per-CTA double-float tail rule of the current pair (FP32 path): u, w and, for
+// the standard tail (s0 = 1/4), sin^2(xi/2), w span / (2 pi), 1 - 2 sin^2(xi/2)
+constexpr size_t kTailBytes = 5 * sizeof(float2);
+
+// a node in double-float words: g w (complex) and cos(xi)
+__device__ __forceinline__ void put_node_df(float4 *A, float2 *Bc, float2 *S0, float2 *S1, size_t i,
+                                            float2 gre, float2 gim, float2 c1)
+{
+    A[i] = make_float4(gre.x, gre.y, gim.x, gim.y);
+    Bc[i] = c1;
+    S0[i] = c1;
+    S1[i] = make_float2(1.f, 0.f);
+}
 
 __device__ __forceinline__ void put_node(float4 *A, float2 *Bc, float2 *S0, float2 *S1, size_t i,
                                          double gre, double gim, double c1)
@@ -114,6 +129,7 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     double2 *Gb = reinterpret_cast<double2 *>(smem_raw);
     double *W = reinterpret_cast<double *>(Gb + TPBN * NC);
     double2 *Prim = reinterpret_cast<double2 *>(W + TPBN * 20);
+    float4 *Tab = reinterpret_cast<float4 *>(Prim + 20 * Mp);
     const int tid = threadIdx.x;
 
     const size_t plane = (size_t)nmax * TPBN;
@@ -121,6 +137,14 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     NB *gC = reinterpret_cast<NB *>(gA + plane);
     NB *gS0 = gC + plane;
     NB *gS1 = gS0 + plane;
+    // double-float tail rule of the current pair (after every CTA's node planes)
+    float2 *tU = reinterpret_cast<float2 *>(scratch + (size_t)gridDim.x * plane * kNodeBytes +
+                                            (size_t)blockIdx.x * nmax * kTailBytes);
+    float2 *tWr = tU + nmax, *tS2 = tWr + nmax, *tWs = tS2 + nmax, *tC1 = tWs + nmax;
+    if constexpr (DF) df_fill_sincos_table(Tab);
+    const double span_std = GB_PI - 2.0 * asin(0.25);
+    const float2 kf = df_from(k);
+    const float2 inv2pi = df_from(1.0 / (2.0 * GB_PI));
 
     constexpr int NOUT = (20 * NC + TPBN - 1) / TPBN;
     const int nchunk = (Mp + NC - 1) / NC;
@@ -141,8 +165,20 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
         const double drho_f = nodes[2 * f + 2] - rho_f0, dz_f = nodes[2 * f + 3] - z_f0;
         const double Le = elem[e], Lf = elem[f];
 
-        __syncthreads();                     // the previous pair has finished reading Prim
+        __syncthreads();                     // the previous pair has finished reading Prim and its tail rule
         for (int i = tid; i < 20 * Mp; i += TPBN) Prim[i] = make_double2(0.0, 0.0);
+        if constexpr (DF) {
+            for (int i = tid; i < ntail; i += TPBN) {
+                const double u = tail_gl[toff + i], w = tail_gl[ntail_total + toff + i];
+                const double st = tail_gl[2 * ntail_total + toff + i];
+                tU[i] = df_from(u);
+                tWr[i] = df_from(w);
+                tS2[i] = df_from(st * st);
+                tWs[i] = df_from(w * span_std / (2.0 * GB_PI));
+                tC1[i] = df_from(1.0 - 2.0 * st * st);
+            }
+            __syncthreads();
+        }
 
         const int nbatch = (ncell + TPBN - 1) / TPBN;
         for (int bt = 0; bt < nbatch; ++bt) {
@@ -199,6 +235,34 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const double xi0 = 2.0 * asin(s0);
                     const double span = GB_PI - xi0;
                     const bool std_tail = s0 == 0.25;          // tabulated half-angle nodes
+                    if constexpr (DF) {
+                        // every tail node in double-float on the FP32 pipe
+                        const float2 d2f = df_from(fmax(d2, 1e-300)), a2f = df_from(rr4);
+                        const float2 xi0f = df_from(xi0), spanf = df_from(span);
+#pragma unroll 2
+                        for (int i = 0; i < ntail; ++i) {
+                            float2 S2, Wn, C1;
+                            if (std_tail) {
+                                S2 = tS2[i]; Wn = tWs[i]; C1 = tC1[i];
+                            } else {
+                                const float2 h2 = df_add(xi0f, df_mul(tU[i], spanf));
+                                float2 sh, chh;
+                                df_sincos(make_float2(0.5f * h2.x, 0.5f * h2.y), Tab, sh, chh);
+                                S2 = df_mul(sh, sh);
+                                C1 = df_add(make_float2(1.f, 0.f), make_float2(-2.f * S2.x, -2.f * S2.y));
+                                Wn = df_mul(df_mul(tWr[i], spanf), inv2pi);
+                            }
+                            const float2 R2 = df_add(d2f, df_mul(a2f, S2));
+                            const float2 iR = df_rsqrt(R2);
+                            const float2 R = df_mul(R2, iR);
+                            float2 sn, cs;
+                            df_sincos(df_reduce(df_mul(kf, R)), Tab, sn, cs);
+                            const float2 gw = df_mul(Wn, iR);
+                            const float2 gre = df_mul(gw, cs), gim = df_mul(gw, sn);
+                            put_node_df(gA, gC, gS0, gS1, (size_t)(NCORE + i) * TPBN + tid, gre,
+                                        make_float2(-gim.x, -gim.y), C1);
+                        }
+                    } else
                     for (int i = 0; i < ntail; ++i) {
                         const double wt = tail_gl[ntail_total + toff + i] * span;
                         double st, ct;
@@ -352,7 +416,8 @@ int near_grid()
 extern "C" long long ghost_bor_near_workspace(int n_tail_max)
 {
     if (n_tail_max < 0) return -1;
-    return 256 + (long long)gb::near_grid() * gb::TPBN * (gb::NCORE + n_tail_max) * (long long)gb::kNodeBytes;
+    return 256 + (long long)gb::near_grid() * (gb::NCORE + n_tail_max) *
+                     ((long long)gb::TPBN * (long long)gb::kNodeBytes + (long long)gb::kTailBytes);
 }
 
 extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
