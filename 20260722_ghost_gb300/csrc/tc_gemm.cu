@@ -38,7 +38,10 @@ struct __align__(1024) TcSmem {
     float a_lo[STAGES][TILE_FLOATS];
     float b_hi[STAGES][TILE_FLOATS];
     float b_lo[STAGES][TILE_FLOATS];
-    float tr[4][32][33];                           // epilogue transposes, one per warp
+    // epilogue staging, 8 KB per epilogue warp: two 32 x 32 FP32 boxes of -acc
+    // in the 128-byte swizzled layout of the C tensor map (TMA reduce-add
+    // path), or one 32 x 33 transpose (load/store path)
+    float ep[4][2][32 * 32];
     unsigned long long full[STAGES];               // TMA -> MMA
     unsigned long long empty[STAGES];              // MMA -> TMA (tcgen05.commit)
     unsigned long long tfull[2];                   // MMA -> epilogue (tcgen05.commit)
@@ -120,6 +123,7 @@ split_b_kernel(int K, int N, int Kp, const float2 *__restrict__ B, long long ldb
 __global__ void __launch_bounds__(TC_THREADS, 2)
 tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_constant__ CUtensorMap map_alo,
                  const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
+                 const __grid_constant__ CUtensorMap map_c, int use_tma_c,
                  int M, int Nr, int Kp, int tiles_n, int tiles_m, int batch, float *__restrict__ C,
                  long long ldc_r, long long sc_r, int *__restrict__ err)
 {
@@ -212,12 +216,28 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
         }
     } else if (warp >= 2) {
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of
-        // the tile); each 32-column slice goes through shared memory so the
-        // read-modify-write of C covers one 128-byte row segment per instruction
+        // the tile), 32 columns at a time.
+        //  TMA path: -acc is staged in shared memory (swizzled like the C
+        //  tensor map) and added to C by a TMA reduce-add, so the epilogue
+        //  issues no global loads; two staging boxes per warp alternate.
+        //  Load/store path (C not 16-byte aligned): each slice is transposed
+        //  through shared memory so the read-modify-write of C covers one
+        //  128-byte row segment per instruction, and each lane prefetches its
+        //  row of the next tile into L2 while that tile's MMAs run.
         const int q = warp & 3;
-        float(*tr)[33] = s.tr[q];
-        int i = 0;
+        auto prefetch_c = [&](int t) {
+            if (use_tma_c || t >= ntiles) return;
+            const int b = t / per_b, r = t % per_b;
+            const int row = (r / tiles_n) * BM + q * 32 + lane, n0 = (r % tiles_n) * BNR;
+            if (row >= M) return;
+            const float *rp = C + (size_t)b * sc_r + (size_t)row * ldc_r;
+            for (int c = n0; c < min(n0 + BNR, Nr); c += 32)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(rp + c));
+        };
+        prefetch_c(blockIdx.x);
+        int i = 0, nbox = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            prefetch_c(t + gridDim.x);
             const int stop = __shfl_sync(0xffffffffu, *failed, 0);
             if (stop) break;
             const uint32_t ab = i & 1, ui = i >> 1;
@@ -234,25 +254,51 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
             for (int c32 = 0; c32 < BNR / 32; ++c32) {
                 float v[32];
                 tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + ab * BNR + (uint32_t)(c32 * 32), v);
+                if (use_tma_c) {
+                    if (n0 + c32 * 32 >= Nr || rows <= 0) continue;
+                    float *box = s.ep[q][nbox & 1];
+                    // the reduce issued from this box two boxes ago has read it
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                    __syncwarp();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) tr[lane][j] = v[j];
-                __syncwarp();
-                const int col = n0 + c32 * 32 + lane;
-                float *cb = C + (size_t)b * sc_r + (size_t)(m0 + q * 32) * ldc_r + col;
-                if (col < Nr && rows > 0) {
-                    // all loads first (the compiler cannot reorder C loads past C stores)
-                    float cv[32];
+                    for (int j4 = 0; j4 < 8; ++j4)
+                        *reinterpret_cast<float4 *>(box + lane * 32 + ((j4 ^ (lane & 7)) << 2)) =
+                            make_float4(-v[4 * j4], -v[4 * j4 + 1], -v[4 * j4 + 2], -v[4 * j4 + 3]);
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        asm volatile("cp.reduce.async.bulk.tensor.3d.global.shared::cta.add.tile.bulk_group"
+                                     " [%0, {%1, %2, %3}], [%4];"
+                                     ::"l"(reinterpret_cast<uint64_t>(&map_c)), "r"(n0 + c32 * 32),
+                                       "r"(m0 + q * 32), "r"(b), "r"(smem_u32(box))
+                                     : "memory");
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    }
+                    ++nbox;
+                } else {
+                    float(*tr)[33] = reinterpret_cast<float(*)[33]>(s.ep[q][0]);
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) cv[j] = (j < rows) ? cb[(size_t)j * ldc_r] : 0.f;
+                    for (int j = 0; j < 32; ++j) tr[lane][j] = v[j];
+                    __syncwarp();
+                    const int col = n0 + c32 * 32 + lane;
+                    float *cb = C + (size_t)b * sc_r + (size_t)(m0 + q * 32) * ldc_r + col;
+                    if (col < Nr && rows > 0) {
+                        // all loads first (the compiler cannot reorder C loads past C stores)
+                        float cv[32];
 #pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (j < rows) cb[(size_t)j * ldc_r] = cv[j] - tr[j][lane];
+                        for (int j = 0; j < 32; ++j) cv[j] = (j < rows) ? cb[(size_t)j * ldc_r] : 0.f;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (j < rows) cb[(size_t)j * ldc_r] = cv[j] - tr[j][lane];
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             if (lane == 0) mbar_arrive(&s.tempty[ab]);          // accumulator free for tile i + 2
         }
+        // every reduce-add has completed before the kernel ends
+        if (use_tma_c && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -277,6 +323,24 @@ bool make_map(CUtensorMap *map, const float *base, int rows, int Kp, int batch)
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// C [batch][M][Nr] FP32 (real view of the complex output), box 32 x 32, 128-byte
+// swizzle, for the reduce-add epilogue; false when C's base or strides are not
+// 16-byte multiples (the kernel then reads and writes C itself)
+bool make_map_c(CUtensorMap *map, float *C, int M, int Nr, int batch, long long ldc_r, long long sc_r)
+{
+    if ((reinterpret_cast<uintptr_t>(C) & 15) || (ldc_r & 3) || (batch > 1 && (sc_r & 3))) return false;
+    auto enc = get_encode();
+    if (!enc) return false;
+    const long long bstride = batch > 1 ? sc_r : (long long)M * ldc_r + ((4 - ((long long)M * ldc_r) % 4) % 4);
+    const cuuint64_t dims[3] = {(cuuint64_t)Nr, (cuuint64_t)M, (cuuint64_t)batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldc_r * 4, (cuuint64_t)bstride * 4};
+    const cuuint32_t box[3] = {32, 32, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -340,8 +404,12 @@ int tc_update(int batch, int M, int N, int K, const float2 *A, long long lda, lo
     const long long ntiles = (long long)tiles_n * tiles_m * batch;
     if (ntiles > 0x7fffffffLL) return GHOST_BOR_EUNSUPPORTED;
     const int grid = (int)(ntiles < sms ? ntiles : sms);      // persistent: one CTA per SM
-    tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, M, 2 * N, Kp, tiles_n, tiles_m, batch,
-                                                     reinterpret_cast<float *>(C), 2 * ldc, 2 * sc, err);
+    CUtensorMap mc;
+    float *Cr = reinterpret_cast<float *>(C);
+    const int use_tma_c = make_map_c(&mc, Cr, M, 2 * N, batch, 2 * ldc, 2 * sc) ? 1 : 0;
+    if (!use_tma_c) mc = mah;                                   // unused by the kernel
+    tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, mc, use_tma_c, M, 2 * N, Kp, tiles_n,
+                                                     tiles_m, batch, Cr, 2 * ldc, 2 * sc, err);
     return check_launch("tc_update");
 }
 
