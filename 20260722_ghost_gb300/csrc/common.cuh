@@ -104,6 +104,27 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b)
     return make_float2(h, e - (h - s));
 }
 
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
+// complex double-float packed as (re.hi, re.lo, im.hi, im.lo)
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 f4(float2 re, float2 im) { return make_float4(re.x, re.y, im.x, im.y); }
+
+// exact FP32 -> FP64 conversion by integer operations (ALU pipe): sign,
+// rebiased exponent and the 23 fraction bits; zeros and subnormal inputs
+// (below 1.2e-38) give 0
+__device__ __forceinline__ double f2d_bits(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    if (ex == 0u) return 0.0;
+    const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+// hi + lo of a double-float rounded to FP64: two integer conversions and one add
+__device__ __forceinline__ double df_to_bits(float2 a) { return f2d_bits(a.x) + f2d_bits(a.y); }
+
 // ----------------------------------------------------------------------------
 // error reporting helpers (host)
 // ----------------------------------------------------------------------------

@@ -30,6 +30,12 @@ constexpr float kDfPiB128_2 = -6.960085841001273e-08f;
 constexpr float kDfPiB128_3 = -2.5803118085395652e-15f;
 constexpr float kDf128ByPi = 40.7436637878418f;
 constexpr int kDfTabN = 257;           // j = -128 .. 128
+// ln 2 / 32 = L1 + L2 + L3, L1 with 13 significant bits (k L1 exact for k < 2^11)
+constexpr float kDfLn2By32_1 = 0.02165985107421875f;
+constexpr float kDfLn2By32_2 = 9.983182280848268e-07f;
+constexpr float kDfLn2By32_3 = 5.14560928046269e-14f;
+constexpr float kDf32ByLn2 = 46.16624069213867f;
+constexpr int kDfExpTabN = 32;         // 2^(j/32), j = 0..31
 
 __device__ __forceinline__ float2 df_two_sum(float a, float b)
 {
@@ -60,6 +66,54 @@ __device__ __forceinline__ void df_fill_sincos_table(float4 *tab)
         const float2 sf = df_from(s), cf = df_from(c);
         tab[i] = make_float4(sf.x, sf.y, cf.x, cf.y);
     }
+}
+
+// table of 2^(j/32), j = 0..31, as double-float; filled cooperatively by a CTA
+__device__ __forceinline__ void df_fill_exp_table(float2 *tab)
+{
+    for (int i = threadIdx.x; i < kDfExpTabN; i += blockDim.x) tab[i] = df_from(exp2((double)i / 32.0));
+}
+
+// 1 / a, a double-float, from an IEEE reciprocal and one Newton step
+__device__ __forceinline__ float2 df_rcp(float2 a)
+{
+    const float y = __frcp_rn(a.x);
+    const float p = a.x * y;
+    const float pe = fmaf(a.x, y, -p);
+    const float e = ((1.0f - p) - pe) - a.y * y;
+    return df_fast(y, y * e);
+}
+
+// e^v and e^v - 1 for 0 <= v < 88 (double-float), Tang's table-driven method:
+// v = (32 n + j) ln2/32 + r, |r| <= ln2/64, e^v = 2^n 2^(j/32) e^r with
+// e^r - 1 = r + r^2/2 + r^3 (1/6 + r/24 + r^2/120 + r^3/720); e^v - 1 comes
+// straight from the series when n = j = 0 (no cancellation for small v)
+__device__ __forceinline__ void df_exp(float2 v, const float2 *__restrict__ tab, float2 &E, float2 &Em1)
+{
+    const float kf = rintf(v.x * kDf32ByLn2);
+    const int k = (int)kf;
+    const float r1 = fmaf(-kf, kDfLn2By32_1, v.x);        // exact
+    const float p2 = kf * kDfLn2By32_2;
+    const float p2e = fmaf(kf, kDfLn2By32_2, -p2);
+    const float2 rs = df_two_sum(r1, -p2);
+    const float2 r = df_fast(rs.x, rs.y - p2e - kf * kDfLn2By32_3 + v.y);
+    const float rr = r.x * r.x;
+    const float rre = fmaf(r.x, r.x, -rr) + 2.0f * r.x * r.y;
+    const float c = r.x * fmaf(r.x, fmaf(r.x, fmaf(r.x, 1.0f / 720.0f, 1.0f / 120.0f), 1.0f / 24.0f), 1.0f / 6.0f);
+    const float2 h = df_two_sum(r.x, 0.5f * rr);
+    const float2 em1r = df_fast(h.x, h.y + r.y + 0.5f * rre + rr * c);
+    if (k == 0) {
+        Em1 = em1r;
+        const float2 o = df_two_sum(1.0f, em1r.x);
+        E = df_fast(o.x, o.y + em1r.y);
+        return;
+    }
+    const float2 o = df_two_sum(1.0f, em1r.x);
+    const float2 er = df_fast(o.x, o.y + em1r.y);
+    const float2 t = df_mul(tab[k & 31], er);
+    const float sc = __int_as_float(((k >> 5) + 127) << 23);     // 2^n, exact
+    E = make_float2(t.x * sc, t.y * sc);
+    Em1 = df_add(E, make_float2(-1.0f, 0.0f));
 }
 
 // 1 / sqrt(x), x > 0 double-float

@@ -32,20 +32,23 @@
 // of 8 samples folded in with Kahan compensation.
 #include "common.cuh"
 #include "samplers.cuh"
+#include "df_math.cuh"
 
 namespace gb {
 namespace {
 
-constexpr int EPB = 4;            // element pairs per CTA
-constexpr int TPB = EPB * 16 * 4; // Gauss-point pairs x order groups
+constexpr int TPB = 256;          // threads: Gauss-point pairs (16 EPB) x order groups (OG)
 constexpr int JC = 32;            // azimuth samples staged per smem chunk
 
-constexpr int OG = 4;                 // order groups: threads sharing one Gauss-point pair
 constexpr int SLAB = 17;              // 16-byte entries per (pair, order) slab of Gs: 16 used + 1 pad
                                       // so that slabs read by neighbouring threads hit distinct banks
-constexpr int PPB = EPB * 16;         // Gauss-point pairs per CTA
+// OG order groups (threads sharing one Gauss-point pair) of NT orders each;
+// EPB = 16 / OG element pairs per CTA.  OG = 4 for up to 62 orders per launch
+// row, OG = 8 (two element pairs per CTA) for up to 126, so that every
+// sample is evaluated once for |m| <= 124.
 
-template <class R, int NT> struct SmemLayout {
+template <class R, int NT, int OG> struct SmemLayout {
+    static constexpr int EPB = 16 / OG, PPB = EPB * 16;
     // gsm  [JC][PPB]        C<R>     samples of the current chunk
     // dcts [JC][OG*NT]      R
     // s2s  [JC]             S2
@@ -60,7 +63,7 @@ template <class R, int NT> struct SmemLayout {
     }
 };
 
-template <class R, int NT>
+template <class R, int NT, int OG>
 __global__ void __launch_bounds__(TPB, 2)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
@@ -72,6 +75,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     using Samp = GreenSampler<R>;
     using S2 = typename Samp::S2;
     constexpr int NOB = OG * NT;
+    constexpr int EPB = 16 / OG, PPB = EPB * 16;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CT *gsm = reinterpret_cast<CT *>(smem_raw);
     R *dcts = reinterpret_cast<R *>(gsm + JC * PPB);
@@ -216,6 +220,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     __syncthreads();
 
     const double ik2 = 1.0 / (k * k);
+    const float2 ik2f = df_from(ik2);
     // contraction: job (ep, n, b) = five order primitives of source node b for
     // both test nodes a.  Results replace the orders in place, so every
     // thread reads first and writes after a barrier (uniform trip count).
@@ -225,7 +230,8 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         const int jep = (job >> 1) / nord, n = (job >> 1) % nord, b = job & 1;
         const int ff = f0 + jep;
         const bool doit = job < njobs && ff < N && abs(e - ff) >= 2 && (!emask || emask[e] || emask[ff]);
-        double2 out[5][2];    // p11, pdd, pds, psd, pss for a = 0, 1
+        double2 out[5][2];    // p11, pdd, pds, psd, pss for a = 0, 1 (FP64 path)
+        float4 outf[5][2];    // the same as double-float words (FP32 path)
         if (doit) {
             if constexpr (sizeof(R) == 4) {
                 // double-float contraction (exact well below an FP32 ulp)
@@ -265,7 +271,8 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
                         df_mac(acc2[4][0], ls, make_float2(qs.x, qs.y)); df_mac(acc2[4][1], ls, make_float2(qs.z, qs.w));
                     }
 #pragma unroll
-                    for (int c = 0; c < 5; ++c) out[c][a] = make_double2(df_to(acc2[c][0]), df_to(acc2[c][1]));
+                    for (int c = 0; c < 5; ++c)
+                        outf[c][a] = make_float4(acc2[c][0].x, acc2[c][0].y, acc2[c][1].x, acc2[c][1].y);
                 }
             } else {
                 const double2 *Gd = Gs + (jep * NOB + n) * SLAB;
@@ -305,7 +312,28 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
             }
         }
         __syncthreads();      // every job of this round has read its orders
-        if (doit) {
+        if constexpr (sizeof(R) == 4) {
+            if (doit) {
+                // mode-local parts in double-float (the FP64 pipe is ~1/64 of FP32)
+                const int o = o0 + n;
+                const float2 ttf = df_mul(df_from(geo[(size_t)10 * P + 4 * e]), df_from(geo[(size_t)10 * P + 4 * ff]));
+                const float2 fmf = df_mulf(ik2f, (float)o), fm2f = df_mulf(fmf, (float)o);
+                float4 *zl = reinterpret_cast<float4 *>(Gs + (jep * NOB + n) * SLAB);
+                float4 *P11f = reinterpret_cast<float4 *>(P11s);
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const int ab = a * 2 + b;
+                    const float4 p11 = outf[0][a], pdd = outf[1][a], pds = outf[2][a], psd = outf[3][a],
+                                 pss = outf[4][a];
+                    P11f[(jep * NOB + n) * 4 + ab] = p11;
+                    zl[0 * 4 + ab] = f4(df_sub(df_mul(ttf, lo2(p11)), df_mul(ik2f, lo2(pdd))),
+                                        df_sub(df_mul(ttf, hi2(p11)), df_mul(ik2f, hi2(pdd))));
+                    zl[1 * 4 + ab] = f4(df_mul(fmf, hi2(pds)), df_neg(df_mul(fmf, lo2(pds))));   // -(j o/k^2) pds
+                    zl[2 * 4 + ab] = f4(df_neg(df_mul(fmf, hi2(psd))), df_mul(fmf, lo2(psd)));   // +(j o/k^2) psd
+                    zl[3 * 4 + ab] = f4(df_neg(df_mul(fm2f, lo2(pss))), df_neg(df_mul(fm2f, hi2(pss))));
+                }
+            }
+        } else if (doit) {
             const int o = o0 + n;
             const double tze = geo[(size_t)10 * P + 4 * e], tzf = geo[(size_t)10 * P + 4 * ff];
             const double tt = tze * tzf;
@@ -329,6 +357,43 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
 
     // mode combination + accumulation into Z[m]
     const int nmodes = m1 - m0 + 1;
+    if constexpr (sizeof(R) == 4) {
+        // double-float; each entry becomes a double only for its atomic add
+        const float2 sre = df_from(sc_re), sim = df_from(sc_im);
+        const float4 *P11f = reinterpret_cast<const float4 *>(P11s);
+        for (int job = tid; job < EPB * nmodes; job += TPB) {
+            const int jep = job / nmodes, m = m0 + job % nmodes;
+            const int ff = f0 + jep;
+            if (ff >= N || abs(e - ff) < 2 || (emask && !emask[e] && !emask[ff])) continue;
+            const int nl = abs(m - 1) - o0, nm = m - o0, nh = m + 1 - o0;
+            const float4 *zl = reinterpret_cast<const float4 *>(Gs + (jep * NOB + nm) * SLAB);
+            const float2 tre = df_from(geo[(size_t)9 * P + 4 * e]), trf = df_from(geo[(size_t)9 * P + 4 * ff]);
+            const float2 htt = df_mulf(df_mul(tre, trf), 0.5f), hre = df_mulf(tre, 0.5f), hrf = df_mulf(trf, 0.5f);
+            double2 *Zm = Z + (size_t)m * mode_stride;
+#pragma unroll
+            for (int ab = 0; ab < 4; ++ab) {
+                const int a = ab >> 1, b = ab & 1;
+                const float4 lo = P11f[(jep * NOB + nl) * 4 + ab];
+                const float4 hi = P11f[(jep * NOB + nh) * 4 + ab];
+                const float2 Sr = df_add(lo2(lo), lo2(hi)), Si = df_add(hi2(lo), hi2(hi));
+                const float2 Dr = df_sub(lo2(lo), lo2(hi)), Di = df_sub(hi2(lo), hi2(hi));
+                float2 br[4], bi[4];
+                const float4 z0 = zl[0 * 4 + ab], z1 = zl[1 * 4 + ab], z2 = zl[2 * 4 + ab], z3 = zl[3 * 4 + ab];
+                br[0] = df_add(df_mul(htt, Sr), lo2(z0)); bi[0] = df_add(df_mul(htt, Si), hi2(z0));
+                br[1] = df_add(df_mul(hre, Di), lo2(z1)); bi[1] = df_sub(hi2(z1), df_mul(hre, Dr));   // t_rho(e) D/(2j)
+                br[2] = df_sub(lo2(z2), df_mul(hrf, Di)); bi[2] = df_add(df_mul(hrf, Dr), hi2(z2));   // -t_rho(f) D/(2j)
+                br[3] = df_add(df_mulf(Sr, 0.5f), lo2(z3)); bi[3] = df_add(df_mulf(Si, 0.5f), hi2(z3));
+                const long long r0 = e + a, c0 = ff + b;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const long long row = r0 + (q >> 1) * Nn, col = c0 + (q & 1) * Nn;
+                    const float2 vr = df_sub(df_mul(sre, br[q]), df_mul(sim, bi[q]));
+                    const float2 vi = df_add(df_mul(sre, bi[q]), df_mul(sim, br[q]));
+                    catomic_add(Zm + row * ldz + col, make_double2(df_to_bits(vr), df_to_bits(vi)));
+                }
+            }
+        }
+    } else {
     for (int job = tid; job < EPB * nmodes; job += TPB) {
         const int jep = job / nmodes, m = m0 + job % nmodes;
         const int ff = f0 + jep;
@@ -357,15 +422,17 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
             }
         }
     }
+    }
 }
 
-template <class R, int NT>
+template <class R, int NT, int OG>
 int launch_far(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                const double *dct, const double *sin2, void *Z, long long ldz, long long ms,
                const unsigned char *emask, const float *dct32, cudaStream_t st)
 {
-    const size_t smem = SmemLayout<R, NT>::bytes();
-    auto kern = far_efie_kernel<R, NT>;
+    constexpr int EPB = 16 / OG;
+    const size_t smem = SmemLayout<R, NT, OG>::bytes();
+    auto kern = far_efie_kernel<R, NT, OG>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("far_efie: smem attribute");
     constexpr int NOB = OG * NT;
@@ -391,15 +458,16 @@ extern "C" int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nx
         ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k > 0.0))
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    // 4 order groups x NT orders per thread: NT = 8 covers |m| <= 29 in one
-    // launch row, NT = 16 covers |m| <= 61 per row
+    // OG order groups x NT orders per thread: (8, 4) covers |m| <= 29 in one
+    // launch row, (16, 4) |m| <= 61 and (16, 8) |m| <= 125 per row
     if (prec == GHOST_BOR_F32) {
-        if (m_max + 1 <= 30) return launch_far<float, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
-        return launch_far<float, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        if (m_max + 1 <= 30) return launch_far<float, 8, 4>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        if (m_max + 1 <= 62) return launch_far<float, 16, 4>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        return launch_far<float, 16, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
     }
     if (prec == GHOST_BOR_F64) {
-        if (m_max + 1 <= 30) return launch_far<double, 8>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
-        return launch_far<double, 16>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        if (m_max + 1 <= 30) return launch_far<double, 8, 4>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
+        return launch_far<double, 16, 4>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z, ldz, mode_stride, elem_mask, dct32, st);
     }
     return GHOST_BOR_EINVAL;
 }

@@ -34,9 +34,12 @@ struct NearSmem {
     // W    [TPBN][20] double  : Galerkin weights of the batch
     // Prim [20][Mp]   double2 : contracted primitives, all orders
     // Tab  [257]     float4  : double-float sin, cos of j pi/128 (FP32 path)
+    // Etab [32]      float2  : double-float 2^(j/32)
+    // Core [2][48]   float2  : double-float sinh-core Gauss nodes and weights
     static size_t bytes(int Mp, int NC) {
         return sizeof(double2) * (size_t)TPBN * NC + sizeof(double) * (size_t)TPBN * 20 +
-               sizeof(double2) * 20 * (size_t)Mp + sizeof(float4) * kDfTabN;
+               sizeof(double2) * 20 * (size_t)Mp + sizeof(float4) * kDfTabN +
+               sizeof(float2) * (kDfExpTabN + 2 * NCORE);
     }
 };
 
@@ -108,6 +111,30 @@ __device__ __forceinline__ void project(float4 (&dacc)[NC], float4 g, float2 cf,
     }
 }
 
+// two nodes at once (double-float): the two recurrences are independent
+// chains, so their latencies overlap
+template <int NC>
+__device__ __forceinline__ void project2(float4 (&dacc)[NC], float4 g0, float2 cf0, float2 &cm0, float2 &cc0,
+                                         float4 g1, float2 cf1, float2 &cm1, float2 &cc1)
+{
+    const float2 gr0 = make_float2(g0.x, g0.y), gi0 = make_float2(g0.z, g0.w);
+    const float2 gr1 = make_float2(g1.x, g1.y), gi1 = make_float2(g1.z, g1.w);
+    const float2 t0 = make_float2(2.f * cf0.x, 2.f * cf0.y), t1 = make_float2(2.f * cf1.x, 2.f * cf1.y);
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+        float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
+        df_mac(ar, gr0, cc0);
+        df_mac(ai, gi0, cc0);
+        df_mac(ar, gr1, cc1);
+        df_mac(ai, gi1, cc1);
+        dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
+        const float2 n0 = df_add(df_mul(t0, cc0), make_float2(-cm0.x, -cm0.y));
+        const float2 n1 = df_add(df_mul(t1, cc1), make_float2(-cm1.x, -cm1.y));
+        cm0 = cc0; cc0 = n0;
+        cm1 = cc1; cc1 = n1;
+    }
+}
+
 // DF = true: the cos(m xi) recurrence and the projection run in double-float
 // (two FP32 words, ~48 bits) instead of FP64; the transcendental functions of
 // each azimuth node are FP64 in both.
@@ -130,6 +157,8 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     double *W = reinterpret_cast<double *>(Gb + TPBN * NC);
     double2 *Prim = reinterpret_cast<double2 *>(W + TPBN * 20);
     float4 *Tab = reinterpret_cast<float4 *>(Prim + 20 * Mp);
+    float2 *Etab = reinterpret_cast<float2 *>(Tab + kDfTabN);
+    float2 *CoreX = Etab + kDfExpTabN, *CoreW = CoreX + NCORE;
     const int tid = threadIdx.x;
 
     const size_t plane = (size_t)nmax * TPBN;
@@ -141,7 +170,14 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     float2 *tU = reinterpret_cast<float2 *>(scratch + (size_t)gridDim.x * plane * kNodeBytes +
                                             (size_t)blockIdx.x * nmax * kTailBytes);
     float2 *tWr = tU + nmax, *tS2 = tWr + nmax, *tWs = tS2 + nmax, *tC1 = tWs + nmax;
-    if constexpr (DF) df_fill_sincos_table(Tab);
+    if constexpr (DF) {
+        df_fill_sincos_table(Tab);
+        df_fill_exp_table(Etab);
+        for (int i = tid; i < NCORE; i += TPBN) {
+            CoreX[i] = df_from(core_gl[i]);
+            CoreW[i] = df_from(core_gl[NCORE + i]);
+        }
+    }
     const double span_std = GB_PI - 2.0 * asin(0.25);
     const float2 kf = df_from(k);
     const float2 inv2pi = df_from(1.0 / (2.0 * GB_PI));
@@ -215,6 +251,40 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const double s0 = fmin(0.25, 20.0 * da);
                     const double vmax = asinh(s0 / da);
                     // -- sinh-graded core: s = (d/a) sinh(v), xi = 2 asin(s)
+                    if constexpr (DF) {
+                        // double-float on the FP32 pipe: sinh and cosh from one
+                        // e^v (and e^v - 1, exact for small v) and its reciprocal
+                        const float2 vmaxf = df_from(vmax), daf = df_from(da);
+                        const float2 d2f = df_from(fmax(d2, 1e-300)), a2f = df_from(rr4);
+                        const float2 one = make_float2(1.f, 0.f);
+#pragma unroll 2
+                        for (int i = 0; i < NCORE; ++i) {
+                            const float2 v = df_mul(CoreX[i], vmaxf);
+                            const float2 wv = df_mul(CoreW[i], vmaxf);
+                            float2 E, Em1;
+                            df_exp(v, Etab, E, Em1);
+                            const float2 iE = df_rcp(E);
+                            const float2 sh2 = df_mul(Em1, df_add(one, iE));        // 2 sinh v
+                            const float2 ch2 = df_add(E, iE);                        // 2 cosh v
+                            float2 sv = df_mul(daf, make_float2(0.5f * sh2.x, 0.5f * sh2.y));
+                            if (sv.x >= 1.0f) sv = one;
+                            const float2 sv2 = df_mul(sv, sv);
+                            float2 om = df_add(one, make_float2(-sv2.x, -sv2.y));
+                            if (om.x < 1e-15f) om = make_float2(1e-15f, 0.f);
+                            // d xi / d v = 2 (d/a) cosh v / sqrt(1 - s^2)
+                            const float2 dxi = df_mul(df_mul(daf, ch2), df_rsqrt(om));
+                            const float2 R2 = df_add(d2f, df_mul(a2f, sv2));
+                            const float2 iR = df_rsqrt(R2);
+                            const float2 R = df_mul(R2, iR);
+                            float2 sn, cs;
+                            df_sincos(df_reduce(df_mul(kf, R)), Tab, sn, cs);
+                            const float2 gw = df_mul(df_mul(df_mul(wv, dxi), iR), inv2pi);
+                            const float2 gre = df_mul(gw, cs), gim = df_mul(gw, sn);
+                            const float2 c1 = df_add(one, make_float2(-2.f * sv2.x, -2.f * sv2.y));
+                            put_node_df(gA, gC, gS0, gS1, (size_t)i * TPBN + tid, gre, make_float2(-gim.x, -gim.y),
+                                        c1);
+                        }
+                    } else
                     for (int i = 0; i < NCORE; ++i) {
                         const double v = core_gl[i] * vmax;
                         const double wv = core_gl[NCORE + i] * vmax;
@@ -300,8 +370,14 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     }
             }
             __syncthreads();                 // the previous batch's GEMM has finished reading W
+            if constexpr (DF) {
+                float2 *Wf = reinterpret_cast<float2 *>(W);
 #pragma unroll
-            for (int i = 0; i < 20; ++i) W[tid * 20 + i] = wl[i];
+                for (int i = 0; i < 20; ++i) Wf[tid * 20 + i] = df_from(wl[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 20; ++i) W[tid * 20 + i] = wl[i];
+            }
             const int cnt = min(TPBN, ncell - bt * TPBN);
 
             for (int ch = 0; ch < nchunk; ++ch) {
@@ -313,7 +389,16 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     else acc[n] = make_double2(0.0, 0.0);
                 }
                 if (valid && !on_axis) {
-                    for (int v = 0; v < nn; ++v) {
+                    int v = 0;
+                    if constexpr (DF) {
+                        for (; v + 1 < nn; v += 2) {
+                            const size_t i = (size_t)v * TPBN + tid, j = i + TPBN;
+                            NB cma = gS0[i], c0a = gS1[i], cmb = gS0[j], c0b = gS1[j];
+                            project2<NC>(acc, gA[i], gC[i], cma, c0a, gA[j], gC[j], cmb, c0b);
+                            if (ch + 1 < nchunk) { gS0[i] = cma; gS1[i] = c0a; gS0[j] = cmb; gS1[j] = c0b; }
+                        }
+                    }
+                    for (; v < nn; ++v) {
                         const size_t i = (size_t)v * TPBN + tid;
                         NB cm1 = gS0[i], c0 = gS1[i];
                         project<NC>(acc, gA[i], gC[i], cm1, c0);
@@ -321,15 +406,20 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     }
                 }
                 __syncthreads();             // the previous chunk's GEMM has finished reading Gb
+                if constexpr (DF) {
+                    // double-float orders and GEMM on the FP32 pipe
+                    float4 *Gf = reinterpret_cast<float4 *>(Gb);
 #pragma unroll
-                for (int n = 0; n < NC; ++n) {
-                    if constexpr (DF)
-                        Gb[tid * NC + n] = make_double2((double)acc[n].x + (double)acc[n].y,
-                                                        (double)acc[n].z + (double)acc[n].w);
-                    else
-                        Gb[tid * NC + n] = acc[n];
+                    for (int n = 0; n < NC; ++n) Gf[tid * NC + n] = acc[n];
+                    if (n0 == 0 && on_axis) {
+                        const float2 ar = df_from(axis0.x), ai = df_from(axis0.y);
+                        Gf[tid * NC] = make_float4(ar.x, ar.y, ai.x, ai.y);
+                    }
+                } else {
+#pragma unroll
+                    for (int n = 0; n < NC; ++n) Gb[tid * NC + n] = acc[n];
+                    if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
                 }
-                if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
                 __syncthreads();
                 // GEMM: Prim(c20, n0 + n) += sum_t W[t][c20] Gb[t][n]; each (c20, n)
                 // belongs to one thread, so the accumulation needs no atomics
@@ -338,12 +428,26 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const int o = tid + r * TPBN;
                     if (o < 20 * NC) {
                         const int c20 = o / NC, n = o % NC;
-                        double2 sacc = make_double2(0.0, 0.0);
-                        for (int t = 0; t < cnt; ++t) {
-                            const double wv = W[t * 20 + c20];
-                            const double2 gv = Gb[t * NC + n];
-                            sacc.x = fma(wv, gv.x, sacc.x);
-                            sacc.y = fma(wv, gv.y, sacc.y);
+                        double2 sacc;
+                        if constexpr (DF) {
+                            const float2 *Wf = reinterpret_cast<const float2 *>(W);
+                            const float4 *Gf = reinterpret_cast<const float4 *>(Gb);
+                            float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
+                            for (int t = 0; t < cnt; ++t) {
+                                const float2 wv = Wf[t * 20 + c20];
+                                const float4 gv = Gf[t * NC + n];
+                                df_mac(sr, wv, make_float2(gv.x, gv.y));
+                                df_mac(si, wv, make_float2(gv.z, gv.w));
+                            }
+                            sacc = make_double2(df_to(sr), df_to(si));
+                        } else {
+                            sacc = make_double2(0.0, 0.0);
+                            for (int t = 0; t < cnt; ++t) {
+                                const double wv = W[t * 20 + c20];
+                                const double2 gv = Gb[t * NC + n];
+                                sacc.x = fma(wv, gv.x, sacc.x);
+                                sacc.y = fma(wv, gv.y, sacc.y);
+                            }
                         }
                         if (n0 + n < Mp) {
                             double2 &pr = Prim[c20 * Mp + n0 + n];

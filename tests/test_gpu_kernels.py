@@ -74,6 +74,30 @@ def test_far_blocks(pkg, oracle, name):
             assert err < tol, (dtype, m, err)
 
 
+def test_far_fill_wide_order_rows(pkg, torch):
+    """|m| <= 90: the FP32 far fill covers every order in one launch row (two
+    element pairs and eight order groups per CTA), the FP64 fill in two rows;
+    both agree to the FP32 fill's accuracy on every mode."""
+    bodies = pkg.bodies
+    eng = pkg.engine
+    nat = pkg._native
+    pts = bodies.cone_sphere_generatrix(0.5, 15.0, 120)
+    prob = eng.BorGpuProblem(pts, 60.0 * 299792458.0 / (2 * math.pi), np.array([0.0, 90.0]), m_max=90)
+    Mb, n = prob.m_max + 1, prob.n
+    st = nat.stream_handle()
+    Z64 = torch.zeros((Mb, n, n), dtype=torch.complex128, device="cuda")
+    Z32 = torch.zeros_like(Z64)
+    prob.fill_far(Z64, nat.F64, 1.0 + 0.0j, st)
+    prob.fill_far(Z32, nat.F32, 1.0 + 0.0j, st)
+    torch.cuda.synchronize()
+    top = Z64.abs().max().item()
+    for m in range(Mb):
+        scale = Z64[m].abs().max().item()
+        err = (Z32[m] - Z64[m]).abs().max().item()
+        assert scale > 0.0
+        assert err < 2e-5 * top and err < 1e-3 * scale, (m, err / scale)
+
+
 @pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40", "openshell_n20"])
 def test_full_operator_and_excitation(pkg, name):
     """assemble_mode (far + near), rhs_mode and farfield_mode vs the reference goldens."""
