@@ -104,6 +104,47 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b)
     return make_float2(h, e - (h - s));
 }
 
+// ----------------------------------------------------------------------------
+// packed FP32 pairs: the f32x2 instructions of sm_100+ do the same operation on
+// both words of a 64-bit register pair, two lanes of work per instruction
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long p2_pk(float2 v)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 p2_up(unsigned long long r)
+{
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 p2_fma(float2 a, float2 b, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(p2_pk(a)), "l"(p2_pk(b)), "l"(p2_pk(c)));
+    return p2_up(d);
+}
+__device__ __forceinline__ float2 p2_add(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(p2_pk(a)), "l"(p2_pk(b)));
+    return p2_up(d);
+}
+__device__ __forceinline__ float2 p2_sub(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(p2_pk(a)), "l"(p2_pk(b)));
+    return p2_up(d);
+}
+__device__ __forceinline__ float2 p2_mul(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(p2_pk(a)), "l"(p2_pk(b)));
+    return p2_up(d);
+}
+
 __device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, df_neg(b)); }
 // complex double-float packed as (re.hi, re.lo, im.hi, im.lo)

@@ -158,36 +158,38 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         if constexpr (sizeof(R) == 4) {
             // FP32: 8-sample blocks folded into the running sums with Kahan
             // compensation (the node-level entries are double differences of
-            // these orders, so their rounding must stay well below an ulp)
+            // these orders, so their rounding must stay well below an ulp).
+            // Packed f32x2 arithmetic on pairs of orders: acc[q] holds the real
+            // parts of orders 2q, 2q + 1 and acc[NT/2 + q] their imaginary parts
+            // (likewise cmp), so one instruction updates two orders.
+            constexpr int H = NT / 2;
             for (int jb = 0; jb < jn; jb += 8) {
-                CT cacc[NT];
+                float2 bR[H], bI[H];
 #pragma unroll
-                for (int n = 0; n < NT; ++n) cacc[n] = mk<R>(R(0), R(0));
+                for (int q = 0; q < H; ++q) { bR[q] = make_float2(0.f, 0.f); bI[q] = bR[q]; }
                 const int je = min(jb + 8, jn);
                 for (int jj = jb; jj < je; ++jj) {
                     const CT gv = gsm[jj * PPB + pp];
+                    const float2 gxx = make_float2(gv.x, gv.x), gyy = make_float2(gv.y, gv.y);
                     const float4 *row = reinterpret_cast<const float4 *>(drow + jj * NOB);
 #pragma unroll
                     for (int n4 = 0; n4 < NT / 4; ++n4) {
                         const float4 c = row[n4];
-                        cacc[4 * n4 + 0].x = fmaf(gv.x, c.x, cacc[4 * n4 + 0].x);
-                        cacc[4 * n4 + 0].y = fmaf(gv.y, c.x, cacc[4 * n4 + 0].y);
-                        cacc[4 * n4 + 1].x = fmaf(gv.x, c.y, cacc[4 * n4 + 1].x);
-                        cacc[4 * n4 + 1].y = fmaf(gv.y, c.y, cacc[4 * n4 + 1].y);
-                        cacc[4 * n4 + 2].x = fmaf(gv.x, c.z, cacc[4 * n4 + 2].x);
-                        cacc[4 * n4 + 2].y = fmaf(gv.y, c.z, cacc[4 * n4 + 2].y);
-                        cacc[4 * n4 + 3].x = fmaf(gv.x, c.w, cacc[4 * n4 + 3].x);
-                        cacc[4 * n4 + 3].y = fmaf(gv.y, c.w, cacc[4 * n4 + 3].y);
+                        const float2 c01 = make_float2(c.x, c.y), c23 = make_float2(c.z, c.w);
+                        bR[2 * n4 + 0] = p2_fma(gxx, c01, bR[2 * n4 + 0]);
+                        bI[2 * n4 + 0] = p2_fma(gyy, c01, bI[2 * n4 + 0]);
+                        bR[2 * n4 + 1] = p2_fma(gxx, c23, bR[2 * n4 + 1]);
+                        bI[2 * n4 + 1] = p2_fma(gyy, c23, bI[2 * n4 + 1]);
                     }
                 }
 #pragma unroll
-                for (int n = 0; n < NT; ++n) {
-                    const float yx = cacc[n].x - cmp[n].x, yy = cacc[n].y - cmp[n].y;
-                    const float tx = acc[n].x + yx, ty = acc[n].y + yy;
-                    cmp[n].x = (tx - acc[n].x) - yx;
-                    cmp[n].y = (ty - acc[n].y) - yy;
-                    acc[n].x = tx;
-                    acc[n].y = ty;
+                for (int q = 0; q < H; ++q) {
+                    const float2 yr = p2_sub(bR[q], cmp[q]), yi = p2_sub(bI[q], cmp[H + q]);
+                    const float2 tr = p2_add(acc[q], yr), ti = p2_add(acc[H + q], yi);
+                    cmp[q] = p2_sub(p2_sub(tr, acc[q]), yr);
+                    cmp[H + q] = p2_sub(p2_sub(ti, acc[H + q]), yi);
+                    acc[q] = tr;
+                    acc[H + q] = ti;
                 }
             }
         } else {
@@ -209,9 +211,14 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     // per-pair orders to smem: FP32 path as double-float words (acc - cmp)
     if constexpr (sizeof(R) == 4) {
         float4 *Gf = reinterpret_cast<float4 *>(Gs);
+        constexpr int H = NT / 2;
 #pragma unroll
-        for (int n = 0; n < NT; ++n)
-            Gf[(ep * NOB + og * NT + n) * SLAB + gh] = make_float4(acc[n].x, -cmp[n].x, acc[n].y, -cmp[n].y);
+        for (int q = 0; q < H; ++q) {
+            Gf[(ep * NOB + og * NT + 2 * q) * SLAB + gh] =
+                make_float4(acc[q].x, -cmp[q].x, acc[H + q].x, -cmp[H + q].x);
+            Gf[(ep * NOB + og * NT + 2 * q + 1) * SLAB + gh] =
+                make_float4(acc[q].y, -cmp[q].y, acc[H + q].y, -cmp[H + q].y);
+        }
     } else {
 #pragma unroll
         for (int n = 0; n < NT; ++n)
