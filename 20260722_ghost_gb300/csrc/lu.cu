@@ -182,61 +182,91 @@ __global__ void laswp_rhs_kernel(int n, int nrhs, C<R> *__restrict__ B, long lon
 }
 
 // X := L^-1 X (unit lower) or U^-1 X (non-unit upper) for an nb-row block,
-// one thread per column.  T points at the nb x nb diagonal block.
+// one thread per column.  T points at the nb x nb diagonal block, held in
+// shared memory; the thread's column of X is staged in shared memory too
+// (column-per-thread layout, conflict-free), so the substitution is a short
+// rolled loop instead of a fully unrolled NB x NB register program whose code
+// would not fit the instruction cache.
+constexpr int TRSM_COLS = 64;        // columns (threads) per CTA
 template <class R, int NB, bool UPPER>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(TRSM_COLS)
 trsm_kernel(int nb, int ncols, const C<R> *__restrict__ T, long long ldt, long long st,
             C<R> *__restrict__ X, long long ldx, long long sx)
 {
     using CT = C<R>;
-    __shared__ CT Ts[NB][NB + 1];
-    __shared__ CT Dinv[NB];
+    extern __shared__ __align__(16) unsigned char trsm_smem[];
+    CT(*Ts)[NB + 1] = reinterpret_cast<CT(*)[NB + 1]>(trsm_smem);
+    CT *Dinv = reinterpret_cast<CT *>(trsm_smem + sizeof(CT) * NB * (NB + 1));
+    CT *Xs = Dinv + NB;                                   // [NB][TRSM_COLS]
     const int b = blockIdx.y;
     const CT *Tb = T + (size_t)b * st;
     for (int i = threadIdx.x; i < nb * nb; i += blockDim.x) {
         const int r = i / nb, c = i % nb;
         Ts[r][c] = Tb[(size_t)r * ldt + c];
     }
-    __syncthreads();
     if (UPPER) {
+        __syncthreads();
         for (int i = threadIdx.x; i < nb; i += blockDim.x) {
             const CT d = Ts[i][i];
             const R den = d.x * d.x + d.y * d.y;
             Dinv[i] = mk<R>(d.x / den, -d.y / den);
         }
-        __syncthreads();
     }
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
+    const bool act = c < ncols;
     CT *Xb = X + (size_t)b * sx + c;
-    CT x[NB];
-#pragma unroll
-    for (int i = 0; i < NB; ++i) x[i] = (i < nb) ? Xb[(size_t)i * ldx] : mk<R>(0, 0);
+    CT *xs = Xs + threadIdx.x;
+    for (int i = 0; i < nb; ++i) xs[i * TRSM_COLS] = act ? Xb[(size_t)i * ldx] : mk<R>(0, 0);
+    __syncthreads();
+    if (!act) return;
     if (!UPPER) {
-#pragma unroll
-        for (int i = 1; i < NB; ++i) {
-            if (i < nb) {
-                CT s = x[i];
-#pragma unroll
-                for (int j = 0; j < i; ++j) s = cfms(Ts[i][j], x[j], s);
-                x[i] = s;
+        for (int i = 1; i < nb; ++i) {
+            CT s0 = xs[i * TRSM_COLS], s1 = mk<R>(0, 0);
+            int j = 0;
+            for (; j + 1 < i; j += 2) {                 // two partial sums
+                s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+                s1 = cfms(Ts[i][j + 1], xs[(j + 1) * TRSM_COLS], s1);
             }
+            if (j < i) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+            xs[i * TRSM_COLS] = cadd(s0, s1);
         }
     } else {
-#pragma unroll
-        for (int i = NB - 1; i >= 0; --i) {
-            if (i < nb) {
-                CT s = x[i];
-#pragma unroll
-                for (int j = i + 1; j < NB; ++j)
-                    if (j < nb) s = cfms(Ts[i][j], x[j], s);
-                x[i] = cmul(s, Dinv[i]);
+        for (int i = nb - 1; i >= 0; --i) {
+            CT s0 = xs[i * TRSM_COLS], s1 = mk<R>(0, 0);
+            int j = i + 1;
+            for (; j + 1 < nb; j += 2) {
+                s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+                s1 = cfms(Ts[i][j + 1], xs[(j + 1) * TRSM_COLS], s1);
             }
+            if (j < nb) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+            xs[i * TRSM_COLS] = cmul(cadd(s0, s1), Dinv[i]);
         }
     }
-#pragma unroll
-    for (int i = 0; i < NB; ++i)
-        if (i < nb) Xb[(size_t)i * ldx] = x[i];
+    for (int i = 0; i < nb; ++i) Xb[(size_t)i * ldx] = xs[i * TRSM_COLS];
+}
+
+template <class R, int NB>
+constexpr size_t trsm_smem_bytes()
+{
+    return sizeof(C<R>) * ((size_t)NB * (NB + 1) + NB + (size_t)NB * TRSM_COLS);
+}
+
+// launch helper: one thread per column, TRSM_COLS columns per CTA
+template <class R, int NB, bool UPPER>
+int trsm_launch(int batch, int nb, int ncols, const C<R> *T, long long ldt, long long st, C<R> *X, long long ldx,
+                long long sx, cudaStream_t s)
+{
+    constexpr size_t smem = trsm_smem_bytes<R, NB>();
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(trsm_kernel<R, NB, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return check_launch("trsm: smem attribute");
+        attr = true;
+    }
+    dim3 g((ncols + TRSM_COLS - 1) / TRSM_COLS, batch);
+    trsm_kernel<R, NB, UPPER><<<g, TRSM_COLS, smem, s>>>(nb, ncols, T, ldt, st, X, ldx, sx);
+    return check_launch(UPPER ? "trsm U" : "trsm L");
 }
 
 // C -= A B,  A: rows x K, B: K x cols, K <= NB; 64 x 64 tiles, 4 x 4 per thread
@@ -396,10 +426,9 @@ int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv
         }
         const int rest = n - k0 - nb;
         if (rest > 0) {
-            dim3 g((rest + 127) / 128, batch);
-            trsm_kernel<R, NB, false><<<g, 128, 0, st>>>(nb, rest, A + (size_t)k0 * lda + k0, lda, sa,
-                                                          A + (size_t)k0 * lda + k0 + nb, lda, sa);
-            if ((rc = check_launch("getrf: trsm"))) return rc;
+            if ((rc = trsm_launch<R, NB, false>(batch, nb, rest, A + (size_t)k0 * lda + k0, lda, sa,
+                                                A + (size_t)k0 * lda + k0 + nb, lda, sa, st)))
+                return rc;
             const C<R> *L21 = A + (size_t)(k0 + nb) * lda + k0;
             const C<R> *U12 = A + (size_t)k0 * lda + k0 + nb;
             C<R> *A22 = A + (size_t)(k0 + nb) * lda + k0 + nb;
@@ -441,15 +470,14 @@ int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long lo
     // updates read and write the right-hand sides once per NBS rows, so on the
     // tensor-core path (whose updates are bound by that traffic) NBS = 4 NB.
     const int NBS = (sizeof(R) == 4 && work) ? kSolveBlocks * NB : NB;
-    dim3 gt((nrhs + 127) / 128, batch);
     int rc;
     for (int k0 = 0; k0 < n; k0 += NBS) {
         const int kb = min(NBS, n - k0);
         for (int j0 = k0; j0 < k0 + kb; j0 += NB) {
             const int nb = min(NB, k0 + kb - j0);
-            trsm_kernel<R, NB, false><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
-                                                           B + (size_t)j0 * ldb, ldb, sb);
-            if ((rc = check_launch("getrs: trsm L"))) return rc;
+            if ((rc = trsm_launch<R, NB, false>(batch, nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
+                                                B + (size_t)j0 * ldb, ldb, sb, st)))
+                return rc;
             if ((rc = update<R>(batch, k0 + kb - j0 - nb, nrhs, nb, A + (size_t)(j0 + nb) * lda + j0, lda, sa,
                                 B + (size_t)j0 * ldb, ldb, sb, B + (size_t)(j0 + nb) * ldb, ldb, sb, work, st)))
                 return rc;
@@ -463,9 +491,9 @@ int getrs_impl(int batch, int n, int nrhs, const C<R> *A, long long lda, long lo
         const int kb = min(NBS, n - k0);
         for (int j0 = k0 + ((kb - 1) / NB) * NB; j0 >= k0; j0 -= NB) {
             const int nb = min(NB, k0 + kb - j0);
-            trsm_kernel<R, NB, true><<<gt, 128, 0, st>>>(nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
-                                                          B + (size_t)j0 * ldb, ldb, sb);
-            if ((rc = check_launch("getrs: trsm U"))) return rc;
+            if ((rc = trsm_launch<R, NB, true>(batch, nb, nrhs, A + (size_t)j0 * lda + j0, lda, sa,
+                                               B + (size_t)j0 * ldb, ldb, sb, st)))
+                return rc;
             if ((rc = update<R>(batch, j0 - k0, nrhs, nb, A + (size_t)k0 * lda + j0, lda, sa,
                                 B + (size_t)j0 * ldb, ldb, sb, B + (size_t)k0 * ldb, ldb, sb, work, st)))
                 return rc;

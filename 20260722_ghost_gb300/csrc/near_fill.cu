@@ -8,12 +8,14 @@
 // A persistent grid of CTAs walks the element pairs (e, f), |e - f| <= 1.
 // Per batch of 128 Gauss-point pairs of the graded cells, each thread first
 // evaluates its pair's azimuth nodes once -- g(xi) times the quadrature weight
-// and cos(xi), all transcendental functions in FP64 -- into a per-CTA global
-// scratch (node-major, so every access is coalesced); then, for each chunk of
-// NC orders, it projects the nodes onto cos(n xi) by the Chebyshev recurrence
-// and the CTA contracts the pairs with the 20 Galerkin weights (5 primitives x
-// 2x2 nodes) as a small GEMM through shared memory.  The FP64 transcendental
-// work is therefore done once per node instead of once per order chunk.
+// and cos(xi) -- into a per-CTA global scratch (node-major, so every access is
+// coalesced); then, for each chunk of orders (NC, the remainder in chunks of
+// 8), it projects the nodes onto cos(n xi) by the Chebyshev recurrence and the
+// CTA contracts the pairs with the 20 Galerkin weights (5 primitives x 2x2
+// nodes) as a small GEMM through shared memory.  The transcendental work is
+// therefore done once per node instead of once per order chunk.  On the FP32
+// path all of it runs in double-float arithmetic (df_math.cuh) on the FP32
+// pipe, which on a GB300 is ~64x the FP64 pipe.
 // Finally the CTA combines orders |m-1|, m, m+1 into the four mode-m blocks and
 // adds scale * block into the output (FP64 band store or dense Z).
 #include <type_traits>
@@ -98,46 +100,168 @@ __device__ __forceinline__ void project(double2 (&acc)[NC], double2 g, double c1
 template <int NC>
 __device__ __forceinline__ void project(float4 (&dacc)[NC], float4 g, float2 cf, float2 &cm1, float2 &c0)
 {
+    // double-float order accumulators are kept as (re.hi, im.hi, re.lo, im.lo)
+    // so that the packed f32x2 instructions of project2 work on (re, im) pairs
     const float2 gr = make_float2(g.x, g.y), gi = make_float2(g.z, g.w);
     const float2 tc = make_float2(2.f * cf.x, 2.f * cf.y);   // exact doubling
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
-        float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
+        float2 ar = make_float2(dacc[n].x, dacc[n].z), ai = make_float2(dacc[n].y, dacc[n].w);
         df_mac(ar, gr, c0);
         df_mac(ai, gi, c0);
-        dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
+        dacc[n] = make_float4(ar.x, ai.x, ar.y, ai.y);
         const float2 cn = df_add(df_mul(tc, c0), make_float2(-cm1.x, -cm1.y));
         cm1 = c0; c0 = cn;
     }
 }
 
-// two nodes at once (double-float): the two recurrences are independent
-// chains, so their latencies overlap
+// Two nodes at once (double-float) on packed f32x2 instructions: the two
+// recurrences run as the lanes of one pair (node a, node b), and each node's
+// multiply-add into the (re, im) accumulators as the lanes of another; every
+// rounding is that of df_mac / df_mul / df_add, so the result is the scalar one.
+// S += G c with G = (re, im) of a node and c broadcast: Gh, Gl the high / low
+// words of G, NGh = -Gh
+__device__ __forceinline__ void p2_df_mac(float2 &Sh, float2 &Sl, float2 Gh, float2 Gl, float2 NGh, float2 Ch,
+                                          float2 Cl)
+{
+    const float2 NP = p2_mul(NGh, Ch);                 // -p
+    const float2 PE = p2_fma(Gh, Ch, NP);              // error of p
+    const float2 T = p2_sub(Sh, NP);                   // s + p
+    const float2 BB = p2_sub(T, Sh);
+    const float2 TE = p2_sub(p2_sub(Sh, p2_sub(T, BB)), p2_add(NP, BB));
+    const float2 X = p2_fma(Gh, Cl, p2_mul(Gl, Ch));
+    Sl = p2_add(Sl, p2_add(p2_add(TE, PE), X));
+    Sh = T;
+}
+
 template <int NC>
 __device__ __forceinline__ void project2(float4 (&dacc)[NC], float4 g0, float2 cf0, float2 &cm0, float2 &cc0,
                                          float4 g1, float2 cf1, float2 &cm1, float2 &cc1)
 {
-    const float2 gr0 = make_float2(g0.x, g0.y), gi0 = make_float2(g0.z, g0.w);
-    const float2 gr1 = make_float2(g1.x, g1.y), gi1 = make_float2(g1.z, g1.w);
-    const float2 t0 = make_float2(2.f * cf0.x, 2.f * cf0.y), t1 = make_float2(2.f * cf1.x, 2.f * cf1.y);
+    const float2 Gh0 = make_float2(g0.x, g0.z), Gl0 = make_float2(g0.y, g0.w), NGh0 = make_float2(-g0.x, -g0.z);
+    const float2 Gh1 = make_float2(g1.x, g1.z), Gl1 = make_float2(g1.y, g1.w), NGh1 = make_float2(-g1.x, -g1.z);
+    // recurrence lanes (node 0, node 1): t = 2 cos(xi), state (c_{n-1}, c_n)
+    const float2 TCh = make_float2(2.f * cf0.x, 2.f * cf1.x), TCl = make_float2(2.f * cf0.y, 2.f * cf1.y);
+    const float2 NTCh = make_float2(-TCh.x, -TCh.y);
+    float2 CMh = make_float2(cm0.x, cm1.x), CMl = make_float2(cm0.y, cm1.y);
+    float2 C0h = make_float2(cc0.x, cc1.x), C0l = make_float2(cc0.y, cc1.y);
 #pragma unroll
     for (int n = 0; n < NC; ++n) {
-        float2 ar = make_float2(dacc[n].x, dacc[n].y), ai = make_float2(dacc[n].z, dacc[n].w);
-        df_mac(ar, gr0, cc0);
-        df_mac(ai, gi0, cc0);
-        df_mac(ar, gr1, cc1);
-        df_mac(ai, gi1, cc1);
-        dacc[n] = make_float4(ar.x, ar.y, ai.x, ai.y);
-        const float2 n0 = df_add(df_mul(t0, cc0), make_float2(-cm0.x, -cm0.y));
-        const float2 n1 = df_add(df_mul(t1, cc1), make_float2(-cm1.x, -cm1.y));
-        cm0 = cc0; cc0 = n0;
-        cm1 = cc1; cc1 = n1;
+        float2 Sh = make_float2(dacc[n].x, dacc[n].y), Sl = make_float2(dacc[n].z, dacc[n].w);
+        p2_df_mac(Sh, Sl, Gh0, Gl0, NGh0, make_float2(C0h.x, C0h.x), make_float2(C0l.x, C0l.x));
+        p2_df_mac(Sh, Sl, Gh1, Gl1, NGh1, make_float2(C0h.y, C0h.y), make_float2(C0l.y, C0l.y));
+        dacc[n] = make_float4(Sh.x, Sh.y, Sl.x, Sl.y);
+        // c_{n+1} = t c_n - c_{n-1}: df_mul then df_add, lane-wise
+        const float2 NP = p2_mul(NTCh, C0h);
+        float2 E = p2_fma(TCh, C0h, NP);
+        E = p2_add(E, p2_fma(TCh, C0l, p2_mul(TCl, C0h)));
+        const float2 H = p2_sub(E, NP);
+        const float2 L = p2_sub(E, p2_add(H, NP));
+        const float2 S = p2_sub(H, CMh);
+        const float2 BB = p2_sub(S, H);
+        float2 F = p2_sub(p2_sub(H, p2_sub(S, BB)), p2_add(CMh, BB));
+        F = p2_sub(p2_add(F, L), CMl);
+        const float2 Nh = p2_add(S, F);
+        const float2 Nl = p2_sub(F, p2_sub(Nh, S));
+        CMh = C0h; CMl = C0l;
+        C0h = Nh; C0l = Nl;
+    }
+    cm0 = make_float2(CMh.x, CMl.x); cc0 = make_float2(C0h.x, C0l.x);
+    cm1 = make_float2(CMh.y, CMl.y); cc1 = make_float2(C0h.y, C0l.y);
+}
+
+// one chunk of NCc orders n0 .. n0 + NCc - 1 for the current batch of point
+// pairs: project every node of this thread's pair onto cos(n xi) (advancing
+// the recurrence state in the scratch when more chunks follow), then contract
+// the batch with the Galerkin weights into Prim
+template <bool DF, int NCc>
+__device__ __forceinline__ void near_chunk(int n0, bool more, bool valid, bool on_axis, double2 axis0, int nn,
+                                           int tid, int cnt, int Mp, typename NodeT<DF>::A *gA,
+                                           typename NodeT<DF>::B *gC, typename NodeT<DF>::B *gS0,
+                                           typename NodeT<DF>::B *gS1, double2 *Gb, double *W, double2 *Prim)
+{
+    using NB = typename NodeT<DF>::B;
+    using Acc = typename std::conditional<DF, float4, double2>::type;
+    constexpr int NOUT = (20 * NCc + TPBN - 1) / TPBN;
+    Acc acc[NCc];
+#pragma unroll
+    for (int n = 0; n < NCc; ++n) {
+        if constexpr (DF) acc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else acc[n] = make_double2(0.0, 0.0);
+    }
+    if (valid && !on_axis) {
+        int v = 0;
+        if constexpr (DF) {
+            for (; v + 1 < nn; v += 2) {
+                const size_t i = (size_t)v * TPBN + tid, j = i + TPBN;
+                NB cma = gS0[i], c0a = gS1[i], cmb = gS0[j], c0b = gS1[j];
+                project2<NCc>(acc, gA[i], gC[i], cma, c0a, gA[j], gC[j], cmb, c0b);
+                if (more) { gS0[i] = cma; gS1[i] = c0a; gS0[j] = cmb; gS1[j] = c0b; }
+            }
+        }
+        for (; v < nn; ++v) {
+            const size_t i = (size_t)v * TPBN + tid;
+            NB cm1 = gS0[i], c0 = gS1[i];
+            project<NCc>(acc, gA[i], gC[i], cm1, c0);
+            if (more) { gS0[i] = cm1; gS1[i] = c0; }
+        }
+    }
+    __syncthreads();             // the previous chunk's GEMM has finished reading Gb
+    if constexpr (DF) {
+        // double-float orders and GEMM on the FP32 pipe
+        float4 *Gf = reinterpret_cast<float4 *>(Gb);
+#pragma unroll
+        for (int n = 0; n < NCc; ++n) Gf[tid * NCc + n] = acc[n];
+        if (n0 == 0 && on_axis) {
+            const float2 ar = df_from(axis0.x), ai = df_from(axis0.y);
+            Gf[tid * NCc] = make_float4(ar.x, ai.x, ar.y, ai.y);
+        }
+    } else {
+#pragma unroll
+        for (int n = 0; n < NCc; ++n) Gb[tid * NCc + n] = acc[n];
+        if (n0 == 0) { Gb[tid * NCc].x += axis0.x; Gb[tid * NCc].y += axis0.y; }
+    }
+    __syncthreads();
+    // GEMM: Prim(c20, n0 + n) += sum_t W[t][c20] Gb[t][n]; each (c20, n)
+    // belongs to one thread, so the accumulation needs no atomics
+#pragma unroll
+    for (int r = 0; r < NOUT; ++r) {
+        const int o = tid + r * TPBN;
+        if (o < 20 * NCc) {
+            const int c20 = o / NCc, n = o % NCc;
+            double2 sacc;
+            if constexpr (DF) {
+                const float2 *Wf = reinterpret_cast<const float2 *>(W);
+                const float4 *Gf = reinterpret_cast<const float4 *>(Gb);
+                float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
+                for (int t = 0; t < cnt; ++t) {
+                    const float2 wv = Wf[t * 20 + c20];
+                    const float4 gv = Gf[t * NCc + n];
+                    df_mac(sr, wv, make_float2(gv.x, gv.z));
+                    df_mac(si, wv, make_float2(gv.y, gv.w));
+                }
+                sacc = make_double2(df_to(sr), df_to(si));
+            } else {
+                sacc = make_double2(0.0, 0.0);
+                for (int t = 0; t < cnt; ++t) {
+                    const double wv = W[t * 20 + c20];
+                    const double2 gv = Gb[t * NCc + n];
+                    sacc.x = fma(wv, gv.x, sacc.x);
+                    sacc.y = fma(wv, gv.y, sacc.y);
+                }
+            }
+            if (n0 + n < Mp) {
+                double2 &pr = Prim[c20 * Mp + n0 + n];
+                pr.x += sacc.x;
+                pr.y += sacc.y;
+            }
+        }
     }
 }
 
-// DF = true: the cos(m xi) recurrence and the projection run in double-float
-// (two FP32 words, ~48 bits) instead of FP64; the transcendental functions of
-// each azimuth node are FP64 in both.
+// DF = true (FP32+IR path): every node's transcendental functions, the cos(m xi)
+// recurrence, the projection and the order GEMM run in double-float (two FP32
+// words, ~48 bits) on the FP32 pipe; DF = false is the plain FP64 path.
 template <bool DF, int NC>
 __global__ void __launch_bounds__(TPBN, 2)
 near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
@@ -182,8 +306,6 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     const float2 kf = df_from(k);
     const float2 inv2pi = df_from(1.0 / (2.0 * GB_PI));
 
-    constexpr int NOUT = (20 * NC + TPBN - 1) / TPBN;
-    const int nchunk = (Mp + NC - 1) / NC;
     const double kk = k;
 
     for (int pi = blockIdx.x; pi < n_pairs; pi += gridDim.x) {
@@ -380,83 +502,16 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
             }
             const int cnt = min(TPBN, ncell - bt * TPBN);
 
-            for (int ch = 0; ch < nchunk; ++ch) {
-                const int n0 = ch * NC;
-                Acc acc[NC];
-#pragma unroll
-                for (int n = 0; n < NC; ++n) {
-                    if constexpr (DF) acc[n] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    else acc[n] = make_double2(0.0, 0.0);
-                }
-                if (valid && !on_axis) {
-                    int v = 0;
-                    if constexpr (DF) {
-                        for (; v + 1 < nn; v += 2) {
-                            const size_t i = (size_t)v * TPBN + tid, j = i + TPBN;
-                            NB cma = gS0[i], c0a = gS1[i], cmb = gS0[j], c0b = gS1[j];
-                            project2<NC>(acc, gA[i], gC[i], cma, c0a, gA[j], gC[j], cmb, c0b);
-                            if (ch + 1 < nchunk) { gS0[i] = cma; gS1[i] = c0a; gS0[j] = cmb; gS1[j] = c0b; }
-                        }
-                    }
-                    for (; v < nn; ++v) {
-                        const size_t i = (size_t)v * TPBN + tid;
-                        NB cm1 = gS0[i], c0 = gS1[i];
-                        project<NC>(acc, gA[i], gC[i], cm1, c0);
-                        if (ch + 1 < nchunk) { gS0[i] = cm1; gS1[i] = c0; }
-                    }
-                }
-                __syncthreads();             // the previous chunk's GEMM has finished reading Gb
-                if constexpr (DF) {
-                    // double-float orders and GEMM on the FP32 pipe
-                    float4 *Gf = reinterpret_cast<float4 *>(Gb);
-#pragma unroll
-                    for (int n = 0; n < NC; ++n) Gf[tid * NC + n] = acc[n];
-                    if (n0 == 0 && on_axis) {
-                        const float2 ar = df_from(axis0.x), ai = df_from(axis0.y);
-                        Gf[tid * NC] = make_float4(ar.x, ar.y, ai.x, ai.y);
-                    }
-                } else {
-#pragma unroll
-                    for (int n = 0; n < NC; ++n) Gb[tid * NC + n] = acc[n];
-                    if (n0 == 0) { Gb[tid * NC].x += axis0.x; Gb[tid * NC].y += axis0.y; }
-                }
-                __syncthreads();
-                // GEMM: Prim(c20, n0 + n) += sum_t W[t][c20] Gb[t][n]; each (c20, n)
-                // belongs to one thread, so the accumulation needs no atomics
-#pragma unroll
-                for (int r = 0; r < NOUT; ++r) {
-                    const int o = tid + r * TPBN;
-                    if (o < 20 * NC) {
-                        const int c20 = o / NC, n = o % NC;
-                        double2 sacc;
-                        if constexpr (DF) {
-                            const float2 *Wf = reinterpret_cast<const float2 *>(W);
-                            const float4 *Gf = reinterpret_cast<const float4 *>(Gb);
-                            float2 sr = make_float2(0.f, 0.f), si = make_float2(0.f, 0.f);
-                            for (int t = 0; t < cnt; ++t) {
-                                const float2 wv = Wf[t * 20 + c20];
-                                const float4 gv = Gf[t * NC + n];
-                                df_mac(sr, wv, make_float2(gv.x, gv.y));
-                                df_mac(si, wv, make_float2(gv.z, gv.w));
-                            }
-                            sacc = make_double2(df_to(sr), df_to(si));
-                        } else {
-                            sacc = make_double2(0.0, 0.0);
-                            for (int t = 0; t < cnt; ++t) {
-                                const double wv = W[t * 20 + c20];
-                                const double2 gv = Gb[t * NC + n];
-                                sacc.x = fma(wv, gv.x, sacc.x);
-                                sacc.y = fma(wv, gv.y, sacc.y);
-                            }
-                        }
-                        if (n0 + n < Mp) {
-                            double2 &pr = Prim[c20 * Mp + n0 + n];
-                            pr.x += sacc.x;
-                            pr.y += sacc.y;
-                        }
-                    }
-                }
-            }
+            // chunks of NC orders, then the remainder in chunks of 8 (or one more
+            // full chunk when more than 16 orders remain)
+            const int nfull = (Mp % NC > 16) ? (Mp + NC - 1) / NC : Mp / NC;
+            const int ntl = nfull * NC >= Mp ? 0 : (Mp - nfull * NC + 7) / 8;
+            for (int ch = 0; ch < nfull; ++ch)
+                near_chunk<DF, NC>(ch * NC, ch + 1 < nfull || ntl > 0, valid, on_axis, axis0, nn, tid, cnt, Mp,
+                                   gA, gC, gS0, gS1, Gb, W, Prim);
+            for (int ch = 0; ch < ntl; ++ch)
+                near_chunk<DF, 8>(nfull * NC + ch * 8, ch + 1 < ntl, valid, on_axis, axis0, nn, tid, cnt, Mp,
+                                  gA, gC, gS0, gS1, Gb, W, Prim);
         }
         __syncthreads();
 

@@ -181,7 +181,8 @@ def load_peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return {"hbm_gbs": d.get("hbm_gbs"), "bf16_tflops": d.get("bf16_tflops"), "source": "measured"}
+        return {"hbm_gbs": d.get("hbm_gbs"), "bf16_tflops": d.get("bf16_tflops"), "sm_max_mhz": d.get("sm_max_mhz"),
+                "source": "measured"}
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
@@ -473,31 +474,40 @@ def roofline(res, peaks, workload):
                "note": "residual B - Z X of all modes, 8 n^2 nrhs (M+1) useful flops per launch, "
                        "computed as 13 exact bf16 slice-pair products on the tensor cores"}
     else:
-        # the fills are compute-bound on the CUDA cores (near: FP64 pipe for the
-        # per-node transcendentals, far: FP32 pipe); the schema's compute roof is
-        # the measured tensor peak, so the FP64 / FP32 pipe context is added
+        # the fills are compute-bound on the CUDA cores (FP32 pipe and instruction
+        # issue); the schema's compute roof is the measured tensor peak, so the
+        # FP32-pipe roof (nominal: 152 SMs x 128 FMA lanes x 2 flops x SM clock)
+        # and the ncu pipe counters of the committed profile are added
         ach = w_sum / t_sum / 1e12
         peak = peaks["bf16_tflops"]
+        fp32_peak = 152 * 128 * 2 * (peaks.get("sm_max_mhz") or 2070.0) * 1e6 / 1e12
         out = {"bound": "tensor", "achieved": round(ach, 3), "peak": peak, "unit": "TFLOP/s",
                "frac": round(ach / peak, 5) if peak else None}
+        ctx = FILL_COUNTERS.get(name, {})
+        out["fp32_pipe"] = dict({"achieved_tflops": round(ach, 3), "nominal_peak_tflops": round(fp32_peak, 1),
+                                 "frac": round(ach / fp32_peak, 4)}, **ctx)
         if name == "near_fill":
-            out["note"] = ("near fill: flops of the double-float cos(m xi) projection; the kernel is bound "
-                           "by the FP64 pipe (transcendentals of every azimuth node), not by the tensor "
-                           "cores it is measured against here")
-            out["fp64_pipe"] = {"nominal_peak_tflops": 1.25, "busy_pct_ncu": 75,
-                                "profile": "profiles/near_efie_cone_sphere_ka20.md"}
+            out["note"] = ("near fill: 4 flops per azimuth node and order of the cos(m xi) projection; each "
+                           "is a double-float multiply-add on the FP32 pipe (~30 FP32 instructions with the "
+                           "recurrence), and every node's transcendentals run in double-float as well")
         else:
-            out["note"] = "far fill: flops of the FP32 DCT; bound by the FP32 pipe and instruction issue"
+            out["note"] = ("far fill: 4 flops per sample and order of the DCT (packed f32x2 FMAs with "
+                           "Kahan-compensated blocks); the sampling (double-float phase, sincosf) and the "
+                           "double-float contraction are not counted")
     out.update({"kernel": name, "launch_ms": round(t_sum / len(ks[name]) * 1e3, 3),
                 "launches_per_step": len(ks[name]) / res["steps"], "share_of_step": shares,
                 "traffic": TRAFFIC.get((name, workload)), "peak_source": peaks["source"]})
     return out
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 1200-segment
-# cone-sphere; None until captured.
+# DRAM bytes (read + write) per launch of the fills, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the named workload;
+# None where not captured.
 TRAFFIC = {}     # (kernel, workload) -> bytes
+
+# ncu pipe counters of the fills on the 600-segment cone-sphere (ka = 20), the
+# profiles under profiles/ (the same kernels as the bench runs)
+FILL_COUNTERS = {}
 
 
 def main():
