@@ -503,11 +503,19 @@ def roofline(res, peaks, workload):
 # DRAM bytes (read + write) per launch of the fills, from one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the named workload;
 # None where not captured.
-TRAFFIC = {}     # (kernel, workload) -> bytes
+TRAFFIC = {     # (kernel, workload) -> bytes per launch
+    ("far_fill", "cone_sphere_ka40"): 4.72e9 + 4.66e9,     # Z_far read + written once
+    ("near_fill", "cone_sphere_ka40"): 65.76e9 + 38.90e9,  # per-CTA node scratch
+}
 
 # ncu pipe counters of the fills on the 600-segment cone-sphere (ka = 20), the
 # profiles under profiles/ (the same kernels as the bench runs)
-FILL_COUNTERS = {}
+FILL_COUNTERS = {
+    "far_fill": {"fma_pipe_busy_pct_ncu": 46.9, "issue_active_pct_ncu": 61.9,
+                 "profile": "profiles/far_efie_cone_sphere_ka20.md"},
+    "near_fill": {"fma_pipe_busy_pct_ncu": 47.5, "issue_active_pct_ncu": 37.8,
+                  "profile": "profiles/near_efie_cone_sphere_ka20.md"},
+}
 
 
 def main():
