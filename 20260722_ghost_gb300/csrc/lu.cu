@@ -187,7 +187,7 @@ __global__ void laswp_rhs_kernel(int n, int nrhs, C<R> *__restrict__ B, long lon
 // (column-per-thread layout, conflict-free), so the substitution is a short
 // rolled loop instead of a fully unrolled NB x NB register program whose code
 // would not fit the instruction cache.
-constexpr int TRSM_COLS = 64;        // columns (threads) per CTA
+constexpr int TRSM_COLS = 128;       // columns (threads) per CTA
 template <class R, int NB, bool UPPER>
 __global__ void __launch_bounds__(TRSM_COLS)
 trsm_kernel(int nb, int ncols, const C<R> *__restrict__ T, long long ldt, long long st,
@@ -219,27 +219,34 @@ trsm_kernel(int nb, int ncols, const C<R> *__restrict__ T, long long ldt, long l
     for (int i = 0; i < nb; ++i) xs[i * TRSM_COLS] = act ? Xb[(size_t)i * ldx] : mk<R>(0, 0);
     __syncthreads();
     if (!act) return;
+    // four partial sums per row keep four independent FMA chains (and their
+    // shared-memory loads) in flight
+    const CT z = mk<R>(0, 0);
     if (!UPPER) {
         for (int i = 1; i < nb; ++i) {
-            CT s0 = xs[i * TRSM_COLS], s1 = mk<R>(0, 0);
+            CT s0 = xs[i * TRSM_COLS], s1 = z, s2 = z, s3 = z;
             int j = 0;
-            for (; j + 1 < i; j += 2) {                 // two partial sums
+            for (; j + 3 < i; j += 4) {
                 s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
                 s1 = cfms(Ts[i][j + 1], xs[(j + 1) * TRSM_COLS], s1);
+                s2 = cfms(Ts[i][j + 2], xs[(j + 2) * TRSM_COLS], s2);
+                s3 = cfms(Ts[i][j + 3], xs[(j + 3) * TRSM_COLS], s3);
             }
-            if (j < i) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
-            xs[i * TRSM_COLS] = cadd(s0, s1);
+            for (; j < i; ++j) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+            xs[i * TRSM_COLS] = cadd(cadd(s0, s1), cadd(s2, s3));
         }
     } else {
         for (int i = nb - 1; i >= 0; --i) {
-            CT s0 = xs[i * TRSM_COLS], s1 = mk<R>(0, 0);
+            CT s0 = xs[i * TRSM_COLS], s1 = z, s2 = z, s3 = z;
             int j = i + 1;
-            for (; j + 1 < nb; j += 2) {
+            for (; j + 3 < nb; j += 4) {
                 s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
                 s1 = cfms(Ts[i][j + 1], xs[(j + 1) * TRSM_COLS], s1);
+                s2 = cfms(Ts[i][j + 2], xs[(j + 2) * TRSM_COLS], s2);
+                s3 = cfms(Ts[i][j + 3], xs[(j + 3) * TRSM_COLS], s3);
             }
-            if (j < nb) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
-            xs[i * TRSM_COLS] = cmul(cadd(s0, s1), Dinv[i]);
+            for (; j < nb; ++j) s0 = cfms(Ts[i][j], xs[j * TRSM_COLS], s0);
+            xs[i * TRSM_COLS] = cmul(cadd(cadd(s0, s1), cadd(s2, s3)), Dinv[i]);
         }
     }
     for (int i = 0; i < nb; ++i) Xb[(size_t)i * ldx] = xs[i * TRSM_COLS];
