@@ -379,10 +379,11 @@ class BorGpuProblem:
             X = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
             nat.call("ghost_bor_convert", 1, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(X),
                      nrhs, X.stride(0), st); mark("solve")
-            # refinement: R0 = B - Z X0 once with the split-word kernel (Z in FP64,
-            # X0 the FP32 solution); for each correction D = A^-1 R the next
-            # residual is R - Z D, and since |D| ~ 1e-5 |X| a tensor-core GEMM
-            # on fl32(Z) is accurate enough for that product
+            # refinement: R0 = B - Z X0 once with exact products (bf16 digit
+            # slices on the tensor cores; the split-word SIMT kernel without them),
+            # Z in FP64 and X0 the FP32 solution; for each correction D = A^-1 R
+            # the next residual is R - Z D, and since |D| ~ 1e-5 |X| a tensor-core
+            # GEMM on fl32(Z) is accurate enough for that product
             R32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
             Ac = None
             z_split = 0

@@ -211,6 +211,9 @@ def replica_throughput(units_per_rank: float, seconds: float) -> float:
 # CPU baseline: the oracle port of the reference algorithm on the host cores
 # ---------------------------------------------------------------------------
 
+_CPU_SOLVERS = {}     # workload -> oracle solver with its complete near cache
+
+
 def cpu_baseline(workload: str, cores: int):
     """Time a bounded sample of the reference algorithm (the oracle port) and
     extrapolate to the full sweep: a slice of the far-field sweep, a subset of
@@ -233,8 +236,14 @@ def cpu_baseline(workload: str, cores: int):
     t0 = time.perf_counter()
     s.prepare(M, efie=True, workers=cores, pairs=sub)
     t_near = (time.perf_counter() - t0) * len(pairs) / len(sub)
-    # one |m|: complete near cache is needed by assemble; fill the rest untimed
-    s.prepare(M, efie=True, workers=cores, pairs=[p for p in pairs if p not in set(sub)])
+    # one |m|: the complete near cache is needed by assemble; the rest is filled
+    # untimed once per workload and kept for later calls (the reference arm's
+    # steps), whose far and near samples above are still computed afresh
+    if workload in _CPU_SOLVERS:
+        s = _CPU_SOLVERS[workload]
+    else:
+        s.prepare(M, efie=True, workers=cores, pairs=[p for p in pairs if p not in set(sub)])
+        _CPU_SOLVERS[workload] = s
     am = max(1, M // 2)
     t0 = time.perf_counter()
     for m in (am, -am):
