@@ -8,8 +8,12 @@
 //           with the LAPACK izamax rule |re| + |im|, first maximum wins)
 //   laswp   row interchanges applied to the columns outside the panel
 //   trsm    U12 = L11^-1 A12, one thread per column, L11 in shared memory
-//   gemm    A22 -= L21 U12 (complex rank-NB update, 64 x 64 tiles)
-// The same trsm/gemm kernels run the forward/back substitutions.
+//   update  A22 -= L21 U12 (complex rank-NB update): the tcgen05 3xTF32 GEMM
+//           of tc_gemm.cu when a workspace is given (FP32), else 64 x 64 SIMT
+//           tiles
+// with one step of look-ahead (the next panel overlaps the rest of the update
+// on a side stream).  The same trsm/update kernels run the forward/back
+// substitutions, in 256-row outer blocks on the tensor-core path.
 #include "common.cuh"
 
 namespace gb {
