@@ -1,0 +1,117 @@
+"""Where the FP32 far fill's error comes from (CPU emulation on the oracle).
+
+The far fill of the FP32+IR path samples g = e^{-jkR}/R in FP32 and forms the
+orders G_n = sum_j t_jn g_j with an FP32 copy of the DCT table, summing 8-sample
+FMA blocks folded in with Kahan compensation (csrc/far_fill.cu); everything
+after the transform is double-float.  This test replays that arithmetic on a
+small cone-sphere with NumPy FP32 rounding, assembles and solves every mode in
+FP64 (oracle), and compares the monostatic far field with the all-FP64 sweep.
+It pins the finding that the FP32 rounding of the table, not of the samples or
+of the sums, sets the floor: an FP64 table cuts the error ~3x, an exact
+transform of the FP32 samples ~10x.
+"""
+import importlib
+import math
+
+import numpy as np
+import pytest
+
+from oracle import bor_oracle as O
+
+f32 = np.float32
+
+
+def _modules():
+    geom = importlib.import_module("20260722_ghost_gb300.geometry")
+    bodies = importlib.import_module("20260722_ghost_gb300.bodies")
+    return geom, bodies
+
+
+def kahan_dct(gr, gi, table, h):
+    """8-sample FMA blocks (one FP32 rounding per product-sum), Kahan fold."""
+    shp = gr.shape[:2] + (table.shape[1],)
+    out = []
+    for g in (gr, gi):
+        acc = np.zeros(shp, f32)
+        cmp = np.zeros(shp, f32)
+        for jb in range(0, h + 1, 8):
+            b = np.zeros(shp, f32)
+            for j in range(jb, min(jb + 8, h + 1)):
+                b = (g[..., j:j + 1].astype(np.float64) * table[j][None, None, :].astype(np.float64) + b).astype(f32)
+            y = (b - cmp).astype(f32)
+            t = (acc + y).astype(f32)
+            cmp = ((t - acc).astype(f32) - y).astype(f32)
+            acc = t
+        out.append(acc.astype(np.float64) - cmp)
+    return out[0] + 1j * out[1]
+
+
+class _Emulated(O.OracleSolver):
+    variant = "fp64"
+
+    def build_far(self, m_max, efie=True, mfie=False, workers=1, elem_range=None):
+        geom, _ = _modules()
+        g = self.geo
+        Nn, ne, go = g.Nn, g.ne, g.go
+        nx = O.n_xi_efie(self.k, float(np.max(g.nodes[:, 0])), m_max)
+        h = nx // 2
+        dct, sin2 = geom.dct_tables(nx, m_max + 2, scale=1.0 / (4.0 * math.pi))
+        self.Zp = np.zeros((9, m_max + 2, Nn, Nn), dtype=np.complex128)
+        for e0 in range(0, ne, 4):
+            e1 = min(e0 + 4, ne)
+            rows = slice(e0 * go, e1 * go)
+            rp, zp = g.rho[rows], g.z[rows]
+            d2 = (rp[:, None] - g.rho[None, :]) ** 2 + (zp[:, None] - g.z[None, :]) ** 2
+            a2 = 4.0 * rp[:, None] * g.rho[None, :]
+            # coincident points belong to near pairs, which are zeroed below
+            R = np.maximum(np.sqrt(d2[..., None] + a2[..., None] * sin2), 1e-30)
+            g64 = np.exp(-1j * self.k * R) / R
+            if self.variant == "fp64":
+                Gn = np.einsum("rpj,jn->rpn", g64, dct)
+            else:
+                gr = np.clip(g64.real, -3e38, 3e38).astype(f32)
+                gi = np.clip(g64.imag, -3e38, 3e38).astype(f32)
+                if self.variant == "gpu":           # FP32 samples, FP32 table, Kahan blocks
+                    Gn = kahan_dct(gr, gi, dct.astype(f32), h)
+                elif self.variant == "table64":     # FP32 samples, FP64 table, Kahan blocks
+                    Gn = kahan_dct(gr, gi, dct, h)
+                else:                               # FP32 samples, exact transform
+                    Gn = np.einsum("rpj,jn->rpn", gr.astype(np.float64) + 1j * gi.astype(np.float64), dct)
+            self._zero_near(Gn, e0, e1)
+            for ci, (lx, rx) in enumerate(self._COMBOS):
+                self._contract(Gn, self.lv[lx][:, rows], self.lv[rx], e0, e1 - e0, self.Zp[ci])
+
+
+def _far_field(pts, freq, thetas, M, variant):
+    s = _Emulated(pts, freq)
+    s.variant = variant
+    s.prepare(M, efie=True, workers=4)
+    F = np.zeros((2, len(thetas)), complex)
+    for m in range(-M, M + 1):
+        Z = s.assemble_efie(m, M)
+        mask = s.basis_mask(m)
+        V = np.stack([s.rhs_efie(m, thetas, "VV"), s.rhs_efie(m, thetas, "HH")], axis=1)
+        B = V.transpose(2, 0, 1).reshape(2 * s.geo.Nn, -1)[mask]
+        X = np.linalg.solve(Z[np.ix_(mask, mask)], B)
+        full = np.zeros((2 * s.geo.Nn, X.shape[1]), complex)
+        full[mask] = X
+        xs = full.T.reshape(len(thetas), 2, -1)
+        F[0] += s.farfield(m, xs[:, 0, :], thetas)[0]
+        F[1] += s.farfield(m, xs[:, 1, :], thetas)[1]
+    return F
+
+
+def test_fp32_dct_table_sets_the_far_fill_floor():
+    _, bodies = _modules()
+    pts = bodies.cone_sphere_generatrix(0.5, 15.0, 80)
+    freq = 10.0 * 299792458.0 / (2 * math.pi)
+    thetas = np.arange(0.0, 180.0001, 2.0)
+    M = 8
+    ref = _far_field(pts, freq, thetas, M, "fp64")
+    err = {}
+    for v in ("gpu", "table64", "exact"):
+        F = _far_field(pts, freq, thetas, M, v)
+        err[v] = float(np.max(np.abs(F - ref)) / np.max(np.abs(ref)))
+    assert 1e-9 < err["gpu"] < 1e-7, err               # the FP32 floor (C2 on the GPU: 4.2e-8)
+    assert err["table64"] < err["gpu"] / 2.5, err
+    assert err["exact"] < err["gpu"] / 5.0, err
