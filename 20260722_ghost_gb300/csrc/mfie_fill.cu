@@ -218,7 +218,8 @@ far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
 // ---------------------------------------------------------------------------
 // near pairs |e - f| <= 1 (graded cells, sinh core + Gauss tail) and mass.
 // Persistent grid; per batch of 128 point pairs each thread evaluates its
-// azimuth nodes once (FP64 transcendentals) into a per-CTA scratch, then each
+// azimuth nodes once (FP64 transcendentals; this kernel is FP64 throughout)
+// into a per-CTA scratch, then each
 // chunk of NCM orders projects from it (see near_fill.cu).
 // ---------------------------------------------------------------------------
 constexpr int NTPB = 128;

@@ -83,9 +83,10 @@ int ghost_bor_sample_mfie(int nr, int np_, int nxi,
  * combine the orders into the mode-m blocks, m = 0..m_max, then ADD
  * scale * [[ztt, ztf], [zft, zff]] into Z[m] (rows 0..Nn-1 = J_t tests,
  * Nn..2Nn-1 = J_phi tests).  Z must be zeroed (or hold other terms) first.
- * `prec` selects the precision of the sampling and the DCT; the contraction,
- * the mode combination and the accumulation into Z are FP64 and Z is always
- * complex double.
+ * `prec` selects the precision: GHOST_BOR_F64 = FP64 throughout;
+ * GHOST_BOR_F32 = FP32 sampling (double-float phase) and DCT (Kahan-compensated
+ * blocks), double-float contraction and mode combination, each entry rounded
+ * to FP64 once before it is added.  Z is always complex double.
  *
  *   geo   [11][P] doubles, P = 4 n_elem (Gauss points, element-major):
  *         rho, z, w, T0*w*rho, T1*w*rho, T0*w, T1*w, dRT0*w, dRT1*w, t_rho, t_z
@@ -115,7 +116,7 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
                               const unsigned char *elem_mask, const float *dct32, void *stream);
 
 /* ------------------------------------------------------------------------
- * FP64 near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
+ * FP64-class near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
  * the graded-cell + sinh-core + Gauss-tail quadrature of the reference.
  *   nodes     [Nn][2] (rho, z);  elem [3][n_elem] (length, t_rho, t_z)
  *   pairs     [n_pairs][4] ints: e, f, cell-table offset, cell count
@@ -126,14 +127,16 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
  *             xi = xi0 + u01 (pi - xi0), xi0 = 2 asin(1/4))
  * Output: if band != NULL, ADD scale * block into band[m][blk][Nn][5]
  * (complex double, blk = tt, tf, ft, ff; column offset -2..2); else into the
- * dense complex double Z[m].  `prec` selects the arithmetic of the cos(m xi)
- * projection: GHOST_BOR_F64 = FP64, GHOST_BOR_F32 = double-float (two FP32
- * words, ~48-bit); the azimuth-point transcendentals are FP64 in both.
+ * dense complex double Z[m].  `prec` selects the arithmetic: GHOST_BOR_F64 =
+ * FP64 throughout; GHOST_BOR_F32 = double-float (two FP32 words, ~48-bit) on
+ * the FP32 pipe for the azimuth-node transcendentals, the cos(m xi) projection
+ * and the order GEMM (agrees with the FP64 result to ~1e-13 of the band).
  * work: ghost_bor_near_workspace(n_tail_max) bytes, 256-byte aligned, where
  * n_tail_max >= every n_tail of `tails`; its first int is a status word set to
  * 1 if a pair had a larger n_tail (that pair is then skipped).  Each CTA of the
- * persistent grid keeps the azimuth nodes of its 128 point pairs there, so
- * the FP64 transcendental functions run once per node.
+ * persistent grid keeps the azimuth nodes of its 128 point pairs there (and
+ * the double-float tail rule of its current pair), so the transcendental
+ * functions run once per node.
  * Replaces _near_pair_data + modal_kernels_near + the near loop of
  * assemble_mode (bor_solver.py:270-336, bor_kernels.py:170-257).
  */
