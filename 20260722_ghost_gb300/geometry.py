@@ -30,10 +30,35 @@ GEO_ROWS = 11      # rho, z, w, T0 w rho, T1 w rho, T0 w, T1 w, dRT0 w, dRT1 w, 
 
 @functools.lru_cache(maxsize=None)
 def _leggauss(n: int) -> Tuple[np.ndarray, np.ndarray]:
-    """Gauss-Legendre nodes and weights on [-1, 1], cached: the rule costs an
-    O(n^3) eigenproblem and the near tail orders (up to 1024) repeat across
-    element pairs, bodies and calls."""
-    x, w = np.polynomial.legendre.leggauss(n)
+    """Gauss-Legendre nodes and weights on [-1, 1] (numpy's leggauss rule),
+    cached: the near tail orders (up to 1024) repeat across element pairs,
+    bodies and calls.  numpy finds the nodes as the eigenvalues of the
+    symmetric tridiagonal Legendre companion matrix with a dense O(n^3)
+    solver; the same eigenvalues come from the tridiagonal solver in O(n^2),
+    followed by numpy's own Newton step, weights, symmetrisation and
+    normalisation, which return the same nodes and weights as leggauss."""
+    L = np.polynomial.legendre
+    try:
+        from scipy.linalg import eigvalsh_tridiagonal
+    except ImportError:               # pragma: no cover - scipy is in every image used
+        eigvalsh_tridiagonal = None
+    if n < 64 or eigvalsh_tridiagonal is None:
+        x, w = L.leggauss(n)
+    else:
+        c = np.zeros(n + 1)
+        c[-1] = 1.0
+        m = L.legcompanion(c)
+        x = eigvalsh_tridiagonal(np.diag(m).copy(), np.diag(m, 1).copy())
+        dy = L.legval(x, c)
+        df = L.legval(x, L.legder(c))
+        x -= dy / df
+        fm = L.legval(x, c[1:])
+        fm /= np.abs(fm).max()
+        df /= np.abs(df).max()
+        w = 1.0 / (fm * df)
+        w = (w + w[::-1]) / 2.0
+        x = (x - x[::-1]) / 2.0
+        w *= 2.0 / w.sum()
     x.flags.writeable = False
     w.flags.writeable = False
     return x, w

@@ -143,3 +143,13 @@ def test_element_mass(pkg, oracle):
             Mm[e + ab // 2, e + ab % 2] += em[e, ab]
     ref = oracle.OracleSolver(D["points"], float(D["freq_hz"])).mass()
     assert np.max(np.abs(Mm - ref)) < 1e-14 * np.max(np.abs(ref))
+
+
+def test_gauss_legendre_rule_is_numpys(pkg):
+    """The cached rule (tridiagonal eigensolver, then numpy's own refinement and
+    weights) returns exactly numpy's leggauss nodes and weights."""
+    g = pkg.geometry
+    for n in (1, 4, 48, 63, 64, 65, 100, 257, 512, 777, 1024):
+        x, w = np.polynomial.legendre.leggauss(n)
+        x2, w2 = g._leggauss(n)
+        assert np.array_equal(x, x2) and np.array_equal(w, w2), n
