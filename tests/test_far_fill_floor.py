@@ -8,13 +8,13 @@ small cone-sphere with NumPy FP32 rounding, assembles and solves every mode in
 FP64 (oracle), and compares the monostatic far field with the all-FP64 sweep.
 It pins the finding that the FP32 rounding of the table, not of the samples or
 of the sums, sets the floor: an FP64 table cuts the error ~3x, an exact
-transform of the FP32 samples ~10x.
+transform of the FP32 samples ~10x, and an exact transform on four base-256
+digits of each operand (the split a tensor-core transform would use) as much.
 """
 import importlib
 import math
 
 import numpy as np
-import pytest
 
 from oracle import bor_oracle as O
 
@@ -75,6 +75,16 @@ class _Emulated(O.OracleSolver):
                     Gn = kahan_dct(gr, gi, dct.astype(f32), h)
                 elif self.variant == "table64":     # FP32 samples, FP64 table, Kahan blocks
                     Gn = kahan_dct(gr, gi, dct, h)
+                elif self.variant == "digits4":     # 4 base-256 digits of g / 2^e and t / 2^f
+                    # (the operand split of a tensor-core transform: row scale from
+                    # |g| <= 1/d of the pair, table scale 2^f >= 4 max |t|)
+                    ex = np.frexp(1.0 / np.sqrt(d2))[1][..., None]
+                    sc = np.ldexp(1.0, ex)
+                    q = 2.0 ** 31
+                    gq = (np.rint(gr / sc * q) + 1j * np.rint(gi / sc * q)) * sc / q
+                    fx = np.frexp(1.0 / h)[1]
+                    tq = np.rint(dct / 2.0 ** fx * q) * 2.0 ** fx / q
+                    Gn = np.einsum("rpj,jn->rpn", gq, tq)
                 else:                               # FP32 samples, exact transform
                     Gn = np.einsum("rpj,jn->rpn", gr.astype(np.float64) + 1j * gi.astype(np.float64), dct)
             self._zero_near(Gn, e0, e1)
@@ -109,9 +119,11 @@ def test_fp32_dct_table_sets_the_far_fill_floor():
     M = 8
     ref = _far_field(pts, freq, thetas, M, "fp64")
     err = {}
-    for v in ("gpu", "table64", "exact"):
+    for v in ("gpu", "table64", "exact", "digits4"):
         F = _far_field(pts, freq, thetas, M, v)
         err[v] = float(np.max(np.abs(F - ref)) / np.max(np.abs(ref)))
     assert 1e-9 < err["gpu"] < 1e-7, err               # the FP32 floor (C2 on the GPU: 4.2e-8)
     assert err["table64"] < err["gpu"] / 2.5, err
     assert err["exact"] < err["gpu"] / 5.0, err
+    # four digits per operand keep the exact transform's accuracy
+    assert err["digits4"] < 1.2 * err["exact"], err
