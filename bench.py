@@ -495,6 +495,12 @@ def roofline(res, peaks, workload):
         ctx = FILL_COUNTERS.get(name, {})
         out["fp32_pipe"] = dict({"achieved_tflops": round(ach, 3), "nominal_peak_tflops": round(fp32_peak, 1),
                                  "frac": round(ach / fp32_peak, 4)}, **ctx)
+        prob = res.get("prob")
+        if name == "far_fill" and prob is not None:
+            # the survey's fill unit: Green's-function samples per second
+            # (every far Gauss-point pair at every half-grid azimuth node)
+            samples = float(4 * prob.N) ** 2 * (prob.n_xi // 2 + 1)
+            out["fp32_pipe"]["samples_per_s"] = float(f"{samples * len(ks[name]) / t_sum:.4g}")
         if name == "near_fill":
             out["note"] = ("near fill: 4 flops per azimuth node and order of the cos(m xi) projection; each "
                            "is a double-float multiply-add on the FP32 pipe (~30 FP32 instructions with the "
