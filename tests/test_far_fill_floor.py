@@ -78,7 +78,8 @@ class _Emulated(O.OracleSolver):
                 elif self.variant == "digits4":     # 4 base-256 digits of g / 2^e and t / 2^f
                     # (the operand split of a tensor-core transform: row scale from
                     # |g| <= 1/d of the pair, table scale 2^f >= 4 max |t|)
-                    ex = np.frexp(1.0 / np.sqrt(d2))[1][..., None]
+                    with np.errstate(divide="ignore"):     # near pairs are zeroed below
+                        ex = np.frexp(1.0 / np.sqrt(d2))[1][..., None]
                     sc = np.ldexp(1.0, ex)
                     q = 2.0 ** 31
                     gq = (np.rint(gr / sc * q) + 1j * np.rint(gi / sc * q)) * sc / q
