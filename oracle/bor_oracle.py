@@ -1,15 +1,16 @@
 """CPU oracle for the BoR-MoM monostatic path -- TEST INFRASTRUCTURE ONLY.
 
-A NumPy restatement of the reference's PEC body-of-revolution solver
-(``bor_solver.solve_bor`` with ``formulation`` "efie" / "cfie",
-``table_precision="double"``, ``assembly="streaming"``).  It is the checker
+A NumPy restatement of the reference's body-of-revolution solver for PEC
+and surface-impedance (Leontovich, ``zs``) bodies (``bor_solver.solve_bor``
+with ``formulation`` "efie" / "cfie" / "mfie", ``table_precision="double"``,
+``assembly="streaming"``).  It is the checker
 that the CUDA product is compared against; the product never imports it.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs may
 import, call or time anything under ``oracle/``.
 
-Parity pinned: ``tests/test_oracle_golden.py`` checks this module against
-golden vectors produced by running the reference itself
-(``tests/golden/make_golden.py``).
+Parity pinned: ``tests/test_oracle_golden.py`` and ``tests/test_oracle_ibc.py``
+check this module against golden vectors produced by running the reference
+itself (``tests/golden/make_golden.py``, ``tests/golden/make_ibc_golden.py``).
 
 Every function cites the reference lines it restates (paths relative to the
 reference project root).  The far-field assembly follows the reference's
@@ -289,8 +290,48 @@ def _mfie_bracket_grid(rp, zp, trp, tzp, rq, zq, trq, tzq, k, xi):
             -p * (Ry * n_tq - Wf_tq * nR), -p * (Ry * n_fq - Wf_fq * nR))
 
 
+def _ibc_bracket_grid(rp, zp, trp, tzp, rq, zq, trq, tzq, k, xi):
+    """Four IBC brackets on per-pair xi grids (bor_kernels.py:449-481): the
+    rotated principal-value kernel p(R) [(W_u . n_q)(R . f_v) - (W_u . f_v)
+    (R . n_q)] with the SOURCE normal n_q = (-tz_q, 0, tr_q), test at
+    phi = 0, source at phi' = -xi."""
+    cx, sx = np.cos(xi), np.sin(xi)
+    Rx = rp[:, None] - rq[:, None] * cx
+    Ry = rq[:, None] * sx
+    Rz = (zp - zq)[:, None] * np.ones_like(cx)
+    R = np.maximum(np.sqrt(Rx ** 2 + Ry ** 2 + Rz ** 2), 1e-300)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        p = (1.0 + 1j * k * R) * np.exp(-1j * k * R) / (4.0 * np.pi * R ** 3)
+        Wt_nq = -(trp * tzq)[:, None] * cx + (tzp * trq)[:, None]
+        Wf_nq = tzq[:, None] * sx
+        D = rp[:, None] * cx - rq[:, None]
+        R_tq = trq[:, None] * D + tzq[:, None] * Rz
+        R_fq = rp[:, None] * sx
+        R_nq = -tzq[:, None] * D + trq[:, None] * Rz
+        Wt_tq = (trp * trq)[:, None] * cx + (tzp * tzq)[:, None]
+        Wt_fq = trp[:, None] * sx
+        Wf_tq = -trq[:, None] * sx
+        Wf_fq = cx
+        return (p * (Wt_nq * R_tq - Wt_tq * R_nq), p * (Wt_nq * R_fq - Wt_fq * R_nq),
+                p * (Wf_nq * R_tq - Wf_tq * R_nq), p * (Wf_nq * R_fq - Wf_fq * R_nq))
+
+
 def near_mfie(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m_max, order=48):
     """Near MFIE modal brackets for m = -m_max..m_max (bor_kernels.py:360-431)."""
+    return _near_brackets(_mfie_bracket_grid, rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q,
+                          k, m_max, order)
+
+
+def near_ibc(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m_max, order=48):
+    """Near IBC modal brackets for m = -m_max..m_max (bor_kernels.py:509-560):
+    the MFIE near grid and +-xi projection applied to the IBC brackets."""
+    return _near_brackets(_ibc_bracket_grid, rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q,
+                          k, m_max, order)
+
+
+def _near_brackets(grid_fn, rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m_max, order):
+    """Sinh-graded core + Gauss tail on xi in (0, pi], brackets at +-xi,
+    projected on e^{-j m xi} (bor_kernels.py:334-357, 360-431)."""
     rho_p = np.atleast_1d(np.asarray(rho_p, float))
     rho_q = np.atleast_1d(np.asarray(rho_q, float))
     z_p = np.atleast_1d(np.asarray(z_p, float))
@@ -309,8 +350,8 @@ def near_mfie(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m_max, order=48
     xi_pos = np.concatenate([xi_c, xi_t], axis=1)
     w_pos = np.concatenate([w_c, w_t], axis=1)
     m = np.arange(-m_max, m_max + 1)
-    Fp = _mfie_bracket_grid(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, xi_pos)
-    Fm = _mfie_bracket_grid(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, -xi_pos)
+    Fp = grid_fn(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, xi_pos)
+    Fm = grid_fn(rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, -xi_pos)
     arg = xi_pos[:, :, None] * m[None, None, :]
     cm, sm = np.cos(arg), np.sin(arg)
     outs = []
@@ -350,6 +391,7 @@ class OracleSolver:
         }
         self.Zp = None      # EFIE primitives [9, M+2, Nn, Nn]
         self.Kb = None      # MFIE brackets [4, 2M+1, Nn, Nn]
+        self.Bb = None      # IBC brackets, Z_s on the source side [4, 2M+1, Nn, Nn]
         self._near: Dict = {}
         self._lock = threading.Lock()
 
@@ -399,6 +441,17 @@ class OracleSolver:
                                np.broadcast_to(xi, (rp.size, n_xi)))
         return tuple(f.reshape(nr, g.P, n_xi) for f in F)
 
+    def _sample_ibc(self, rows: slice, n_xi: int):
+        """IBC brackets on the uniform xi grid (bor_streaming.py:296-317)."""
+        g = self.geo
+        xi = 2.0 * np.pi * np.arange(n_xi) / n_xi - np.pi
+        nr = rows.stop - rows.start
+        one = np.ones((nr, g.P))
+        a = [(v[rows][:, None] * one).ravel() for v in (g.rho, g.z, g.ptr, g.ptz)]
+        b = [(v[None, :] * one).ravel() for v in (g.rho, g.z, g.ptr, g.ptz)]
+        F = _ibc_bracket_grid(*a, *b, self.k, np.broadcast_to(xi, (a[0].size, n_xi)))
+        return tuple(f.reshape(nr, g.P, n_xi) for f in F)
+
     def _zero_near(self, K, e0, e1):
         """bor_streaming.py:343-349."""
         go, ne = self.geo.go, self.geo.ne
@@ -425,10 +478,13 @@ class OracleSolver:
         return max(1, rows // g.go)
 
     def build_far(self, m_max: int, efie: bool = True, mfie: bool = False,
-                  workers: int = 1, elem_range: Optional[Tuple[int, int]] = None):
+                  workers: int = 1, elem_range: Optional[Tuple[int, int]] = None,
+                  ibc_zs_pt: Optional[np.ndarray] = None):
         """Far blocks for all orders in one sweep (bor_streaming.py:220-268).
         elem_range restricts the sweep to a slice of test elements (used only
-        to time a bounded sample of the build)."""
+        to time a bounded sample of the build).  ibc_zs_pt (Z_s per Gauss
+        point) adds the IBC bracket blocks with Z_s in the source weights
+        (bor_streaming.py:153-155, 255-258)."""
         g = self.geo
         Nn, ne, go = g.Nn, g.ne, g.go
         rho_max = float(np.max(g.nodes[:, 0]))
@@ -443,7 +499,13 @@ class OracleSolver:
             self.Zp = np.zeros((9, m_max + 2, Nn, Nn), dtype=np.complex128)
         if mfie:
             self.Kb = np.zeros((4, 2 * m_max + 1, Nn, Nn), dtype=np.complex128)
-        te = self._tile_elems(max(nx_e, nx_b if mfie else 0), 6 if mfie else 2, workers)
+        ibc = ibc_zs_pt is not None
+        if ibc:
+            self.Bb = np.zeros((4, 2 * m_max + 1, Nn, Nn), dtype=np.complex128)
+            wz = g.w * g.rho * np.asarray(ibc_zs_pt, dtype=complex)
+            rv_ibc = np.stack([g.T0 * wz, g.T1 * wz])
+        brk = mfie or ibc
+        te = self._tile_elems(max(nx_e, nx_b if brk else 0), 6 if brk else 2, workers)
         lo, hi = (0, ne) if elem_range is None else elem_range
 
         def tile(e0):
@@ -463,6 +525,12 @@ class OracleSolver:
                     Km = spec[..., bins] * (2.0 * np.pi * ph_b)
                     self._zero_near(Km, e0, e1)
                     self._contract(Km, self.lv["1"][:, rows], self.lv["1"], e0, re, self.Kb[uv])
+            if ibc:
+                for uv, F in enumerate(self._sample_ibc(rows, nx_b)):
+                    spec = np.fft.fft(F, axis=-1)
+                    Km = spec[..., bins] * (2.0 * np.pi * ph_b)
+                    self._zero_near(Km, e0, e1)
+                    self._contract(Km, self.lv["1"][:, rows], rv_ibc, e0, re, self.Bb[uv])
 
         starts = list(range(lo, hi, te))
         if workers <= 1:
@@ -520,17 +588,36 @@ class OracleSolver:
         self._near[key] = data
         return data
 
+    def near_ibc_data(self, e: int, f: int, m_max: int):
+        """bor_solver.py:481-497."""
+        key = ("ibc", m_max, e, f)
+        if key in self._near:
+            return self._near[key]
+        g = self.geo
+        s, sp_, w = cell_points(near_kind(e, f))
+        rp, zp, T0p, T1p, _, _, Lp = g.points_on_element(e, s)
+        rq, zq, T0q, T1q, _, _, Lq = g.points_on_element(f, sp_)
+        Kn = near_ibc(rp, zp, np.full_like(rp, g.trho[e]), np.full_like(rp, g.tz[e]),
+                      rq, zq, np.full_like(rq, g.trho[f]), np.full_like(rq, g.tz[f]),
+                      self.k, m_max)
+        data = (w * Lp * Lq, rp, np.vstack([T0p, T1p]), rq, np.vstack([T0q, T1q]), Kn)
+        self._near[key] = data
+        return data
+
     def prepare(self, m_max: int, efie=True, mfie=False, workers=1,
-                pairs: Optional[List[Tuple[int, int]]] = None):
+                pairs: Optional[List[Tuple[int, int]]] = None,
+                ibc_zs_pt: Optional[np.ndarray] = None):
         """Far sweep + near caches (bor_solver.py:578-608)."""
         if pairs is None:
-            self.build_far(m_max, efie=efie, mfie=mfie, workers=workers)
+            self.build_far(m_max, efie=efie, mfie=mfie, workers=workers, ibc_zs_pt=ibc_zs_pt)
             pairs = self.near_pairs()
         jobs = []
         if efie:
             jobs += [(self.near_efie_data, p) for p in pairs]
         if mfie:
             jobs += [(self.near_mfie_data, p) for p in pairs]
+        if ibc_zs_pt is not None:
+            jobs += [(self.near_ibc_data, p) for p in pairs]
         if workers <= 1:
             for fn, (e, f) in jobs:
                 fn(e, f, m_max)
@@ -567,10 +654,31 @@ class OracleSolver:
         C = 1j * k * self.eta * 2.0 * np.pi
         return C * np.block([[ztt, ztf], [zft, zff]])
 
-    def mass(self) -> np.ndarray:
-        """bor_solver.py:389-397."""
+    def mass(self, weight: Optional[np.ndarray] = None) -> np.ndarray:
+        """bor_solver.py:389-397 (weight: per Gauss point, e.g. Z_s)."""
         g = self.geo
-        return 2.0 * np.pi * (g.BT * (g.w * g.rho)[None, :]) @ g.BT.T
+        wgt = g.w * g.rho if weight is None else g.w * g.rho * np.asarray(weight)
+        return 2.0 * np.pi * (g.BT * wgt[None, :]) @ g.BT.T
+
+    def assemble_ibc_extra(self, m: int, m_max: int, zs_pt: np.ndarray,
+                           zs_elem: np.ndarray) -> np.ndarray:
+        """IBC-EFIE terms from eliminating M = -Z_s n x J (bor_solver.py:
+        499-552): (1/2) <W, Z_s J> + the rotated principal-value brackets
+        with Z_s at the source; the far part comes from build_far(ibc_zs_pt),
+        near pairs are weighted by the source element's Z_s."""
+        mi = m + m_max
+        blocks = [self.Bb[uv, mi].copy() for uv in range(4)]
+        for (e, f) in self.near_pairs():
+            if abs(zs_elem[f]) == 0.0:
+                continue
+            w, rp, Tp, rq, Tq, Kn = self.near_ibc_data(e, f, m_max)
+            rr = rp * rq * w * zs_elem[f]
+            for uv in range(4):
+                blocks[uv][e:e + 2, f:f + 2] += 2.0 * np.pi * np.einsum(
+                    "ip,p,jp->ij", Tp, rr * Kn[uv][:, mi], Tq)
+        Mz = self.mass(zs_pt)
+        ktt, ktf, kft, kff = blocks
+        return np.block([[0.5 * Mz + ktt, ktf], [kft, 0.5 * Mz + kff]])
 
     def assemble_mfie(self, m: int, m_max: int) -> np.ndarray:
         """Z_MFIE = M/2 - K (bor_solver.py:399-435) on streamed brackets."""
@@ -641,19 +749,34 @@ class OracleSolver:
         c = g.w * g.rho * P
         return np.concatenate([(c * et) @ g.BT.T, (c * ef) @ g.BT.T], axis=1)
 
-    def farfield(self, m: int, sols: np.ndarray, thetas_deg) -> Tuple[np.ndarray, np.ndarray]:
-        """farfield_mode (bor_solver.py:659-708, PEC) for solution rows
-        sols [n_theta, 2Nn] at the matching angles: (F_theta, F_phi)."""
+    def farfield(self, m: int, sols: np.ndarray, thetas_deg,
+                 zs_pt: Optional[np.ndarray] = None) -> Tuple[np.ndarray, np.ndarray]:
+        """farfield_mode (bor_solver.py:659-708) for solution rows
+        sols [n_theta, 2Nn] at the matching angles: (F_theta, F_phi).  With
+        zs_pt the eliminated magnetic current M_t = Z_s J_phi,
+        M_phi = -Z_s J_t radiates too (bor_solver.py:697-707)."""
         g = self.geo
         Nn = g.Nn
         st, ct, P, Icos, Isin, I1 = self._bessel_parts(m, np.atleast_1d(thetas_deg), -1)
         Jt = sols[:, :Nn] @ g.BT
         Jf = sols[:, Nn:] @ g.BT
         common = g.w * g.rho * P
-        pth = np.sum(common * (Jt * (ct * g.ptr * Icos - st * g.ptz * I1) + Jf * (-ct * Isin)), axis=1)
-        pph = np.sum(common * (Jt * g.ptr * Isin + Jf * Icos), axis=1)
+
+        def proj_theta(Xt, Xf):
+            return np.sum(common * (Xt * (ct * g.ptr * Icos - st * g.ptz * I1) + Xf * (-ct * Isin)),
+                          axis=1)
+
+        def proj_phi(Xt, Xf):
+            return np.sum(common * (Xt * g.ptr * Isin + Xf * Icos), axis=1)
+
         pref = -1j * self.k * ETA0 / (4.0 * math.pi)
-        return pref * pth, pref * pph
+        fth, fph = pref * proj_theta(Jt, Jf), pref * proj_phi(Jt, Jf)
+        if zs_pt is not None:
+            Mt, Mf = zs_pt * Jf, -zs_pt * Jt
+            pm = 1j * self.k / (4.0 * math.pi)
+            fth = fth - pm * proj_phi(Mt, Mf)
+            fph = fph + pm * proj_theta(Mt, Mf)
+        return fth, fph
 
 
 def default_n_modes(points, freq_hz: float, thetas_deg) -> int:
@@ -668,9 +791,11 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
               cfie_alpha: float = 0.5, n_modes: Optional[int] = None,
               mode_tol: float = 1e-6, gauss_order: int = 4, workers: int = 1,
               keep_per_mode: bool = False, modes_subset=None,
-              timings: Optional[Dict[str, float]] = None) -> Dict:
-    """Monostatic PEC RCS (bor_solver.py:820-1004 with table_precision
+              timings: Optional[Dict[str, float]] = None, zs=None) -> Dict:
+    """Monostatic RCS (bor_solver.py:820-1004 with table_precision
     "double", assembly "streaming") and the mode loop (bor_solver.py:711-801).
+    zs: None (PEC), a complex scalar or one value per element: the IBC-EFIE
+    (bor_solver.py:850-864, 929-934, 947-949); the CFIE with Z_s raises.
 
     modes_subset (tuple of |m|) solves only those |m| -- used to time a bounded
     sample; the result then holds partial sums."""
@@ -683,8 +808,24 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
     alpha = float(cfie_alpha) if form == "cfie" else (1.0 if form == "efie" else 0.0)
     sol = OracleSolver(points, freq_hz, gauss_order)
     Nn = sol.geo.Nn
+    zs_pt = zs_elem = None
+    if zs is not None:
+        za = np.asarray(zs, dtype=complex)
+        if za.ndim == 0:
+            zs_elem = np.full(sol.geo.ne, complex(za))
+        elif len(za) != sol.geo.ne:
+            raise ValueError("zs array must have one entry per generatrix element.")
+        else:
+            zs_elem = za.copy()
+        zs_pt = zs_elem[sol.geo.elem]
+        if np.all(np.abs(zs_pt) == 0.0):
+            zs_pt = None
+        elif form == "cfie":
+            raise ValueError("CFIE with surface impedance is not supported; use 'efie'.")
+    ibc = zs_pt is not None and alpha > 0.0
     t0 = time.perf_counter()
-    sol.prepare(m_max, efie=alpha > 0.0, mfie=alpha < 1.0, workers=workers)
+    sol.prepare(m_max, efie=alpha > 0.0, mfie=alpha < 1.0, workers=workers,
+                ibc_zs_pt=zs_pt if ibc else None)
     t1 = time.perf_counter()
     pols = ("VV", "HH")
     F = np.zeros((2, len(thetas)), dtype=np.complex128)
@@ -697,6 +838,8 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
             Z = np.zeros((2 * Nn, 2 * Nn), dtype=np.complex128)
             if alpha > 0.0:
                 Z += alpha * sol.assemble_efie(m, m_max)
+                if ibc:
+                    Z += alpha * sol.assemble_ibc_extra(m, m_max, zs_pt, zs_elem)
             if alpha < 1.0:
                 Z += (1.0 - alpha) * ETA0 * sol.assemble_mfie(m, m_max)
             mask = sol.basis_mask(m)
@@ -719,8 +862,8 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
             full = np.zeros((2 * Nn, X.shape[1]), dtype=np.complex128)
             full[mask] = X
             xs = full.T.reshape(len(thetas), 2, 2 * Nn)
-            fth, _ = sol.farfield(m, xs[:, 0, :], thetas)
-            _, fph = sol.farfield(m, xs[:, 1, :], thetas)
+            fth, _ = sol.farfield(m, xs[:, 0, :], thetas, zs_pt=zs_pt)
+            _, fph = sol.farfield(m, xs[:, 1, :], thetas, zs_pt=zs_pt)
             dF[0] += fth
             dF[1] += fph
             if keep_per_mode:

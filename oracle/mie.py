@@ -1,8 +1,9 @@
 """Mie-series backscatter of a PEC sphere -- TEST INFRASTRUCTURE ONLY.
 
 Restates the reference's analytic oracle (mie_sphere.py:42-77 Riccati-Bessel
-functions, :74-77 Wiscombe truncation, :96-101 PEC coefficients, :178-184
-backscatter sum, :231-235 sigma_pec_sphere), e^{+jwt} convention.
+functions, :74-77 Wiscombe truncation, :96-101 PEC coefficients, :104-121
+Leontovich impedance coefficients, :178-184 backscatter sum, :231-242
+sigma_pec_sphere / sigma_impedance_sphere), e^{+jwt} convention.
 """
 
 import math
@@ -31,16 +32,34 @@ def _zeta(nmax, x):
     return x * yn, x * ym1 - n * yn
 
 
-def sigma_pec_sphere(radius_m: float, freq_hz: float) -> float:
-    k = 2.0 * math.pi * freq_hz / C0
-    x = k * radius_m
+ETA0 = 376.730313668
+
+
+def _sphere_coefficients(x: float, g: complex):
+    """Mie coefficients (A_n, B_n) of a sphere of size x whose surface obeys
+    E_tan = Z_s n x H with g = j Z_s / eta0 (g = 0: PEC).  TM:
+    dpsi + A dxi = g (psi + A xi); TE: psi + B xi = -g (dpsi + B dxi), the
+    relative sign that gives zero backscatter at Z_s = eta0 (Weston)."""
     nmax = max(6, int(math.ceil(x + 4.05 * x ** (1.0 / 3.0))) + 12)
     psi, dpsi = _psi(nmax, x)
     zeta, dzeta = _zeta(nmax, x)
     xi, dxi = psi - 1j * zeta, dpsi - 1j * dzeta
-    a = -dpsi / dxi
-    b = -psi / xi
-    n = np.arange(1, nmax + 1)
+    return -(dpsi - g * psi) / (dxi - g * xi), -(psi + g * dpsi) / (xi + g * dxi)
+
+
+def _backscatter(k: float, a: np.ndarray, b: np.ndarray) -> float:
+    n = np.arange(1, len(a))
     s = np.sum(((-1.0) ** n) * (2 * n + 1) * (a[1:] - b[1:]))
     lam = 2.0 * math.pi / k
     return float((lam ** 2 / (4.0 * math.pi)) * abs(s) ** 2)
+
+
+def sigma_pec_sphere(radius_m: float, freq_hz: float) -> float:
+    k = 2.0 * math.pi * freq_hz / C0
+    return _backscatter(k, *_sphere_coefficients(k * radius_m, 0.0))
+
+
+def sigma_impedance_sphere(radius_m: float, freq_hz: float, zs_ohm: complex) -> float:
+    """Backscatter of a Leontovich (surface-impedance) sphere."""
+    k = 2.0 * math.pi * freq_hz / C0
+    return _backscatter(k, *_sphere_coefficients(k * radius_m, 1j * complex(zs_ohm) / ETA0))

@@ -49,7 +49,8 @@ def kahan_dct(gr, gi, table, h):
 class _Emulated(O.OracleSolver):
     variant = "fp64"
 
-    def build_far(self, m_max, efie=True, mfie=False, workers=1, elem_range=None):
+    def build_far(self, m_max, efie=True, mfie=False, workers=1, elem_range=None,
+                  ibc_zs_pt=None):
         geom, _ = _modules()
         g = self.geo
         Nn, ne, go = g.Nn, g.ne, g.go

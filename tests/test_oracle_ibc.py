@@ -1,0 +1,98 @@
+"""The oracle's surface-impedance (IBC-EFIE) restatement against the reference.
+
+Pinned to tests/golden/ibc_conesphere_n40.npz, made by running the reference
+(tests/golden/make_ibc_golden.py): the per-mode IBC operator additions, full
+solves with a tapered and a scalar Z_s, and the impedance-sphere Mie series.
+Also checks the algebra a GPU fill of the IBC brackets relies on: the four
+rotated principal-value brackets are p(R) times {1, sin^2(xi/2), sin(xi)}
+with per-pair coefficients -- the same three azimuth transforms of p as the
+MFIE brackets, so only the coefficients and the (complex, per source element)
+Z_s weight differ.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+
+@pytest.fixture(scope="module")
+def D():
+    return load_golden("ibc_conesphere_n40")
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b)))
+
+
+def test_ibc_operator_matches_reference(oracle, D):
+    s = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    zs = D["zs_taper"]
+    zs_pt = zs[s.geo.elem]
+    m_max = int(D["m_max"])
+    s.prepare(m_max, efie=False, mfie=False, workers=4, ibc_zs_pt=zs_pt)
+    for m in D["modes"]:
+        assert _rel(s.assemble_ibc_extra(int(m), m_max, zs_pt, zs), D[f"Zi_{m}"]) < 1e-12, m
+
+
+@pytest.mark.parametrize("tag", ["taper", "scalar"])
+def test_ibc_solve_matches_reference(oracle, D, tag):
+    zs = D["zs_taper"] if tag == "taper" else 120.0 - 80.0j
+    r = oracle.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], formulation="efie",
+                         zs=zs, n_modes=int(D["m_max"]), mode_tol=0.0, workers=4)
+    assert _rel(r["amp_vv"], D[f"amp_vv_{tag}"]) < 1e-10
+    assert _rel(r["amp_hh"], D[f"amp_hh_{tag}"]) < 1e-10
+
+
+def test_impedance_mie_matches_reference(D):
+    from oracle import mie
+    for (a, f, zr, zi), want in zip(D["mie_cases"], D["mie_sigma"]):
+        got = mie.sigma_impedance_sphere(a, f, complex(zr, zi))
+        assert abs(got - want) <= 1e-14 * max(abs(want), 1e-300)
+    # Weston: a Z_s = eta0 sphere has no backscatter; Z_s = 0 is the PEC sphere
+    assert mie.sigma_impedance_sphere(1.0, 477.1e6, mie.ETA0) == 0.0
+    assert mie.sigma_impedance_sphere(1.0, 477.1e6, 0.0) == mie.sigma_pec_sphere(1.0, 477.1e6)
+
+
+def test_ibc_input_errors(oracle, D):
+    with pytest.raises(ValueError):
+        oracle.solve_bor(D["points"], float(D["freq_hz"]), [0.0], formulation="cfie", zs=50.0,
+                         n_modes=2)
+    with pytest.raises(ValueError):
+        oracle.solve_bor(D["points"], float(D["freq_hz"]), [0.0], zs=np.ones(3), n_modes=2)
+
+
+def test_ibc_brackets_reduce_to_three_transforms(oracle):
+    """B_tt = p (-N0 - 2 s2 (t_z rho - t_rho dz)),  B_ff = p (c0 + 2 s2 (t'_z rho' + t'_rho dz)),
+    B_tf = p sin(xi) (t_z t'_rho rho - t_rho t'_z rho' - t_rho t'_rho dz),  B_ft = p sin(xi) dz,
+    with d = (dr, dz) = test - source, N0 = t_rho dz - t_z dr, c0 = dr t'_z - dz t'_rho,
+    s2 = sin^2(xi/2); t = test tangent, t' = source tangent (unit)."""
+    rng = np.random.default_rng(7)
+    n = 400
+    rp, rq = rng.uniform(0.05, 1.0, n), rng.uniform(0.05, 1.0, n)
+    zp, zq = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    a, b = rng.uniform(0, 2 * math.pi, n), rng.uniform(0, 2 * math.pi, n)
+    trp, tzp, trq, tzq = np.cos(a), np.sin(a), np.cos(b), np.sin(b)
+    # near pairs too: sources a few 1e-3 away from the test point
+    rq[:100] = rp[:100] + rng.uniform(-3e-3, 3e-3, 100)
+    zq[:100] = zp[:100] + rng.uniform(-3e-3, 3e-3, 100)
+    xi = rng.uniform(-math.pi, math.pi, (n, 64))
+    xi[:100, :8] = rng.uniform(-1e-2, 1e-2, (100, 8))
+    k = 30.0
+    B = oracle._ibc_bracket_grid(rp, zp, trp, tzp, rq, zq, trq, tzq, k, xi)
+    dr, dz = (rp - rq)[:, None], (zp - zq)[:, None]
+    R = np.sqrt(dr ** 2 + dz ** 2 + 4 * (rp * rq)[:, None] * np.sin(xi / 2) ** 2)
+    p = (1 + 1j * k * R) * np.exp(-1j * k * R) / (4 * np.pi * R ** 3)
+    s2, sx = np.sin(xi / 2) ** 2, np.sin(xi)
+    tr_p, tz_p, tr_q, tz_q = (v[:, None] for v in (trp, tzp, trq, tzq))
+    N0 = tr_p * dz - tz_p * dr
+    c0 = dr * tz_q - dz * tr_q
+    red = (p * (-N0 - 2 * s2 * (tz_p * rp[:, None] - tr_p * dz)),
+           p * sx * (tz_p * tr_q * rp[:, None] - tr_p * tz_q * rq[:, None] - tr_p * tr_q * dz),
+           p * sx * dz,
+           p * (c0 + 2 * s2 * (tz_q * rq[:, None] + tr_q * dz)))
+    # bound: |p| times the size of the largest product term (rho ~ 1)
+    scale = np.abs(p) * (1.0 + np.abs(dz) + rp[:, None] + rq[:, None])
+    for got, want in zip(red, B):
+        assert np.max(np.abs(got - want) / scale) < 1e-13
