@@ -173,8 +173,9 @@ class BorPecSolver:
 
     Operators are built on the GPU for all modes 0..m_max at once (FP64) and
     returned per mode as complex128 NumPy arrays for compatibility; mode -m is
-    D Z(m) D for both operators.  The EFIE and MFIE operators and the
-    plane-wave excitations / far field are provided (no IBC / PMCHWT).
+    D Z(m) D for both operators.  The EFIE and MFIE operators, the mass
+    blocks, the plane-wave excitations (E and H) and the PEC far field are
+    provided; the IBC / PMCHWT operators raise NotImplementedError.
     """
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,
@@ -256,6 +257,15 @@ class BorPecSolver:
     def basis_mask(self, m: int) -> np.ndarray:
         return _basis_mask(self.gen, m)
 
+    def mass_blocks(self, weight=None) -> np.ndarray:
+        """2 pi B_T diag(w rho weight) B_T^T, node-based [Nn, Nn]
+        (bor_solver.py:389-397); ``weight`` per Gauss point (default 1, e.g.
+        Z_s for an impedance surface).  Geometry only, like ``B_T``."""
+        wgt = self.g.w * self.g.rho
+        if weight is not None:
+            wgt = wgt * np.asarray(weight)
+        return 2.0 * np.pi * (self.B_T * wgt[None, :]) @ self.B_T.T
+
     # -- excitation / far field (GPU kernels, one angle) --------------------
     def _excitation(self, m: int, theta_inc_deg: float, coef_e: float, coef_h: float):
         import torch
@@ -282,6 +292,14 @@ class BorPecSolver:
         (bor_solver.py:437-461)."""
         V = self._excitation(m, theta_inc_deg, 0.0, 1.0)
         return V[:, 0 if pol.upper() in ("VV", "THETA", "TM") else 1].copy()
+
+    def rhs_h_mode(self, m: int, theta_inc_deg: float, pol: str) -> np.ndarray:
+        """Unrotated <W, H_inc> (bor_solver.py:647-657): the incident H of one
+        polarisation is the E of the other over eta0 (VV: H = -y P / eta0,
+        HH: H = e_theta P / eta0), so it is rhs_mode with the pair swapped."""
+        if pol.upper() in ("VV", "THETA", "TM"):
+            return -self.rhs_mode(m, theta_inc_deg, "HH") / ETA0
+        return self.rhs_mode(m, theta_inc_deg, "VV") / ETA0
 
     def farfield_mode(self, m: int, sol: np.ndarray, theta_s_deg: float,
                       zs_pt: Optional[np.ndarray] = None,

@@ -104,3 +104,17 @@ def test_adjoint_identity_on_oracle(pkg, oracle):
     assert np.max(np.abs(y - y_exact)) < 1e-7 * np.max(np.abs(y_exact))
     adj = -c * (np.sum(Dx * dV, axis=0) + np.sum(y * (dV - dZ @ x0), axis=0))
     assert np.max(np.abs(adj - fd)) < 1e-6 * np.max(np.abs(fd))
+
+
+def test_mass_blocks_match_oracle(pkg, oracle):
+    """BorPecSolver.mass_blocks (geometry only) = the oracle's mass term, plain
+    and weighted per Gauss point (the Z_s mass of an impedance surface)."""
+    import importlib
+    bs = importlib.import_module("20260722_ghost_gb300.bor_solver")
+    D = load_golden("conesphere_n40")
+    s = bs.BorPecSolver(D["points"], float(D["freq_hz"]))
+    o = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    w = np.linspace(50.0, 300.0, s.P) - 20.0j
+    for weight in (None, w):
+        got, want = s.mass_blocks(weight), o.mass(weight)
+        assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want))

@@ -54,3 +54,20 @@ def test_snapshot_sweep_and_grid_match_reference(pkg, e2e, precision, tol):
     scale = max(np.max(np.abs(ref[f"e2e_{ch}"])) for ch in ("VV", "HH"))
     for ch in ("VV", "HH", "VH"):
         assert np.max(np.abs(g["amp"][ch] - ref[f"e2e_{ch}"])) < tol * scale
+
+
+def test_rhs_h_mode_is_the_swapped_excitation(pkg):
+    """BorPecSolver.rhs_h_mode (<W, H_inc>, bor_solver.py:647-657) against the
+    reference's E excitations with the polarisations swapped, over eta0."""
+    from conftest import load_golden
+    bs = importlib.import_module("20260722_ghost_gb300.bor_solver")
+    G = load_golden("sphere_n24")
+    s = bs.BorPecSolver(G["points"], float(G["freq_hz"]))
+    eta0 = 376.730313668
+    for m in G["modes"]:
+        m = int(m)
+        for it, th in enumerate(G["thetas"][::3]):
+            for pol, other, sign in (("VV", "HH", -1.0), ("HH", "VV", 1.0)):
+                want = sign * G[f"Ve_{m}_{other}"][3 * it] / eta0
+                got = s.rhs_h_mode(m, th, pol)
+                assert np.max(np.abs(got - want)) <= 1e-12 * max(np.max(np.abs(want)), 1e-300)
