@@ -7,7 +7,8 @@ Also checks the algebra a GPU fill of the IBC brackets relies on: the four
 rotated principal-value brackets are p(R) times {1, sin^2(xi/2), sin(xi)}
 with per-pair coefficients -- the same three azimuth transforms of p as the
 MFIE brackets, so only the coefficients and the (complex, per source element)
-Z_s weight differ.
+Z_s weight differ -- and the far field of J and the eliminated magnetic
+current by reciprocity with a modified excitation.
 """
 import math
 
@@ -96,3 +97,38 @@ def test_ibc_brackets_reduce_to_three_transforms(oracle):
     scale = np.abs(p) * (1.0 + np.abs(dz) + rp[:, None] + rq[:, None])
     for got, want in zip(red, B):
         assert np.max(np.abs(got - want) / scale) < 1e-13
+
+
+def test_ibc_far_field_by_reciprocity(oracle):
+    """The far field of J plus the eliminated M = -Z_s n x J equals the PEC
+    reciprocity form with the excitation V_E - V_H^Zs:
+    F_theta = c (D (V_E,VV - V_H,VV^Zs))^T x, F_phi = -c (D (V_E,HH - V_H,HH^Zs))^T x,
+    c = -j k eta0 / 4 pi, D = diag(I, -I), V_H^Zs the rotated n x H_inc
+    excitation with Gauss weights w rho Z_s -- so a GPU far field needs only
+    those excitation vectors, not a second projection."""
+    import importlib
+    bodies = importlib.import_module("20260722_ghost_gb300.bodies")
+    s = oracle.OracleSolver(bodies.cone_sphere_generatrix(0.3, 15.0, 24), 20.0 * oracle.C0 / (2 * math.pi))
+    g = s.geo
+    rng = np.random.default_rng(3)
+    zs_pt = (rng.uniform(20, 300, g.ne) + 1j * rng.uniform(-100, 100, g.ne))[g.elem]
+    th = np.array([10.0, 47.0, 90.0, 133.0])
+    Dg = np.concatenate([np.ones(g.Nn), -np.ones(g.Nn)])
+    c = -1j * s.k * oracle.ETA0 / (4 * math.pi)
+
+    def v_h(m, pol):                          # rhs_mfie with Gauss weights w rho Z_s
+        st, ct, P, Ic, Is, I1 = s._bessel_parts(m, th, 1)
+        if pol == "VV":
+            et, ef = Ic, -(g.ptr * Is)
+        else:
+            et, ef = ct * Is, ct * g.ptr * Ic - st * g.ptz * I1
+        w = g.w * g.rho * P * zs_pt / oracle.ETA0
+        return np.concatenate([(w * et) @ g.BT.T, (w * ef) @ g.BT.T], axis=1)
+
+    for m in (0, 1, -2, 3):
+        x = rng.standard_normal((len(th), 2 * g.Nn)) + 1j * rng.standard_normal((len(th), 2 * g.Nn))
+        fth, fph = s.farfield(m, x, th, zs_pt=zs_pt)
+        rth = c * np.sum(Dg * (s.rhs_efie(m, th, "VV") - v_h(m, "VV")) * x, axis=1)
+        rph = -c * np.sum(Dg * (s.rhs_efie(m, th, "HH") - v_h(m, "HH")) * x, axis=1)
+        assert np.max(np.abs(rth - fth)) <= 1e-13 * np.max(np.abs(fth))
+        assert np.max(np.abs(rph - fph)) <= 1e-13 * np.max(np.abs(fph))
