@@ -118,3 +118,21 @@ def test_mass_blocks_match_oracle(pkg, oracle):
     for weight in (None, w):
         got, want = s.mass_blocks(weight), o.mass(weight)
         assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64", "float64", "int32", "uint8"])
+def test_guard_band_helper_detects_margin_writes(dtype):
+    """The guard-band buffers of the GPU stage test, on CPU tensors: writes
+    inside the view keep check() true, one element past either end fails it."""
+    import torch
+    from guard_bands import guarded
+    dt = getattr(torch, dtype)
+    v, chk = guarded((3, 5, 7), dt, "cpu")
+    assert tuple(v.shape) == (3, 5, 7) and v.is_contiguous() and chk()
+    assert (v.data_ptr() - chk.base.data_ptr()) % 256 == 0
+    v.fill_(1)
+    assert chk()
+    for idx in (chk.pad - 1, chk.pad + v.numel()):
+        w, chk2 = guarded((3, 5, 7), dt, "cpu")
+        chk2.base[idx] = 1
+        assert not chk2(), idx
