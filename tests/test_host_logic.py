@@ -136,3 +136,37 @@ def test_guard_band_helper_detects_margin_writes(dtype):
         w, chk2 = guarded((3, 5, 7), dt, "cpu")
         chk2.base[idx] = 1
         assert not chk2(), idx
+
+
+def test_drop_in_arguments_and_no_cpu_fallback(pkg):
+    """solve_bor rejects bad arguments as the reference does (before any device
+    work) and, with valid arguments and no CUDA device, raises instead of
+    computing anything on the host."""
+    import importlib
+    import torch
+    bs = importlib.import_module("20260722_ghost_gb300.bor_solver")
+    pts = pkg.bodies.sphere_generatrix(1.0, 12)
+    f = 3e8
+    with pytest.raises(ValueError):
+        bs.solve_bor(pts, f, [0.0], formulation="pmchwt")
+    with pytest.raises(ValueError):
+        bs.solve_bor(pts, f, [0.0], table_precision="half")
+    with pytest.raises(ValueError):
+        bs.solve_bor(pts, f, [0.0], assembly="fmm")
+    with pytest.raises(ValueError):
+        bs.solve_bor_batch([{"points": pts, "freq_hz": f}], [0.0], table_precision="quad")
+    with pytest.raises(NotImplementedError):
+        bs.solve_bor(pts, f, [0.0], zs=50.0)
+
+    def abort():
+        raise InterruptedError("cancelled")
+
+    with pytest.raises(InterruptedError):
+        bs.solve_bor(pts, f, [0.0], check_abort=abort)
+    with pytest.raises(NotImplementedError):
+        bs.BorPecSolver(pts, f, medium=(2.0, 1.0))
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            bs.solve_bor(pts, f, [0.0, 90.0])
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            bs.BorPecSolver(pts, f).assemble_mode(0, 2)
