@@ -75,6 +75,14 @@ class BorGpuProblem:
                  cfie_alpha: float = 0.5):
         if gauss_order != 4:
             raise NotImplementedError("the GPU kernels are specialised for gauss_order=4")
+        # non-finite inputs would reach the kernels' index arithmetic (tail
+        # orders, n_xi); the reference lets them through to NaN results
+        if not np.all(np.isfinite(np.asarray(points, dtype=float))):
+            raise ValueError("generatrix nodes must be finite")
+        if not np.all(np.isfinite(np.asarray(thetas_deg, dtype=float))):
+            raise ValueError("aspect angles must be finite")
+        if not (math.isfinite(float(freq_hz)) and float(freq_hz) > 0.0):
+            raise ValueError("freq_hz must be a positive finite frequency")
         torch = _torch()
         nat.load()
         self.torch = torch

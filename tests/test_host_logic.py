@@ -170,3 +170,17 @@ def test_drop_in_arguments_and_no_cpu_fallback(pkg):
             bs.solve_bor(pts, f, [0.0, 90.0])
         with pytest.raises(RuntimeError, match="no CPU fallback"):
             bs.BorPecSolver(pts, f).assemble_mode(0, 2)
+
+
+def test_non_finite_inputs_rejected_before_device_work(pkg):
+    """NaN / inf nodes or angles and non-positive frequencies never reach a
+    kernel: BorGpuProblem raises ValueError before touching the device."""
+    import importlib
+    eng = importlib.import_module("20260722_ghost_gb300.engine")
+    pts = pkg.bodies.sphere_generatrix(1.0, 12)
+    bad = pts.copy()
+    bad[3, 0] = np.nan
+    for args in ((bad, 3e8, [0.0]), (pts, 3e8, [0.0, np.inf]), (pts, float("nan"), [0.0]),
+                 (pts, -1.0, [0.0]), (pts, 0.0, [0.0])):
+        with pytest.raises(ValueError):
+            eng.BorGpuProblem(*args)
