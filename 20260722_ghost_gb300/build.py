@@ -46,8 +46,21 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
+def _ensure_rule_table():
+    """The Gauss-Legendre tail rules that the host set-up reads
+    (geometry._leggauss); optional -- without the file they are recomputed
+    in each process -- so a failure here never fails the build."""
+    try:
+        from . import geometry
+        if not geometry.leggauss_table_ok():
+            geometry.write_leggauss_table()
+    except Exception as exc:          # noqa: BLE001
+        print(f"note: Gauss-Legendre rule table not written ({exc})")
+
+
 def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if not force and up_to_date():
+        _ensure_rule_table()
         return LIB
     os.makedirs(OBJDIR, exist_ok=True)
     cc = nvcc()
@@ -69,6 +82,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    _ensure_rule_table()
     return LIB
 
 

@@ -17,6 +17,8 @@ from __future__ import annotations
 
 import functools
 import math
+import os
+import platform
 from dataclasses import dataclass, field
 from typing import Dict, List, Tuple
 
@@ -28,15 +30,57 @@ AXIS_TOL = 1e-12
 GEO_ROWS = 11      # rho, z, w, T0 w rho, T1 w rho, T0 w, T1 w, dRT0 w, dRT1 w, t_rho, t_z
 
 
+_LEG_LO, _LEG_HI = 64, 1024          # the near tail orders
+_LEG_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "leggauss_64_1024.npz")
+_leg_table = None                    # (offsets, x, w) from _LEG_FILE, or False when absent / stale
+
+
+def _leg_stamp() -> str:
+    # the rules come from this machine's numpy / LAPACK: a table made elsewhere is stale
+    return f"numpy {np.__version__} on {platform.machine()}"
+
+
+def _leg_from_table(n: int):
+    """Rule n from the table written at build time on this machine, or None."""
+    global _leg_table
+    if _leg_table is None:
+        table = False
+        try:
+            with np.load(_LEG_FILE) as d:
+                if str(d["stamp"]) == _leg_stamp():
+                    table = (d["offsets"], d["x"], d["w"])
+        except (OSError, KeyError, ValueError):
+            pass
+        _leg_table = table
+    if not _leg_table:
+        return None
+    offs, x, w = _leg_table
+    o = int(offs[n - _LEG_LO])
+    return x[o:o + n].copy(), w[o:o + n].copy()
+
+
 @functools.lru_cache(maxsize=None)
 def _leggauss(n: int) -> Tuple[np.ndarray, np.ndarray]:
     """Gauss-Legendre nodes and weights on [-1, 1] (numpy's leggauss rule),
     cached: the near tail orders (up to 1024) repeat across element pairs,
-    bodies and calls.  numpy finds the nodes as the eigenvalues of the
+    bodies and calls, and orders 64..1024 are also read from a table that the
+    build writes with this same function (a fresh process then skips ~1-5 s
+    of rule construction).  numpy finds the nodes as the eigenvalues of the
     symmetric tridiagonal Legendre companion matrix with a dense O(n^3)
     solver; the same eigenvalues come from the tridiagonal solver in O(n^2),
     followed by numpy's own Newton step, weights, symmetrisation and
     normalisation, which return the same nodes and weights as leggauss."""
+    if _LEG_LO <= n <= _LEG_HI:
+        r = _leg_from_table(n)
+        if r is not None:
+            x, w = r
+            x.flags.writeable = False
+            w.flags.writeable = False
+            return x, w
+    return _leggauss_compute(n)
+
+
+def _leggauss_compute(n: int) -> Tuple[np.ndarray, np.ndarray]:
     L = np.polynomial.legendre
     try:
         from scipy.linalg import eigvalsh_tridiagonal
@@ -62,6 +106,41 @@ def _leggauss(n: int) -> Tuple[np.ndarray, np.ndarray]:
     x.flags.writeable = False
     w.flags.writeable = False
     return x, w
+
+
+def _rules_for(ns):
+    return [(n, _leggauss_compute(n)) for n in ns]
+
+
+def write_leggauss_table(path: str = _LEG_FILE, workers: int = 1) -> str:
+    """Compute every tail rule (orders 64..1024) with _leggauss_compute and
+    store them in one file for _leggauss.  Serial by default (~15 s); with
+    workers > 1 the orders are split over spawned processes, which only a
+    caller whose main module is import-safe may ask for."""
+    ns = list(range(_LEG_LO, _LEG_HI + 1))
+    if workers > 1:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+        chunks = [ns[i::workers] for i in range(workers)]
+        with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+            rules = dict(r for part in ex.map(_rules_for, chunks) for r in part)
+    else:
+        rules = dict(_rules_for(ns))
+    offsets = np.concatenate([[0], np.cumsum(ns[:-1])]).astype(np.int64)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path[:-4] + ".tmp.npz"
+    np.savez(tmp, offsets=offsets, x=np.concatenate([rules[n][0] for n in ns]),
+             w=np.concatenate([rules[n][1] for n in ns]), stamp=_leg_stamp())
+    os.replace(tmp, path)
+    return path
+
+
+def leggauss_table_ok(path: str = _LEG_FILE) -> bool:
+    try:
+        with np.load(path) as d:
+            return str(d["stamp"]) == _leg_stamp() and len(d["offsets"]) == _LEG_HI - _LEG_LO + 1
+    except (OSError, KeyError, ValueError):
+        return False
 
 
 class Generatrix:

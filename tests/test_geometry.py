@@ -153,3 +153,16 @@ def test_gauss_legendre_rule_is_numpys(pkg):
         x, w = np.polynomial.legendre.leggauss(n)
         x2, w2 = g._leggauss(n)
         assert np.array_equal(x, x2) and np.array_equal(w, w2), n
+
+
+def test_rule_table_equals_computed_rules():
+    """The Gauss-Legendre table written by the build holds exactly what
+    _leggauss_compute returns (when the table is present)."""
+    import importlib
+    g = importlib.import_module("20260722_ghost_gb300.geometry")
+    if not g.leggauss_table_ok():
+        pytest.skip("rule table not built")
+    for n in (64, 65, 100, 257, 512, 1000, 1024):
+        x, w = g._leg_from_table(n)
+        xc, wc = g._leggauss_compute(n)
+        assert np.array_equal(x, xc) and np.array_equal(w, wc), n
