@@ -76,13 +76,14 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
         return obj
 
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
-        objs = list(ex.map(compile_one, _sources()))
+        pending = ex.map(compile_one, _sources())
+        _ensure_rule_table()           # host work while the compilers run
+        objs = list(pending)
     tmp = LIB + ".tmp"
     r = subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
-    _ensure_rule_table()
     return LIB
 
 
