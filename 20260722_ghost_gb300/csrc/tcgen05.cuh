@@ -1,7 +1,7 @@
 // tcgen05.cuh -- shared inline-PTX helpers of the tensor-core kernels (sm_103a):
 // mbarriers with bounded waits, TMA tile loads, UMMA shared-memory descriptors,
-// tcgen05 commit / TMEM loads, and the driver entry point of the tensor-map
-// encoder.
+// tcgen05 commit / TMEM loads, and the CUDA driver-API entry point of the
+// tensor-map encoder.
 #pragma once
 #include "common.cuh"
 

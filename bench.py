@@ -497,7 +497,7 @@ def roofline(res, peaks, workload):
                                  "frac": round(ach / fp32_peak, 4)}, **ctx)
         prob = res.get("prob")
         if name == "far_fill" and prob is not None:
-            # the survey's fill unit: Green's-function samples per second
+            # the fill's natural unit: Green's-function samples per second
             # (every far Gauss-point pair at every half-grid azimuth node)
             samples = float(4 * prob.N) ** 2 * (prob.n_xi // 2 + 1)
             out["fp32_pipe"]["samples_per_s"] = float(f"{samples * len(ks[name]) / t_sum:.4g}")
