@@ -166,3 +166,28 @@ def test_rule_table_equals_computed_rules():
         x, w = g._leg_from_table(n)
         xc, wc = g._leggauss_compute(n)
         assert np.array_equal(x, xc) and np.array_equal(w, wc), n
+
+
+def test_random_batch_matches_its_definition(pkg):
+    """The 64-body batch (seed 0): closed bodies drawn from +z to -z with
+    rho >= 0, equal-arc segments, 12 segments per wavelength, the stated
+    parameter ranges and |m| rule, and the same arrays for the same seed."""
+    b = pkg.bodies
+    batch = b.random_bodies(64, seed=0)
+    again = b.random_bodies(64, seed=0)
+    assert len(batch) == 64
+    for x, y in zip(batch, again):
+        assert np.array_equal(x["points"], y["points"]) and x["freq_hz"] == y["freq_hz"]
+    for x in batch:
+        p = x["points"]
+        assert len(p) == x["n"] + 1 and 200 <= x["n"] <= 1600
+        assert p[0, 0] == pytest.approx(0.0, abs=1e-12) and p[-1, 0] == pytest.approx(0.0, abs=1e-12)
+        assert np.all(p[:, 0] >= -1e-12) and p[0, 1] > p[-1, 1]
+        seg = np.hypot(*np.diff(p, axis=0).T)
+        assert seg.max() / seg.min() < 1.01
+        assert 1.0 <= x["L"] <= 4.0 and 0.2 <= x["R0"] <= 0.8
+        assert all(abs(a) <= 0.1 / (i + 1) for i, a in enumerate(x["a_k"]))
+        arclen = seg.sum()
+        assert x["k"] * arclen / x["n"] == pytest.approx(2.0 * math.pi / 12.0, rel=1e-12)
+        assert x["m_max"] == math.ceil(x["k"] * p[:, 0].max()) + 10
+    assert len({x["n"] for x in batch}) > 50             # the sizes spread over the range
