@@ -191,3 +191,19 @@ def test_random_batch_matches_its_definition(pkg):
         assert x["k"] * arclen / x["n"] == pytest.approx(2.0 * math.pi / 12.0, rel=1e-12)
         assert x["m_max"] == math.ceil(x["k"] * p[:, 0].max()) + 10
     assert len({x["n"] for x in batch}) > 50             # the sizes spread over the range
+
+
+def test_bspline_body_definition(pkg):
+    """The B-spline body of the gradient workload: clamped cubic basis (a
+    partition of unity), closed on the axis from z = +1 to z = -1, radii
+    bounded by the control radii, monotone in z (the control z are)."""
+    b = pkg.bodies
+    radii = np.random.default_rng(0).uniform(0.3, 0.6, 64)
+    pts, B = b.bspline_body(radii, 600)
+    assert pts.shape == (601, 2) and B.shape == (601, 66)
+    np.testing.assert_allclose(B.sum(axis=1), 1.0, atol=1e-14)
+    assert np.all(B >= -1e-15)
+    assert pts[0, 0] == 0.0 and pts[-1, 0] == 0.0
+    assert pts[0, 1] == pytest.approx(1.0) and pts[-1, 1] == pytest.approx(-1.0)
+    assert np.all(np.diff(pts[:, 1]) < 0)
+    assert np.all(pts[1:-1, 0] > 0.0) and pts[:, 0].max() <= radii.max() + 1e-12
