@@ -3,14 +3,16 @@
 A NumPy restatement of the reference's body-of-revolution solver for PEC
 and surface-impedance (Leontovich, ``zs``) bodies (``bor_solver.solve_bor``
 with ``formulation`` "efie" / "cfie" / "mfie", ``table_precision="double"``,
-``assembly="streaming"``).  It is the checker
+``assembly="streaming"``) and for homogeneous penetrable bodies
+(``solve_bor_dielectric``, PMCHWT).  It is the checker
 that the CUDA product is compared against; the product never imports it.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs may
 import, call or time anything under ``oracle/``.
 
-Parity pinned: ``tests/test_oracle_golden.py`` and ``tests/test_oracle_ibc.py``
-check this module against golden vectors produced by running the reference
-itself (``tests/golden/make_golden.py``, ``tests/golden/make_ibc_golden.py``).
+Parity pinned: ``tests/test_oracle_golden.py``, ``tests/test_oracle_ibc.py``
+and ``tests/test_oracle_pmchwt.py`` check this module against golden vectors
+produced by running the reference itself (``tests/golden/make_golden.py``,
+``make_ibc_golden.py``, ``make_pmchwt_golden.py``).
 
 Every function cites the reference lines it restates (paths relative to the
 reference project root).  The far-field assembly follows the reference's
@@ -364,6 +366,17 @@ def _near_brackets(grid_fn, rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, m
     return tuple(outs)
 
 
+def causal_medium(eps_r: complex, mu_r: complex) -> Tuple[complex, complex]:
+    """(refractive index m, relative impedance mu_r / m) with Im(m) <= 0 and
+    Re(m) >= 0 (bor_solver.py:161-172)."""
+    m = np.sqrt(complex(eps_r) * complex(mu_r))
+    if m.imag > 0.0:
+        m = -m
+    if m.real < 0.0:
+        m = -m
+    return m, complex(mu_r) / m
+
+
 # ---------------------------------------------------------------------------
 # the solver
 # ---------------------------------------------------------------------------
@@ -375,10 +388,14 @@ class OracleSolver:
     _COMBOS = (("r", "r"), ("z", "z"), ("r", "1"), ("1", "r"), ("1", "1"),
                ("d", "d"), ("d", "s"), ("s", "d"), ("s", "s"))  # bor_streaming.py:370-371
 
-    def __init__(self, points, freq_hz: float, gauss_order: int = 4):
+    def __init__(self, points, freq_hz: float, gauss_order: int = 4, medium=None):
         self.geo = Geom(points, gauss_order)
-        self.k = 2.0 * math.pi * freq_hz / C0
-        self.eta = ETA0
+        k0 = 2.0 * math.pi * freq_hz / C0
+        if medium is None:
+            self.k, self.eta = k0, ETA0
+        else:                                  # bor_solver.py:194-200
+            m_idx, eta_r = causal_medium(*medium)
+            self.k, self.eta = k0 * m_idx, ETA0 * eta_r
         self.freq_hz = freq_hz
         g = self.geo
         wrho = g.w * g.rho
@@ -402,7 +419,7 @@ class OracleSolver:
         sin2 = np.ascontiguousarray(np.sin(0.5 * xi) ** 2)
         rp = np.ascontiguousarray(g.rho[rows])
         zp = np.ascontiguousarray(g.z[rows])
-        if _SAMPLER is not None:
+        if _SAMPLER is not None and not np.iscomplexobj(self.k):
             out = np.empty((len(rp), g.P, n_xi), dtype=np.complex128)
             _SAMPLER.oracle_sample_g(len(rp), g.P, n_xi, _dp(rp), _dp(zp),
                                      _dp(np.ascontiguousarray(g.rho)),
@@ -666,19 +683,35 @@ class OracleSolver:
         499-552): (1/2) <W, Z_s J> + the rotated principal-value brackets
         with Z_s at the source; the far part comes from build_far(ibc_zs_pt),
         near pairs are weighted by the source element's Z_s."""
+        ktt, ktf, kft, kff = self.rot_pv_blocks(m, m_max, zs_elem)
+        Mz = self.mass(zs_pt)
+        return np.block([[0.5 * Mz + ktt, ktf], [kft, 0.5 * Mz + kff]])
+
+    def rot_pv_blocks(self, m: int, m_max: int, zs_elem: Optional[np.ndarray] = None):
+        """The four rotated principal-value blocks B_tt, B_tf, B_ft, B_ff of
+        mode m with an optional source weight per element (bor_solver.py:
+        497-532): far part from build_far(ibc_zs_pt = that weight per Gauss
+        point, or ones), near pairs weighted by the source element's value."""
         mi = m + m_max
         blocks = [self.Bb[uv, mi].copy() for uv in range(4)]
         for (e, f) in self.near_pairs():
-            if abs(zs_elem[f]) == 0.0:
+            welem = 1.0 if zs_elem is None else zs_elem[f]
+            if abs(welem) == 0.0:
                 continue
             w, rp, Tp, rq, Tq, Kn = self.near_ibc_data(e, f, m_max)
-            rr = rp * rq * w * zs_elem[f]
+            rr = rp * rq * w * welem
             for uv in range(4):
                 blocks[uv][e:e + 2, f:f + 2] += 2.0 * np.pi * np.einsum(
                     "ip,p,jp->ij", Tp, rr * Kn[uv][:, mi], Tq)
-        Mz = self.mass(zs_pt)
-        ktt, ktf, kft, kff = blocks
-        return np.block([[0.5 * Mz + ktt, ktf], [kft, 0.5 * Mz + kff]])
+        return blocks
+
+    def pmchwt_P(self, m: int, m_max: int) -> np.ndarray:
+        """PMCHWT operator P in this medium acting on a magnetic current in the
+        same (t, phi) bases: the unweighted rotated blocks with the source
+        columns remapped (n x t = phi, n x phi = -t; bor_solver.py:554-576).
+        Needs build_far / prepare with ibc_zs_pt = ones."""
+        btt, btf, bft, bff = self.rot_pv_blocks(m, m_max)
+        return np.block([[-btf, btt], [-bff, bft]])
 
     def assemble_mfie(self, m: int, m_max: int) -> np.ndarray:
         """Z_MFIE = M/2 - K (bor_solver.py:399-435) on streamed brackets."""
@@ -750,7 +783,8 @@ class OracleSolver:
         return np.concatenate([(c * et) @ g.BT.T, (c * ef) @ g.BT.T], axis=1)
 
     def farfield(self, m: int, sols: np.ndarray, thetas_deg,
-                 zs_pt: Optional[np.ndarray] = None) -> Tuple[np.ndarray, np.ndarray]:
+                 zs_pt: Optional[np.ndarray] = None,
+                 msol: Optional[np.ndarray] = None) -> Tuple[np.ndarray, np.ndarray]:
         """farfield_mode (bor_solver.py:659-708) for solution rows
         sols [n_theta, 2Nn] at the matching angles: (F_theta, F_phi).  With
         zs_pt the eliminated magnetic current M_t = Z_s J_phi,
@@ -771,8 +805,12 @@ class OracleSolver:
 
         pref = -1j * self.k * ETA0 / (4.0 * math.pi)
         fth, fph = pref * proj_theta(Jt, Jf), pref * proj_phi(Jt, Jf)
+        Mt = Mf = None
         if zs_pt is not None:
             Mt, Mf = zs_pt * Jf, -zs_pt * Jt
+        elif msol is not None:                 # a magnetic-current solution (PMCHWT)
+            Mt, Mf = msol[:, :Nn] @ g.BT, msol[:, Nn:] @ g.BT
+        if Mt is not None:
             pm = 1j * self.k / (4.0 * math.pi)
             fth = fth - pm * proj_phi(Mt, Mf)
             fph = fph + pm * proj_theta(Mt, Mf)
@@ -913,3 +951,82 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
     if keep_per_mode:
         out["per_mode"] = per_mode
     return out
+
+
+def solve_bor_dielectric(points, freq_hz: float, thetas_deg, eps_r: complex, mu_r: complex = 1.0,
+                         n_modes: Optional[int] = None, gauss_order: int = 4,
+                         mode_tol: float = 1e-6, workers: int = 1) -> Dict:
+    """Monostatic RCS of a closed homogeneous penetrable body by per-mode
+    PMCHWT (bor_solver.py:1019-1095).  Unknowns J (2Nn) and M' = M / eta0
+    (2Nn); with T the EFIE operator and P the rotated principal-value
+    operator of each medium (exterior e, interior i):
+
+        [ T_e + T_i             -eta0 (P_e + P_i)          ] [J ]   [ <W, E_inc>      ]
+        [ eta0 (P_e + P_i)    T_e + (eta0/eta_i)^2 T_i     ] [M'] = [ eta0 <W, H_inc> ]
+
+    and the far field radiates J and M in air."""
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    if n_modes is None:
+        n_modes = default_n_modes(points, freq_hz, thetas)
+    m_max = int(n_modes)
+    se = OracleSolver(points, freq_hz, gauss_order)
+    si = OracleSolver(points, freq_hz, gauss_order, medium=(eps_r, mu_r))
+    Nn = se.geo.Nn
+    ones = np.ones(se.geo.P)
+    for s in (se, si):
+        s.prepare(m_max, efie=True, workers=workers, ibc_zs_pt=ones)
+    eta_ratio2 = (ETA0 / si.eta) ** 2
+    F = np.zeros((2, len(thetas)), dtype=np.complex128)
+
+    def solve_am(am):
+        dF = np.zeros_like(F)
+        res = 0.0
+        for m in ([0] if am == 0 else [am, -am]):
+            T_e, T_i = se.assemble_efie(m, m_max), si.assemble_efie(m, m_max)
+            P = ETA0 * (se.pmchwt_P(m, m_max) + si.pmchwt_P(m, m_max))
+            A = np.block([[T_e + T_i, -P], [P, T_e + eta_ratio2 * T_i]])
+            mask = np.tile(se.basis_mask(m), 2)
+            A = A[np.ix_(mask, mask)]
+            # <W, E_inc> and eta0 <W, H_inc> (bor_solver.py:647-657, 1068-1070)
+            cols = [np.concatenate([se.rhs_efie(m, thetas, "VV"), -se.rhs_efie(m, thetas, "HH")], axis=1),
+                    np.concatenate([se.rhs_efie(m, thetas, "HH"), se.rhs_efie(m, thetas, "VV")], axis=1)]
+            B = np.stack(cols, axis=1).transpose(2, 0, 1).reshape(4 * Nn, 2 * len(thetas))[mask]
+            X = np.linalg.solve(A, B)
+            bn = float(np.linalg.norm(B))
+            if bn > 0.0:
+                res = max(res, float(np.linalg.norm(A @ X - B)) / bn)
+            full = np.zeros((4 * Nn, X.shape[1]), dtype=np.complex128)
+            full[mask] = X
+            xs = full.T.reshape(len(thetas), 2, 4 * Nn)
+            fth, _ = se.farfield(m, xs[:, 0, :2 * Nn], thetas, msol=ETA0 * xs[:, 0, 2 * Nn:])
+            _, fph = se.farfield(m, xs[:, 1, :2 * Nn], thetas, msol=ETA0 * xs[:, 1, 2 * Nn:])
+            dF[0] += fth
+            dF[1] += fph
+        return dF, res
+
+    with ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        results = list(ex.map(solve_am, range(m_max + 1)))
+    modes_used, quiet, max_res = 0, 0, 0.0
+    for am, (dF, res) in enumerate(results):       # the reference's truncation (bor_solver.py:777-794)
+        F += dF
+        max_res = max(max_res, res)
+        modes_used = am
+        if float(np.max(np.abs(dF))) < mode_tol * max(float(np.max(np.abs(F))), 1e-30):
+            quiet += 1
+            if quiet >= 2:
+                break
+        else:
+            quiet = 0
+    return {
+        "theta_deg": thetas.tolist(),
+        "sigma_vv": (4.0 * math.pi * np.abs(F[0]) ** 2).tolist(),
+        "sigma_hh": (4.0 * math.pi * np.abs(F[1]) ** 2).tolist(),
+        "amp_vv": F[0].tolist(),
+        "amp_hh": F[1].tolist(),
+        "modes_used": modes_used,
+        "n_unknowns": int(4 * Nn),
+        "formulation": "pmchwt",
+        "eps_r": complex(eps_r),
+        "mu_r": complex(mu_r),
+        "linear_residual": max_res,
+    }

@@ -63,3 +63,33 @@ def sigma_impedance_sphere(radius_m: float, freq_hz: float, zs_ohm: complex) -> 
     """Backscatter of a Leontovich (surface-impedance) sphere."""
     k = 2.0 * math.pi * freq_hz / C0
     return _backscatter(k, *_sphere_coefficients(k * radius_m, 1j * complex(zs_ohm) / ETA0))
+
+
+def _causal_index(eps_r: complex, mu_r: complex) -> complex:
+    """sqrt(eps_r mu_r) with Im <= 0 and Re >= 0."""
+    m = np.sqrt(complex(eps_r) * complex(mu_r))
+    if m.imag > 0.0:
+        m = -m
+    if m.real < 0.0:
+        m = -m
+    return m
+
+
+def sigma_dielectric_sphere(radius_m: float, eps_r: complex, mu_r: complex, freq_hz: float) -> float:
+    """Backscatter of a homogeneous (possibly lossy, magnetic) sphere: interior
+    field C psi_n(m x); continuity of the tangential fields gives
+    A_n = -(psi' psi_m - w psi_m' psi) / (xi' psi_m - w psi_m' xi) with
+    w = m / eps_r (TM) or m / mu_r (TE)."""
+    k = 2.0 * math.pi * freq_hz / C0
+    x = k * radius_m
+    m = _causal_index(eps_r, mu_r)
+    X = max(x, abs(m) * x)
+    nmax = max(6, int(math.ceil(X + 4.05 * X ** (1.0 / 3.0))) + 12)
+    psi, dpsi = _psi(nmax, x)
+    zeta, dzeta = _zeta(nmax, x)
+    xi, dxi = psi - 1j * zeta, dpsi - 1j * dzeta
+    psim, dpsim = _psi(nmax, m * x)
+    wa, wb = m / complex(eps_r), m / complex(mu_r)
+    a = -(dpsi * psim - wa * dpsim * psi) / (dxi * psim - wa * dpsim * xi)
+    b = -(dpsi * psim - wb * dpsim * psi) / (dxi * psim - wb * dpsim * xi)
+    return _backscatter(k, a, b)

@@ -1,0 +1,67 @@
+"""Generate tests/golden/pmchwt_sphere_n24.npz by running the REFERENCE's
+homogeneous-dielectric PMCHWT path (bor_solver.solve_bor_dielectric).
+
+Run where the reference tree is mounted (default /root/reference, override
+with GHOST_REFERENCE_DIR):
+
+    python tests/golden/make_pmchwt_golden.py        # ~1 min
+
+Stored (FP64): a 24-segment sphere (a = 0.5 m, ka = 2); for a lossy
+dielectric medium the interior EFIE operator T_i and the PMCHWT operators P_e
+(air) and P_i of modes 0 and 2; full solves for a lossy, a lossless and a
+lossy magnetic medium; the dielectric-sphere Mie backscatter of a few cases.
+"""
+
+import importlib
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+sys.path.insert(0, REF)
+sys.path.insert(0, REPO)
+
+import bor_kernels as rk      # noqa: E402  (reference)
+import bor_solver as rs       # noqa: E402  (reference)
+import mie_sphere as rmie     # noqa: E402  (reference)
+
+bodies = importlib.import_module("20260722_ghost_gb300.bodies")
+
+MEDIA = [(2.5 - 0.2j, 1.0), (4.0, 1.0), (2.0 - 0.1j, 1.5 - 0.2j)]
+
+
+def main():
+    pts = bodies.sphere_generatrix(0.5, 24)
+    k = 4.0
+    f = k * rk.C0 / (2.0 * math.pi)
+    m_max = 8
+    thetas = np.arange(0.0, 180.0001, 30.0)
+    out = {"points": pts, "freq_hz": f, "k": k, "m_max": m_max, "thetas": thetas,
+           "media": np.array(MEDIA, dtype=complex), "modes": np.array([0, 2])}
+    se = rs.BorPecSolver(pts, f)
+    si = rs.BorPecSolver(pts, f, medium=MEDIA[0])
+    for s in (se, si):
+        s.prepare_operators(m_max, efie=True, ibc=True, workers=8)
+    for m in out["modes"]:
+        out[f"Ti_{m}"] = si.assemble_mode(int(m), m_max)
+        out[f"Pe_{m}"] = se.assemble_pmchwt_P(int(m), m_max)
+        out[f"Pi_{m}"] = si.assemble_pmchwt_P(int(m), m_max)
+    for i, (eps, mu) in enumerate(MEDIA):
+        r = rs.solve_bor_dielectric(pts, f, thetas, eps, mu, n_modes=m_max, mode_tol=0.0, workers=8)
+        out[f"amp_vv_{i}"] = np.array(r["amp_vv"])
+        out[f"amp_hh_{i}"] = np.array(r["amp_hh"])
+    cases = [(0.5, 300e6, 2.5, 1.0), (0.3, 1e9, 4.0 - 0.5j, 1.0), (1.0, 200e6, 2.0 - 0.1j, 1.5 - 0.2j),
+             (0.2, 2e9, 10.0, 1.0)]
+    out["mie_cases"] = np.array([[a, fr, complex(e).real, complex(e).imag, complex(u).real, complex(u).imag]
+                                 for a, fr, e, u in cases])
+    out["mie_sigma"] = np.array([rmie.sigma_dielectric_sphere(a, e, u, fr) for a, fr, e, u in cases])
+    np.savez_compressed(os.path.join(HERE, "pmchwt_sphere_n24.npz"), **out)
+    print("written")
+
+
+if __name__ == "__main__":
+    main()
