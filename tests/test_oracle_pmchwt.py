@@ -59,3 +59,25 @@ def test_causal_medium_branch(oracle):
     m, eta_r = oracle.causal_medium(4.0 - 1.0j, 1.0)
     assert m.imag <= 0.0 and m.real >= 0.0
     assert abs(m * m - (4.0 - 1.0j)) < 1e-14 and abs(eta_r - 1.0 / m) < 1e-15
+
+
+def test_magnetic_current_far_field_by_reciprocity(oracle, D):
+    """The far field of a magnetic current m (nodal, like the PMCHWT M) is the
+    reciprocity dot with the OTHER polarisation's E excitation:
+    F_theta^M = (j k / 4 pi) (D V_HH)^T m, F_phi^M = (j k / 4 pi) (D V_VV)^T m --
+    so a GPU far field needs no second projection kernel."""
+    import math
+    s = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    Nn = s.geo.Nn
+    th = np.array([15.0, 60.0, 90.0, 140.0])
+    Dg = np.concatenate([np.ones(Nn), -np.ones(Nn)])
+    pm = 1j * s.k / (4 * math.pi)
+    rng = np.random.default_rng(5)
+    for m in (0, 1, -3):
+        x = np.zeros((len(th), 2 * Nn), complex)
+        msol = rng.standard_normal((len(th), 2 * Nn)) + 1j * rng.standard_normal((len(th), 2 * Nn))
+        fth, fph = s.farfield(m, x, th, msol=msol)
+        want_th = pm * np.sum(Dg * s.rhs_efie(m, th, "HH") * msol, axis=1)
+        want_ph = pm * np.sum(Dg * s.rhs_efie(m, th, "VV") * msol, axis=1)
+        assert np.max(np.abs(fth - want_th)) <= 1e-13 * np.max(np.abs(want_th))
+        assert np.max(np.abs(fph - want_ph)) <= 1e-13 * np.max(np.abs(want_ph))
