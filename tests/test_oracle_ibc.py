@@ -132,3 +132,58 @@ def test_ibc_far_field_by_reciprocity(oracle):
         rph = -c * np.sum(Dg * (s.rhs_efie(m, th, "HH") - v_h(m, "HH")) * x, axis=1)
         assert np.max(np.abs(rth - fth)) <= 1e-13 * np.max(np.abs(fth))
         assert np.max(np.abs(rph - fph)) <= 1e-13 * np.max(np.abs(fph))
+
+
+def _pair_coefs(kind, rp, zp, trp, tzp, rq, zq, trq, tzq):
+    """Per-pair coefficients (c0..c5) of the three-transform bracket fill:
+    K_tt = c0 C[p] + c1 C[p s2], K_ff = c2 C[p] + c3 C[p s2], K_tf = -j c4 S,
+    K_ft = -j c5 S.  "mfie": the set of csrc/mfie_fill.cu (bracket_coefs);
+    "ibc": the rotated principal-value brackets of the identity above."""
+    dr, dz = rp - rq, zp - zq
+    if kind == "mfie":
+        X0, N0 = trp * tzq - tzp * trq, trp * dz - tzp * dr
+        A0, D0 = trp * dr + tzp * dz, trp * trq + tzp * tzq
+        c0 = dr * tzq - dz * trq
+        c1 = 2.0 * (A0 * tzp * trq + trp * rq * X0 + D0 * tzp * rq + trp * trq * N0)
+        return [-c0, -c1, N0, -2.0 * (N0 - rq * tzp), dz, -(rq * X0 + trq * N0)]
+    return [-(trp * dz - tzp * dr), -2.0 * (tzp * rp - trp * dz), dr * tzq - dz * trq,
+            2.0 * (tzq * rq + trq * dz), tzp * trq * rp - trp * tzq * rq - trp * trq * dz, dz]
+
+
+@pytest.mark.parametrize("kind", ["mfie", "ibc"])
+def test_three_transform_fill_reproduces_bracket_blocks(oracle, pkg, kind):
+    """The GPU bracket fill's formulation, emulated on the host: half-grid
+    transforms C[p], C[p s2], S of p = (1 + jkR) e^{-jkR} / R^3 with the
+    kernel's own tables (geometry.bracket_tables), per-pair coefficients, the
+    -j sine convention and the T w rho Galerkin weights.  With the MFIE set it
+    reproduces the oracle's FFT-of-brackets MFIE blocks, with the IBC set its
+    unit-weight IBC blocks (m = 0..M)."""
+    geom = pkg.geometry
+    pts = pkg.bodies.cone_sphere_generatrix(0.3, 15.0, 24)
+    k, M = 20.0, 6
+    o = oracle.OracleSolver(pts, k * oracle.C0 / (2 * math.pi))
+    o.build_far(M, efie=False, mfie=kind == "mfie",
+                ibc_zs_pt=np.ones(o.geo.P) if kind == "ibc" else None)
+    store = o.Kb if kind == "mfie" else o.Bb
+    gen = geom.Generatrix(pts)
+    geo = geom.pack_geo(geom.gauss_on_generatrix(gen, 4))
+    N, P = gen.n_elems, 4 * gen.n_elems
+    tab, s2 = geom.bracket_tables(geom.n_xi_bracket(k, float(np.max(gen.nodes[:, 0])), M), M)
+    rho, z, tr, tz = geo[0], geo[1], geo[9], geo[10]
+    e_of = np.arange(P) // 4
+    pi, qi = np.meshgrid(np.arange(P), np.arange(P), indexing="ij")
+    far = (np.abs(e_of[pi] - e_of[qi]) >= 2)[..., None]
+    R = np.maximum(np.sqrt(((rho[pi] - rho[qi]) ** 2 + (z[pi] - z[qi]) ** 2)[..., None]
+                           + (4 * rho[pi] * rho[qi])[..., None] * s2), 1e-30)
+    p = (1 + 1j * k * R) * np.exp(-1j * k * R) / R ** 3
+    T = np.einsum("pqj,tjm->tpqm", p, tab)
+    c = [x[..., None] for x in _pair_coefs(kind, rho[pi], z[pi], tr[pi], tz[pi], rho[qi], z[qi],
+                                           tr[qi], tz[qi])]
+    K = [c[0] * T[0] + c[1] * T[1], -1j * c[4] * T[2], -1j * c[5] * T[2], c[2] * T[0] + c[3] * T[1]]
+    W = np.zeros((N + 1, P))
+    W[e_of, np.arange(P)] += geo[3]
+    W[e_of + 1, np.arange(P)] += geo[4]
+    scale = np.max(np.abs(store))
+    for uv in range(4):
+        got = np.einsum("ip,pqm,jq->mij", W, K[uv] * far, W)
+        assert np.max(np.abs(got - store[uv, M:])) <= 1e-13 * scale, uv
