@@ -3,8 +3,8 @@
 A NumPy restatement of the reference's body-of-revolution solver for PEC
 and surface-impedance (Leontovich, ``zs``) bodies (``bor_solver.solve_bor``
 with ``formulation`` "efie" / "cfie" / "mfie", ``table_precision="double"``,
-``assembly="streaming"``) and for homogeneous penetrable bodies
-(``solve_bor_dielectric``, PMCHWT).  It is the checker
+``assembly="streaming"``) and for homogeneous penetrable and coated PEC
+bodies (``solve_bor_dielectric``, ``solve_bor_coated_pec``, PMCHWT).  It is the checker
 that the CUDA product is compared against; the product never imports it.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs may
 import, call or time anything under ``oracle/``.
@@ -1030,3 +1030,239 @@ def solve_bor_dielectric(points, freq_hz: float, thetas_deg, eps_r: complex, mu_
         "mu_r": complex(mu_r),
         "linear_residual": max_res,
     }
+
+
+# ---------------------------------------------------------------------------
+# two surfaces in one medium: cross operators and the coated PEC body
+# ---------------------------------------------------------------------------
+
+def _segment_distance(p0, p1, q0, q1) -> float:
+    """Minimum distance of two non-crossing 2-D segments (bor_solver.py:1101-1112)."""
+    def pt_seg(c, a, b):
+        ab = b - a
+        t = min(1.0, max(0.0, float(np.dot(c - a, ab) / max(np.dot(ab, ab), 1e-300))))
+        return float(np.hypot(*(c - (a + t * ab))))
+    return min(pt_seg(p0, q0, q1), pt_seg(p1, q0, q1), pt_seg(q0, p0, p1), pt_seg(q1, p0, p1))
+
+
+class CrossOperators:
+    """EFIE (T) and rotated principal-value (P) blocks between two different
+    generatrices in one medium: test bases on sp, sources on sq
+    (bor_solver.py:1115-1295).  Element pairs closer than near_factor times
+    the longer element are integrated on a tensor Gauss grid of near_order
+    points per side with the near kernels.  Surfaces that share an endpoint
+    (coating junctions) are not restated here."""
+
+    def __init__(self, sp: OracleSolver, sq: OracleSolver, near_factor: float = 2.0,
+                 near_order: int = 12):
+        if not np.isclose(complex(sp.k), complex(sq.k)):
+            raise ValueError("Cross operators need both solvers in the same medium.")
+        self.sp, self.sq, self.k, self.eta = sp, sq, sp.k, sp.eta
+        self.near_order = near_order
+        gp, gq = sp.geo, sq.geo
+        diag = max(float(np.max(gp.nodes)) - float(np.min(gp.nodes)),
+                   float(np.max(gq.nodes)) - float(np.min(gq.nodes)), 1e-9)
+        touch = 1e-9 * diag
+        self.near_pairs = []
+        for e in range(gp.ne):
+            pe = (gp.nodes[e], gp.nodes[e + 1])
+            for f in range(gq.ne):
+                qf = (gq.nodes[f], gq.nodes[f + 1])
+                if any(float(np.hypot(*(a - b))) <= touch for a in pe for b in qf):
+                    raise NotImplementedError("surfaces that share an endpoint (junctions)")
+                d = _segment_distance(pe[0], pe[1], qf[0], qf[1])
+                if d <= touch:
+                    raise ValueError("Cross-operator surfaces cross or touch.")
+                if d < near_factor * max(gp.lengths[e], gq.lengths[f]):
+                    self.near_pairs.append((e, f))
+        self._G = self._B = None
+        self._near: Dict = {}
+
+    def _tables(self, m_max: int):
+        """Far kernels of every point pair by FFT over xi (bor_kernels.py:132-167,
+        482-506), near pairs zeroed."""
+        if self._G is not None:
+            return self._G, self._B
+        gp, gq, k = self.sp.geo, self.sq.geo, self.k
+        rp, zp = gp.rho[:, None], gp.z[:, None]
+        rq, zq = gq.rho[None, :], gq.z[None, :]
+        osc = float(np.max(2.0 * abs(k) * np.sqrt(np.maximum(rp * rq, 0.0))))
+        nx = int(2 ** math.ceil(math.log2(max(64, 4 * (m_max + 2), 6 * (osc + 4)))))
+        xi = 2.0 * np.pi * np.arange(nx) / nx - np.pi
+        d2 = (rp - rq) ** 2 + (zp - zq) ** 2
+        R = np.maximum(np.sqrt(d2[..., None] + (4.0 * rp * rq)[..., None] * np.sin(0.5 * xi) ** 2),
+                       1e-300)
+        orders = np.arange(m_max + 2)
+        G = np.fft.fft(np.exp(-1j * k * R) / (4.0 * np.pi * R), axis=-1)[..., :m_max + 2] \
+            * (np.exp(1j * np.pi * orders) * (2.0 * np.pi / nx))
+        nb = int(2 ** math.ceil(math.log2(max(128, 6 * (m_max + 2), 8 * (osc + 4)))))
+        xib = 2.0 * np.pi * np.arange(nb) / nb - np.pi
+        one = np.ones((gp.P, gq.P))
+        a = [(v[:, None] * one).ravel() for v in (gp.rho, gp.z, gp.ptr, gp.ptz)]
+        b = [(v[None, :] * one).ravel() for v in (gq.rho, gq.z, gq.ptr, gq.ptz)]
+        ms = np.arange(-m_max, m_max + 1)
+        bins = np.where(ms >= 0, ms, nb + ms)
+        ph = np.exp(1j * np.pi * ms) * (2.0 * np.pi / nb)
+        B = [(np.fft.fft(F, axis=-1)[:, bins] * ph).reshape(gp.P, gq.P, -1)
+             for F in _ibc_bracket_grid(*a, *b, k, np.broadcast_to(xib, (a[0].size, nb)))]
+        for (e, f) in self.near_pairs:
+            sel = np.ix_(gp.elem == e, gq.elem == f)
+            G[sel] = 0.0
+            for Bi in B:
+                Bi[sel] = 0.0
+        self._G, self._B = G, B
+        return G, B
+
+    def _near_data(self, e: int, f: int, m_max: int):
+        key = (e, f)
+        if key in self._near:
+            return self._near[key]
+        x, w = np.polynomial.legendre.leggauss(self.near_order)
+        u, w1 = 0.5 * (x + 1.0), 0.5 * w
+        S, SP = np.meshgrid(u, u, indexing="ij")
+        W = np.outer(w1, w1).ravel()
+        gp, gq = self.sp.geo, self.sq.geo
+        rp, zp, T0p, T1p, D0p, D1p, Lp = gp.points_on_element(e, S.ravel())
+        rq, zq, T0q, T1q, D0q, D1q, Lq = gq.points_on_element(f, SP.ravel())
+        Gm = near_G(rp, zp, rq, zq, self.k, m_max)
+        Bn = near_ibc(rp, zp, np.full_like(rp, gp.trho[e]), np.full_like(rp, gp.tz[e]),
+                      rq, zq, np.full_like(rq, gq.trho[f]), np.full_like(rq, gq.tz[f]), self.k, m_max)
+        data = (W * Lp * Lq, rp, rq, np.vstack([T0p, T1p]), np.vstack([D0p, D1p]),
+                np.vstack([T0q, T1q]), np.vstack([D0q, D1q]), Gm, Bn)
+        self._near[key] = data
+        return data
+
+    def assemble_T(self, m: int, m_max: int) -> np.ndarray:
+        """Cross EFIE operator [2Np, 2Nq], C = j k eta 2 pi of the medium
+        (bor_solver.py:1221-1262, _pair_blocks :130-154)."""
+        k, gp, gq = self.k, self.sp.geo, self.sq.geo
+        G, _ = self._tables(m_max)
+        am = abs(m)
+        Gn = G[..., am]
+        Gc = 0.5 * (G[..., abs(am - 1)] + G[..., am + 1])
+        Gs = (G[..., abs(am - 1)] - G[..., am + 1]) / 2j
+        if m < 0:
+            Gs = -Gs
+        rrw = (gp.rho * gp.w)[:, None] * (gq.rho * gq.w)[None, :]
+        Ksc = gp.w[:, None] * gq.w[None, :] * Gn
+        ztt = gp.BT @ (rrw * (np.outer(gp.ptr, gq.ptr) * Gc + np.outer(gp.ptz, gq.ptz) * Gn)) @ gq.BT.T \
+            - (1.0 / k ** 2) * (gp.BD @ Ksc @ gq.BD.T)
+        ztf = gp.BT @ (rrw * (gp.ptr[:, None] * Gs)) @ gq.BT.T - (1j * m / k ** 2) * (gp.BD @ Ksc @ gq.BT.T)
+        zft = gp.BT @ (-rrw * (gq.ptr[None, :] * Gs)) @ gq.BT.T + (1j * m / k ** 2) * (gp.BT @ Ksc @ gq.BD.T)
+        zff = gp.BT @ (rrw * Gc) @ gq.BT.T - (m ** 2 / k ** 2) * (gp.BT @ Ksc @ gq.BT.T)
+        c = lambda A, kk, B: np.einsum("ip,p,jp->ij", A, kk, B)    # noqa: E731
+        for (e, f) in self.near_pairs:
+            w, rp, rq, Tp, Dp, Tq, Dq, Gt, _ = self._near_data(e, f, m_max)
+            gn = Gt[:, am]
+            gc = 0.5 * (Gt[:, abs(am - 1)] + Gt[:, am + 1])
+            gs = (Gt[:, abs(am - 1)] - Gt[:, am + 1]) / 2j
+            if m < 0:
+                gs = -gs
+            rr = rp * rq * w
+            ksc = w * gn
+            rs, cs = slice(e, e + 2), slice(f, f + 2)
+            ztt[rs, cs] += c(Tp, rr * (gp.trho[e] * gq.trho[f] * gc + gp.tz[e] * gq.tz[f] * gn), Tq) \
+                - (1.0 / k ** 2) * c(Dp, ksc, Dq)
+            ztf[rs, cs] += c(Tp, rr * gp.trho[e] * gs, Tq) - (1j * m / k ** 2) * c(Dp, ksc, Tq)
+            zft[rs, cs] += c(Tp, -rr * gq.trho[f] * gs, Tq) + (1j * m / k ** 2) * c(Tp, ksc, Dq)
+            zff[rs, cs] += c(Tp, rr * gc, Tq) - (m ** 2 / k ** 2) * c(Tp, ksc, Tq)
+        C = 1j * k * self.eta * 2.0 * np.pi
+        return C * np.block([[ztt, ztf], [zft, zff]])
+
+    def assemble_P(self, m: int, m_max: int) -> np.ndarray:
+        """Cross rotated principal-value operator [2Np, 2Nq] (bor_solver.py:1264-1289)."""
+        gp, gq = self.sp.geo, self.sq.geo
+        _, Bt = self._tables(m_max)
+        Wp = gp.BT * (gp.w * gp.rho)[None, :]
+        Wq = gq.BT * (gq.w * gq.rho)[None, :]
+        blocks = [2.0 * np.pi * Wp @ Bt[uv][..., m + m_max] @ Wq.T for uv in range(4)]
+        for (e, f) in self.near_pairs:
+            w, rp, rq, Tp, _, Tq, _, _, Bn = self._near_data(e, f, m_max)
+            rr = rp * rq * w
+            for uv in range(4):
+                blocks[uv][e:e + 2, f:f + 2] += 2.0 * np.pi * np.einsum(
+                    "ip,p,jp->ij", Tp, rr * Bn[uv][:, m + m_max], Tq)
+        btt, btf, bft, bff = blocks
+        return np.block([[-btf, btt], [-bff, bft]])
+
+
+def solve_bor_coated_pec(points_outer, points_core, freq_hz: float, thetas_deg, eps_r: complex,
+                         mu_r: complex = 1.0, n_modes: Optional[int] = None, gauss_order: int = 4,
+                         mode_tol: float = 1e-6, near_factor: float = 2.0, near_order: int = 12,
+                         workers: int = 1) -> Dict:
+    """Monostatic RCS of a PEC core fully covered by a homogeneous coating
+    (bor_solver.py:1298-1395).  Unknowns J_o, M'_o = M_o / eta0 on the outer
+    interface and J_c on the core:
+
+      [ T_e + T_L        -eta0 (P_e + P_L)          -T_L^oc      ] [J_o ]   [ V_E      ]
+      [ eta0 (P_e + P_L)  T_e + (eta0/eta_L)^2 T_L  -eta0 P_L^oc ] [M'_o] = [ eta0 V_H ]
+      [ T_L^co           -eta0 P_L^co               -T_L^cc      ] [J_c ]   [ 0        ]
+
+    and only (J_o, M_o) radiate in air."""
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    if n_modes is None:
+        n_modes = default_n_modes(points_outer, freq_hz, thetas)
+    m_max = int(n_modes)
+    se = OracleSolver(points_outer, freq_hz, gauss_order)
+    sLo = OracleSolver(points_outer, freq_hz, gauss_order, medium=(eps_r, mu_r))
+    sLc = OracleSolver(points_core, freq_hz, gauss_order, medium=(eps_r, mu_r))
+    Xoc = CrossOperators(sLo, sLc, near_factor, near_order)
+    Xco = CrossOperators(sLc, sLo, near_factor, near_order)
+    No, Nc = se.geo.Nn, sLc.geo.Nn
+    ntot = 4 * No + 2 * Nc
+    for s in (se, sLo):
+        s.prepare(m_max, efie=True, workers=workers, ibc_zs_pt=np.ones(s.geo.P))
+    sLc.prepare(m_max, efie=True, workers=workers)
+    eta_ratio2 = (ETA0 / sLo.eta) ** 2
+    iJ, iM, iC = slice(0, 2 * No), slice(2 * No, 4 * No), slice(4 * No, ntot)
+    F = np.zeros((2, len(thetas)), dtype=np.complex128)
+
+    def solve_am(am):
+        dF = np.zeros_like(F)
+        for m in ([0] if am == 0 else [am, -am]):
+            P = ETA0 * (se.pmchwt_P(m, m_max) + sLo.pmchwt_P(m, m_max))
+            T_e, T_L = se.assemble_efie(m, m_max), sLo.assemble_efie(m, m_max)
+            A = np.zeros((ntot, ntot), dtype=np.complex128)
+            A[iJ, iJ] = T_e + T_L
+            A[iJ, iM] = -P
+            A[iJ, iC] = -Xoc.assemble_T(m, m_max)
+            A[iM, iJ] = P
+            A[iM, iM] = T_e + eta_ratio2 * T_L
+            A[iM, iC] = -ETA0 * Xoc.assemble_P(m, m_max)
+            A[iC, iJ] = Xco.assemble_T(m, m_max)
+            A[iC, iM] = -ETA0 * Xco.assemble_P(m, m_max)
+            A[iC, iC] = -sLc.assemble_efie(m, m_max)
+            mo = se.basis_mask(m)
+            mask = np.concatenate([mo, mo, sLc.basis_mask(m)])
+            A = A[np.ix_(mask, mask)]
+            V = np.zeros((len(thetas), 2, ntot), dtype=np.complex128)
+            V[:, 0, iJ], V[:, 0, iM] = se.rhs_efie(m, thetas, "VV"), -se.rhs_efie(m, thetas, "HH")
+            V[:, 1, iJ], V[:, 1, iM] = se.rhs_efie(m, thetas, "HH"), se.rhs_efie(m, thetas, "VV")
+            B = V.transpose(2, 0, 1).reshape(ntot, 2 * len(thetas))[mask]
+            full = np.zeros((ntot, B.shape[1]), dtype=np.complex128)
+            full[mask] = np.linalg.solve(A, B)
+            xs = full.T.reshape(len(thetas), 2, ntot)
+            fth, _ = se.farfield(m, xs[:, 0, iJ], thetas, msol=ETA0 * xs[:, 0, iM])
+            _, fph = se.farfield(m, xs[:, 1, iJ], thetas, msol=ETA0 * xs[:, 1, iM])
+            dF[0] += fth
+            dF[1] += fph
+        return dF
+
+    with ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        results = list(ex.map(solve_am, range(m_max + 1)))
+    modes_used, quiet = 0, 0
+    for am, dF in enumerate(results):
+        F += dF
+        modes_used = am
+        if float(np.max(np.abs(dF))) < mode_tol * max(float(np.max(np.abs(F))), 1e-30):
+            quiet += 1
+            if quiet >= 2:
+                break
+        else:
+            quiet = 0
+    return {"theta_deg": thetas.tolist(),
+            "sigma_vv": (4.0 * math.pi * np.abs(F[0]) ** 2).tolist(),
+            "sigma_hh": (4.0 * math.pi * np.abs(F[1]) ** 2).tolist(),
+            "amp_vv": F[0].tolist(), "amp_hh": F[1].tolist(), "modes_used": modes_used,
+            "n_unknowns": int(ntot), "formulation": "pmchwt-coated",
+            "eps_r": complex(eps_r), "mu_r": complex(mu_r)}

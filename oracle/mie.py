@@ -93,3 +93,30 @@ def sigma_dielectric_sphere(radius_m: float, eps_r: complex, mu_r: complex, freq
     a = -(dpsi * psim - wa * dpsim * psi) / (dxi * psim - wa * dpsim * xi)
     b = -(dpsi * psim - wb * dpsim * psi) / (dxi * psim - wb * dpsim * xi)
     return _backscatter(k, a, b)
+
+
+def sigma_coated_pec_sphere(core_radius_m: float, outer_radius_m: float, eps_r: complex,
+                            mu_r: complex, freq_hz: float) -> float:
+    """Backscatter of a PEC sphere (radius b) inside one homogeneous layer
+    (outer radius a): the layer field D psi_n(m k r) + E zeta_n(m k r) with
+    E / D fixed by the PEC core (TM: U' = 0, TE: U = 0 at r = b), then the
+    outer-interface continuity of the dielectric sphere."""
+    if not (0.0 < core_radius_m < outer_radius_m):
+        raise ValueError("Require 0 < core radius < outer radius.")
+    k = 2.0 * math.pi * freq_hz / C0
+    x = k * outer_radius_m
+    m = _causal_index(eps_r, mu_r)
+    X = max(x, abs(m) * x)
+    nmax = max(6, int(math.ceil(X + 4.05 * X ** (1.0 / 3.0))) + 12)
+    psi, dpsi = _psi(nmax, x)
+    zeta, dzeta = _zeta(nmax, x)
+    xi, dxi = psi - 1j * zeta, dpsi - 1j * dzeta
+    pa, dpa = _psi(nmax, m * k * outer_radius_m)
+    za, dza = _zeta(nmax, m * k * outer_radius_m)
+    pb, dpb = _psi(nmax, m * k * core_radius_m)
+    zb, dzb = _zeta(nmax, m * k * core_radius_m)
+    out = []
+    for ratio, w in ((dpb / dzb, m / complex(eps_r)), (pb / zb, m / complex(mu_r))):
+        fa, dfa = pa - ratio * za, dpa - ratio * dza
+        out.append(-(dpsi * fa - w * dfa * psi) / (dxi * fa - w * dfa * xi))
+    return _backscatter(k, out[0], out[1])

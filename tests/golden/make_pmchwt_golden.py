@@ -1,5 +1,6 @@
-"""Generate tests/golden/pmchwt_sphere_n24.npz by running the REFERENCE's
-homogeneous-dielectric PMCHWT path (bor_solver.solve_bor_dielectric).
+"""Generate tests/golden/pmchwt_sphere_n24.npz and coated_sphere.npz by running
+the REFERENCE's PMCHWT paths (bor_solver.solve_bor_dielectric,
+BorCrossOperators, solve_bor_coated_pec).
 
 Run where the reference tree is mounted (default /root/reference, override
 with GHOST_REFERENCE_DIR):
@@ -10,6 +11,9 @@ Stored (FP64): a 24-segment sphere (a = 0.5 m, ka = 2); for a lossy
 dielectric medium the interior EFIE operator T_i and the PMCHWT operators P_e
 (air) and P_i of modes 0 and 2; full solves for a lossy, a lossless and a
 lossy magnetic medium; the dielectric-sphere Mie backscatter of a few cases.
+Coated: a 12-segment PEC sphere (0.4 m) inside a 16-segment coating (0.5 m),
+ka = 1.5; the cross operators T and P between the two surfaces (both
+directions) for mode 1; a full solve; the coated-sphere Mie backscatter.
 """
 
 import importlib
@@ -60,7 +64,32 @@ def main():
                                  for a, fr, e, u in cases])
     out["mie_sigma"] = np.array([rmie.sigma_dielectric_sphere(a, e, u, fr) for a, fr, e, u in cases])
     np.savez_compressed(os.path.join(HERE, "pmchwt_sphere_n24.npz"), **out)
+    coated()
     print("written")
+
+
+def coated():
+    outer, core = bodies.sphere_generatrix(0.5, 16), bodies.sphere_generatrix(0.4, 12)
+    k, m_max, eps, mu = 3.0, 4, 2.5 - 0.3j, 1.0
+    f = k * rk.C0 / (2.0 * math.pi)
+    thetas = np.arange(0.0, 180.0001, 45.0)
+    out = {"outer": outer, "core": core, "freq_hz": f, "m_max": m_max, "thetas": thetas,
+           "eps": eps, "mu": mu}
+    sLo = rs.BorPecSolver(outer, f, medium=(eps, mu))
+    sLc = rs.BorPecSolver(core, f, medium=(eps, mu))
+    Xoc, Xco = rs.BorCrossOperators(sLo, sLc), rs.BorCrossOperators(sLc, sLo)
+    for X, tag in ((Xoc, "oc"), (Xco, "co")):
+        X.prepare(m_max)
+        out[f"T_{tag}"] = X.assemble_T(1, m_max)
+        out[f"P_{tag}"] = X.assemble_P(1, m_max)
+    r = rs.solve_bor_coated_pec(outer, core, f, thetas, eps, mu, n_modes=m_max, mode_tol=0.0, workers=8)
+    out["amp_vv"], out["amp_hh"] = np.array(r["amp_vv"]), np.array(r["amp_hh"])
+    cases = [(0.4, 0.5, 300e6, 2.5 - 0.3j, 1.0), (0.2, 0.3, 1e9, 4.0, 1.0),
+             (0.8, 1.0, 200e6, 2.0 - 0.1j, 1.5 - 0.2j)]
+    out["mie_cases"] = np.array([[b, a, fr, complex(e).real, complex(e).imag, complex(u).real,
+                                  complex(u).imag] for b, a, fr, e, u in cases])
+    out["mie_sigma"] = np.array([rmie.sigma_coated_pec_sphere(b, a, e, u, fr) for b, a, fr, e, u in cases])
+    np.savez_compressed(os.path.join(HERE, "coated_sphere.npz"), **out)
 
 
 if __name__ == "__main__":

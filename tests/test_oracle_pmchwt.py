@@ -81,3 +81,50 @@ def test_magnetic_current_far_field_by_reciprocity(oracle, D):
         want_ph = pm * np.sum(Dg * s.rhs_efie(m, th, "VV") * msol, axis=1)
         assert np.max(np.abs(fth - want_th)) <= 1e-13 * np.max(np.abs(want_th))
         assert np.max(np.abs(fph - want_ph)) <= 1e-13 * np.max(np.abs(want_ph))
+
+
+@pytest.fixture(scope="module")
+def Dc():
+    return load_golden("coated_sphere")
+
+
+def test_cross_operators_match_reference(oracle, Dc):
+    """T and P between the coating and the core, both directions (the cross
+    terms of the coated system), against the reference's BorCrossOperators."""
+    M, f, medium = int(Dc["m_max"]), float(Dc["freq_hz"]), (complex(Dc["eps"]), complex(Dc["mu"]))
+    so = oracle.OracleSolver(Dc["outer"], f, medium=medium)
+    sc = oracle.OracleSolver(Dc["core"], f, medium=medium)
+    for X, tag in ((oracle.CrossOperators(so, sc), "oc"), (oracle.CrossOperators(sc, so), "co")):
+        assert X.near_pairs                     # the thin layer puts pairs on the near grid
+        assert _rel(X.assemble_T(1, M), Dc[f"T_{tag}"]) < 1e-12, tag
+        assert _rel(X.assemble_P(1, M), Dc[f"P_{tag}"]) < 1e-12, tag
+
+
+def test_coated_pec_solve_matches_reference(oracle, Dc):
+    r = oracle.solve_bor_coated_pec(Dc["outer"], Dc["core"], float(Dc["freq_hz"]), Dc["thetas"],
+                                    complex(Dc["eps"]), complex(Dc["mu"]), n_modes=int(Dc["m_max"]),
+                                    mode_tol=0.0, workers=4)
+    assert _rel(r["amp_vv"], Dc["amp_vv"]) < 1e-10
+    assert _rel(r["amp_hh"], Dc["amp_hh"]) < 1e-10
+    assert r["n_unknowns"] == 4 * len(Dc["outer"]) + 2 * len(Dc["core"])
+
+
+def test_coated_mie_matches_reference(Dc):
+    from oracle import mie
+    for (b, a, f, er, ei, ur, ui), want in zip(Dc["mie_cases"], Dc["mie_sigma"]):
+        got = mie.sigma_coated_pec_sphere(b, a, complex(er, ei), complex(ur, ui), f)
+        assert abs(got - want) <= 1e-14 * want
+    with pytest.raises(ValueError):
+        mie.sigma_coated_pec_sphere(0.5, 0.4, 2.0, 1.0, 3e8)
+
+
+def test_cross_operators_reject_junctions(oracle):
+    """Surfaces sharing an endpoint (coating terminations) are not restated."""
+    import importlib
+    bodies = importlib.import_module("20260722_ghost_gb300.bodies")
+    a = bodies.sphere_generatrix(0.5, 8)
+    b = a.copy()
+    b[1:-1, 0] *= 0.8                          # same poles: the two surfaces touch on the axis
+    sa, sb = oracle.OracleSolver(a, 3e8), oracle.OracleSolver(b, 3e8)
+    with pytest.raises(NotImplementedError):
+        oracle.CrossOperators(sa, sb)
