@@ -1,6 +1,6 @@
 """``.grim`` export of body-of-revolution results (reference module
 ``grim_io``: export_result_to_grim grim_io.py:210-262, save_bor_az_el_grim
-grim_io.py:265-311).
+grim_io.py:265-311) and its dBke CSV export (grim_io.py:50-78, 314-377).
 
 A ``.grim`` file is a NumPy ``.npz`` archive: axes ``azimuths``,
 ``elevations``, ``frequencies`` (float64), ``polarizations`` (one label),
@@ -194,3 +194,67 @@ def save_bor_az_el_grim(grid: Dict[str, Any], output_path: str,
         }
         out.append(os.path.abspath(_write(payload, f"{root}_{ch}")))
     return out
+
+
+# ---------------------------------------------------------------------------
+# dBke (knife-edge normalised scattering width) CSV export (grim_io.py:40-78, 314-377)
+# ---------------------------------------------------------------------------
+
+C0 = 299_792_458.0
+_HZ_PER = {"hz": 1.0, "khz": 1.0e3, "mhz": 1.0e6, "ghz": 1.0e9}
+
+
+def _to_hz(value: float, unit: str = "GHz") -> float:
+    return float(value) * _HZ_PER.get(str(unit or "GHz").strip().lower(), 1.0e9)
+
+
+def compute_dbke_from_linear(rcs_linear: float, frequency_value: float,
+                             frequency_unit: str = "GHz") -> float:
+    """Absolute dBke of a linear 2-D scattering width: 10 log10(k sigma_2d),
+    k = 2 pi f / c0; non-finite or non-positive widths count as 1e-12."""
+    lin = float(rcs_linear)
+    if not math.isfinite(lin) or lin <= 0.0:
+        lin = _TINY
+    f = _to_hz(frequency_value, frequency_unit)
+    if not math.isfinite(f) or f <= 0.0:
+        raise ValueError("frequency_value must be a positive finite frequency.")
+    return 10.0 * math.log10(((2.0 * math.pi * f) / C0) * lin)
+
+
+def compute_linear_from_dbke(dbke_value: float, frequency_value: float,
+                             frequency_unit: str = "GHz") -> float:
+    """The linear 2-D scattering width of an absolute dBke value."""
+    f = _to_hz(frequency_value, frequency_unit)
+    if not math.isfinite(f) or f <= 0.0:
+        raise ValueError("frequency_value must be a positive finite frequency.")
+    return (C0 / (2.0 * math.pi * f)) * (10.0 ** (float(dbke_value) / 10.0))
+
+
+def export_result_to_dbke_csv(result: Dict[str, Any], output_path: str, source_path: str = "",
+                              history: str = "") -> str:
+    """Write the samples, sorted by (frequency, incidence, scattering angle),
+    as CSV with an absolute dBke column (a 2-D quantity; kept so the module
+    is a complete stand-in for the reference's)."""
+    samples = result.get("samples", []) or []
+    if not samples:
+        raise ValueError("No solver samples were returned, nothing to export.")
+    out = output_path if output_path.lower().endswith(".csv") else output_path + ".csv"
+    key = lambda r: (float(r.get("frequency_ghz", 0.0)), float(r.get("theta_inc_deg", 0.0)),  # noqa: E731
+                     float(r.get("theta_scat_deg", 0.0)))
+    cols = ["frequency_ghz", "theta_inc_deg", "theta_scat_deg", "rcs_linear", "rcs_db", "dbke",
+            "rcs_amp_real", "rcs_amp_imag", "rcs_amp_phase_deg", "source_path", "history"]
+    g = lambda v: f"{float(v):.12g}"                                                              # noqa: E731
+    with open(out, "w", encoding="utf-8", newline="") as fh:
+        fh.write(",".join(cols) + "\n")
+        for r in sorted(samples, key=key):
+            lin = float(r.get("rcs_linear", 0.0))
+            if not math.isfinite(lin) or lin <= 0.0:
+                lin = _TINY
+            f = float(r.get("frequency_ghz", 0.0))
+            db = float(r.get("rcs_db", 10.0 * math.log10(lin)))
+            fh.write(",".join([g(f), g(r.get("theta_inc_deg", 0.0)), g(r.get("theta_scat_deg", 0.0)),
+                               g(lin), g(db), g(compute_dbke_from_linear(lin, f, "GHz")),
+                               g(r.get("rcs_amp_real", 0.0)), g(r.get("rcs_amp_imag", 0.0)),
+                               g(r.get("rcs_amp_phase_deg", 0.0)), source_path.replace(",", ";"),
+                               history.replace(",", ";")]) + "\n")
+    return os.path.abspath(out)

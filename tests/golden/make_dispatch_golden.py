@@ -12,7 +12,7 @@ Two kinds of fixture:
     recording stand-in of tests/dispatch_stub.py: what reaches the solver
     (meshes bit for bit, frequencies, formulation) and the result rows;
     the exception type of each malformed input; bor_az_el_grid on the
-    stand-in results; the .grim files its exporters write.
+    stand-in results; the .grim and dBke CSV files its exporters write.
   * end to end -- the reference's own FP64 solve (table_precision="double")
     of a small PEC sphere snapshot at two frequencies, VV and HH, and its
     radar-frame grid, for the GPU test of the same call.
@@ -92,6 +92,8 @@ def main():
         s["theta_inc_deg"] = 0.0 if i % 2 else 22.5
     rg.export_result_to_grim(bist, os.path.join(gdir, "bistatic"), history="h")
     rg.save_bor_az_el_grim(tilted, os.path.join(gdir, "azel"), source_path="s", history="h")
+    rg.export_result_to_dbke_csv(res["VV"], os.path.join(gdir, "sphere_vv"), source_path="a,b",
+                                 history="h")
 
     # end to end: the reference's FP64 solve of a small sphere snapshot
     sph = {"segments": [stub.segment("s", stub.arc(0.1, 0.0, 0.0, 180.0, 16),

@@ -181,10 +181,15 @@ def test_grim_files_match_reference(fx, tmp_path):
     written += G.export_result_to_grim(bist, str(tmp_path / "bistatic"), history="h")
     grid = D.bor_az_el_grid(gi["VV"], gi["HH"], gi["az"], gi["el"], 30.0, 20.0)
     written += G.save_bor_az_el_grim(grid, str(tmp_path / "azel"), source_path="s", history="h")
+    written.append(G.export_result_to_dbke_csv(gi["VV"], str(tmp_path / "sphere_vv"), source_path="a,b",
+                                               history="h"))
     assert sorted(os.path.basename(p) for p in written) == sorted(os.listdir(gdir))
     for p in written:
         name = os.path.basename(p)
-        if name.startswith("azel"):
+        if name.endswith(".csv"):
+            with open(p) as a, open(os.path.join(gdir, name)) as b:
+                assert a.read() == b.read()
+        elif name.startswith("azel"):
             # the grid itself agrees to 1e-12 (test above); the float32 files to rounding
             a, b = np.load(p), np.load(os.path.join(gdir, name))
             assert sorted(a.files) == sorted(b.files)
