@@ -1266,3 +1266,128 @@ def solve_bor_coated_pec(points_outer, points_core, freq_hz: float, thetas_deg, 
             "amp_vv": F[0].tolist(), "amp_hh": F[1].tolist(), "modes_used": modes_used,
             "n_unknowns": int(ntot), "formulation": "pmchwt-coated",
             "eps_r": complex(eps_r), "mu_r": complex(mu_r)}
+
+
+def solve_multiregion(surfaces, regions, freq_hz: float, thetas_deg, n_modes: Optional[int] = None,
+                      gauss_order: int = 4, mode_tol: float = 1e-6, near_factor: float = 2.0,
+                      near_order: int = 12, workers: int = 1) -> Dict:
+    """Multi-region PMCHWT for surfaces that meet no other surface off the
+    axis (bor_solver.py:1805-2073 without junctions).  surfaces: [(points,
+    is_conductor)]; regions: [{"medium": None | (eps, mu), "bounds":
+    [(surface, sigma)], "exterior": bool}].  Unknowns per surface: J (2Nn)
+    and, for interfaces, M' = M / eta0 (2Nn).  For every region r and ordered
+    pair (i, j) of its bounding surfaces, with s = sigma_i sigma_j and the
+    medium's operators: A[J_i, J_j] += s T, A[J_i, M_j] -= eta0 s P,
+    A[M_i, J_j] += eta0 s P, A[M_i, M_j] += (eta0 / eta_r)^2 s T.  The
+    exterior region's bounding surfaces carry the excitation and radiate."""
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    is_cond = [bool(c) for (_, c) in surfaces]
+    adj = [[] for _ in surfaces]
+    for ri, reg in enumerate(regions):
+        for (si, _) in reg["bounds"]:
+            adj[si].append(ri)
+    ext = next(ri for ri, r in enumerate(regions) if r.get("exterior"))
+    solv = {(si, ri): OracleSolver(pts, freq_hz, gauss_order, medium=regions[ri]["medium"])
+            for si, (pts, _) in enumerate(surfaces) for ri in adj[si]}
+    for si in range(len(surfaces)):
+        g = solv[(si, adj[si][0])].geo
+        if not (g.on_axis(0) and g.on_axis(g.Nn - 1)):
+            raise NotImplementedError("surfaces with off-axis ends (junctions)")
+    X = {(ri, si, sj): CrossOperators(solv[(si, ri)], solv[(sj, ri)], near_factor, near_order)
+         for ri, reg in enumerate(regions) for (si, _) in reg["bounds"] for (sj, _) in reg["bounds"]
+         if si != sj}
+    Nn = [solv[(si, adj[si][0])].geo.Nn for si in range(len(surfaces))]
+    offJ, offM, n_full = [], [], 0
+    for si in range(len(surfaces)):
+        offJ.append(n_full)
+        n_full += 2 * Nn[si]
+        offM.append(None if is_cond[si] else n_full)
+        n_full += 0 if is_cond[si] else 2 * Nn[si]
+    if n_modes is None:
+        k0 = 2.0 * math.pi * freq_hz / C0
+        rho = max(float(np.max(np.asarray(p, float)[:, 0])) for p, _ in surfaces)
+        n_modes = int(math.ceil(k0 * rho * max(float(np.max(np.abs(np.sin(np.radians(thetas))))), 0.05))) + 12
+    m_max = int(n_modes)
+    for (si, ri), s in solv.items():
+        s.prepare(m_max, efie=True, workers=workers,
+                  ibc_zs_pt=None if is_cond[si] else np.ones(s.geo.P))
+    F = np.zeros((2, len(thetas)), dtype=np.complex128)
+
+    def sl(off, si):
+        return slice(off, off + 2 * Nn[si])
+
+    def solve_am(am):
+        dF = np.zeros_like(F)
+        for m in ([0] if am == 0 else [am, -am]):
+            A = np.zeros((n_full, n_full), dtype=np.complex128)
+            for ri, reg in enumerate(regions):
+                eta2 = (ETA0 / solv[(reg["bounds"][0][0], ri)].eta) ** 2
+                for (si, gi) in reg["bounds"]:
+                    for (sj, gj) in reg["bounds"]:
+                        ss = gi * gj
+                        if si == sj:
+                            T = solv[(si, ri)].assemble_efie(m, m_max)
+                            P = None if is_cond[si] else solv[(si, ri)].pmchwt_P(m, m_max)
+                        else:
+                            T = X[(ri, si, sj)].assemble_T(m, m_max)
+                            P = X[(ri, si, sj)].assemble_P(m, m_max)
+                        A[sl(offJ[si], si), sl(offJ[sj], sj)] += ss * T
+                        if offM[sj] is not None:
+                            A[sl(offJ[si], si), sl(offM[sj], sj)] += -ETA0 * ss * P
+                        if offM[si] is not None:
+                            A[sl(offM[si], si), sl(offJ[sj], sj)] += ETA0 * ss * P
+                            if offM[sj] is not None:
+                                A[sl(offM[si], si), sl(offM[sj], sj)] += eta2 * ss * T
+            mask = np.zeros(n_full, dtype=bool)
+            for si in range(len(surfaces)):
+                bm = solv[(si, adj[si][0])].basis_mask(m)
+                mask[sl(offJ[si], si)] = bm
+                if offM[si] is not None:
+                    mask[sl(offM[si], si)] = bm
+            V = np.zeros((len(thetas), 2, n_full), dtype=np.complex128)
+            for (si, _) in regions[ext]["bounds"]:
+                s = solv[(si, ext)]
+                vv, hh = s.rhs_efie(m, thetas, "VV"), s.rhs_efie(m, thetas, "HH")
+                V[:, 0, sl(offJ[si], si)], V[:, 1, sl(offJ[si], si)] = vv, hh
+                if offM[si] is not None:             # eta0 <W, H_inc>
+                    V[:, 0, sl(offM[si], si)], V[:, 1, sl(offM[si], si)] = -hh, vv
+            B = V.transpose(2, 0, 1).reshape(n_full, 2 * len(thetas))[mask]
+            full = np.zeros((n_full, B.shape[1]), dtype=np.complex128)
+            full[mask] = np.linalg.solve(A[np.ix_(mask, mask)], B)
+            xs = full.T.reshape(len(thetas), 2, n_full)
+            for (si, _) in regions[ext]["bounds"]:
+                s = solv[(si, ext)]
+                ms = [None if offM[si] is None else ETA0 * xs[:, p, sl(offM[si], si)] for p in (0, 1)]
+                dF[0] += s.farfield(m, xs[:, 0, sl(offJ[si], si)], thetas, msol=ms[0])[0]
+                dF[1] += s.farfield(m, xs[:, 1, sl(offJ[si], si)], thetas, msol=ms[1])[1]
+        return dF
+
+    with ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        results = list(ex.map(solve_am, range(m_max + 1)))
+    modes_used, quiet = 0, 0
+    for am, dF in enumerate(results):
+        F += dF
+        modes_used = am
+        if float(np.max(np.abs(dF))) < mode_tol * max(float(np.max(np.abs(F))), 1e-30):
+            quiet += 1
+            if quiet >= 2:
+                break
+        else:
+            quiet = 0
+    return {"theta_deg": thetas.tolist(),
+            "sigma_vv": (4.0 * math.pi * np.abs(F[0]) ** 2).tolist(),
+            "sigma_hh": (4.0 * math.pi * np.abs(F[1]) ** 2).tolist(),
+            "amp_vv": F[0].tolist(), "amp_hh": F[1].tolist(), "modes_used": modes_used,
+            "n_unknowns": int(n_full)}
+
+
+def solve_bor_coated2_pec(points_outer, points_mid, points_core, freq_hz: float, thetas_deg,
+                          eps_inner: complex, mu_inner: complex, eps_outer: complex,
+                          mu_outer: complex, **kw) -> Dict:
+    """A PEC core under two full coating layers (bor_solver.py:2074-2098)."""
+    return solve_multiregion(
+        [(points_outer, False), (points_mid, False), (points_core, True)],
+        [{"medium": None, "bounds": [(0, +1)], "exterior": True},
+         {"medium": (eps_outer, mu_outer), "bounds": [(0, -1), (1, +1)]},
+         {"medium": (eps_inner, mu_inner), "bounds": [(1, -1), (2, +1)]}],
+        freq_hz, thetas_deg, **kw)

@@ -1,6 +1,7 @@
-"""Generate tests/golden/pmchwt_sphere_n24.npz and coated_sphere.npz by running
-the REFERENCE's PMCHWT paths (bor_solver.solve_bor_dielectric,
-BorCrossOperators, solve_bor_coated_pec).
+"""Generate tests/golden/pmchwt_sphere_n24.npz, coated_sphere.npz and
+layered_sphere.npz by running the REFERENCE's PMCHWT paths
+(bor_solver.solve_bor_dielectric, BorCrossOperators, solve_bor_coated_pec,
+solve_bor_coated2_pec).
 
 Run where the reference tree is mounted (default /root/reference, override
 with GHOST_REFERENCE_DIR):
@@ -14,6 +15,7 @@ lossy magnetic medium; the dielectric-sphere Mie backscatter of a few cases.
 Coated: a 12-segment PEC sphere (0.4 m) inside a 16-segment coating (0.5 m),
 ka = 1.5; the cross operators T and P between the two surfaces (both
 directions) for mode 1; a full solve; the coated-sphere Mie backscatter.
+Layered: a PEC sphere under two full layers (three closed surfaces), one solve.
 """
 
 import importlib
@@ -90,6 +92,22 @@ def coated():
                                   complex(u).imag] for b, a, fr, e, u in cases])
     out["mie_sigma"] = np.array([rmie.sigma_coated_pec_sphere(b, a, e, u, fr) for b, a, fr, e, u in cases])
     np.savez_compressed(os.path.join(HERE, "coated_sphere.npz"), **out)
+    layered()
+
+
+def layered():
+    """Two full layers over a PEC core (the multi-region system without junctions)."""
+    outer, mid, core = (bodies.sphere_generatrix(0.5, 14), bodies.sphere_generatrix(0.42, 12),
+                        bodies.sphere_generatrix(0.35, 10))
+    f = 3.0 * rk.C0 / (2.0 * math.pi)
+    thetas = np.arange(0.0, 180.0001, 60.0)
+    media = (2.0 - 0.1j, 1.0, 3.0 - 0.4j, 1.2)          # inner eps, mu; outer eps, mu
+    r = rs.solve_bor_coated2_pec(outer, mid, core, f, thetas, *media, n_modes=3, mode_tol=0.0,
+                                 workers=8)
+    np.savez_compressed(os.path.join(HERE, "layered_sphere.npz"), outer=outer, mid=mid, core=core,
+                        freq_hz=f, thetas=thetas, media=np.array(media, dtype=complex), m_max=3,
+                        amp_vv=np.array(r["amp_vv"]), amp_hh=np.array(r["amp_hh"]),
+                        n_unknowns=r["n_unknowns"])
 
 
 if __name__ == "__main__":

@@ -1,10 +1,13 @@
-"""The oracle's homogeneous-dielectric PMCHWT restatement against the reference.
+"""The oracle's PMCHWT restatements against the reference.
 
-Pinned to tests/golden/pmchwt_sphere_n24.npz (tests/golden/make_pmchwt_golden.py,
-the reference's own solve_bor_dielectric path): the interior EFIE operator in
-a lossy medium (complex k), the PMCHWT operators P of both media, full solves
-for lossy, lossless and lossy magnetic spheres, and the dielectric-sphere Mie
-series.  These are the operators a GPU PMCHWT path would be checked against.
+Pinned to fixtures made by tests/golden/make_pmchwt_golden.py with the
+reference's own solvers: the interior EFIE operator in a lossy medium
+(complex k), the PMCHWT operators P of both media and full solves for lossy,
+lossless and lossy magnetic spheres (pmchwt_sphere_n24.npz); the cross-surface
+T and P and the solve of a coated PEC sphere (coated_sphere.npz); a PEC
+sphere under two layers through the multi-region system (layered_sphere.npz);
+the dielectric- and coated-sphere Mie series.  These are the operators a GPU
+PMCHWT path would be checked against.
 """
 import numpy as np
 import pytest
@@ -128,3 +131,14 @@ def test_cross_operators_reject_junctions(oracle):
     sa, sb = oracle.OracleSolver(a, 3e8), oracle.OracleSolver(b, 3e8)
     with pytest.raises(NotImplementedError):
         oracle.CrossOperators(sa, sb)
+
+
+def test_two_layer_coated_pec_matches_reference(oracle):
+    """The multi-region system (no junctions): a PEC core under two full
+    layers, against the reference's solve_bor_coated2_pec."""
+    L = load_golden("layered_sphere")
+    r = oracle.solve_bor_coated2_pec(L["outer"], L["mid"], L["core"], float(L["freq_hz"]), L["thetas"],
+                                     *L["media"], n_modes=int(L["m_max"]), mode_tol=0.0, workers=4)
+    assert r["n_unknowns"] == int(L["n_unknowns"])
+    assert _rel(r["amp_vv"], L["amp_vv"]) < 1e-10
+    assert _rel(r["amp_hh"], L["amp_hh"]) < 1e-10
