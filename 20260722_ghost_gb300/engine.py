@@ -153,6 +153,10 @@ class BorGpuProblem:
         self.tensor_cores = True     # FP32 LU / solve / residual updates on tcgen05 (3xTF32)
         self.update_ws_bytes = 4 << 30   # scratch bound of one residual-update GEMM launch
         self.exact_residual = True       # first residual with exact products (bf16 Ozaki slices)
+        # FP32 far fill with the azimuth transform on the bf16 tensor cores (exact
+        # digit products); False selects the SIMT FP32 transform of far_fill.cu
+        self.far_tc = True
+        self._far_tc_ws = None
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
@@ -176,8 +180,29 @@ class BorGpuProblem:
                 + self.update_ws_bytes)
 
     # -- stages -----------------------------------------------------------
+    def _far_tc_work(self, stream: int):
+        """Digit planes of the DCT table for the tensor-core far fill (built once
+        per problem on the device) and the fill's status word."""
+        if self._far_tc_ws is None:
+            lib = nat.load()
+            nbytes = int(lib.ghost_bor_far_efie_tc_workspace(self.m_max, self.n_xi))
+            ws = self.torch.empty(nbytes, dtype=self.torch.uint8, device=self.device)
+            nat.call("ghost_bor_far_efie_tc_tables", self.m_max, self.n_xi, nat.ptr(self.d_dct),
+                     nat.ptr(self.d_sin2), nat.ptr(ws), nbytes, stream)
+            self._far_tc_ws = ws
+        return self._far_tc_ws
+
+    def check_far_status(self):
+        if self._far_tc_ws is not None and int(self._far_tc_ws[:4].view(self.torch.int32)[0]) != 0:
+            raise RuntimeError("a bounded tensor-core wait gave up in the far fill")
+
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
         ld = Z.shape[-1]
+        if precision == nat.F32 and self.far_tc:
+            ws = self._far_tc_work(stream)
+            nat.call("ghost_bor_far_efie_tc", self.N, self.m_max, self.n_xi, self.k, scale.real, scale.imag,
+                     nat.ptr(self.d_geo), nat.ptr(ws), ws.numel(), nat.ptr(Z), ld, Z.stride(0), stream)
+            return
         nat.call("ghost_bor_far_efie_masked", precision, self.N, self.m_max, self.n_xi, self.k,
                  scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_dct),
                  nat.ptr(self.d_sin2), nat.ptr(Z), ld, Z.stride(0), 0,
@@ -494,6 +519,7 @@ class BorGpuProblem:
         info_h = info.cpu().numpy()
         torch.cuda.synchronize()
         self.check_near_status()
+        self.check_far_status()
         names = list(ev)
         tm = {f"{b}_s": ev[a].elapsed_time(ev[b]) / 1e3 for a, b in zip(names[:-1], names[1:])}
         tm["gpu_total_s"] = ev[names[0]].elapsed_time(ev[names[-1]]) / 1e3

@@ -115,6 +115,30 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
                               void *Z, long long ldz, long long mode_stride,
                               const unsigned char *elem_mask, const float *dct32, void *stream);
 
+/* Tensor-core form of the FP32 EFIE far fill: the same sampling, contraction,
+ * mode combination and accumulation as ghost_bor_far_efie(GHOST_BOR_F32, ...),
+ * with the even DCT over the azimuth samples computed on the bf16 tensor cores
+ * (tcgen05) from four balanced 8-bit digits of the samples and of the table:
+ * the level-0 digit products accumulate exactly, the transform carries
+ * ~2^-30 of each Gauss-point pair's bound |g| <= 1/|Delta| instead of the
+ * FP32 table and sums of the SIMT transform.  Z is complex double; the
+ * contribution is ADDED.
+ *   work  ghost_bor_far_efie_tc_workspace(m_max, nxi) bytes, 256-byte
+ *         aligned, prepared once per (m_max, nxi, table) by
+ *         ghost_bor_far_efie_tc_tables from the `dct` / `sin2` tables of
+ *         ghost_bor_far_efie; its first int is a status word, set to 1 if a
+ *         bounded pipeline wait gave up (the launch is then incomplete).
+ * Returns GHOST_BOR_EUNSUPPORTED when nxi/2 + 1 exceeds 2^17 samples.
+ * Replaces StreamingFarBlocks._build_range + efie_blocks
+ * (bor_streaming.py:220-268, 320-376, 388-407) like ghost_bor_far_efie. */
+long long ghost_bor_far_efie_tc_workspace(int m_max, int nxi);
+int ghost_bor_far_efie_tc_tables(int m_max, int nxi, const double *dct, const double *sin2,
+                                 void *work, long long work_bytes, void *stream);
+int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k,
+                          double scale_re, double scale_im, const double *geo,
+                          void *work, long long work_bytes,
+                          void *Z, long long ldz, long long mode_stride, void *stream);
+
 /* ------------------------------------------------------------------------
  * FP64-class near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
  * the graded-cell + sinh-core + Gauss-tail quadrature of the reference.

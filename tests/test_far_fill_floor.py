@@ -9,7 +9,9 @@ FP64 (oracle), and compares the monostatic far field with the all-FP64 sweep.
 It pins the finding that the FP32 rounding of the table, not of the samples or
 of the sums, sets the floor: an FP64 table cuts the error ~3x, an exact
 transform of the FP32 samples ~10x, and an exact transform on four base-256
-digits of each operand (the split a tensor-core transform would use) as much.
+digits of each operand (the split of the tensor-core fill, far_fill_tc.cu) as
+much, provided that each of its truncating FP32 accumulators holds digit
+products of one grid only (level 0 | level 1 | levels 2-3).
 """
 import importlib
 import math
@@ -43,6 +45,57 @@ def kahan_dct(gr, gi, table, h):
             cmp = ((t - acc).astype(f32) - y).astype(f32)
             acc = t
         out.append(acc.astype(np.float64) - cmp)
+    return out[0] + 1j * out[1]
+
+
+def _digits(t, nd=4):
+    """Balanced base-256 digits of t (exact FP64 arithmetic), scaled by 2^-8s."""
+    out = []
+    w = 1.0
+    for _ in range(nd):
+        d = np.rint(t)
+        out.append(d * w)
+        t = (t - d) * 256.0
+        w *= 2.0 ** -8
+    return out
+
+
+def _add_rz(acc, x):
+    """acc + x rounded toward zero to FP32 (a truncating accumulator)."""
+    s = acc.astype(np.float64) + x
+    r = s.astype(f32)
+    over = np.abs(r.astype(np.float64)) > np.abs(s)
+    r[over] = np.nextafter(r[over], f32(0))
+    return r
+
+
+TC_GROUPS = ([(0, 0)], [(0, 1), (1, 0)], [(0, 2), (1, 1), (2, 0), (0, 3), (1, 2), (2, 1), (3, 0)])
+
+
+def tc_dct(gr, gi, d2, table, h, bA=7, groups=TC_GROUPS):
+    """The transform of far_fill_tc.cu: FP32 samples on the grid 2^(bA - e_r) of
+    the row bound |g| <= 1/|Delta| and the table on 2^sT (largest entry 128),
+    four digits each; each accumulator (level 0 | level 1 | levels 2 and 3)
+    adds its digit products one 16-sample MMA step at a time in FP32 rounded
+    toward zero (the worst case of a tensor core's accumulation)."""
+    with np.errstate(divide="ignore"):                 # near pairs are zeroed afterwards
+        v = 1.0 / np.sqrt(d2) * (1.0 + 2.0 ** -12)
+    e = np.frexp(v)[1][..., None]                      # v < 2^e
+    sc = np.ldexp(1.0, bA - e)
+    sT = 7 - (np.frexp(np.max(np.abs(table)))[1] - 1)
+    T = _digits(np.ldexp(table, sT))
+    out = []
+    for g in (gr, gi):
+        A = _digits(g.astype(np.float64) * sc)
+        tot = np.zeros(g.shape[:2] + (table.shape[1],))
+        for grp in groups:
+            acc = np.zeros(tot.shape, f32)
+            for k0 in range(0, h + 1, 16):
+                ks = slice(k0, min(k0 + 16, h + 1))
+                for sa, tb in grp:
+                    acc = _add_rz(acc, np.einsum("rpj,jn->rpn", A[sa][..., ks], T[tb][ks]))
+            tot += acc.astype(np.float64)
+        out.append(tot * np.ldexp(1.0, e - bA - sT))
     return out[0] + 1j * out[1]
 
 
@@ -87,6 +140,8 @@ class _Emulated(O.OracleSolver):
                     fx = np.frexp(1.0 / h)[1]
                     tq = np.rint(dct / 2.0 ** fx * q) * 2.0 ** fx / q
                     Gn = np.einsum("rpj,jn->rpn", gq, tq)
+                elif self.variant == "tc":          # the tensor-core fill (far_fill_tc.cu)
+                    Gn = tc_dct(gr, gi, d2, dct, h)
                 else:                               # FP32 samples, exact transform
                     Gn = np.einsum("rpj,jn->rpn", gr.astype(np.float64) + 1j * gi.astype(np.float64), dct)
             self._zero_near(Gn, e0, e1)
@@ -121,7 +176,7 @@ def test_fp32_dct_table_sets_the_far_fill_floor():
     M = 8
     ref = _far_field(pts, freq, thetas, M, "fp64")
     err = {}
-    for v in ("gpu", "table64", "exact", "digits4"):
+    for v in ("gpu", "table64", "exact", "digits4", "tc"):
         F = _far_field(pts, freq, thetas, M, v)
         err[v] = float(np.max(np.abs(F - ref)) / np.max(np.abs(ref)))
     assert 1e-9 < err["gpu"] < 1e-7, err               # the FP32 floor (C2 on the GPU: 4.2e-8)
@@ -129,3 +184,5 @@ def test_fp32_dct_table_sets_the_far_fill_floor():
     assert err["exact"] < err["gpu"] / 5.0, err
     # four digits per operand keep the exact transform's accuracy
     assert err["digits4"] < 1.2 * err["exact"], err
+    # and so does the tensor-core fill's split (exact level 0, FP32 level >= 1)
+    assert err["tc"] < 1.2 * err["exact"], err

@@ -98,6 +98,37 @@ def test_far_fill_wide_order_rows(pkg, torch):
         assert err < 2e-5 * top and err < 1e-3 * scale, (m, err / scale)
 
 
+@pytest.mark.parametrize("m_max,n_seg,k", [(20, 60, 20.0), (50, 80, 40.0), (90, 120, 60.0), (200, 60, 60.0)])
+def test_far_fill_tensor_cores(pkg, torch, m_max, n_seg, k):
+    """The tensor-core FP32 far fill (exact digit transform) against the FP64
+    fill on every mode: tiles of 32, 64 and 128 orders, one and two launch
+    rows (|m| = 200), 129..513 azimuth samples; it is far closer to FP64 than
+    the SIMT FP32 transform."""
+    eng = pkg.engine
+    nat = pkg._native
+    pts = pkg.bodies.cone_sphere_generatrix(0.5, 15.0, n_seg)
+    prob = eng.BorGpuProblem(pts, k * 299792458.0 / (2 * math.pi), np.array([0.0, 90.0]), m_max=m_max)
+    Mb, n = prob.m_max + 1, prob.n
+    st = nat.stream_handle()
+    Z64 = torch.zeros((Mb, n, n), dtype=torch.complex128, device="cuda")
+    Ztc = torch.zeros_like(Z64)
+    Zs = torch.zeros_like(Z64)
+    prob.fill_far(Z64, nat.F64, 1.0 + 0.0j, st)
+    prob.far_tc = True
+    prob.fill_far(Ztc, nat.F32, 1.0 + 0.0j, st)
+    prob.far_tc = False
+    prob.fill_far(Zs, nat.F32, 1.0 + 0.0j, st)
+    torch.cuda.synchronize()
+    prob.check_far_status()
+    top = Z64.abs().max().item()
+    e_tc = (Ztc - Z64).abs().amax(dim=(1, 2)).cpu().numpy() / top
+    e_simt = (Zs - Z64).abs().amax(dim=(1, 2)).cpu().numpy() / top
+    print(f"\nM={m_max} N={n_seg} k={k} n_xi={prob.n_xi}: max rel err tc {e_tc.max():.3e} simt {e_simt.max():.3e}")
+    assert np.all(np.isfinite(e_tc))
+    assert e_tc.max() < 2e-6, e_tc
+    assert e_tc.max() < e_simt.max(), (e_tc.max(), e_simt.max())
+
+
 @pytest.mark.parametrize("name", ["sphere_n24", "conesphere_n40", "openshell_n20"])
 def test_full_operator_and_excitation(pkg, name):
     """assemble_mode (far + near), rhs_mode and farfield_mode vs the reference goldens."""
