@@ -8,8 +8,13 @@
 //
 // Splitting: every row i of A gets a power-of-two scale 2^e_i >= its largest
 // magnitude, every complex column j of X a scale 2^f_j; each scaled value u
-// (|u| < 1) is written as q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31 with
-// integers |q_s| <= 128 (balanced base-256 digits), which bf16 holds exactly.
+// (|u| < 1) is written as q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31 (+ q5 2^-39
+// for A) with integers |q_s| <= 128 (balanced base-256 digits), which bf16
+// holds exactly.  A takes five digits: most entries of a row are far below
+// its largest (the near-diagonal blocks), and with four the truncation,
+// 2^-32 of the row scale, left ~2.6e-8 of ||B|| in the residual of the
+// 1200-segment cone-sphere -- the floor of the refined far field; four digits
+// hold the FP32 solution's entries within 2^-8 of their column scale exactly.
 // A product q_s q_t (|.| <= 2^14) is exact in the FP32 accumulator, and so is
 // any sum of them below 2^24: the slice pairs with the same s + t share one
 // TMEM accumulator ("level" L = s + t - 2, scale 2^(-14 - 8 L)), at most four
@@ -17,9 +22,9 @@
 // (192 * 4 * 2^14 < 2^24).  After each chunk the five levels are folded into
 // double-float (hi, lo) register accumulators; pairs with s + t > 6 are
 // dropped (below 2^-40 of the row and column scales).  The result carries
-// ~2^-32 of the row / column scales (the truncation of the fourth digit) --
-// far below the FP32-product floor (~2^-24) of a split-word SIMT residual --
-// and runs at tensor-core rate.
+// ~2^-40 of the row scales and ~2^-32 of the column scales -- far below the
+// FP32-product floor (~2^-24) of a split-word SIMT residual -- and runs at
+// tensor-core rate.
 //
 // The near band is added to Z_far before the split (A = Z_far + band), so the
 // epilogue only forms R = B - P in FP64 and zeroes the masked rows.
@@ -31,7 +36,8 @@
 namespace gb {
 namespace {
 
-constexpr int XS = 4;                    // slices per operand
+constexpr int XSA = 5;                   // slices of A (Z_far rows)
+constexpr int XS = 4;                    // slices of Bt (the FP32 solution: 4 slices hold it exactly)
 constexpr int XBM = 128;                 // tile rows
 constexpr int XBN = 64;                  // tile real columns (32 complex rhs)
 constexpr int XBK = 64;                  // real K per stage (64 bf16 = one 128-byte swizzle row)
@@ -44,7 +50,7 @@ constexpr int XA_TILE = XBM * XBK;       // bf16 elements
 constexpr int XB_TILE = XBN * XBK;
 
 struct __align__(1024) XSmem {
-    __nv_bfloat16 a[2][XS][XA_TILE];     // 2 stages x 4 slices x 16 KB
+    __nv_bfloat16 a[2][XSA][XA_TILE];    // 2 stages x 5 slices x 16 KB
     __nv_bfloat16 b[2][XS][XB_TILE];     // 2 stages x 4 slices x 8 KB
     unsigned long long full[2];
     unsigned long long mma[2];
@@ -76,20 +82,21 @@ __device__ __forceinline__ int scale_exp(double m)
 //   v / 2^e ~ q1 2^-7 + q2 2^-15 + q3 2^-23 + q4 2^-31,  |q_s| <= 128,
 // by integer arithmetic on the IEEE bits: W = round(v 2^(31 - e)) (|W| <= 2^31)
 // is split into balanced base-256 digits with arithmetic shifts.
-__device__ __forceinline__ void digits(double v, int e, float (&q)[XS])
+template <int NS>
+__device__ __forceinline__ void digits(double v, int e, float (&q)[NS])
 {
     const long long bits = __double_as_longlong(v);
     const int E = (int)((bits >> 52) & 0x7ff);
     long long W = 0;
     if (E != 0) {                                    // zero and subnormals -> 0 (below 2^-1022)
         const long long m = (bits & 0xfffffffffffffLL) | 0x10000000000000LL;
-        const int sh = (E - 1075) + 31 - e;          // v = m 2^(E - 1075)
+        const int sh = (E - 1075) + (8 * NS - 1) - e;  // v = m 2^(E - 1075)
         if (sh >= 0) W = m << sh;
         else if (sh > -64) W = (m + (1LL << (-sh - 1))) >> (-sh);
         if (bits < 0) W = -W;
     }
 #pragma unroll
-    for (int s = XS - 1; s >= 1; --s) {
+    for (int s = NS - 1; s >= 1; --s) {
         const long long t = (W + 128) >> 8;          // floor((W + 128) / 256)
         q[s] = (float)(int)(W - (t << 8));
         W = t;
@@ -154,12 +161,12 @@ __global__ void slice_a_kernel(int batch, int n, int Nn, int Kp, const double2 *
         const double2 v = (k < n) ? cadd(Z[(size_t)b * sz + (size_t)i * ldz + k], band_at(band, b, Nn, i, k))
                                   : make_double2(0.0, 0.0);
         const int e = ex[bi];
-        float qr[XS], qi[XS];
+        float qr[XSA], qi[XSA];
         digits(v.x, e, qr);
         digits(v.y, e, qi);
         const size_t o = (size_t)bi * Kp + 2 * (size_t)k;
 #pragma unroll
-        for (int s = 0; s < XS; ++s) {
+        for (int s = 0; s < XSA; ++s) {
             __nv_bfloat162 w;
             w.x = __float2bfloat16_rn(qr[s]);
             w.y = __float2bfloat16_rn(qi[s]);
@@ -231,7 +238,7 @@ __device__ __forceinline__ bool row_masked(const int *mr, int r)
 }
 
 struct XMaps {
-    CUtensorMap a[XS];
+    CUtensorMap a[XSA];
     CUtensorMap b[XS];
 };
 
@@ -263,7 +270,7 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s.tmem_base;
-    const uint32_t stage_bytes = (uint32_t)(XS * (XA_TILE + XB_TILE) * 2);
+    const uint32_t stage_bytes = (uint32_t)((XSA * XA_TILE + XS * XB_TILE) * 2);
 
     // producer state (thread 0 only)
     uint32_t full_phase[2] = {0, 0}, mma_phase[2] = {0, 0};
@@ -273,10 +280,9 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
         const int st = ks & 1;
         mbar_expect_tx(&s.full[st], stage_bytes);
 #pragma unroll
-        for (int q = 0; q < XS; ++q) {
-            tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
-            tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
-        }
+        for (int q = 0; q < XSA; ++q) tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
+#pragma unroll
+        for (int q = 0; q < XS; ++q) tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
     };
     auto wait_mma = [&](int st) {
         if (!pending[st]) return;
@@ -307,7 +313,8 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
 #pragma unroll
                 for (int L = 0; L < XLEV; ++L) {
                     const int lev = L + 2;
-                    const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XS ? lev - 1 : XS;
+                    // A slice sa (1..XSA) with Bt slice lev - sa (1..XS)
+                    const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XSA ? lev - 1 : XSA;
                     for (int sa = s_lo; sa <= s_hi; ++sa) {
                         const int sb = lev - sa;
                         const uint32_t ab = smem_u32(s.a[st][sa - 1]), bb = smem_u32(s.b[st][sb - 1]);
@@ -442,7 +449,7 @@ extern "C" long long ghost_bor_residual_exact_workspace(int batch, int n, int nr
     using namespace gb;
     const long long Kp = kp_of(n);
     auto up = [](long long x) { return (x + 255) / 256 * 256; };
-    return 256 + up(4LL * batch * n) + up(4LL * batch * nrhs) + up(2LL * XS * batch * n * Kp) +
+    return 256 + up(4LL * batch * n) + up(4LL * batch * nrhs) + up(2LL * XSA * batch * n * Kp) +
            up(2LL * XS * batch * 2 * nrhs * Kp);
 }
 
@@ -466,7 +473,7 @@ extern "C" int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
     int *ex = reinterpret_cast<int *>(w + 256);
     int *fx = reinterpret_cast<int *>(w + 256 + up(4LL * batch * n));
     __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(w + 256 + up(4LL * batch * n) + up(4LL * batch * nrhs));
-    __nv_bfloat16 *Bs = As + up(2LL * XS * batch * n * Kp) / 2;
+    __nv_bfloat16 *Bs = As + up(2LL * XSA * batch * n * Kp) / 2;
     const size_t aplane = (size_t)batch * n * Kp, bplane = (size_t)batch * 2 * nrhs * Kp;
 
     if (cudaMemsetAsync(errp, 0, sizeof(int), st) != cudaSuccess ||
@@ -492,9 +499,9 @@ extern "C" int ghost_bor_residual_exact(int batch, int n, int nrhs, int Nn,
         if ((rc = check_launch("residual_exact: slice B"))) return rc;
     }
     XMaps maps;
-    for (int q = 0; q < XS; ++q) {
+    for (int q = 0; q < XSA; ++q) {
         if (!make_map_bf16(&maps.a[q], As + q * aplane, n, Kp, batch, XBM) ||
-            !make_map_bf16(&maps.b[q], Bs + q * bplane, 2 * nrhs, Kp, batch, XBN)) {
+            (q < XS && !make_map_bf16(&maps.b[q], Bs + q * bplane, 2 * nrhs, Kp, batch, XBN))) {
             set_last_error("residual_exact: cuTensorMapEncodeTiled failed");
             return GHOST_BOR_ECUDA;
         }

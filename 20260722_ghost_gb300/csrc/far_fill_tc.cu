@@ -16,39 +16,37 @@
 //   row r (one point pair, re or im): g 2^(bA - e_r) = d0 + d1 2^-8 + d2 2^-16 + d3 2^-24
 //   table:                            T 2^sT         = t0 + t1 2^-8 + t2 2^-16 + t3 2^-24
 //
-// |d0| <= 2^bA, |t0| <= 128, |d1..d3|, |t1..t3| <= 128.  e_r is the analytic
-// bound of the row, |g| = 1/R <= 1/|Delta| (R^2 = Delta^2 + 4 rho rho'
-// sin^2(xi/2)); sT scales the table's largest entry to 128.  Every digit, with
-// its 2^-8s weight, is exact in bf16, and every digit product is exact in
-// FP32.  The tensor core's FP32 accumulation is not rounded to nearest, so
-// each accumulator holds only terms on one grid:
-//   ACC0  level 0 (d0 t0): integers whose sum over all samples stays below
-//         2^24 (bA is chosen from the number of samples so that
-//         K 2^bA 128 <= 2^24): exact;
-//   ACC1  level 1 (d0 t1, d1 t0): integers of 2^-8, exact while the partial
-//         sums stay below 2^16 (a random walk of digit products; beyond that
-//         the error is ~2^-32 of the row bound);
-//   ACC2  levels 2 and 3 (seven products, ~2^-16 of ACC0): its rounding is
-//         below 2^-40 of the row bound per step.
-// The products with s + t > 3 are dropped (< 2^-32).  Mixing levels 1..3 in
-// one accumulator costs ~60x in accuracy at 1025 samples (CPU emulation with
-// truncating adds).  The epilogue forms ACC0 + ACC1 + ACC2 as a double-float
-// and scales it back.
+// with integer digits |d0| <= 2^bA, |t0| <= 128, |d1..d3|, |t1..t3| <= 128 (bf16
+// holds them exactly, and every digit product exactly in FP32).  e_r is the
+// analytic bound of the row, |g| = 1/R <= 1/|Delta| (R^2 = Delta^2 + 4 rho rho'
+// sin^2(xi/2)); sT scales the table's largest entry to 128.  The samples come
+// from a sampler ~50x more accurate than FP32 (TcGreen below) as two FP32
+// words, and the digit split takes both.  The tensor core's FP32
+// accumulation is not rounded to nearest, so each digit level s + t = L has
+// an accumulator of its own, ACC_L, which adds integers only:
+//   ACC0  (d0 t0): its sums stay below 2^24 (bA is chosen from the number of
+//         samples K so that K 2^bA 128 <= 2^24): exact;
+//   ACC1..ACC3: sums of 2..4 products per sample, random walks far below 2^24
+//         (where one does reach it, its rounding is ~2^-32 of the row bound).
+// The products with s + t > 3 are dropped (< 2^-32 of the row bound).  One
+// accumulator for levels 1..3 costs ~60x in accuracy at 1025 samples (CPU
+// emulation with truncating adds).  The epilogue forms
+// ACC0 + 2^-8 ACC1 + 2^-16 ACC2 + 2^-24 ACC3 as a double-float and scales it.
 //
 // Kernel structure (one CTA per SM, persistent over tiles; a tile is one test
 // element e x four source elements f0..f0+3, i.e. 64 Gauss-point pairs, for
 // one range of orders):
-//   warps 6..13  producers: sample g (FP32, double-float phase) for 8
+//   warps 6..13  producers: sample g (TcGreen, FP32 word pairs) for 8
 //                consecutive samples of one point pair, split them into the
 //                four digit planes and store them into the A stage in the
 //                UMMA K-major 64-byte-swizzled layout (32 samples per stage);
 //   warp 4       TMA: the table digit planes of the stage (B operand);
-//   warp 5       MMA: 10 tcgen05.mma kind::f16 per 16 samples into ACC0..2
+//   warp 5       MMA: 10 tcgen05.mma kind::f16 per 16 samples into ACC0..3
 //                (for tiles of up to 64 orders two TMEM accumulator sets, so a
 //                tile's epilogue overlaps the next tile's transform; one set
-//                of 3 x 128 columns for 128-order tiles);
+//                of 4 x 128 columns for 128-order tiles);
 //   warps 0..3   epilogue, warp w = element pair w: TMEM -> double-float
-//                orders in shared memory (32 orders per chunk), then the
+//                orders in shared memory (16 orders per chunk), then the
 //                double-float contraction with the Galerkin weights, the
 //                mode combination and the FP64 atomic accumulation into Z of
 //                far_fill.cu.
@@ -82,6 +80,7 @@ template <int N> struct __align__(1024) TcSmem {
     float4 zl[NEPI][RING * 2 * 16];      // per-warp mode-local blocks of every (order, orientation, block, a b)
     float4 p11[NEPI][RING * 2 * 4];      // per-warp 11-primitive of every (order, orientation, a b)
     float2 w[NEPI][2][24];               // test / source element weights (double-float)
+    float4 sc_tab[kDfTabN];              // sin, cos (j pi / 128) as double-float words
     unsigned long long a_full[2], b_full[2], st_empty[2], t_full[2], t_empty[2], drain;
     uint32_t tmem_base;
     int failed;
@@ -127,23 +126,95 @@ __device__ __forceinline__ int row_exp(double d2)
     return ilogb(v) + 1;
 }
 
-__device__ __forceinline__ float rnd_int(float x)        // round to nearest integer, |x| < 2^22
+// Green's function samples g = exp(-j k R) / R (the 1/(4 pi) is in the table),
+// each of re, im as an unnormalised pair hi + lo accurate to ~3e-9 of |g|
+// (FP32 sincosf and rcp give ~1e-7, the floor of the FP32 fill):
+//   R^2 = d^2 + a^2 s2 in double-float; R = r + rl and 1/R = y (1 + eps) from one
+//   rsqrt and first-order corrections; k R in double-float, reduced to t in
+//   [-pi, pi] by the three-word 2 pi of samplers.cuh;
+//   sin and cos of t by Tang's table-driven method: t = j pi/128 + r,
+//   |r| <= pi/256, with sin, cos (j pi/128) as double-float words (df_math.cuh
+//   table), sin r = r - r^3/6 (next term < 2.5e-12) and
+//   cos r - 1 = -r^2/2 + r^4/24 (next term < 5e-15); the table word carries the
+//   value and one FP32 correction the rest, so the error is a few FP32
+//   roundings of |correction| <= 0.013.
+struct TcGreen {
+    float d2h, d2l, a2h, a2l, kh, kl;
+    __device__ void init(double d2, double a2, double k) {
+        d2h = (float)d2; d2l = (float)(d2 - (double)d2h);
+        a2h = (float)a2; a2l = (float)(a2 - (double)a2h);
+        kh = (float)k;   kl = (float)(k - (double)kh);
+    }
+    // g as (re.hi, re.lo, im.hi, im.lo)
+    __device__ __forceinline__ float4 operator()(float2 s2, const float4 *__restrict__ tab) const {
+        const float p = a2h * s2.x;
+        const float pe = fmaf(a2h, s2.x, -p);
+        const float t = d2h + p;
+        const float bb = t - d2h;
+        const float te = (d2h - (t - bb)) + (p - bb);
+        const float lo = te + pe + fmaf(a2h, s2.y, a2l * s2.x) + d2l;
+        const float R2 = t + lo;
+        const float R2l = lo - (R2 - t);
+        const float y = rsqrtf(R2);
+        const float r = R2 * y;
+        const float rl = 0.5f * (fmaf(-r, r, R2) + R2l) * y;
+        const float eps = fmaf(-r, y, 1.0f) - rl * y;        // 1/R = y (1 + eps)
+        const float ph = kh * r;
+        const float phl = fmaf(kh, r, -ph) + fmaf(kh, rl, kl * r);
+        const float q = rintf(ph * kInvTwoPi);
+        const float t1 = fmaf(-q, kTwoPiA, ph);             // exact
+        const float qb = -q * kTwoPiB;                      // exact
+        const float t2 = t1 + qb;
+        const float tb = t2 - t1;
+        const float t2e = (t1 - (t2 - tb)) + (qb - tb);
+        const float dt = fmaf(-q, kTwoPiC, phl) + t2e;
+        const float jf = fminf(128.0f, fmaxf(-128.0f, rintf(t2 * kDf128ByPi)));
+        const float r0 = fmaf(-jf, kDfPiB128_1, t2);        // exact
+        const float rv = fmaf(-jf, kDfPiB128_2, r0 + dt);
+        const float r2 = rv * rv;
+        const float sr = fmaf(rv * r2, -1.0f / 6.0f, rv);   // sin r
+        const float c1 = r2 * fmaf(r2, 1.0f / 24.0f, -0.5f); // cos r - 1
+        const float4 T = tab[(int)jf + 128];                 // sin hi, sin lo, cos hi, cos lo
+        const float s_lo = fmaf(T.z, sr, fmaf(T.x, c1, T.y)) + T.w * sr;
+        const float c_lo = fmaf(-T.x, sr, fmaf(T.z, c1, T.w)) - T.y * sr;
+        const float yl = y * eps, ya = y + yl;
+        const float gr = y * T.z;
+        const float grl = fmaf(y, T.z, -gr) + fmaf(ya, c_lo, yl * T.z);
+        const float gi = y * T.x;
+        const float gil = fmaf(y, T.x, -gi) + fmaf(ya, s_lo, yl * T.x);
+        return make_float4(gr, grl, -gi, -gil);
+    }
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float2 d)
 {
-    return (x + 12582912.0f) - 12582912.0f;
+    const __nv_bfloat162 q = __floats2bfloat162_rn(d.x, d.y);
+    return *reinterpret_cast<const uint32_t *>(&q);
 }
 
-// four digit planes (scaled by 2^-8s) of a pair of values on the grid 2^(bA - e)
-__device__ __forceinline__ void split4(float2 v, float sc, uint32_t (&out)[ND])
+// four balanced base-256 digits (integers, |d| <= 128) of two values hi + lo on
+// the grid 2^(bA - e): packed FP32 pairs, rounding by the 1.5 * 2^23 shift.  The
+// sampler's pairs are not normalised (|lo| reaches ~1% of |g|, and hi ~ 0 where
+// the table's cosine or sine vanishes), so a two-sum normalises them first;
+// the remainder after the top digit then takes the error word with one
+// rounding (~2^-25 of a digit)
+__device__ __forceinline__ void split4(float2 hi, float2 lo, float sc, uint32_t (&out)[ND])
 {
-    float2 t = make_float2(v.x * sc, v.y * sc);
-    float w = 1.0f;
+    const float2 scv = make_float2(sc, sc), rn = make_float2(12582912.0f, 12582912.0f),
+                 b256 = make_float2(256.0f, 256.0f);
+    const float2 th = p2_mul(hi, scv), tl = p2_mul(lo, scv);
+    float2 t = p2_add(th, tl);
+    const float2 bb = p2_sub(t, th);
+    const float2 te = p2_add(p2_sub(th, p2_sub(t, bb)), p2_sub(tl, bb));
+    float2 d = p2_sub(p2_add(t, rn), rn);
+    out[0] = pack_bf16(d);
+    t = p2_add(p2_sub(t, d), te);
 #pragma unroll
-    for (int s = 0; s < ND; ++s) {
-        const float2 d = make_float2(rnd_int(t.x), rnd_int(t.y));
-        const __nv_bfloat162 q = __floats2bfloat162_rn(d.x * w, d.y * w);
-        out[s] = *reinterpret_cast<const uint32_t *>(&q);
-        t = make_float2((t.x - d.x) * 256.0f, (t.y - d.y) * 256.0f);
-        w *= 0x1p-8f;
+    for (int s = 1; s < ND; ++s) {
+        t = p2_mul(t, b256);
+        d = p2_sub(p2_add(t, rn), rn);
+        out[s] = pack_bf16(d);
+        t = p2_sub(t, d);
     }
 }
 
@@ -196,14 +267,15 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
     const int nrows = (M + 1 + (N - 2) - 1) / (N - 2);
     const long long ntiles = (long long)nrows * NE * fgroups;
     const int nst = (h + 1 + TK - 1) / TK;            // stages per tile
-    constexpr int NSET = (6 * N <= 512) ? 2 : 1;       // accumulator sets (ACC0, ACC1, ACC2) in TMEM
-    constexpr uint32_t TMEM_COLS = (NSET * 3 * N <= 256) ? 256 : 512;
+    constexpr int NSET = (8 * N <= 512) ? 2 : 1;       // accumulator sets (ACC0..ACC3) in TMEM
+    constexpr uint32_t TMEM_COLS = (NSET * 4 * N <= 256) ? 256 : 512;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      ::"r"(smem_u32(&s.tmem_base)), "r"(TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    df_fill_sincos_table(s.sc_tab);
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
             mbar_init(&s.a_full[i], NPROD);
@@ -262,7 +334,8 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 ++ti;
                 if (tuse > 0 && !mbar_wait(&s.t_empty[set], (uint32_t)((tuse - 1) & 1))) { fail(); break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t acc0 = tmem + (uint32_t)(set * 3 * N), acc1 = acc0 + N, acc2 = acc0 + 2 * N;
+                const uint32_t acc0 = tmem + (uint32_t)(set * 4 * N), acc1 = acc0 + N, acc2 = acc0 + 2 * N,
+                               acc3 = acc0 + 3 * N;
                 bool ok = true;
                 for (int ks = 0; ks < nst; ++ks, ++gs) {
                     const int st = (int)(gs & 1);
@@ -280,10 +353,10 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                         umma<N>(acc2, ad(0), bd(2), acc);
                         umma<N>(acc2, ad(1), bd(1), 1u);
                         umma<N>(acc2, ad(2), bd(0), 1u);
-                        umma<N>(acc2, ad(0), bd(3), 1u);
-                        umma<N>(acc2, ad(1), bd(2), 1u);
-                        umma<N>(acc2, ad(2), bd(1), 1u);
-                        umma<N>(acc2, ad(3), bd(0), 1u);
+                        umma<N>(acc3, ad(0), bd(3), acc);
+                        umma<N>(acc3, ad(1), bd(2), 1u);
+                        umma<N>(acc3, ad(2), bd(1), 1u);
+                        umma<N>(acc3, ad(3), bd(0), 1u);
                     }
                     umma_commit(&s.st_empty[st]);
                 }
@@ -305,7 +378,7 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
             if (!tile_live(tg, NE)) continue;
             const int f = tg.f0 + ep;
             const bool act = pair_active(tg.e, f, NE);
-            GreenSampler<float> smp;
+            TcGreen smp;
             float sc = 0.f;
             if (act) {
                 const int p = 4 * tg.e + (pp >> 2), q = 4 * f + (pp & 3);
@@ -322,20 +395,14 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 if (use > 0 && !mbar_wait(&s.st_empty[st], (uint32_t)((use - 1) & 1))) { fail(); break; }
                 if (act) {
                     const int j0 = ks * TK + jq * 8;
-                    float2 re[4], im[4];                      // (sample 2i, 2i + 1)
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        float2 g0 = make_float2(0.f, 0.f), g1 = g0;
-                        if (j0 + 2 * i <= h) g0 = smp(s2q[ks * TK + 2 * i]);
-                        if (j0 + 2 * i + 1 <= h) g1 = smp(s2q[ks * TK + 2 * i + 1]);
-                        re[i] = make_float2(g0.x, g1.x);
-                        im[i] = make_float2(g0.y, g1.y);
-                    }
                     uint32_t wre[4][ND], wim[4][ND];
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
-                        split4(re[i], sc, wre[i]);
-                        split4(im[i], sc, wim[i]);
+                        float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
+                        if (j0 + 2 * i <= h) g0 = smp(s2q[ks * TK + 2 * i], s.sc_tab);
+                        if (j0 + 2 * i + 1 <= h) g1 = smp(s2q[ks * TK + 2 * i + 1], s.sc_tab);
+                        split4(make_float2(g0.x, g1.x), make_float2(g0.y, g1.y), sc, wre[i]);
+                        split4(make_float2(g0.z, g1.z), make_float2(g0.w, g1.w), sc, wim[i]);
                     }
                     unsigned char *abase = reinterpret_cast<unsigned char *>(s.a[st][0]);
 #pragma unroll
@@ -396,22 +463,24 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 ttf = df_mul(df_from(geo[(size_t)10 * P + 4 * e]), df_from(geo[(size_t)10 * P + 4 * f]));
             }
             __syncwarp();
-            const uint32_t trow = tmem + ((uint32_t)(ep * 32) << 16) + (uint32_t)(set * 3 * N);
+            const uint32_t trow = tmem + ((uint32_t)(ep * 32) << 16) + (uint32_t)(set * 4 * N);
             for (int qc = 0; qc < nch; ++qc) {
                 const int c_hi = min(CH, nord - qc * CH);      // orders of this chunk
-                // (1) orders as double-float words: ACC0 + ACC1 (exact, two-sum) + ACC2,
-                //     times 2^(e_r - bA - sT)
+                // (1) orders as double-float words, ACC0 + 2^-8 ACC1 (two-sum, exact) +
+                //     2^-16 ACC2 + 2^-24 ACC3, times 2^(e_r - bA - sT)
                 if (act) {
-                    float a0[16], a1[16], a2[16];
+                    float a0[16], a1[16], a2[16], a3[16];
                     tmem_ld16(trow + (uint32_t)(qc * CH), a0);
                     tmem_ld16(trow + (uint32_t)(N + qc * CH), a1);
                     tmem_ld16(trow + (uint32_t)(2 * N + qc * CH), a2);
+                    tmem_ld16(trow + (uint32_t)(3 * N + qc * CH), a3);
 #pragma unroll
                     for (int c = 0; c < 16; ++c) {
                         if (c < c_hi) {
-                            const float sh = a0[c] + a1[c];
+                            const float x1 = a1[c] * 0x1p-8f;
+                            const float sh = a0[c] + x1;
                             const float bb = sh - a0[c];
-                            const float sl = (a0[c] - (sh - bb)) + (a1[c] - bb) + a2[c];
+                            const float sl = (a0[c] - (sh - bb)) + (x1 - bb) + fmaf(a3[c], 0x1p-24f, a2[c] * 0x1p-16f);
                             const int slot = (qc * CH + c) % RING;
                             float2 *dst = reinterpret_cast<float2 *>(G + slot * SLAB + pp) + cre;
                             *dst = make_float2(sh * scl, sl * scl);
@@ -561,13 +630,11 @@ __global__ void tc_table_digits_kernel(int h, int Mp, int Npad, int Kpad, const 
          i += (long long)gridDim.x * blockDim.x) {
         const int o = (int)(i / Kpad), j = (int)(i % Kpad);
         double t = (o < Mp && j <= h) ? ldexp(dct[(size_t)j * Mp + o], sT) : 0.0;
-        double w = 1.0;
 #pragma unroll
         for (int s = 0; s < ND; ++s) {
             const double d = rint(t);
-            bd[(size_t)s * total + i] = __float2bfloat16_rn((float)(d * w));
+            bd[(size_t)s * total + i] = __float2bfloat16_rn((float)d);
             t = (t - d) * 256.0;
-            w *= 0x1p-8;
         }
         if (o == 0) {
             const double v = (j <= h) ? sin2[j] : 0.0;

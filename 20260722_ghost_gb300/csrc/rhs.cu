@@ -18,6 +18,7 @@ namespace gb {
 namespace {
 
 constexpr int MAX_ORD = 512;      // J_n table held per thread (orders 0..M+1)
+constexpr int kMaxGridY = 65535;  // grid y limit: points and nodes stride over it
 constexpr double ETA0 = 376.730313668;
 
 // Bessel J_0..J_nmax(x), x >= 0, into out[0..nmax] (strided).
@@ -56,16 +57,18 @@ __global__ void bessel_phase_kernel(int P, int Mp, int T, double k, const double
                                     double2 *__restrict__ Ph)
 {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
-    const int p = blockIdx.y;
     if (it >= T) return;
     const double th = thetas[it] * (GB_PI / 180.0);
     double st, ct;
     sincos(th, &st, &ct);
-    const double rho = geo[p], z = geo[P + p];
-    bessel_table(k * rho * st, Mp - 1, Jtab + (size_t)p * Mp * T + it, T);
-    double s, c;
-    sincos(k * ct * z, &s, &c);
-    Ph[(size_t)p * T + it] = make_double2(c, s);
+    // Gauss points stride over grid y (at most 65535 blocks in y)
+    for (int p = blockIdx.y; p < P; p += gridDim.y) {
+        const double rho = geo[p], z = geo[P + p];
+        bessel_table(k * rho * st, Mp - 1, Jtab + (size_t)p * Mp * T + it, T);
+        double s, c;
+        sincos(k * ct * z, &s, &c);
+        Ph[(size_t)p * T + it] = make_double2(c, s);
+    }
 }
 
 __device__ __forceinline__ double2 ipow_times(int n, double v)
@@ -79,7 +82,7 @@ __device__ __forceinline__ double2 ipow_times(int n, double v)
     }
 }
 
-// B[m][row][2 it + pol]: one thread per (it), blockIdx.y = node, blockIdx.z = m
+// B[m][row][2 it + pol]: one thread per (it), nodes striding over grid y, blockIdx.z = m
 __global__ void rhs_kernel(int N, int Nn, int Mp, int T, double k, double ce, double ch,
                            const double *__restrict__ geo, const double *__restrict__ thetas,
                            const double *__restrict__ Jtab, const double2 *__restrict__ Ph,
@@ -87,13 +90,13 @@ __global__ void rhs_kernel(int N, int Nn, int Mp, int T, double k, double ce, do
                            long long ldb, long long mode_stride)
 {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y;
     const int m = blockIdx.z;
     if (it >= T) return;
     const int P = 4 * N;
     const double th = thetas[it] * (GB_PI / 180.0);
     double st, ct;
     sincos(th, &st, &ct);
+    for (int i = blockIdx.y; i < Nn; i += gridDim.y) {
     double2 vt[2] = {make_double2(0, 0), make_double2(0, 0)};   // [pol]
     double2 vf[2] = {make_double2(0, 0), make_double2(0, 0)};
     const int nlo = abs(m - 1), nhi = m + 1;
@@ -146,6 +149,7 @@ __global__ void rhs_kernel(int N, int Nn, int Mp, int T, double k, double ce, do
     Bm[(size_t)i * ldb + 2 * it + 1] = mt ? z : vt[1];
     Bm[(size_t)(Nn + i) * ldb + 2 * it + 0] = mf ? z : vf[0];
     Bm[(size_t)(Nn + i) * ldb + 2 * it + 1] = mf ? z : vf[1];
+    }
 }
 
 template <class R>
@@ -203,11 +207,11 @@ extern "C" int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
     double *Jtab = reinterpret_cast<double *>(work);
     double2 *Ph = reinterpret_cast<double2 *>(
         (reinterpret_cast<uintptr_t>(Jtab + (size_t)P * Mp * n_theta) + 15) & ~uintptr_t(15));
-    dim3 g1((n_theta + 63) / 64, P);
+    dim3 g1((n_theta + 63) / 64, P < kMaxGridY ? P : kMaxGridY);
     bessel_phase_kernel<<<g1, 64, 0, st>>>(P, Mp, n_theta, k, geo, thetas_deg, Jtab, Ph);
     int rc = check_launch("rhs: bessel");
     if (rc) return rc;
-    dim3 g2((n_theta + 63) / 64, n_elem + 1, m_max + 1);
+    dim3 g2((n_theta + 63) / 64, n_elem + 1 < kMaxGridY ? n_elem + 1 : kMaxGridY, m_max + 1);
     rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, n_theta, k, coef_e, coef_h, geo, thetas_deg,
                                   Jtab, Ph, mask_rows, reinterpret_cast<double2 *>(B), ldb, mode_stride);
     return check_launch("rhs");
@@ -259,7 +263,9 @@ extern "C" int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, 
 // streams, other host threads) race on it and must be serialised by the
 // caller.  The first call on each device looks up the array's device address
 // with cudaGetSymbolAddress while that device is current; make that first call
-// before any stream capture.
+// before any stream capture.  The address is cached per device ordinal for the
+// life of the process: after cudaDeviceReset it is stale, so a process that
+// resets a device must not call this entry point on it again.
 // ---------------------------------------------------------------------------
 namespace gb {
 namespace {
@@ -317,11 +323,11 @@ extern "C" int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double 
         double *Jtab = reinterpret_cast<double *>(scratch);
         double2 *Ph = reinterpret_cast<double2 *>(
             (reinterpret_cast<uintptr_t>(Jtab + (size_t)P * Mp * T) + 15) & ~uintptr_t(15));
-        dim3 g1((T + 63) / 64, (unsigned)P);
+        dim3 g1((T + 63) / 64, (unsigned)(P < kMaxGridY ? P : kMaxGridY));
         bessel_phase_kernel<<<g1, 64, 0, st>>>((int)P, Mp, T, k, geo, thetas_deg + it0, Jtab, Ph);
         int rc = check_launch("rhs_noalloc: bessel");
         if (rc) return rc;
-        dim3 g2((T + 63) / 64, n_elem + 1, m_max + 1);
+        dim3 g2((T + 63) / 64, n_elem + 1 < kMaxGridY ? n_elem + 1 : kMaxGridY, m_max + 1);
         rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, T, k, coef_e, coef_h, geo, thetas_deg + it0,
                                       Jtab, Ph, mask_rows, reinterpret_cast<double2 *>(B) + 2 * (size_t)it0,
                                       ldb, mode_stride);

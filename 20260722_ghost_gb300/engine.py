@@ -145,11 +145,16 @@ class BorGpuProblem:
             self.d_btab = torch.as_tensor(btab, dtype=f64, device=dev)
             self.d_bsin2 = torch.as_tensor(bs2, dtype=f64, device=dev)
             self.d_emass = torch.as_tensor(element_mass(self.g, self.N), dtype=f64, device=dev)
-        # residual norm (relative to ||B||) where the refinement stops.  The exact
-        # first residual and the tensor-core updates resolve ~1e-11, but the
-        # FP32 far fill already perturbs the operator by ~4e-8 of its largest
-        # entries, so corrections below that change nothing measurable
-        self.refine_floor = 2e-8
+        # residual norm (relative to ||B||) where the refinement stops.  The
+        # tensor-core far fill perturbs the operator by ~4e-9 of its largest
+        # entries; the mode systems of closed bodies are ill-conditioned (the
+        # FP32 solve is off by up to ~20% in some modes), so the residual is
+        # driven well below that for the surface currents as well
+        self.refine_floor = 2e-9
+        # residual updates R -= Z D with exact products (the bf16-digit kernel of
+        # the first residual); False: R -= fl32(Z) D on the 3xTF32 GEMM, which
+        # leaves a drift (Z - fl32(Z)) (X - X0) of ~1e-8 in the residual
+        self.exact_updates = True
         self.tensor_cores = True     # FP32 LU / solve / residual updates on tcgen05 (3xTF32)
         self.update_ws_bytes = 4 << 30   # scratch bound of one residual-update GEMM launch
         self.exact_residual = True       # first residual with exact products (bf16 Ozaki slices)
@@ -174,9 +179,11 @@ class BorGpuProblem:
         if precision == "fp64":
             return Mb * (2 * nn * 16 + 3 * rhs * 16) + ve
         tc = 4 * 128 * Mb * (2 * self.n + 4 * max(self.n, self.nrhs)) * 2
-        # Zf (c128), A and its unfactored copy (c64), B and X (c128), X32 and R32
-        # (c64), the near band, LU / solve scratch and the residual-update scratch
-        return (Mb * (nn * 16 + 2 * nn * 8 + 2 * rhs * 16 + 2 * rhs * 8 + 4 * self.Nn * 5 * 16) + tc + ve
+        # Zf (c128), A (c64) and, with GEMM updates, its unfactored copy, B and
+        # X (c128), the FP64 residual of the exact updates, X32 and R32 (c64),
+        # the near band, LU / solve scratch and the residual-update scratch
+        upd = rhs * 16 if self.exact_updates else nn * 8
+        return (Mb * (nn * 16 + nn * 8 + upd + 2 * rhs * 16 + 2 * rhs * 8 + 4 * self.Nn * 5 * 16) + tc + ve
                 + self.update_ws_bytes)
 
     # -- stages -----------------------------------------------------------
@@ -319,7 +326,7 @@ class BorGpuProblem:
         return Z
 
     # -- the sweep ---------------------------------------------------------
-    def sweep(self, precision: str = "fp32ir", max_refine: int = 3,
+    def sweep(self, precision: str = "fp32ir", max_refine: int = 5,
               check_abort: Optional[Callable] = None, keep: bool = False) -> SweepResult:
         torch = self.torch
         if precision not in ("fp64", "fp32ir"):
@@ -412,21 +419,25 @@ class BorGpuProblem:
             X = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
             nat.call("ghost_bor_convert", 1, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(X),
                      nrhs, X.stride(0), st); mark("solve")
-            # refinement: R0 = B - Z X0 once with exact products (bf16 digit
-            # slices on the tensor cores; the split-word SIMT kernel without them),
-            # Z in FP64 and X0 the FP32 solution; for each correction D = A^-1 R
-            # the next residual is R - Z D, and since |D| ~ 1e-5 |X| a tensor-core
-            # GEMM on fl32(Z) is accurate enough for that product
+            # refinement: R0 = B - Z X0 with exact products (bf16 digit slices on
+            # the tensor cores; the split-word SIMT kernel without them), Z in FP64
+            # and X0 the FP32 solution; for each correction D = A^-1 R the next
+            # residual is R - Z D, again with exact products (FP64 R, in place).
+            # A GEMM on fl32(Z) for that product would leave the drift
+            # (Z - fl32(Z)) (X - X0) in the residual, and X - X0 reaches ~20% of X
+            # in ill-conditioned modes
             R32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
             Ac = None
             z_split = 0
-            if (self.tensor_cores and max_refine > 0) or keep:
+            exact_upd = self.tensor_cores and self.exact_residual and self.exact_updates
+            if (self.tensor_cores and max_refine > 0 and not exact_upd) or keep:
                 # fl32(Z), masked like A, for the residual updates (and the adjoint);
                 # composed before Z_far is overwritten by its FP32 words
                 Ac = torch.empty((Mb, n, n), dtype=c64, device=self.device)
                 nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
                          nat.ptr(self.d_masks), nat.ptr(Ac), n, Ac.stride(0), st)
             k0 = kstart()
+            R64 = None
             if self.tensor_cores and self.exact_residual:
                 # exact products on the bf16 tensor cores, modes in chunks that
                 # bound the slice workspace
@@ -435,14 +446,20 @@ class BorGpuProblem:
                 ex_ws = torch.empty(int(lib.ghost_bor_residual_exact_workspace(chunk, n, nrhs)),
                                     dtype=torch.uint8, device=self.device)
                 ex_flags = torch.zeros((Mb + chunk - 1) // chunk, dtype=torch.int32, device=self.device)
-                for ci, b0 in enumerate(range(0, Mb, chunk)):
-                    nb = min(chunk, Mb - b0)
-                    nat.call("ghost_bor_residual_exact", nb, n, nrhs, Nn, nat.ptr(Zf[b0]), n, Zf.stride(0),
-                             nat.ptr(band[b0]), nat.ptr(self.d_masks[b0]), nat.ptr(X32[b0]), nat.ptr(B[b0]),
-                             nrhs, B.stride(0), 0, nat.ptr(R32[b0]), nat.ptr(norms[b0]), nat.ptr(ex_ws),
-                             ex_ws.numel(), st)
-                    ex_flags[ci:ci + 1].copy_(ex_ws[:4].view(torch.int32))
-                del ex_ws
+                if exact_upd and max_refine > 0:
+                    R64 = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
+
+                def exact_residual(Xin, Bin, Rout):
+                    """Rout = Bin - (Z_far + Z_near) Xin (Xin FP32), norms[:, 0] = ||Rout||^2."""
+                    for ci, b0 in enumerate(range(0, Mb, chunk)):
+                        nb = min(chunk, Mb - b0)
+                        nat.call("ghost_bor_residual_exact", nb, n, nrhs, Nn, nat.ptr(Zf[b0]), n, Zf.stride(0),
+                                 nat.ptr(band[b0]), nat.ptr(self.d_masks[b0]), nat.ptr(Xin[b0]), nat.ptr(Bin[b0]),
+                                 nrhs, Bin.stride(0), nat.ptr(None if Rout is None else Rout[b0]),
+                                 nat.ptr(R32[b0]), nat.ptr(norms[b0]), nat.ptr(ex_ws), ex_ws.numel(), st)
+                        torch.maximum(ex_flags[ci:ci + 1], ex_ws[:4].view(torch.int32), out=ex_flags[ci:ci + 1])
+
+                exact_residual(X32, B, R64)
             else:
                 if self.tensor_cores:
                     # Z_far is read only by the first residual from here on: split it in
@@ -454,9 +471,7 @@ class BorGpuProblem:
                          nat.ptr(band), nat.ptr(self.d_masks), nat.ptr(X32), nat.ptr(B), nrhs, B.stride(0), 0,
                          nat.ptr(R32), nat.ptr(norms), st)
             kend("residual", k0)
-            if ex_flags is not None and int(ex_flags.max()) != 0:
-                raise RuntimeError("a bounded tensor-core wait gave up in the exact residual")
-            bn2 = torch.clamp(norms[:, 1], min=1e-300)
+            bn2 = torch.clamp(norms[:, 1].clone(), min=1e-300)
             rel = float(torch.sqrt(torch.max(norms[:, 0] / bn2)))
             history = [rel]
             prev = None
@@ -473,7 +488,10 @@ class BorGpuProblem:
                 nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
                          nat.ptr(X), nrhs, X.stride(0), st)
                 k0 = kstart()
-                if self.tensor_cores:
+                if R64 is not None:
+                    # R -= (Z_far + Z_near) D with exact products, in FP64 (in place)
+                    exact_residual(X32, R64, R64)
+                elif self.tensor_cores:
                     if up_ws is None:
                         per = int(lib.ghost_bor_cgemm_tc_workspace(1, n, nrhs, n))
                         chunk = max(1, min(Mb, int(self.update_ws_bytes // max(per, 1))))
@@ -494,14 +512,20 @@ class BorGpuProblem:
                              nat.ptr(Rd), nat.ptr(R32), nat.ptr(norms), st)
                     del Rd
                 kend("residual_update", k0)
-                rn = torch.linalg.vector_norm(R32, dim=(1, 2)).double() ** 2
-                norms[:, 0].copy_(rn)
+                if R64 is not None:
+                    rn = norms[:, 0].clone()
+                    norms[:, 1].copy_(bn2)          # the kernel's second norm is of its input, R
+                else:
+                    rn = torch.linalg.vector_norm(R32, dim=(1, 2)).double() ** 2
+                    norms[:, 0].copy_(rn)
                 rel = float(torch.sqrt(torch.max(rn / bn2)))
                 history.append(rel)
                 iters += 1
                 abort()
             if status is not None and int(status.max()) != 0:
                 raise RuntimeError("a bounded tensor-core wait gave up in the residual update")
+            if ex_flags is not None and int(ex_flags.max()) != 0:
+                raise RuntimeError("a bounded tensor-core wait gave up in the exact residual")
             mark("residual")
             if lu_ws is not None:
                 flags = torch.stack([lu_ws[:4].view(torch.int32)[0], rs_ws[:4].view(torch.int32)[0]])
@@ -509,7 +533,7 @@ class BorGpuProblem:
                     raise RuntimeError("a bounded tensor-core wait gave up in the LU / solve kernels")
             lu = dict(prec=nat.F32, A=A, ipiv=ipiv, op=Ac, work=rs_ws)
             if not keep:
-                del Zf, A, Ac, R32, X32, band
+                del Zf, A, Ac, R32, X32, band, R64
         dF = torch.empty((Mb, nrhs), dtype=c128, device=self.device)
         nat.call("ghost_bor_farfield", nat.F64, Mb, n, nrhs, Nn, self.k, nat.ptr(self.d_mode_w),
                  nat.ptr(Ve), nrhs, Ve.stride(0), nat.ptr(X), nrhs, X.stride(0), nat.ptr(dF), st)

@@ -115,14 +115,17 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
                               void *Z, long long ldz, long long mode_stride,
                               const unsigned char *elem_mask, const float *dct32, void *stream);
 
-/* Tensor-core form of the FP32 EFIE far fill: the same sampling, contraction,
- * mode combination and accumulation as ghost_bor_far_efie(GHOST_BOR_F32, ...),
- * with the even DCT over the azimuth samples computed on the bf16 tensor cores
- * (tcgen05) from four balanced 8-bit digits of the samples and of the table:
- * the level-0 digit products accumulate exactly, the transform carries
- * ~2^-30 of each Gauss-point pair's bound |g| <= 1/|Delta| instead of the
- * FP32 table and sums of the SIMT transform.  Z is complex double; the
- * contribution is ADDED.
+/* Tensor-core form of the FP32-pipe EFIE far fill: the same contraction, mode
+ * combination and accumulation as ghost_bor_far_efie(GHOST_BOR_F32, ...), with
+ * (i) Green's-function samples as pairs of FP32 words accurate to ~3e-9 (a
+ * double-float phase and table-driven sin / cos instead of sincosf), (ii) the
+ * even DCT over the azimuth samples on the bf16 tensor cores (tcgen05) from
+ * four balanced 8-bit integer digits of the samples and of the table, one
+ * TMEM accumulator per digit level, and (iii) each far element pair sampled
+ * once and contracted in both orientations (the kernel is symmetric in the
+ * point pair).  The operator agrees with the FP64 fill to ~4e-9 of its largest
+ * entry (the SIMT FP32 fill: ~7e-8).  Z is complex double; the contribution
+ * is ADDED.
  *   work  ghost_bor_far_efie_tc_workspace(m_max, nxi) bytes, 256-byte
  *         aligned, prepared once per (m_max, nxi, table) by
  *         ghost_bor_far_efie_tc_tables from the `dct` / `sin2` tables of
@@ -250,7 +253,10 @@ int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
  * array: 4*n_elem*((m_max+2)*8 + 16) > 64 MiB - 256.  Calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.  The
  * first call on a device looks the array up (cudaGetSymbolAddress) and should
- * come before any stream capture.  No counterpart in the reference.
+ * come before any stream capture; the looked-up address is kept for the life
+ * of the process, so it is stale after cudaDeviceReset of that device (do not
+ * call this entry point on a device after resetting it).  No counterpart in
+ * the reference.
  * ghost_bor_rhs_noalloc_capacity() returns the array size in bytes. */
 long long ghost_bor_rhs_noalloc_capacity(void);
 int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double k,

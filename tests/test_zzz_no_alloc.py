@@ -7,7 +7,8 @@ excitation from a workspace that lives in a static device array inside the
 library.  This file checks, through the C ABI, that two calls in a row give the
 same excitation as ghost_bor_rhs with a caller workspace, including a problem
 that needs several angle blocks, and that oversized problems are rejected.
-It is named to run last so a failure here does not hide other results.
+It is named to be collected last (after every test_zz_* file) so a failure
+here does not hide other results.
 """
 import math
 
