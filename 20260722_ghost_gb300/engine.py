@@ -155,6 +155,13 @@ class BorGpuProblem:
         # the first residual); False: R -= fl32(Z) D on the 3xTF32 GEMM, which
         # leaves a drift (Z - fl32(Z)) (X - X0) of ~1e-8 in the residual
         self.exact_updates = True
+        # with exact updates, the number of leading corrections updated exactly:
+        # the first correction is the large one (up to ~20% of X in
+        # ill-conditioned modes) and its drift is what matters for the far field;
+        # later, small corrections take the GEMM update.  None = all exact (with
+        # refine_floor ~1e-11 this brings the surface currents within ~3e-5 of
+        # the FP64 solve; the default leaves ~6e-4 there and ~1e-9 in the far field)
+        self.exact_update_iters = 1
         self.tensor_cores = True     # FP32 LU / solve / residual updates on tcgen05 (3xTF32)
         self.update_ws_bytes = 4 << 30   # scratch bound of one residual-update GEMM launch
         self.exact_residual = True       # first residual with exact products (bf16 Ozaki slices)
@@ -430,7 +437,8 @@ class BorGpuProblem:
             Ac = None
             z_split = 0
             exact_upd = self.tensor_cores and self.exact_residual and self.exact_updates
-            if (self.tensor_cores and max_refine > 0 and not exact_upd) or keep:
+            n_exact = max_refine if self.exact_update_iters is None else min(max_refine, self.exact_update_iters)
+            if (self.tensor_cores and max_refine > 0 and (not exact_upd or n_exact < max_refine)) or keep:
                 # fl32(Z), masked like A, for the residual updates (and the adjoint);
                 # composed before Z_far is overwritten by its FP32 words
                 Ac = torch.empty((Mb, n, n), dtype=c64, device=self.device)
@@ -488,7 +496,7 @@ class BorGpuProblem:
                 nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
                          nat.ptr(X), nrhs, X.stride(0), st)
                 k0 = kstart()
-                if R64 is not None:
+                if R64 is not None and it < n_exact:
                     # R -= (Z_far + Z_near) D with exact products, in FP64 (in place)
                     exact_residual(X32, R64, R64)
                 elif self.tensor_cores:
@@ -512,7 +520,7 @@ class BorGpuProblem:
                              nat.ptr(Rd), nat.ptr(R32), nat.ptr(norms), st)
                     del Rd
                 kend("residual_update", k0)
-                if R64 is not None:
+                if R64 is not None and it < n_exact:
                     rn = norms[:, 0].clone()
                     norms[:, 1].copy_(bn2)          # the kernel's second norm is of its input, R
                 else:

@@ -49,3 +49,23 @@ def test_autograd_function(pkg):
     J_ref, g_ref = adj.bspline_rcs_and_gradient(radii, n_seg, f, th, pol="HH", m_max=M, precision="fp64")
     assert abs(J.item() - J_ref) < 1e-10 * abs(J_ref)
     assert np.max(np.abs(r.grad.numpy() - g_ref)) < 1e-8 * np.max(np.abs(g_ref))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32ir"])
+def test_adjoint_matches_reference_finite_differences(pkg, precision):
+    """Against the reference's own FP64 solve_bor: central differences of the
+    mean HH cross-section for every radius at h = 1e-4 and 5e-5 m
+    (tests/golden/bspline_fd_ref.npz, made by tests/golden/make_fullsize_golden.py),
+    Richardson-extrapolated; the objective itself to 1e-10."""
+    from conftest import load_golden
+    D = load_golden("bspline_fd_ref")
+    adj = pkg.adjoint
+    radii, n_seg, f, th, M = _case()
+    np.testing.assert_array_equal(radii, D["radii"])
+    np.testing.assert_array_equal(th, D["thetas"])
+    J, g = adj.bspline_rcs_and_gradient(radii, n_seg, f, th, pol="HH", m_max=M, precision=precision)
+    g1 = (D["Jp_h1"] - D["Jm_h1"]) / (2 * D["h1"])
+    g2 = (D["Jp_h2"] - D["Jm_h2"]) / (2 * D["h2"])
+    fd = (4.0 * g2 - g1) / 3.0
+    assert abs(J - float(D["J0"])) < (1e-10 if precision == "fp64" else 1e-6) * abs(float(D["J0"]))
+    assert np.max(np.abs(g - fd)) < 1e-3 * np.max(np.abs(fd)), (g, fd)
