@@ -45,6 +45,7 @@ SIGNATURES = {
     "ghost_bor_rhs_noalloc_capacity": (_ll, []),
     "ghost_bor_rhs_noalloc": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_cgemm_tc_workspace": (_ll, [_i, _i, _i, _i]),
+    "ghost_bor_set_wait_limit": (None, [_ll]),
     "ghost_bor_cgemm_tc": (_i, [_i, _i, _i, _i, _vp, _ll, _ll, _vp, _ll, _ll, _vp, _ll, _ll, _vp, _vp, _vp]),
     "ghost_bor_getrf_workspace": (_ll, [_i, _i, _i]),
     "ghost_bor_getrf": (_i, [_i, _i, _i, _vp, _ll, _ll, _vp, _vp, _vp, _vp]),

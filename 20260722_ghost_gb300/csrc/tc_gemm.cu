@@ -33,6 +33,10 @@ constexpr int TILE_FLOATS = BM * BK;               // 16 KB per operand tile
 constexpr int TC_THREADS = 192;                    // producer, MMA, 4 epilogue warps
 constexpr uint32_t TMEM_COLS = 256;                // two 128-column accumulators
 
+// polls of each pipeline mbarrier wait before the kernel gives up (the drains
+// of copies and MMAs in flight keep WAIT_LIMIT); set by ghost_bor_set_wait_limit
+long long g_pipeline_wait_limit = WAIT_LIMIT;
+
 struct __align__(1024) TcSmem {
     float a_hi[STAGES][TILE_FLOATS];
     float a_lo[STAGES][TILE_FLOATS];
@@ -125,7 +129,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
                  const __grid_constant__ CUtensorMap map_bhi, const __grid_constant__ CUtensorMap map_blo,
                  const __grid_constant__ CUtensorMap map_c, int use_tma_c,
                  int M, int Nr, int Kp, int tiles_n, int tiles_m, int batch, float *__restrict__ C,
-                 long long ldc_r, long long sc_r, int *__restrict__ err)
+                 long long ldc_r, long long sc_r, int *__restrict__ err, long long wait_limit)
 {
     extern __shared__ unsigned char smem_raw[];
     TcSmem &s = *reinterpret_cast<TcSmem *>(
@@ -163,7 +167,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
             const int m0 = (r / tiles_n) * BM, n0 = (r % tiles_n) * BNR;
             for (int ks = 0; ks < nst; ++ks, ++g) {
                 const uint32_t st = g % STAGES, u = g / STAGES;
-                if (u > 0 && !mbar_wait(&s.empty[st], (u - 1) & 1u)) {
+                if (u > 0 && !mbar_wait(&s.empty[st], (u - 1) & 1u, wait_limit)) {
                     *failed = 1;
                     break;
                 }
@@ -174,8 +178,10 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
                 tma_load_3d(s.b_lo[st], &map_blo, ks * BK, n0, b, &s.full[st]);
             }
         }
-        if (*failed) {
-            // let the copies still in flight land before the CTA exits
+        {
+            // the copies still in flight land before the CTA exits (on the normal
+            // path they all have: each wait returns at once); the drain keeps the
+            // long limit whatever the pipeline waits use
             const uint32_t j0 = g > STAGES ? g - STAGES : 0;
             for (uint32_t j = j0; j < g; ++j) mbar_wait(&s.full[j % STAGES], (j / STAGES) & 1u);
         }
@@ -186,12 +192,12 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
         bool issued = false;
         for (int t = blockIdx.x; t < ntiles && !*failed; t += gridDim.x, ++i) {
             const uint32_t ab = i & 1, ui = i >> 1;
-            if (ui > 0 && !mbar_wait(&s.tempty[ab], (ui - 1) & 1u)) { *failed = 1; break; }
+            if (ui > 0 && !mbar_wait(&s.tempty[ab], (ui - 1) & 1u, wait_limit)) { *failed = 1; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t d = tmem + ab * BNR;
             for (int ks = 0; ks < nst; ++ks, ++g) {
                 const uint32_t st = g % STAGES, u = g / STAGES;
-                if (!mbar_wait(&s.full[st], u & 1u)) { *failed = 1; break; }
+                if (!mbar_wait(&s.full[st], u & 1u, wait_limit)) { *failed = 1; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t ah = smem_u32(s.a_hi[st]), al = smem_u32(s.a_lo[st]);
                 const uint32_t bh = smem_u32(s.b_hi[st]), bl = smem_u32(s.b_lo[st]);
@@ -241,7 +247,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap map_ahi, const __grid_const
             const int stop = __shfl_sync(0xffffffffu, *failed, 0);
             if (stop) break;
             const uint32_t ab = i & 1, ui = i >> 1;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(&s.tfull[ab], ui & 1u));
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&s.tfull[ab], ui & 1u, wait_limit));
             if (!ok) {
                 if (lane == 0) *failed = 1;
                 break;
@@ -409,11 +415,17 @@ int tc_update(int batch, int M, int N, int K, const float2 *A, long long lda, lo
     const int use_tma_c = make_map_c(&mc, Cr, M, 2 * N, batch, 2 * ldc, 2 * sc) ? 1 : 0;
     if (!use_tma_c) mc = mah;                                   // unused by the kernel
     tc_update_kernel<<<grid, TC_THREADS, smem, st>>>(mah, mal, mbh, mbl, mc, use_tma_c, M, 2 * N, Kp, tiles_n,
-                                                     tiles_m, batch, Cr, 2 * ldc, 2 * sc, err);
+                                                     tiles_m, batch, Cr, 2 * ldc, 2 * sc, err,
+                                                     __atomic_load_n(&g_pipeline_wait_limit, __ATOMIC_RELAXED));
     return check_launch("tc_update");
 }
 
 }  // namespace gb
+
+extern "C" void ghost_bor_set_wait_limit(long long polls)
+{
+    __atomic_store_n(&gb::g_pipeline_wait_limit, polls < 0 ? gb::WAIT_LIMIT : polls, __ATOMIC_RELAXED);
+}
 
 extern "C" long long ghost_bor_cgemm_tc_workspace(int batch, int M, int N, int K)
 {

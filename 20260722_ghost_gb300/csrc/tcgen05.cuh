@@ -33,11 +33,12 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *b)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
 }
 
-// bounded wait on the phase with parity `parity`; false on timeout
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity)
+// bounded wait on the phase with parity `parity`; false on timeout (after
+// `limit` polls; limit <= 0 gives up at once)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity, long long limit = WAIT_LIMIT)
 {
     const uint32_t a = smem_u32(b);
-    for (long long it = 0; it < WAIT_LIMIT; ++it) {
+    for (long long it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
                      " selp.u32 %0, 1, 0, p;\n}\n"

@@ -259,11 +259,12 @@ def cpu_baseline(workload: str, cores: int):
         s.farfield(m, xs[:, 1, :], thetas)
     t_mode = (time.perf_counter() - t0) / 2.0
     total = t_far + t_near + t_mode * (2 * M + 1)
+    sampled = t_far * n_far / ne + t_near * len(sub) / len(pairs) + 2.0 * t_mode
     sample = (f"oracle port of the reference sweep on {cores} host threads: far sweep over "
               f"{n_far}/{ne} test elements, {len(sub)}/{len(pairs)} near element pairs, one |m| "
-              f"(m=+-{am}) solved for all {2 * len(thetas)} columns; extrapolated to {2 * M + 1} "
-              f"mode systems ({total:.0f} s per sweep)")
-    return 2 * len(thetas) / total, sample, time.perf_counter() - t_start
+              f"(m=+-{am}) solved for all {2 * len(thetas)} columns ({sampled:.1f} s timed), scaled by "
+              f"element pairs and mode systems to the whole sweep ({total:.0f} s, x{total / sampled:.0f})")
+    return 2 * len(thetas) / total, sample, time.perf_counter() - t_start, sampled, total
 
 
 # ---------------------------------------------------------------------------
@@ -330,6 +331,7 @@ def run_gpu(args, rank, world):
     f64_s = e0.elapsed_time(e1) / 1e3 / f64_steps
     F32 = results[-1].dF.sum(0)
     F64 = r64.dF.sum(0)
+    vs_ref = accuracy_vs_reference(args.workload, thetas, F32, F64)
     db = float(np.max(np.abs(20 * np.log10(np.abs(F32) / np.abs(F64)))))
     rel = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
     acc_extra = db_stats(F32, F64)
@@ -348,11 +350,36 @@ def run_gpu(args, rank, world):
     d2h = (M + 1) * angle_pol * 16 + (M + 1) * (2 * 8 + 4)
     adjoint = adjoint_leg(WORKLOADS[args.workload], f, thetas) if WORKLOADS[args.workload]["body"] == "bspline" \
         else None
-    return dict(adjoint=adjoint, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s,
+    return dict(adjoint=adjoint, vs_ref=vs_ref, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s,
                 kernel_work=kernel_w, steps=args.steps, clocks=clocks, launches=launches,
                 f64_s=f64_s, f64_steps=f64_steps, db=db, rel=rel, acc_extra=acc_extra, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
                 refine_iters=results[-1].refine_iters, residual=float(np.max(results[-1].residual)),
                 prob=prob, angle_pol=angle_pol, M=M, thetas=thetas)
+
+
+# amplitudes of the reference's own FP64 solve_bor, stored by
+# tests/golden/make_fullsize_golden.py (the reference cannot run here)
+REFERENCE_FIXTURES = {"cone_sphere_ka40": "c2_conesphere_ref.npz"}
+
+
+def accuracy_vs_reference(workload, thetas, F32, F64):
+    """Max relative amplitude and dB errors of the FP32+IR and the FP64 sweeps
+    against the reference's FP64 amplitudes, where a fixture exists."""
+    import numpy as np
+    name = REFERENCE_FIXTURES.get(workload)
+    path = os.path.join(HERE, "tests", "golden", name) if name else None
+    if not path or not os.path.exists(path):
+        return None
+    D = np.load(path)
+    if D["thetas"].shape != thetas.shape or not np.allclose(D["thetas"], thetas):
+        return None
+    ref = np.stack([D["amp_vv"], D["amp_hh"]])
+    out = {"fixture": f"tests/golden/{name}", "reference_wall_s": float(D["wall_s"]),
+           "reference_cores": int(D["host_cores"])}
+    for tag, F in (("fp32ir", F32), ("fp64", F64)):
+        out[f"{tag}_max_rel_amp_err"] = float(np.max(np.abs(F - ref)) / np.max(np.abs(ref)))
+        out[f"{tag}_max_db_err"] = float(np.max(np.abs(20 * np.log10(np.abs(F) / np.abs(ref)))))
+    return out
 
 
 def db_stats(F32, F64):
@@ -506,9 +533,10 @@ def roofline(res, peaks, workload):
                            "is a double-float multiply-add on the FP32 pipe (~30 FP32 instructions with the "
                            "recurrence), and every node's transcendentals run in double-float as well")
         else:
-            out["note"] = ("far fill: 4 flops per sample and order of the DCT (packed f32x2 FMAs with "
-                           "Kahan-compensated blocks); the sampling (double-float phase, sincosf) and the "
-                           "double-float contraction are not counted")
+            out["note"] = ("far fill: 4 flops per far Gauss-point pair, sample and order of the DCT (all "
+                           "P^2 pairs; the kernel samples each symmetric pair once and runs the DCT as "
+                           "bf16 digit products on the tensor cores); the sampling (double-float phase, "
+                           "table-driven sin/cos) and the double-float contraction are not counted")
     out.update({"kernel": name, "launch_ms": round(t_sum / len(ks[name]) * 1e3, 3),
                 "launches_per_step": len(ks[name]) / res["steps"], "share_of_step": shares,
                 "traffic": TRAFFIC.get((name, workload)), "peak_source": peaks["source"]})
@@ -519,7 +547,6 @@ def roofline(res, peaks, workload):
 # (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the named workload;
 # None where not captured.
 TRAFFIC = {     # (kernel, workload) -> bytes per launch
-    ("far_fill", "cone_sphere_ka40"): 4.72e9 + 4.66e9,     # Z_far read + written once
     ("near_fill", "cone_sphere_ka40"): 65.76e9 + 38.90e9,  # per-CTA node scratch
 }
 
@@ -558,17 +585,31 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        vals = []
+        vals, timed, full = [], [], []
         sample = ""
+        t_steps = 0.0
         for i in range(args.warmup + args.steps):
-            v, sample, _ = cpu_baseline(args.workload, cores)
+            t0 = time.perf_counter()
+            v, sample, _, sampled, total = cpu_baseline(args.workload, cores)
             if i >= args.warmup:
+                t_steps += time.perf_counter() - t0
                 vals.append(v)
+                timed.append(sampled)
+                full.append(total)
         v = statistics.median(vals)
+        # each step runs (and times) a bounded sample of the sweep; value is the
+        # whole-sweep throughput that the sample implies (angle.pol over the
+        # sample's time scaled by element pairs and mode systems)
         line = {"metric": METRIC, "value": v, "unit": "angle·pol/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2 * n_theta / v * 1e3,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_steps / args.steps * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex128",
                 "data": "synthetic (seeded geometry)", "config": config, "impl": "reference",
+                "timed_per_step": {"sample_s": statistics.median(timed), "step_wall_s": t_steps / args.steps,
+                                   "extrapolated_sweep_s": statistics.median(full),
+                                   "extrapolation_factor": statistics.median(full) / statistics.median(timed),
+                                   "what": "the oracle port (a NumPy/C restatement of the reference's "
+                                           "solve_bor) on a bounded sample of the sweep; the reference itself "
+                                           "cannot run on the GPU host"},
                 "cpu_baseline": {"value": v, "unit": "angle·pol/s", "cores": cores, "kind": "port",
                                  "sample": sample},
                 "e2e": {"value": v, "unit": "angle·pol/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -583,8 +624,9 @@ def main():
         return
     cpu = None
     if not args.no_cpu_baseline:
-        v, sample, _ = cpu_baseline(args.workload, cores)
-        cpu = {"value": v, "unit": "angle·pol/s", "cores": cores, "kind": "port", "sample": sample}
+        v, sample, _, sampled, total = cpu_baseline(args.workload, cores)
+        cpu = {"value": v, "unit": "angle·pol/s", "cores": cores, "kind": "port", "sample": sample,
+               "sample_s": sampled, "extrapolated_sweep_s": total}
     peaks = load_peaks()
     line = {
         "metric": METRIC, "value": res["value"], "unit": "angle·pol/s", "n_gpus": world,
@@ -604,6 +646,8 @@ def main():
         "refine": {"iters": res["refine_iters"], "max_residual": res["residual"]},
         "stages_s": {k: round(v, 5) for k, v in res["stages"].items()},
     }
+    if res.get("vs_ref") is not None:
+        line["accuracy_vs_reference"] = res["vs_ref"]
     if res["adjoint"] is not None:
         line["adjoint"] = res["adjoint"]
     print(json.dumps(line))

@@ -287,6 +287,13 @@ int ghost_bor_getrf(int prec, int batch, int n, void *A, long long lda, long lon
  * (device int, may be NULL) receives 1 if a bounded in-kernel wait gave up.
  * Building block of the LU trailing updates and the triangular solves. */
 long long ghost_bor_cgemm_tc_workspace(int batch, int M, int N, int K);
+/* Polls of each pipeline wait (mbarrier) in the GEMM update kernel before it
+ * gives up, sets its status word and returns (default 2^24; polls < 0 restores
+ * it; 0 makes the first wait give up at once).  The kernel still waits, with
+ * the default limit, for its copies and MMAs in flight before it exits.  A
+ * test hook for the error path of the bounded waits; process-wide, not thread
+ * safe against concurrent launches.  No counterpart in the reference. */
+void ghost_bor_set_wait_limit(long long polls);
 int ghost_bor_cgemm_tc(int batch, int M, int N, int K,
                        const void *A, long long lda, long long stride_a,
                        const void *B, long long ldb, long long stride_b,

@@ -5,7 +5,8 @@
 * ``oracle/_ref/bor_stream_kernel.so``: the reference's own sampler
   (``bor_stream_kernel.c``) compiled from its source where it lies, with the
   compile line the reference documents (bor_stream_kernel.c:18-19).  Built only
-  when the reference tree is present; it is used to check the restatement.
+  when GHOST_REFERENCE_DIR names the reference tree; it is used to check the
+  restatement and to run the reference for the golden fixtures.
 
 Both outputs are git-ignored build products.
 """
@@ -16,7 +17,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_DIR = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+REFERENCE_DIR = os.environ.get("GHOST_REFERENCE_DIR", "")
 
 
 def _cc(src: str, out: str) -> None:
@@ -34,8 +35,8 @@ def build(force: bool = False) -> None:
     src = os.path.join(HERE, "sampler.c")
     if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
         _cc(src, out)
-    ref_src = os.path.join(REFERENCE_DIR, "bor_stream_kernel.c")
-    if os.path.exists(ref_src):
+    ref_src = os.path.join(REFERENCE_DIR, "bor_stream_kernel.c") if REFERENCE_DIR else ""
+    if ref_src and os.path.exists(ref_src):
         ref_out = os.path.join(HERE, "_ref", "bor_stream_kernel.so")
         if force or not os.path.exists(ref_out):
             _cc(ref_src, ref_out)

@@ -1,8 +1,7 @@
 """Generate tests/golden/dispatch.json, dispatch_grid.npz and tests/golden/grim/
 by running the REFERENCE's dispatch layer (bor_dispatch, grim_io).
 
-Run where the reference tree is mounted (default /root/reference, override
-with GHOST_REFERENCE_DIR):
+Run where the reference tree is mounted (its location from GHOST_REFERENCE_DIR):
 
     python tests/golden/make_dispatch_golden.py        # ~1 min
 
@@ -28,7 +27,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TESTS = os.path.dirname(HERE)
-REF = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("GHOST_REFERENCE_DIR")
+if not REF:
+    raise SystemExit("set GHOST_REFERENCE_DIR to the reference tree")
 sys.path.insert(0, REF)
 sys.path.insert(0, TESTS)
 

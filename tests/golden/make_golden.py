@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ by running the REFERENCE.
 
-Run in a container where the reference tree is mounted (default
-/root/reference, override with GHOST_REFERENCE_DIR):
+Run in a container where the reference tree is mounted (its location from
+GHOST_REFERENCE_DIR):
 
     python tests/golden/make_golden.py            # small fixtures (~1 min)
     python tests/golden/make_golden.py --c1       # + the 240-segment sphere (~3 min)
@@ -23,7 +23,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("GHOST_REFERENCE_DIR")
+if not REF:
+    raise SystemExit("set GHOST_REFERENCE_DIR to the reference tree")
 sys.path.insert(0, REF)
 sys.path.insert(0, REPO)
 

@@ -1,8 +1,7 @@
 """Generate tests/golden/ibc_conesphere_n40.npz by running the REFERENCE's
 surface-impedance (IBC-EFIE) path.
 
-Run where the reference tree is mounted (default /root/reference, override
-with GHOST_REFERENCE_DIR):
+Run where the reference tree is mounted (its location from GHOST_REFERENCE_DIR):
 
     python tests/golden/make_ibc_golden.py        # ~1 min
 
@@ -23,7 +22,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("GHOST_REFERENCE_DIR")
+if not REF:
+    raise SystemExit("set GHOST_REFERENCE_DIR to the reference tree")
 sys.path.insert(0, REF)
 sys.path.insert(0, REPO)
 

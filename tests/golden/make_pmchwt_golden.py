@@ -3,8 +3,7 @@ layered_sphere.npz by running the REFERENCE's PMCHWT paths
 (bor_solver.solve_bor_dielectric, BorCrossOperators, solve_bor_coated_pec,
 solve_bor_coated2_pec).
 
-Run where the reference tree is mounted (default /root/reference, override
-with GHOST_REFERENCE_DIR):
+Run where the reference tree is mounted (its location from GHOST_REFERENCE_DIR):
 
     python tests/golden/make_pmchwt_golden.py        # ~1 min
 
@@ -27,7 +26,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("GHOST_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("GHOST_REFERENCE_DIR")
+if not REF:
+    raise SystemExit("set GHOST_REFERENCE_DIR to the reference tree")
 sys.path.insert(0, REF)
 sys.path.insert(0, REPO)
 
