@@ -2,7 +2,8 @@
 
 Drop-in modules mirroring the reference project's entry points:
 
-    bor_solver     solve_bor, solve_bor_pec, BorPecSolver, sphere_generatrix, ...
+    bor_solver     solve_bor, solve_bor_pec, solve_bor_batch, BorPecSolver, sphere_generatrix, ...
+    batch          BorGpuBatch (size classes, CUDA-graph replay), Autotuner
     bor_streaming  StreamingFarBlocks, estimate_streaming_gb
     adjoint        bspline_rcs (torch.autograd.Function), ShapeGradient
     bor_dispatch   solve_monostatic_rcs_bor, solve_adaptive_frequency_sweep_bor,
@@ -15,13 +16,13 @@ All numerics run on one GPU through libghost_bor.so (C ABI in include/ghost_bor.
 from . import bodies, geometry  # noqa: F401
 from .build import build  # noqa: F401
 
-__all__ = ["bodies", "geometry", "build", "bor_solver", "bor_streaming", "engine", "adjoint",
+__all__ = ["bodies", "geometry", "build", "bor_solver", "bor_streaming", "engine", "batch", "adjoint",
            "bor_dispatch", "grim_io"]
 
 
 def __getattr__(name):
     # the GPU modules import torch lazily so that a CPU-only import stays cheap
-    if name in ("bor_solver", "bor_streaming", "engine", "_native", "adjoint", "bor_dispatch",
+    if name in ("bor_solver", "bor_streaming", "engine", "batch", "_native", "adjoint", "bor_dispatch",
                 "grim_io"):
         import importlib
         return importlib.import_module(f".{name}", __name__)

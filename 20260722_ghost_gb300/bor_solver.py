@@ -124,13 +124,17 @@ def _result(prob: BorGpuProblem, res, thetas, form: str, precision: str, mode_to
 
 def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: float = 0.5,
                     mode_tol: float = 1e-6, table_precision: str = "auto",
-                    progress: Optional[Callable] = None) -> List[Dict]:
+                    progress: Optional[Callable] = None, use_graphs: bool = True,
+                    autotune: bool = True) -> List[Dict]:
     """Monostatic RCS of many bodies of revolution on one GPU.
 
     ``bodies``: iterable of dicts with ``points``, ``freq_hz`` and optionally
-    ``n_modes`` (or ``m_max``).  The host set-up of the next body (geometry,
-    near tables, device upload) runs on a worker thread while the GPU sweeps
-    the current one; each sweep batches every mode of its body.  Returns one
+    ``n_modes`` (or ``m_max``).  FP32+IR EFIE sweeps run as size classes
+    (batch.BorGpuBatch): the bodies of a class share one LU, one set of
+    substitutions and one refinement for all their modes, and each class's
+    sweep is a captured CUDA graph; the class width and the near-fill grid come
+    from the autotuner's cache.  FP64 and CFIE / MFIE sweeps run body by body,
+    the next body's host set-up overlapping the current sweep.  Returns one
     ``solve_bor`` result dict per body, in order.  No counterpart in the
     reference (its callers loop over bodies).
     """
@@ -148,6 +152,18 @@ def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: f
         return prob, t0, time.perf_counter()
 
     out: List[Dict] = []
+    if precision == "fp32ir" and form == "efie" and items:
+        from .batch import Autotuner, BorGpuBatch
+        with ThreadPoolExecutor(max_workers=4) as ex:
+            made = list(ex.map(setup, items))
+        probs = [m[0] for m in made]
+        batch = BorGpuBatch(probs, tuner=Autotuner() if autotune else None)
+        results = batch.sweep(use_graphs=use_graphs)
+        for i, ((prob, t0, t1), res) in enumerate(zip(made, results)):
+            out.append(_result(prob, res, thetas, form, precision, mode_tol, None, t0, t1))
+            if progress is not None:
+                progress(i + 1, len(items))
+        return out
     with ThreadPoolExecutor(max_workers=1) as ex:
         nxt = ex.submit(setup, items[0]) if items else None
         for i in range(len(items)):

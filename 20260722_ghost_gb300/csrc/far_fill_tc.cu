@@ -686,11 +686,18 @@ int launch_tc(const TcLayout &L, int NE, int M, int h, double k, double sre, dou
     }
     const size_t smem = sizeof(TcSmem<N>) + 1024;
     auto kern = far_efie_tc_kernel<N>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("far_efie_tc: smem attribute");
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // once per process (and outside any stream capture: the first launch)
+    static bool attr = false;
+    static int nsm = 0;
+    if (!attr) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return check_launch("far_efie_tc: smem attribute");
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+            nsm = 1;
+        attr = true;
+    }
     const int fgroups = (NE + 3) / 4;
     const int nrows = (M + 1 + (N - 2) - 1) / (N - 2);
     const long long ntiles = (long long)nrows * NE * fgroups;

@@ -562,15 +562,24 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
 
 namespace gb {
 // persistent grid of the near kernels: two CTAs per SM
+int g_near_ctas_per_sm = 2;
+
 int near_grid()
 {
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
         sms = 1;
-    return 2 * sms;
+    return __atomic_load_n(&g_near_ctas_per_sm, __ATOMIC_RELAXED) * sms;
 }
 }  // namespace gb
+
+extern "C" int ghost_bor_set_near_grid(int ctas_per_sm)
+{
+    if (ctas_per_sm < 0 || ctas_per_sm > 8) return GHOST_BOR_EINVAL;
+    __atomic_store_n(&gb::g_near_ctas_per_sm, ctas_per_sm == 0 ? 2 : ctas_per_sm, __ATOMIC_RELAXED);
+    return GHOST_BOR_OK;
+}
 
 extern "C" long long ghost_bor_near_workspace(int n_tail_max)
 {
@@ -600,8 +609,14 @@ extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
     if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     auto kern = df ? near_efie_kernel<true, kNcDf> : near_efie_kernel<false, kNc64>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("near_efie: smem attribute");
+    // the largest dynamic shared memory, once per kernel (and before any
+    // stream capture: the first launch); each launch asks for what it needs
+    static bool attr[2] = {false, false};
+    if (!attr[df ? 1 : 0]) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
+            return check_launch("near_efie: smem attribute");
+        attr[df ? 1 : 0] = true;
+    }
     int *status = reinterpret_cast<int *>(work);
     if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_efie: memset");
     const int grid = n_pairs < near_grid() ? n_pairs : near_grid();

@@ -415,25 +415,28 @@ def kernel_work(prob, name):
 
 
 def run_batch(args, rank, world):
-    """Batch workload: every body's sweep back to back (value), the public
-    solve_bor_batch with host inputs (e2e), FP64 plain on every 16th body."""
+    """Batch workload: the 64 seeded bodies as size classes (batch.BorGpuBatch:
+    one LU / substitution / refinement for all modes of the bodies of a class;
+    classes stream through memory when the batch does not fit), the same bodies
+    back to back through the single-body sweep, the public solve_bor_batch with
+    host inputs (e2e), and FP64 plain on every 16th body."""
     import numpy as np
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     eng = importlib.import_module(PKG + ".engine")
     bs = importlib.import_module(PKG + ".bor_solver")
     nat = importlib.import_module(PKG + "._native")
+    bmod = importlib.import_module(PKG + ".batch")
     w = WORKLOADS[args.workload]
     bodies = importlib.import_module(PKG + ".bodies").random_bodies(w["n_bodies"], 0)
     thetas = np.arange(0.0, 180.0 + 1e-9, w["dtheta"])
     probs = [eng.BorGpuProblem(b["points"], b["freq_hz"], thetas, m_max=b["m_max"]) for b in bodies]
     angle_pol = 2 * len(thetas) * len(bodies)
+    batch = bmod.BorGpuBatch(probs, tuner=bmod.Autotuner())
 
     for _ in range(args.warmup):
-        for p in probs:
-            p.sweep("fp32ir")
+        batch.sweep()
     torch.cuda.synchronize()
-    stages, kernel_s, kernel_w = {}, {}, {}
     l0 = nat.launch_count()
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
         torch.cuda.synchronize()
@@ -442,24 +445,33 @@ def run_batch(args, rank, world):
         e0.record()
         last = []
         for _ in range(args.steps):
-            last = []
-            for p in probs:
-                r = p.sweep("fp32ir")
-                last.append(r)
-                for kk, v in r.timings.items():
-                    stages[kk] = stages.get(kk, 0.0) + v / args.steps
-                for kk, v in r.kernel_s.items():
-                    kernel_s.setdefault(kk, []).extend(v)
-                    kernel_w.setdefault(kk, []).extend([kernel_work(p, kk)] * len(v))
+            last = batch.sweep()
         e1.record()
         torch.cuda.synchronize()
     launches = nat.launch_count() - l0
+    if batch.resident():            # graph replays launch no library kernel from the host
+        launches = args.steps * sum(c.launches for c in batch.classes)
     dev_s = max_over_ranks(e0.elapsed_time(e1) / 1e3 / args.steps)
     value = replica_throughput(angle_pol, dev_s)
     clocks = clk.summary()
+    # the same bodies back to back through the single-body sweep
+    stages, kernel_s, kernel_w = {}, {}, {}
+    e0.record()
+    single = []
+    for p in probs:
+        r = p.sweep("fp32ir")
+        single.append(r)
+        for kk, v in r.timings.items():
+            stages[kk] = stages.get(kk, 0.0) + v
+        for kk, v in r.kernel_s.items():
+            kernel_s.setdefault(kk, []).extend(v)
+            kernel_w.setdefault(kk, []).extend([kernel_work(p, kk)] * len(v))
+    e1.record()
+    torch.cuda.synchronize()
+    b2b_s = e0.elapsed_time(e1) / 1e3
     # FP64 plain on every 16th body; the speed-up is taken on the same bodies
     sample = list(range(0, len(probs), 16))
-    t32 = sum(last[i].timings["gpu_total_s"] for i in sample)
+    t32 = sum(single[i].timings["gpu_total_s"] for i in sample)
     e0.record()
     r64 = {i: probs[i].sweep("fp64") for i in sample}
     e1.record()
@@ -478,12 +490,15 @@ def run_batch(args, rank, world):
     h2d = sum(p.h2d_bytes() for p in probs)
     d2h = sum((p.m_max + 1) * 2 * len(thetas) * 16 + (p.m_max + 1) * 20 for p in probs)
     return dict(adjoint=None, value=value, dev_s=dev_s, stages=stages, kernel_s=kernel_s, kernel_work=kernel_w,
-                steps=args.steps, clocks=clocks, launches=launches, f64_s=t64 * dev_s / max(t32, 1e-12),
-                f64_steps=1, f64_note=f"FP64 plain on bodies {sample}: {t64:.2f} s vs FP32+IR {t32:.2f} s, "
-                                      "scaled to the batch by that ratio",
+                steps=1, clocks=clocks, launches=launches, f64_s=t64 * dev_s / max(t32, 1e-12),
+                f64_steps=1, f64_note=f"FP64 plain on bodies {sample}: {t64:.2f} s vs FP32+IR {t32:.2f} s "
+                                      "(single-body sweeps), scaled to the batch by that ratio",
                 db=db, rel=rel, e2e_s=e2e_s, h2d=h2d, d2h=d2h,
                 refine_iters=max(r.refine_iters for r in last), residual=float(max(np.max(r.residual) for r in last)),
-                angle_pol=angle_pol / world * world, M=max(p.m_max for p in probs), thetas=thetas)
+                angle_pol=angle_pol / world * world, M=max(p.m_max for p in probs), thetas=thetas,
+                batch={"classes": batch.summary(), "resident": batch.resident(),
+                       "back_to_back_s": b2b_s, "back_to_back_angle_pol_s": angle_pol / b2b_s,
+                       "batched_s": dev_s, "roofline_note": "roofline and stage times of the back-to-back pass"})
 
 
 def roofline(res, peaks, workload):
@@ -648,6 +663,8 @@ def main():
     }
     if res.get("vs_ref") is not None:
         line["accuracy_vs_reference"] = res["vs_ref"]
+    if res.get("batch") is not None:
+        line["batch"] = res["batch"]
     if res["adjoint"] is not None:
         line["adjoint"] = res["adjoint"]
     print(json.dumps(line))

@@ -142,6 +142,12 @@ int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k,
                           void *work, long long work_bytes,
                           void *Z, long long ldz, long long mode_stride, void *stream);
 
+/* Persistent grid of the near fills: CTAs per SM (default 2; 0 restores it,
+ * at most 8).  The workspace size (ghost_bor_near_workspace,
+ * ghost_bor_near_mfie_workspace) depends on it: query it after a change.  A
+ * tuning knob, process-wide.  No counterpart in the reference. */
+int ghost_bor_set_near_grid(int ctas_per_sm);
+
 /* ------------------------------------------------------------------------
  * FP64-class near/self EFIE fill for the element pairs (e, f), |e - f| <= 1, with
  * the graded-cell + sinh-core + Gauss-tail quadrature of the reference.
