@@ -72,19 +72,26 @@ constexpr int TC_THREADS = (W_PROD0 + NPROD) * 32;
 constexpr int CH = 16;               // orders per epilogue chunk (one tcgen05.ld .x16 per accumulator)
 constexpr int RING = CH + 2;         // order slabs per warp: a chunk plus the two carried orders
 constexpr int SLAB = 17;             // float4 entries per order slab: 16 point pairs + 1 pad
+// float4 entries per order slot of the mode-local blocks (4 blocks x 4 (a, b),
+// + 2 pad) and of the 11-primitive (4 (a, b), + 6 pad): the pads put the 16
+// orders of a chunk's lanes on distinct shared-memory banks
+constexpr int ZLS = 18;
+constexpr int P11S = 10;
 
 template <int N> struct __align__(1024) TcSmem {
     __nv_bfloat16 a[2][ND][TM * TK];     // A stages: 128 rows x 64 B per digit plane
     __nv_bfloat16 b[2][ND][N * TK];      // B stages: N orders x 64 B per digit plane
-    float4 g[NEPI][RING * SLAB];         // per-warp orders of its element pair (double-float)
-    float4 zl[NEPI][RING * 2 * 16];      // per-warp mode-local blocks of every (order, orientation, block, a b)
-    float4 p11[NEPI][RING * 2 * 4];      // per-warp 11-primitive of every (order, orientation, a b)
+    float4 g[NEPI][RING * SLAB];         // per-warp orders of its element pair (complex double-float)
+    float4 zl[NEPI][RING * ZLS];         // per-warp mode-local blocks of every (order, block, a b)
+    float4 p11[NEPI][RING * P11S];       // per-warp 11-primitive of every (order, a b)
     float2 w[NEPI][2][24];               // test / source element weights (double-float)
     float4 sc_tab[kDfTabN];              // sin, cos (j pi / 128) as double-float words
     unsigned long long a_full[2], b_full[2], st_empty[2], t_full[2], t_empty[2], drain;
     uint32_t tmem_base;
     int failed;
 };
+
+static_assert(sizeof(TcSmem<128>) + 1024 <= 227 * 1024, "TC far fill shared memory");
 
 // instruction descriptor: D f32, A/B bf16 (kind::f16), both K-major, M = 128, N
 template <int N> constexpr uint32_t idesc_bf16()
@@ -119,11 +126,45 @@ __device__ __forceinline__ uint32_t sw64_off(int r, int c)
     return (uint32_t)((r >> 3) * 512 + (r & 7) * 64 + ((c ^ ((r >> 1) & 3)) << 4));
 }
 
-// exponent e of the row bound 1/|Delta| (|g| < 2^e for every sample of the pair)
-__device__ __forceinline__ int row_exp(double d2)
+__device__ __forceinline__ float2 bcast(float x) { return make_float2(x, x); }
+
+// |Delta|^2 = (rho_p - rho_q)^2 + (z_p - z_q)^2 of a point pair in double-float.
+// Written with _rn intrinsics, which the compiler neither contracts nor
+// reorders, so that the producers and the epilogue derive bit-identical row
+// exponents from it
+__device__ __forceinline__ float2 pair_d2(float2 rp, float2 zp, float2 rq, float2 zq)
 {
-    const double v = 1.0 / sqrt(d2) * (1.0 + 0x1p-12);
-    return ilogb(v) + 1;
+    float2 d[2];
+    const float2 a[2] = {rp, zp}, b[2] = {rq, zq};
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        const float s = __fsub_rn(a[i].x, b[i].x);
+        const float bb = __fsub_rn(s, a[i].x);
+        const float e = __fadd_rn(__fadd_rn(__fsub_rn(a[i].x, __fsub_rn(s, bb)), __fsub_rn(-b[i].x, bb)),
+                                  __fsub_rn(a[i].y, b[i].y));
+        const float hh = __fadd_rn(s, e);
+        d[i] = make_float2(hh, __fsub_rn(e, __fsub_rn(hh, s)));
+    }
+    float p[2], pe[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        p[i] = __fmul_rn(d[i].x, d[i].x);
+        pe[i] = __fmaf_rn(__fmul_rn(2.0f, d[i].x), d[i].y, __fmaf_rn(d[i].x, d[i].x, -p[i]));
+    }
+    const float s = __fadd_rn(p[0], p[1]);
+    const float bb = __fsub_rn(s, p[0]);
+    const float e = __fadd_rn(__fadd_rn(__fsub_rn(p[0], __fsub_rn(s, bb)), __fsub_rn(p[1], bb)), __fadd_rn(pe[0], pe[1]));
+    const float hh = __fadd_rn(s, e);
+    return make_float2(hh, __fsub_rn(e, __fsub_rn(hh, s)));
+}
+
+// exponent e of the row bound 1/|Delta| (|g| < 2^e for every sample of the
+// pair): the exponent field of rsqrt(|Delta|^2) (1 + 2^-10), the factor
+// covering rsqrtf's and the sampler's relative errors (< 2^-20)
+__device__ __forceinline__ int row_exp(float d2)
+{
+    const float v = __fmul_rn(rsqrtf(d2), 1.0f + 0x1p-10f);
+    return ((__float_as_int(v) >> 23) & 0xff) - 126;
 }
 
 // Green's function samples g = exp(-j k R) / R (the 1/(4 pi) is in the table),
@@ -140,49 +181,58 @@ __device__ __forceinline__ int row_exp(double d2)
 //   roundings of |correction| <= 0.013.
 struct TcGreen {
     float d2h, d2l, a2h, a2l, kh, kl;
-    __device__ void init(double d2, double a2, double k) {
-        d2h = (float)d2; d2l = (float)(d2 - (double)d2h);
-        a2h = (float)a2; a2l = (float)(a2 - (double)a2h);
-        kh = (float)k;   kl = (float)(k - (double)kh);
+    __device__ void init(float2 d2, float2 a2, float2 k) {
+        d2h = d2.x; d2l = d2.y;
+        a2h = a2.x; a2l = a2.y;
+        kh = k.x;   kl = k.y;
     }
-    // g as (re.hi, re.lo, im.hi, im.lo)
-    __device__ __forceinline__ float4 operator()(float2 s2, const float4 *__restrict__ tab) const {
-        const float p = a2h * s2.x;
-        const float pe = fmaf(a2h, s2.x, -p);
-        const float t = d2h + p;
-        const float bb = t - d2h;
-        const float te = (d2h - (t - bb)) + (p - bb);
-        const float lo = te + pe + fmaf(a2h, s2.y, a2l * s2.x) + d2l;
-        const float R2 = t + lo;
-        const float R2l = lo - (R2 - t);
-        const float y = rsqrtf(R2);
-        const float r = R2 * y;
-        const float rl = 0.5f * (fmaf(-r, r, R2) + R2l) * y;
-        const float eps = fmaf(-r, y, 1.0f) - rl * y;        // 1/R = y (1 + eps)
-        const float ph = kh * r;
-        const float phl = fmaf(kh, r, -ph) + fmaf(kh, rl, kl * r);
-        const float q = rintf(ph * kInvTwoPi);
-        const float t1 = fmaf(-q, kTwoPiA, ph);             // exact
-        const float qb = -q * kTwoPiB;                      // exact
-        const float t2 = t1 + qb;
-        const float tb = t2 - t1;
-        const float t2e = (t1 - (t2 - tb)) + (qb - tb);
-        const float dt = fmaf(-q, kTwoPiC, phl) + t2e;
-        const float jf = fminf(128.0f, fmaxf(-128.0f, rintf(t2 * kDf128ByPi)));
-        const float r0 = fmaf(-jf, kDfPiB128_1, t2);        // exact
-        const float rv = fmaf(-jf, kDfPiB128_2, r0 + dt);
-        const float r2 = rv * rv;
-        const float sr = fmaf(rv * r2, -1.0f / 6.0f, rv);   // sin r
-        const float c1 = r2 * fmaf(r2, 1.0f / 24.0f, -0.5f); // cos r - 1
-        const float4 T = tab[(int)jf + 128];                 // sin hi, sin lo, cos hi, cos lo
-        const float s_lo = fmaf(T.z, sr, fmaf(T.x, c1, T.y)) + T.w * sr;
-        const float c_lo = fmaf(-T.x, sr, fmaf(T.z, c1, T.w)) - T.y * sr;
-        const float yl = y * eps, ya = y + yl;
-        const float gr = y * T.z;
-        const float grl = fmaf(y, T.z, -gr) + fmaf(ya, c_lo, yl * T.z);
-        const float gi = y * T.x;
-        const float gil = fmaf(y, T.x, -gi) + fmaf(ya, s_lo, yl * T.x);
-        return make_float4(gr, grl, -gi, -gil);
+    // g of two samples (sin^2 words s2h, s2l of samples A and B) with the f32x2
+    // instructions: (re.hi, re.lo, im.hi, im.lo) each as an (A, B) pair.  The
+    // negations -p, -r, ... are exact products with negated factors, so each
+    // lane takes the same steps as the scalar formulas
+    __device__ __forceinline__ void pair(float2 s2h, float2 s2l, const float4 *__restrict__ tab, float2 &gr,
+                                         float2 &grl, float2 &gi, float2 &gil) const {
+        const float2 A2H = bcast(a2h), D2H = bcast(d2h), KH = bcast(kh);
+        const float2 pn = p2_mul(bcast(-a2h), s2h);                          // -p, p = a2h s2h
+        const float2 pe = p2_fma(A2H, s2h, pn);
+        const float2 t = p2_sub(D2H, pn);                                    // d2h + p
+        const float2 bb = p2_sub(t, D2H);
+        const float2 te = p2_sub(p2_sub(D2H, p2_sub(t, bb)), p2_add(pn, bb)); // (d2h - (t - bb)) + (p - bb)
+        const float2 lo = p2_add(p2_add(p2_add(te, pe), p2_fma(A2H, s2l, p2_mul(bcast(a2l), s2h))), bcast(d2l));
+        const float2 R2 = p2_add(t, lo);
+        const float2 R2l = p2_sub(lo, p2_sub(R2, t));
+        const float2 y = make_float2(rsqrtf(R2.x), rsqrtf(R2.y)), yn = make_float2(-y.x, -y.y);
+        const float2 r = p2_mul(R2, y), rn = p2_mul(R2, yn);                 // r, -r
+        const float2 rl = p2_mul(p2_mul(bcast(0.5f), p2_add(p2_fma(rn, r, R2), R2l)), y);
+        const float2 eps = p2_sub(p2_fma(rn, y, bcast(1.0f)), p2_mul(rl, y));   // 1/R = y (1 + eps)
+        const float2 ph = p2_mul(KH, r), phn = p2_mul(bcast(-kh), r);
+        const float2 phl = p2_add(p2_fma(KH, r, phn), p2_fma(KH, rl, p2_mul(bcast(kl), r)));
+        const float2 rn2 = bcast(12582912.0f);                               // 1.5 2^23: round to nearest even
+        const float2 q = p2_sub(p2_add(p2_mul(ph, bcast(kInvTwoPi)), rn2), rn2);
+        const float2 t1 = p2_fma(q, bcast(-kTwoPiA), ph);                    // exact
+        const float2 qb = p2_mul(q, bcast(-kTwoPiB));                        // exact
+        const float2 t2 = p2_add(t1, qb);
+        const float2 tb = p2_sub(t2, t1);
+        const float2 t2e = p2_add(p2_sub(t1, p2_sub(t2, tb)), p2_sub(qb, tb));
+        const float2 dt = p2_add(p2_fma(q, bcast(-kTwoPiC), phl), t2e);
+        float2 jf = p2_sub(p2_add(p2_mul(t2, bcast(kDf128ByPi)), rn2), rn2);
+        jf = make_float2(fminf(128.0f, fmaxf(-128.0f, jf.x)), fminf(128.0f, fmaxf(-128.0f, jf.y)));
+        const float2 r0 = p2_fma(jf, bcast(-kDfPiB128_1), t2);               // exact
+        const float2 rv = p2_fma(jf, bcast(-kDfPiB128_2), p2_add(r0, dt));
+        const float2 r2 = p2_mul(rv, rv);
+        const float2 sr = p2_fma(p2_mul(rv, r2), bcast(-1.0f / 6.0f), rv);  // sin r
+        const float2 c1 = p2_mul(r2, p2_fma(r2, bcast(1.0f / 24.0f), bcast(-0.5f)));   // cos r - 1
+        const float4 TA = tab[(int)jf.x + 128], TB = tab[(int)jf.y + 128];  // sin hi, sin lo, cos hi, cos lo
+        const float2 Sh = make_float2(TA.x, TB.x), Sl = make_float2(TA.y, TB.y), Ch = make_float2(TA.z, TB.z),
+                     Cl = make_float2(TA.w, TB.w), Shn = make_float2(-TA.x, -TB.x);
+        const float2 s_lo = p2_add(p2_fma(Ch, sr, p2_fma(Sh, c1, Sl)), p2_mul(Cl, sr));
+        const float2 c_lo = p2_sub(p2_fma(Shn, sr, p2_fma(Ch, c1, Cl)), p2_mul(Sl, sr));
+        const float2 yl = p2_mul(y, eps), ya = p2_add(y, yl);
+        gr = p2_mul(y, Ch);
+        grl = p2_add(p2_fma(y, Ch, p2_mul(yn, Ch)), p2_fma(ya, c_lo, p2_mul(yl, Ch)));
+        // the imaginary part -y sin: returned as +y sin, the caller negates its digit scale
+        gi = p2_mul(y, Sh);
+        gil = p2_add(p2_fma(y, Sh, p2_mul(yn, Sh)), p2_fma(ya, s_lo, p2_mul(yl, Sh)));
     }
 };
 
@@ -217,6 +267,69 @@ __device__ __forceinline__ void split4(float2 hi, float2 lo, float sc, uint32_t 
         t = p2_sub(t, d);
     }
 }
+
+// complex double-float with its parts packed for the f32x2 instructions:
+// h = (re.hi, im.hi), l = (re.lo, im.lo), so that one packed instruction takes
+// the same step for the real and the imaginary part.  In shared memory as a
+// float4 (re.hi, im.hi, re.lo, im.lo)
+struct cdf {
+    float2 h, l;
+};
+__device__ __forceinline__ cdf cdf_of(float4 v) { return {make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+__device__ __forceinline__ float4 cdf_f4(const cdf &a) { return make_float4(a.h.x, a.h.y, a.l.x, a.l.y); }
+__device__ __forceinline__ cdf cdf_zero() { return {make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
+__device__ __forceinline__ cdf cdf_neg(const cdf &a) { return {make_float2(-a.h.x, -a.h.y), make_float2(-a.l.x, -a.l.y)}; }
+__device__ __forceinline__ cdf cdf_j(const cdf &a) { return {make_float2(-a.h.y, a.h.x), make_float2(-a.l.y, a.l.x)}; }
+__device__ __forceinline__ cdf cdf_mj(const cdf &a) { return {make_float2(a.h.y, -a.h.x), make_float2(a.l.y, -a.l.x)}; }
+__device__ __forceinline__ cdf cdf_half(const cdf &a) { return {p2_mul(a.h, bcast(0.5f)), p2_mul(a.l, bcast(0.5f))}; }
+
+// s += a w with w a real double-float (df_mac on both parts); s.l is left
+// unnormalised, |s.l| << |s.h|
+__device__ __forceinline__ void cdf_mac(cdf &s, const cdf &a, float2 w)
+{
+    const float2 W = bcast(w.x);
+    const float2 pn = p2_mul(a.h, bcast(-w.x));                              // -p, p = a.h w.hi
+    const float2 pe = p2_fma(a.h, W, pn);                                    // a.h w.hi - p, exact
+    const float2 t = p2_sub(s.h, pn);                                        // s.h + p
+    const float2 bb = p2_sub(t, s.h);
+    const float2 te = p2_sub(p2_sub(s.h, p2_sub(t, bb)), p2_add(pn, bb));    // two-sum error
+    const float2 cr = p2_fma(a.h, bcast(w.y), p2_mul(a.l, W));
+    s.l = p2_add(s.l, p2_add(p2_add(te, pe), cr));
+    s.h = t;
+}
+// a w with w a real double-float, renormalised (df_mul on both parts)
+__device__ __forceinline__ cdf cdf_mulr(const cdf &a, float2 w)
+{
+    const float2 W = bcast(w.x);
+    const float2 pn = p2_mul(a.h, bcast(-w.x));
+    const float2 e = p2_add(p2_fma(a.h, W, pn), p2_fma(a.h, bcast(w.y), p2_mul(a.l, W)));
+    const float2 h = p2_sub(e, pn);                                          // p + e
+    return {h, p2_sub(e, p2_add(h, pn))};                                    // e - (h - p)
+}
+// a + b and a - b, renormalised (df_add on both parts)
+__device__ __forceinline__ cdf cdf_add(const cdf &a, const cdf &b)
+{
+    const float2 s = p2_add(a.h, b.h);
+    const float2 bb = p2_sub(s, a.h);
+    const float2 e = p2_add(p2_add(p2_add(p2_sub(a.h, p2_sub(s, bb)), p2_sub(b.h, bb)), a.l), b.l);
+    const float2 h = p2_add(s, e);
+    return {h, p2_sub(e, p2_sub(h, s))};
+}
+__device__ __forceinline__ cdf cdf_sub(const cdf &a, const cdf &b)
+{
+    const float2 s = p2_sub(a.h, b.h);
+    const float2 bb = p2_sub(s, a.h);                                        // ~ -b.h
+    const float2 e = p2_sub(p2_add(p2_sub(p2_sub(a.h, p2_sub(s, bb)), p2_add(b.h, bb)), a.l), b.l);
+    const float2 h = p2_add(s, e);
+    return {h, p2_sub(e, p2_sub(h, s))};
+}
+
+// -v of a complex double by its sign bits (integer operations)
+__device__ __forceinline__ double dneg(double x)
+{
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+__device__ __forceinline__ double2 dneg2(double2 v) { return make_double2(dneg(v.x), dneg(v.y)); }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 {
@@ -254,8 +367,8 @@ __device__ __forceinline__ bool tile_live(const TileGeo &g, int N) { return g.f0
 
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int M, int h, double k,
-                   double sc_re, double sc_im, const double *__restrict__ geo,
+far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int M, int h, float2 kf,
+                   float2 ik2f, float2 sre, float2 sim, const float2 *__restrict__ geo,
                    const float2 *__restrict__ s2f, const int *__restrict__ hdr, int bA,
                    double2 *__restrict__ Z, long long ldz, long long mode_stride, int *__restrict__ status)
 {
@@ -371,7 +484,9 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
         // ---------------- producers: samples -> digit planes of the A stage
         const int pt = tid - W_PROD0 * 32;
         const int ep = pt >> 6, jq = (pt >> 4) & 3, pp = pt & 15;
-        const float2 *s2q = s2f + jq * 8;
+        // sin^2 of this thread's 8 samples of a stage: 64 aligned bytes (s2f holds Kpad
+        // entries), as (hi_j, hi_j+1, lo_j, lo_j+1) for each even j
+        const float4 *s2q = reinterpret_cast<const float4 *>(s2f + jq * 8);
         long long gs = 0;
         for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
             const TileGeo tg = tile_of(t, NE, fgroups);
@@ -382,11 +497,11 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
             float sc = 0.f;
             if (act) {
                 const int p = 4 * tg.e + (pp >> 2), q = 4 * f + (pp & 3);
-                const double rp = geo[p], zp = geo[P + p], rq = geo[q], zq = geo[P + q];
-                const double dr = rp - rq, dz = zp - zq;
-                const double d2 = dr * dr + dz * dz;
-                smp.init(d2, 4.0 * rp * rq, k);
-                sc = ldexpf(1.0f, bA - row_exp(d2));
+                const float2 rp = geo[p], zp = geo[P + p], rq = geo[q], zq = geo[P + q];
+                const float2 d2 = pair_d2(rp, zp, rq, zq);
+                const float2 a2 = df_mul(rp, rq);
+                smp.init(d2, make_float2(4.0f * a2.x, 4.0f * a2.y), kf);
+                sc = ldexpf(1.0f, bA - row_exp(d2.x));
             }
             const int r_re = ep * 32 + pp, r_im = r_re + 16;
             for (int ks = 0; ks < nst; ++ks, ++gs) {
@@ -396,13 +511,17 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 if (act) {
                     const int j0 = ks * TK + jq * 8;
                     uint32_t wre[4][ND], wim[4][ND];
+                    float4 s4[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) s4[i] = s2q[ks * (TK / 2) + i];
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
-                        float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), g1 = g0;
-                        if (j0 + 2 * i <= h) g0 = smp(s2q[ks * TK + 2 * i], s.sc_tab);
-                        if (j0 + 2 * i + 1 <= h) g1 = smp(s2q[ks * TK + 2 * i + 1], s.sc_tab);
-                        split4(make_float2(g0.x, g1.x), make_float2(g0.y, g1.y), sc, wre[i]);
-                        split4(make_float2(g0.z, g1.z), make_float2(g0.w, g1.w), sc, wim[i]);
+                        // samples j0 + 2i, j0 + 2i + 1; those past h (zero table rows) are zeroed
+                        float2 gr, grl, gi, gil;
+                        smp.pair(make_float2(s4[i].x, s4[i].y), make_float2(s4[i].z, s4[i].w), s.sc_tab, gr, grl, gi, gil);
+                        const float2 live = make_float2(j0 + 2 * i <= h ? 1.0f : 0.0f, j0 + 2 * i + 1 <= h ? 1.0f : 0.0f);
+                        split4(p2_mul(gr, live), p2_mul(grl, live), sc, wre[i]);
+                        split4(p2_mul(gi, live), p2_mul(gil, live), -sc, wim[i]);
                     }
                     unsigned char *abase = reinterpret_cast<unsigned char *>(s.a[st][0]);
 #pragma unroll
@@ -429,9 +548,6 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
         float4 *ZL = s.zl[ep];
         float4 *P11 = s.p11[ep];
         float2 *we = s.w[ep][0], *wf = s.w[ep][1];
-        const double ik2 = 1.0 / (k * k);
-        const float2 ik2f = df_from(ik2);
-        const float2 sre = df_from(sc_re), sim = df_from(sc_im);
         long long ti = 0;
         for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
             const TileGeo tg = tile_of(t, NE, fgroups);
@@ -452,16 +568,16 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
             float2 tre = make_float2(0.f, 0.f), trf = tre, ttf = tre;
             if (act) {
                 if (lane < 24) {
-                    we[lane] = df_from(geo[(size_t)(3 + lane / 4) * P + 4 * e + (lane % 4)]);
-                    wf[lane] = df_from(geo[(size_t)(3 + lane / 4) * P + 4 * f + (lane % 4)]);
+                    we[lane] = geo[(size_t)(3 + lane / 4) * P + 4 * e + (lane % 4)];
+                    wf[lane] = geo[(size_t)(3 + lane / 4) * P + 4 * f + (lane % 4)];
                 }
                 const int p = 4 * e + (pp >> 2), q = 4 * f + (pp & 3);
-                const double dr = geo[p] - geo[q], dz = geo[P + p] - geo[P + q];
-                scl = ldexpf(1.0f, row_exp(dr * dr + dz * dz) - bA - sT);
-                tre = df_from(geo[(size_t)9 * P + 4 * e]);
-                trf = df_from(geo[(size_t)9 * P + 4 * f]);
-                ttf = df_mul(df_from(geo[(size_t)10 * P + 4 * e]), df_from(geo[(size_t)10 * P + 4 * f]));
+                scl = ldexpf(1.0f, row_exp(pair_d2(geo[p], geo[P + p], geo[q], geo[P + q]).x) - bA - sT);
+                tre = geo[(size_t)9 * P + 4 * e];
+                trf = geo[(size_t)9 * P + 4 * f];
+                ttf = df_mul(geo[(size_t)10 * P + 4 * e], geo[(size_t)10 * P + 4 * f]);
             }
+            const float2 htt = df_mulf(df_mul(tre, trf), 0.5f), hre = df_mulf(tre, 0.5f), hrf = df_mulf(trf, 0.5f);
             __syncwarp();
             const uint32_t trow = tmem + ((uint32_t)(ep * 32) << 16) + (uint32_t)(set * 4 * N);
             for (int qc = 0; qc < nch; ++qc) {
@@ -475,15 +591,25 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                     tmem_ld16(trow + (uint32_t)(2 * N + qc * CH), a2);
                     tmem_ld16(trow + (uint32_t)(3 * N + qc * CH), a3);
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
+                    for (int c = 0; c < 16; c += 2) {
                         if (c < c_hi) {
-                            const float x1 = a1[c] * 0x1p-8f;
-                            const float sh = a0[c] + x1;
-                            const float bb = sh - a0[c];
-                            const float sl = (a0[c] - (sh - bb)) + (x1 - bb) + fmaf(a3[c], 0x1p-24f, a2[c] * 0x1p-16f);
-                            const int slot = (qc * CH + c) % RING;
-                            float2 *dst = reinterpret_cast<float2 *>(G + slot * SLAB + pp) + cre;
-                            *dst = make_float2(sh * scl, sl * scl);
+                            const float2 A0 = make_float2(a0[c], a0[c + 1]);
+                            const float2 x1 = p2_mul(make_float2(a1[c], a1[c + 1]), bcast(0x1p-8f));
+                            const float2 sh = p2_add(A0, x1);
+                            const float2 bb = p2_sub(sh, A0);
+                            const float2 sl = p2_add(p2_add(p2_sub(A0, p2_sub(sh, bb)), p2_sub(x1, bb)),
+                                                     p2_fma(make_float2(a3[c], a3[c + 1]), bcast(0x1p-24f),
+                                                            p2_mul(make_float2(a2[c], a2[c + 1]), bcast(0x1p-16f))));
+                            const float2 H = p2_mul(sh, bcast(scl)), L = p2_mul(sl, bcast(scl));
+                            // (re.hi, im.hi, re.lo, im.lo) of point pair pp: this lane holds part cre
+                            float *d0 = reinterpret_cast<float *>(G + ((qc * CH + c) % RING) * SLAB + pp) + cre;
+                            d0[0] = H.x;
+                            d0[2] = L.x;
+                            if (c + 1 < c_hi) {
+                                float *d1 = reinterpret_cast<float *>(G + ((qc * CH + c + 1) % RING) * SLAB + pp) + cre;
+                                d1[0] = H.y;
+                                d1[2] = L.y;
+                            }
                         }
                     }
                 }
@@ -495,9 +621,14 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 }
                 if (!act) continue;
                 __syncwarp();
-                // (2) contraction of both orientations: lane = (order, source node b);
-                //     orientation 0 tests on e, sources on f; orientation 1 the mirror,
-                //     whose point-pair orders are the transpose
+                // (2) contraction: lane = (order, source node b).  The test and the
+                //     source vectors of an element are the same six Gauss-point vectors
+                //     V = (rho T_a w, T_a w, dRT_a w), so with M = V_e^T G V_f both
+                //     orientations read the same 20 entries of M: the forms
+                //     (11, dd, ds, sd, ss) of test node a of e and source node b of f
+                //     are M's entries ((x, a), (y, b)), and those of the mirror (test
+                //     node b of f, source node a of e) are the same entries with ds and
+                //     sd exchanged.  Stored once, for orientation 0
                 {
                     const int nl = qc * CH + (lane >> 1), b = lane & 1;
                     if ((lane >> 1) < c_hi) {
@@ -505,87 +636,85 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                         const float4 *Gf = G + slot * SLAB;
                         const int o = o0 + nl;
                         const float2 fmf = df_mulf(ik2f, (float)o), fm2f = df_mulf(fmf, (float)o);
+                        // G V_f of source node b: (1, s, d) vectors
+                        cdf GR1[4], GRs[4], GRd[4];
+#pragma unroll
+                        for (int g = 0; g < 4; ++g) {
+                            cdf r1 = cdf_zero(), rs = r1, rd = r1;
+#pragma unroll
+                            for (int hq = 0; hq < 4; ++hq) {
+                                const cdf gv = cdf_of(Gf[g * 4 + hq]);
+                                cdf_mac(r1, gv, wf[(0 + b) * 4 + hq]);
+                                cdf_mac(rs, gv, wf[(2 + b) * 4 + hq]);
+                                cdf_mac(rd, gv, wf[(4 + b) * 4 + hq]);
+                            }
+                            GR1[g] = r1;
+                            GRs[g] = rs;
+                            GRd[g] = rd;
+                        }
+                        float4 *zl = ZL + slot * ZLS;
 #pragma unroll 1
-                        for (int ori = 0; ori < 2; ++ori) {
-                            const float2 *wt = ori ? wf : we, *ws = ori ? we : wf;
-                            float4 GR1[4], GRs[4], GRd[4];
+                        for (int a = 0; a < 2; ++a) {
+                            cdf acc[5];
+#pragma unroll
+                            for (int c = 0; c < 5; ++c) acc[c] = cdf_zero();
 #pragma unroll
                             for (int g = 0; g < 4; ++g) {
-                                float2 r1 = make_float2(0, 0), i1 = r1, rs = r1, is = r1, rd = r1, id = r1;
-#pragma unroll
-                                for (int hq = 0; hq < 4; ++hq) {
-                                    const float4 gv = Gf[ori ? hq * 4 + g : g * 4 + hq];
-                                    const float2 gr = make_float2(gv.x, gv.y), gi = make_float2(gv.z, gv.w);
-                                    const float2 w1 = ws[(0 + b) * 4 + hq], wsv = ws[(2 + b) * 4 + hq],
-                                                 wd = ws[(4 + b) * 4 + hq];
-                                    df_mac(r1, gr, w1); df_mac(i1, gi, w1);
-                                    df_mac(rs, gr, wsv); df_mac(is, gi, wsv);
-                                    df_mac(rd, gr, wd); df_mac(id, gi, wd);
-                                }
-                                GR1[g] = make_float4(r1.x, r1.y, i1.x, i1.y);
-                                GRs[g] = make_float4(rs.x, rs.y, is.x, is.y);
-                                GRd[g] = make_float4(rd.x, rd.y, id.x, id.y);
+                                const float2 l1 = we[(0 + a) * 4 + g], ls = we[(2 + a) * 4 + g], ld = we[(4 + a) * 4 + g];
+                                cdf_mac(acc[0], GR1[g], l1);
+                                cdf_mac(acc[1], GRd[g], ld);
+                                cdf_mac(acc[2], GRs[g], ld);
+                                cdf_mac(acc[3], GRd[g], ls);
+                                cdf_mac(acc[4], GRs[g], ls);
                             }
-                            float4 *zl = ZL + (slot * 2 + ori) * 16;
-#pragma unroll 1
-                            for (int a = 0; a < 2; ++a) {
-                                float2 acc2[5][2];
-#pragma unroll
-                                for (int c = 0; c < 5; ++c) { acc2[c][0] = make_float2(0, 0); acc2[c][1] = make_float2(0, 0); }
-#pragma unroll
-                                for (int g = 0; g < 4; ++g) {
-                                    const float2 l1 = wt[(0 + a) * 4 + g], ls = wt[(2 + a) * 4 + g], ld = wt[(4 + a) * 4 + g];
-                                    const float4 q1 = GR1[g], qs = GRs[g], qd = GRd[g];
-                                    df_mac(acc2[0][0], l1, make_float2(q1.x, q1.y)); df_mac(acc2[0][1], l1, make_float2(q1.z, q1.w));
-                                    df_mac(acc2[1][0], ld, make_float2(qd.x, qd.y)); df_mac(acc2[1][1], ld, make_float2(qd.z, qd.w));
-                                    df_mac(acc2[2][0], ld, make_float2(qs.x, qs.y)); df_mac(acc2[2][1], ld, make_float2(qs.z, qs.w));
-                                    df_mac(acc2[3][0], ls, make_float2(qd.x, qd.y)); df_mac(acc2[3][1], ls, make_float2(qd.z, qd.w));
-                                    df_mac(acc2[4][0], ls, make_float2(qs.x, qs.y)); df_mac(acc2[4][1], ls, make_float2(qs.z, qs.w));
-                                }
-                                // p11, pdd, pds, psd, pss of test node a, source node b -> mode-local parts
-                                const int ab = a * 2 + b;
-                                const float2 p11r = acc2[0][0], p11i = acc2[0][1];
-                                P11[(slot * 2 + ori) * 4 + ab] = make_float4(p11r.x, p11r.y, p11i.x, p11i.y);
-                                zl[0 * 4 + ab] = f4(df_sub(df_mul(ttf, p11r), df_mul(ik2f, acc2[1][0])),
-                                                    df_sub(df_mul(ttf, p11i), df_mul(ik2f, acc2[1][1])));
-                                zl[1 * 4 + ab] = f4(df_mul(fmf, acc2[2][1]), df_neg(df_mul(fmf, acc2[2][0])));   // -(j o/k^2) pds
-                                zl[2 * 4 + ab] = f4(df_neg(df_mul(fmf, acc2[3][1])), df_mul(fmf, acc2[3][0]));   // +(j o/k^2) psd
-                                zl[3 * 4 + ab] = f4(df_neg(df_mul(fm2f, acc2[4][0])), df_neg(df_mul(fm2f, acc2[4][1])));
-                            }
+                            // p11, pdd, pds, psd, pss of test node a, source node b -> mode-local parts
+                            const int ab = a * 2 + b;
+                            P11[slot * P11S + ab] = cdf_f4(acc[0]);
+                            zl[0 * 4 + ab] = cdf_f4(cdf_sub(cdf_mulr(acc[0], ttf), cdf_mulr(acc[1], ik2f)));
+                            zl[1 * 4 + ab] = cdf_f4(cdf_mj(cdf_mulr(acc[2], fmf)));     // -(j o/k^2) pds
+                            zl[2 * 4 + ab] = cdf_f4(cdf_j(cdf_mulr(acc[3], fmf)));      // +(j o/k^2) psd
+                            zl[3 * 4 + ab] = cdf_f4(cdf_neg(cdf_mulr(acc[4], fm2f)));
                         }
                     }
                 }
                 __syncwarp();
-                // (3) modes whose orders |m-1|, m, m+1 are all in the ring now, both orientations
+                // (3) modes whose orders |m-1|, m, m+1 are all in the ring now: lane =
+                //     (mode, a b).  The blocks of orientation 0 (rows e + a, columns
+                //     f + b) are tt, t-phi, phi-t, phi-phi = b0..b3; the mirror's
+                //     (rows f + b, columns e + a) follow from the exchange of ds and sd
+                //     and of the tangents t_rho(e), t_rho(f) in the t-phi / phi-t parts:
+                //     b0, -b2, -b1, b3
                 const int mlo = (qc == 0) ? m0 : o0 + qc * CH - 1;
                 const int mhi = min(m1, o0 + qc * CH + c_hi - 2);
                 const int nm = mhi - mlo + 1;
-                for (int job = lane; job < 8 * nm; job += 32) {
-                    const int ori = job & 1, ab = (job >> 1) & 3, m = mlo + (job >> 3);
+                for (int job = lane; job < 4 * nm; job += 32) {
+                    const int ab = job & 3, m = mlo + (job >> 2);
                     const int a = ab >> 1, b = ab & 1;
-                    const float2 t_te = ori ? trf : tre, t_so = ori ? tre : trf;      // t_rho of test / source
-                    const float2 htt = df_mulf(df_mul(t_te, t_so), 0.5f), hre = df_mulf(t_te, 0.5f),
-                                 hrf = df_mulf(t_so, 0.5f);
                     const int sl = (abs(m - 1) - o0) % RING, sm = (m - o0) % RING, sh = (m + 1 - o0) % RING;
-                    const float4 lo = P11[(sl * 2 + ori) * 4 + ab], hi = P11[(sh * 2 + ori) * 4 + ab];
-                    const float4 *zl = ZL + (sm * 2 + ori) * 16;
-                    const float2 Sr = df_add(lo2(lo), lo2(hi)), Si = df_add(hi2(lo), hi2(hi));
-                    const float2 Dr = df_sub(lo2(lo), lo2(hi)), Di = df_sub(hi2(lo), hi2(hi));
-                    float2 br[4], bi[4];
-                    const float4 z0 = zl[0 * 4 + ab], z1 = zl[1 * 4 + ab], z2 = zl[2 * 4 + ab], z3 = zl[3 * 4 + ab];
-                    br[0] = df_add(df_mul(htt, Sr), lo2(z0)); bi[0] = df_add(df_mul(htt, Si), hi2(z0));
-                    br[1] = df_add(df_mul(hre, Di), lo2(z1)); bi[1] = df_sub(hi2(z1), df_mul(hre, Dr));
-                    br[2] = df_sub(lo2(z2), df_mul(hrf, Di)); bi[2] = df_add(df_mul(hrf, Dr), hi2(z2));
-                    br[3] = df_add(df_mulf(Sr, 0.5f), lo2(z3)); bi[3] = df_add(df_mulf(Si, 0.5f), hi2(z3));
-                    double2 *Zm = Z + (size_t)m * mode_stride;
-                    const long long r0 = (ori ? f : e) + a, c0 = (ori ? e : f) + b;
+                    const cdf lo = cdf_of(P11[sl * P11S + ab]), hi = cdf_of(P11[sh * P11S + ab]);
+                    const float4 *zl = ZL + sm * ZLS;
+                    const cdf S = cdf_add(lo, hi), D = cdf_sub(lo, hi);
+                    cdf bq[4];
+                    bq[0] = cdf_add(cdf_mulr(S, htt), cdf_of(zl[0 * 4 + ab]));
+                    bq[1] = cdf_add(cdf_mulr(cdf_mj(D), hre), cdf_of(zl[1 * 4 + ab]));
+                    bq[2] = cdf_add(cdf_mulr(cdf_j(D), hrf), cdf_of(zl[2 * 4 + ab]));
+                    bq[3] = cdf_add(cdf_half(S), cdf_of(zl[3 * 4 + ab]));
+                    double2 v[4];
 #pragma unroll
                     for (int qb = 0; qb < 4; ++qb) {
-                        const long long row = r0 + (qb >> 1) * Nn, col = c0 + (qb & 1) * Nn;
-                        const float2 vr = df_sub(df_mul(sre, br[qb]), df_mul(sim, bi[qb]));
-                        const float2 vi = df_add(df_mul(sre, bi[qb]), df_mul(sim, br[qb]));
-                        catomic_add(Zm + row * ldz + col, make_double2(df_to_bits(vr), df_to_bits(vi)));
+                        // (sre + j sim) b
+                        const cdf w = cdf_add(cdf_mulr(bq[qb], sre), cdf_mulr(cdf_j(bq[qb]), sim));
+                        v[qb] = make_double2(df_to_bits(make_float2(w.h.x, w.l.x)), df_to_bits(make_float2(w.h.y, w.l.y)));
                     }
+                    double2 *Zm = Z + (size_t)m * mode_stride;
+                    const long long re = e + a, cf = f + b;
+#pragma unroll
+                    for (int qb = 0; qb < 4; ++qb)
+                        catomic_add(Zm + (re + (qb >> 1) * Nn) * ldz + cf + (qb & 1) * Nn, v[qb]);
+                    catomic_add(Zm + cf * ldz + re, v[0]);
+                    catomic_add(Zm + cf * ldz + re + Nn, dneg2(v[2]));
+                    catomic_add(Zm + (cf + Nn) * ldz + re, dneg2(v[1]));
+                    catomic_add(Zm + (cf + Nn) * ldz + re + Nn, v[3]);
                 }
                 __syncwarp();
             }
@@ -601,7 +730,8 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
 }
 
 // ---------------------------------------------------------------- tables
-// header: [0] status, [1] sT; then s2f [Kpad] float2; then the digit planes
+// header: [0] status, [1] sT; then s2f, sin^2 of the Kpad samples as double-float
+// words, in pairs of samples (hi_j, hi_j+1, lo_j, lo_j+1); then the digit planes
 // bd [ND][Npad][Kpad] bf16 (orders as rows, samples contiguous)
 __global__ void tc_table_scale_kernel(int h, int Mp, const double *__restrict__ dct, int *__restrict__ hdr)
 {
@@ -637,19 +767,34 @@ __global__ void tc_table_digits_kernel(int h, int Mp, int Npad, int Kpad, const 
             t = (t - d) * 256.0;
         }
         if (o == 0) {
+            // sample pairs (j, j + 1), j even, as (hi_j, hi_j+1, lo_j, lo_j+1)
             const double v = (j <= h) ? sin2[j] : 0.0;
             const float hi = (float)v;
-            s2f[j] = make_float2(hi, (float)(v - (double)hi));
+            float *w = reinterpret_cast<float *>(s2f) + 4 * (j >> 1) + (j & 1);
+            w[0] = hi;
+            w[2] = (float)(v - (double)hi);
         }
+    }
+}
+
+// the geometry rows of the far kernels ([11][P] doubles) as double-float words,
+// so that the fill's per-tile set-up runs on the FP32 pipe
+constexpr int kGeoRows = 11;
+__global__ void tc_geo_kernel(long long n, const double *__restrict__ geo, float2 *__restrict__ gf)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double v = geo[i];
+        const float hi = (float)v;
+        gf[i] = make_float2(hi, (float)(v - (double)hi));
     }
 }
 
 struct TcLayout {
     int N, Npad, Kpad;
-    long long s2_off, bd_off, bytes;
+    long long s2_off, bd_off, geo_off, bytes;
 };
 
-TcLayout tc_layout(int m_max, int nxi)
+TcLayout tc_layout(int n_elem, int m_max, int nxi)
 {
     TcLayout L;
     const int Mp = m_max + 2;
@@ -660,12 +805,13 @@ TcLayout tc_layout(int m_max, int nxi)
     L.Kpad = ((h + 1 + TK - 1) / TK) * TK;
     L.s2_off = 256;
     L.bd_off = 256 + ((8LL * L.Kpad + 255) / 256) * 256;
-    L.bytes = L.bd_off + 2LL * ND * L.Npad * L.Kpad;
+    L.geo_off = ((L.bd_off + 2LL * ND * L.Npad * L.Kpad + 255) / 256) * 256;
+    L.bytes = L.geo_off + 8LL * kGeoRows * 4 * n_elem;
     return L;
 }
 
 template <int N>
-int launch_tc(const TcLayout &L, int NE, int M, int h, double k, double sre, double sim, const double *geo,
+int launch_tc(const TcLayout &L, int NE, int M, int h, float2 kf, float2 ik2f, float2 sre, float2 sim,
               unsigned char *w, int bA, double2 *Z, long long ldz, long long ms, cudaStream_t st)
 {
     auto enc = get_encode();
@@ -702,7 +848,8 @@ int launch_tc(const TcLayout &L, int NE, int M, int h, double k, double sre, dou
     const int nrows = (M + 1 + (N - 2) - 1) / (N - 2);
     const long long ntiles = (long long)nrows * NE * fgroups;
     const int grid = (int)(ntiles < nsm ? ntiles : nsm);
-    kern<<<grid, TC_THREADS, smem, st>>>(map, NE, NE + 1, M, h, k, sre, sim, geo,
+    kern<<<grid, TC_THREADS, smem, st>>>(map, NE, NE + 1, M, h, kf, ik2f, sre, sim,
+                                         reinterpret_cast<const float2 *>(w + L.geo_off),
                                          reinterpret_cast<const float2 *>(w + L.s2_off),
                                          reinterpret_cast<const int *>(w), bA, Z, ldz, ms,
                                          reinterpret_cast<int *>(w));
@@ -712,10 +859,10 @@ int launch_tc(const TcLayout &L, int NE, int M, int h, double k, double sre, dou
 }  // namespace
 }  // namespace gb
 
-extern "C" long long ghost_bor_far_efie_tc_workspace(int m_max, int nxi)
+extern "C" long long ghost_bor_far_efie_tc_workspace(int n_elem, int m_max, int nxi)
 {
-    if (m_max < 0 || nxi < 2 || (nxi & 1)) return -1;
-    return gb::tc_layout(m_max, nxi).bytes;
+    if (n_elem < 0 || m_max < 0 || nxi < 2 || (nxi & 1)) return -1;
+    return gb::tc_layout(n_elem, m_max, nxi).bytes;
 }
 
 extern "C" int ghost_bor_far_efie_tc_tables(int m_max, int nxi, const double *dct, const double *sin2,
@@ -723,10 +870,10 @@ extern "C" int ghost_bor_far_efie_tc_tables(int m_max, int nxi, const double *dc
 {
     using namespace gb;
     if (m_max < 0 || nxi < 2 || (nxi & 1) || !dct || !sin2 || !work ||
-        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_far_efie_tc_workspace(m_max, nxi))
+        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_far_efie_tc_workspace(0, m_max, nxi))
         return GHOST_BOR_EINVAL;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const TcLayout L = tc_layout(m_max, nxi);
+    const TcLayout L = tc_layout(0, m_max, nxi);
     unsigned char *w = reinterpret_cast<unsigned char *>(work);
     const int h = nxi / 2, Mp = m_max + 2;
     tc_table_scale_kernel<<<1, 1024, 0, st>>>(h, Mp, dct, reinterpret_cast<int *>(w));
@@ -746,7 +893,7 @@ extern "C" int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k, d
 {
     using namespace gb;
     if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !Z || !work ||
-        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_far_efie_tc_workspace(m_max, nxi) ||
+        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_far_efie_tc_workspace(n_elem, m_max, nxi) ||
         ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k > 0.0))
         return GHOST_BOR_EINVAL;
     const int h = nxi / 2;
@@ -755,10 +902,20 @@ extern "C" int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k, d
     while (bA > 1 && (long long)(h + 1) << (bA + 7) > (1LL << 24)) --bA;
     if ((long long)(h + 1) << (bA + 7) > (1LL << 24)) return GHOST_BOR_EUNSUPPORTED;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const TcLayout L = tc_layout(m_max, nxi);
+    const TcLayout L = tc_layout(n_elem, m_max, nxi);
     unsigned char *w = reinterpret_cast<unsigned char *>(work);
+    const long long ng = (long long)kGeoRows * 4 * n_elem;
+    tc_geo_kernel<<<(int)((ng + 255) / 256 < 1024 ? (ng + 255) / 256 : 1024), 256, 0, st>>>(
+        ng, geo, reinterpret_cast<float2 *>(w + L.geo_off));
+    const int rc = check_launch("far_efie_tc: geometry words");
+    if (rc) return rc;
+    auto split = [](double v) {
+        const float hi = (float)v;
+        return make_float2(hi, (float)(v - (double)hi));
+    };
+    const float2 kf = split(k), ik2f = split(1.0 / (k * k)), sre = split(scale_re), sim = split(scale_im);
     double2 *Zd = reinterpret_cast<double2 *>(Z);
-    if (L.N == 32) return launch_tc<32>(L, n_elem, m_max, h, k, scale_re, scale_im, geo, w, bA, Zd, ldz, mode_stride, st);
-    if (L.N == 64) return launch_tc<64>(L, n_elem, m_max, h, k, scale_re, scale_im, geo, w, bA, Zd, ldz, mode_stride, st);
-    return launch_tc<128>(L, n_elem, m_max, h, k, scale_re, scale_im, geo, w, bA, Zd, ldz, mode_stride, st);
+    if (L.N == 32) return launch_tc<32>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
+    if (L.N == 64) return launch_tc<64>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
+    return launch_tc<128>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
 }

@@ -196,10 +196,11 @@ class BorGpuProblem:
     # -- stages -----------------------------------------------------------
     def _far_tc_work(self, stream: int):
         """Digit planes of the DCT table for the tensor-core far fill (built once
-        per problem on the device) and the fill's status word."""
+        per problem on the device), room for the fill's double-float geometry
+        words and its status word."""
         if self._far_tc_ws is None:
             lib = nat.load()
-            nbytes = int(lib.ghost_bor_far_efie_tc_workspace(self.m_max, self.n_xi))
+            nbytes = int(lib.ghost_bor_far_efie_tc_workspace(self.N, self.m_max, self.n_xi))
             ws = self.torch.empty(nbytes, dtype=self.torch.uint8, device=self.device)
             nat.call("ghost_bor_far_efie_tc_tables", self.m_max, self.n_xi, nat.ptr(self.d_dct),
                      nat.ptr(self.d_sin2), nat.ptr(ws), nbytes, stream)

@@ -126,15 +126,18 @@ int ghost_bor_far_efie_masked(int prec, int n_elem, int m_max, int nxi, double k
  * point pair).  The operator agrees with the FP64 fill to ~4e-9 of its largest
  * entry (the SIMT FP32 fill: ~7e-8).  Z is complex double; the contribution
  * is ADDED.
- *   work  ghost_bor_far_efie_tc_workspace(m_max, nxi) bytes, 256-byte
- *         aligned, prepared once per (m_max, nxi, table) by
+ *   work  ghost_bor_far_efie_tc_workspace(n_elem, m_max, nxi) bytes,
+ *         256-byte aligned, prepared once per (m_max, nxi, table) by
  *         ghost_bor_far_efie_tc_tables from the `dct` / `sin2` tables of
- *         ghost_bor_far_efie; its first int is a status word, set to 1 if a
- *         bounded pipeline wait gave up (the launch is then incomplete).
+ *         ghost_bor_far_efie (any n_elem's workspace holds the tables; the
+ *         rest is room for the geometry rows as double-float words, which
+ *         each fill call writes from `geo` before its transform); its first
+ *         int is a status word, set to 1 if a bounded pipeline wait gave up
+ *         (the launch is then incomplete).
  * Returns GHOST_BOR_EUNSUPPORTED when nxi/2 + 1 exceeds 2^17 samples.
  * Replaces StreamingFarBlocks._build_range + efie_blocks
  * (bor_streaming.py:220-268, 320-376, 388-407) like ghost_bor_far_efie. */
-long long ghost_bor_far_efie_tc_workspace(int m_max, int nxi);
+long long ghost_bor_far_efie_tc_workspace(int n_elem, int m_max, int nxi);
 int ghost_bor_far_efie_tc_tables(int m_max, int nxi, const double *dct, const double *sin2,
                                  void *work, long long work_bytes, void *stream);
 int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k,

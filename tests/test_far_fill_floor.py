@@ -111,7 +111,7 @@ def tc_dct(samples, d2, table, h, bA=7):
     adding its products one 16-sample MMA step at a time in FP32 rounded toward
     zero (the worst case of a tensor core's accumulation)."""
     with np.errstate(divide="ignore"):                 # near pairs are zeroed afterwards
-        v = 1.0 / np.sqrt(d2) * (1.0 + 2.0 ** -12)
+        v = 1.0 / np.sqrt(d2.astype(f32).astype(np.float64)) * (1.0 + 2.0 ** -10)
     e = np.frexp(v)[1][..., None]                      # v < 2^e
     sc = np.ldexp(1.0, bA - e).astype(f32)
     sT = 7 - (np.frexp(np.max(np.abs(table)))[1] - 1)

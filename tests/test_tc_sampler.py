@@ -56,7 +56,9 @@ TAB = np.array([[*split(np.sin(np.pi * (i - 128) / 128)), *split(np.cos(np.pi * 
 
 
 def tc_green(d2, a2, k, s2, seed_ulps=0):
-    """NumPy FP32 replay of TcGreen::operator(); returns the (hi, lo) FP32 words of re and im."""
+    """NumPy FP32 replay of TcGreen::pair (each lane of its f32x2 steps); returns
+    the (hi, lo) FP32 words of re and im (the kernel carries +y sin for the
+    imaginary part and negates its digit scale instead)."""
     d2h, d2l = split(d2)
     a2h, a2l = split(a2)
     kh, kl = split(np.full_like(np.asarray(d2, f64), k))
