@@ -331,18 +331,17 @@ __device__ __forceinline__ double dneg(double x)
 }
 __device__ __forceinline__ double2 dneg2(double2 v) { return make_double2(dneg(v.x), dneg(v.y)); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+// 16 columns of this warp's 32 TMEM lanes; the loads are asynchronous until
+// tmem_wait_ld, so several can be in flight before one wait
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
 {
-    uint32_t r[16];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32"
                  " {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                    "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
                  : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 struct TileGeo {
     int row, e, f0;
@@ -585,11 +584,20 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
                 // (1) orders as double-float words, ACC0 + 2^-8 ACC1 (two-sum, exact) +
                 //     2^-16 ACC2 + 2^-24 ACC3, times 2^(e_r - bA - sT)
                 if (act) {
+                    uint32_t u0[16], u1[16], u2[16], u3[16];
+                    tmem_ld16(trow + (uint32_t)(qc * CH), u0);
+                    tmem_ld16(trow + (uint32_t)(N + qc * CH), u1);
+                    tmem_ld16(trow + (uint32_t)(2 * N + qc * CH), u2);
+                    tmem_ld16(trow + (uint32_t)(3 * N + qc * CH), u3);
+                    tmem_wait_ld();
                     float a0[16], a1[16], a2[16], a3[16];
-                    tmem_ld16(trow + (uint32_t)(qc * CH), a0);
-                    tmem_ld16(trow + (uint32_t)(N + qc * CH), a1);
-                    tmem_ld16(trow + (uint32_t)(2 * N + qc * CH), a2);
-                    tmem_ld16(trow + (uint32_t)(3 * N + qc * CH), a3);
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) {
+                        a0[c] = __uint_as_float(u0[c]);
+                        a1[c] = __uint_as_float(u1[c]);
+                        a2[c] = __uint_as_float(u2[c]);
+                        a3[c] = __uint_as_float(u3[c]);
+                    }
 #pragma unroll
                     for (int c = 0; c < 16; c += 2) {
                         if (c < c_hi) {

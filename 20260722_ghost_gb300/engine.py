@@ -34,7 +34,7 @@ from __future__ import annotations
 import math
 import time
 from dataclasses import dataclass, field
-from typing import Callable, Dict, List, Optional
+from typing import Callable, Dict, List, Optional, Tuple
 
 import numpy as np
 
@@ -63,6 +63,9 @@ class SweepResult:
     info: Optional[np.ndarray] = None
     gpu_launches: int = 0
     res_history: List[float] = field(default_factory=list)
+    # [iterations + 1, M+1] relative residual of every mode before each correction
+    # and after the last (FP32+IR sweeps)
+    res_history_modes: Optional[np.ndarray] = None
     # device seconds of single launches, bracketed by CUDA events on the launch stream
     kernel_s: Dict[str, List[float]] = field(default_factory=dict)
 
@@ -454,21 +457,24 @@ class BorGpuProblem:
                 chunk = max(1, min(Mb, int(self.update_ws_bytes // max(per, 1))))
                 ex_ws = torch.empty(int(lib.ghost_bor_residual_exact_workspace(chunk, n, nrhs)),
                                     dtype=torch.uint8, device=self.device)
-                ex_flags = torch.zeros((Mb + chunk - 1) // chunk, dtype=torch.int32, device=self.device)
+                ex_flags = torch.zeros(1, dtype=torch.int32, device=self.device)
                 if exact_upd and max_refine > 0:
                     R64 = torch.empty((Mb, n, nrhs), dtype=c128, device=self.device)
 
-                def exact_residual(Xin, Bin, Rout):
-                    """Rout = Bin - (Z_far + Z_near) Xin (Xin FP32), norms[:, 0] = ||Rout||^2."""
-                    for ci, b0 in enumerate(range(0, Mb, chunk)):
-                        nb = min(chunk, Mb - b0)
-                        nat.call("ghost_bor_residual_exact", nb, n, nrhs, Nn, nat.ptr(Zf[b0]), n, Zf.stride(0),
-                                 nat.ptr(band[b0]), nat.ptr(self.d_masks[b0]), nat.ptr(Xin[b0]), nat.ptr(Bin[b0]),
-                                 nrhs, Bin.stride(0), nat.ptr(None if Rout is None else Rout[b0]),
-                                 nat.ptr(R32[b0]), nat.ptr(norms[b0]), nat.ptr(ex_ws), ex_ws.numel(), st)
-                        torch.maximum(ex_flags[ci:ci + 1], ex_ws[:4].view(torch.int32), out=ex_flags[ci:ci + 1])
+                def exact_residual(Xin, Bin, Rout, runs):
+                    """Rout = Bin - (Z_far + Z_near) Xin (Xin FP32), norms[:, 0] = ||Rout||^2,
+                    for the modes of `runs` ([b0, b1) ranges)."""
+                    for r0, r1 in runs:
+                        for b0 in range(r0, r1, chunk):
+                            nb = min(chunk, r1 - b0)
+                            nat.call("ghost_bor_residual_exact", nb, n, nrhs, Nn, nat.ptr(Zf[b0]), n, Zf.stride(0),
+                                     nat.ptr(band[b0]), nat.ptr(self.d_masks[b0]), nat.ptr(Xin[b0]),
+                                     nat.ptr(Bin[b0]), nrhs, Bin.stride(0),
+                                     nat.ptr(None if Rout is None else Rout[b0]), nat.ptr(R32[b0]),
+                                     nat.ptr(norms[b0]), nat.ptr(ex_ws), ex_ws.numel(), st)
+                            torch.maximum(ex_flags, ex_ws[:4].view(torch.int32), out=ex_flags)
 
-                exact_residual(X32, B, R64)
+                exact_residual(X32, B, R64, [(0, Mb)])
             else:
                 if self.tensor_cores:
                     # Z_far is read only by the first residual from here on: split it in
@@ -481,54 +487,65 @@ class BorGpuProblem:
                          nat.ptr(R32), nat.ptr(norms), st)
             kend("residual", k0)
             bn2 = torch.clamp(norms[:, 1].clone(), min=1e-300)
-            rel = float(torch.sqrt(torch.max(norms[:, 0] / bn2)))
-            history = [rel]
-            prev = None
+            rel_d = torch.sqrt(norms[:, 0] / bn2)
+            rel_m = rel_d.cpu().numpy()
+            history = [float(rel_m.max())]
+            hist_modes = [rel_d]
+            live = np.ones(Mb, dtype=bool)
+            prev_m = None
             up_ws = status = None
             for it in range(max_refine):
-                # stop at the residual floor or on stagnation
-                if rel < self.refine_floor or (prev is not None and rel > 0.5 * prev):
+                # each mode stops at the residual floor or when its residual no longer
+                # halves; the corrections run on the runs of modes still live
+                live &= rel_m >= self.refine_floor
+                if prev_m is not None:
+                    live &= rel_m <= 0.5 * prev_m
+                if not live.any():
                     break
-                prev = rel
-                nat.call("ghost_bor_convert", 3, Mb, n, nrhs, nat.ptr(R32), nrhs, R32.stride(0),
-                         nat.ptr(X32), nrhs, X32.stride(0), st)
-                nat.call("ghost_bor_getrs", nat.F32, Mb, n, nrhs, nat.ptr(A), n, A.stride(0),
-                         nat.ptr(ipiv), nat.ptr(X32), nrhs, X32.stride(0), nat.ptr(rs_ws), st)
-                nat.call("ghost_bor_convert", 2, Mb, n, nrhs, nat.ptr(X32), nrhs, X32.stride(0),
-                         nat.ptr(X), nrhs, X.stride(0), st)
+                prev_m = rel_m
+                runs = mode_runs(live)
+                for r0, r1 in runs:
+                    nb = r1 - r0
+                    nat.call("ghost_bor_convert", 3, nb, n, nrhs, nat.ptr(R32[r0]), nrhs, R32.stride(0),
+                             nat.ptr(X32[r0]), nrhs, X32.stride(0), st)
+                    nat.call("ghost_bor_getrs", nat.F32, nb, n, nrhs, nat.ptr(A[r0]), n, A.stride(0),
+                             nat.ptr(ipiv[r0]), nat.ptr(X32[r0]), nrhs, X32.stride(0), nat.ptr(rs_ws), st)
+                    nat.call("ghost_bor_convert", 2, nb, n, nrhs, nat.ptr(X32[r0]), nrhs, X32.stride(0),
+                             nat.ptr(X[r0]), nrhs, X.stride(0), st)
                 k0 = kstart()
                 if R64 is not None and it < n_exact:
                     # R -= (Z_far + Z_near) D with exact products, in FP64 (in place)
-                    exact_residual(X32, R64, R64)
+                    exact_residual(X32, R64, R64, runs)
                 elif self.tensor_cores:
                     if up_ws is None:
                         per = int(lib.ghost_bor_cgemm_tc_workspace(1, n, nrhs, n))
                         chunk = max(1, min(Mb, int(self.update_ws_bytes // max(per, 1))))
                         up_ws = torch.empty(int(lib.ghost_bor_cgemm_tc_workspace(chunk, n, nrhs, n)),
                                             dtype=torch.uint8, device=self.device)
-                        status = torch.zeros(((Mb + chunk - 1) // chunk) * max_refine, dtype=torch.int32,
-                                             device=self.device)
-                    for ci, b0 in enumerate(range(0, Mb, chunk)):
-                        nb = min(chunk, Mb - b0)
-                        nat.call("ghost_bor_cgemm_tc", nb, n, nrhs, n, nat.ptr(Ac[b0]), n, Ac.stride(0),
-                                 nat.ptr(X32[b0]), nrhs, X32.stride(0), nat.ptr(R32[b0]), nrhs, R32.stride(0),
-                                 nat.ptr(up_ws), nat.ptr(status[it * ((Mb + chunk - 1) // chunk) + ci]), st)
+                        status = torch.zeros(1, dtype=torch.int32, device=self.device)
+                    for r0, r1 in runs:
+                        for b0 in range(r0, r1, chunk):
+                            nb = min(chunk, r1 - b0)
+                            nat.call("ghost_bor_cgemm_tc", nb, n, nrhs, n, nat.ptr(Ac[b0]), n, Ac.stride(0),
+                                     nat.ptr(X32[b0]), nrhs, X32.stride(0), nat.ptr(R32[b0]), nrhs,
+                                     R32.stride(0), nat.ptr(up_ws), nat.ptr(status), st)
                 else:
                     # SIMT path: the split-word residual of the updated solution
-                    Rd = torch.empty_like(B)
-                    nat.call("ghost_bor_residual", Mb, n, nrhs, Nn, nat.ptr(Zf), n, Zf.stride(0),
-                             nat.ptr(band), nat.ptr(self.d_masks), nat.ptr(X), nat.ptr(B), nrhs, B.stride(0),
-                             nat.ptr(Rd), nat.ptr(R32), nat.ptr(norms), st)
-                    del Rd
+                    for r0, r1 in runs:
+                        Rd = torch.empty_like(B[r0:r1])
+                        nat.call("ghost_bor_residual", r1 - r0, n, nrhs, Nn, nat.ptr(Zf[r0]), n, Zf.stride(0),
+                                 nat.ptr(band[r0]), nat.ptr(self.d_masks[r0]), nat.ptr(X[r0]), nat.ptr(B[r0]),
+                                 nrhs, B.stride(0), nat.ptr(Rd), nat.ptr(R32[r0]), nat.ptr(norms[r0]), st)
+                        del Rd
                 kend("residual_update", k0)
-                if R64 is not None and it < n_exact:
-                    rn = norms[:, 0].clone()
-                    norms[:, 1].copy_(bn2)          # the kernel's second norm is of its input, R
-                else:
-                    rn = torch.linalg.vector_norm(R32, dim=(1, 2)).double() ** 2
-                    norms[:, 0].copy_(rn)
-                rel = float(torch.sqrt(torch.max(rn / bn2)))
-                history.append(rel)
+                if not (R64 is not None and it < n_exact):
+                    for r0, r1 in runs:
+                        norms[r0:r1, 0] = torch.linalg.vector_norm(R32[r0:r1], dim=(1, 2)).double() ** 2
+                norms[:, 1].copy_(bn2)              # the kernels' second norm is of their input
+                rel_d = torch.sqrt(norms[:, 0] / bn2)
+                rel_m = rel_d.cpu().numpy()
+                history.append(float(rel_m.max()))
+                hist_modes.append(rel_d)
                 iters += 1
                 abort()
             if status is not None and int(status.max()) != 0:
@@ -559,13 +576,26 @@ class BorGpuProblem:
         ks = {k: [a.elapsed_time(b) / 1e3 for a, b in v] for k, v in kev.items()}
         dF_h = dF_h.reshape(Mb, self.T, 2).transpose(0, 2, 1)
         out = SweepResult(dF=np.ascontiguousarray(dF_h), residual=res, refine_iters=iters, timings=tm,
-                          info=info_h, res_history=history if precision == "fp32ir" else [], kernel_s=ks)
+                          info=info_h, res_history=history if precision == "fp32ir" else [], kernel_s=ks,
+                          res_history_modes=(torch.stack(hist_modes).cpu().numpy() if precision == "fp32ir"
+                                             else None))
         if keep:
             out.X = X
             out.B = B
             out.Ve = Ve
             out.lu = lu          # factors, pivots and the unfactored (masked) operator
         return out
+
+
+def mode_runs(live: np.ndarray) -> List[Tuple[int, int]]:
+    """[b0, b1) ranges of consecutive True entries of a per-mode mask."""
+    idx = np.flatnonzero(live)
+    if idx.size == 0:
+        return []
+    cut = np.flatnonzero(np.diff(idx) > 1)
+    starts = np.concatenate([[idx[0]], idx[cut + 1]])
+    ends = np.concatenate([idx[cut], [idx[-1]]]) + 1
+    return [(int(a), int(b)) for a, b in zip(starts, ends)]
 
 
 def replay_truncation(dF: np.ndarray, mode_tol: float):

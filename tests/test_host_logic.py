@@ -184,3 +184,20 @@ def test_non_finite_inputs_rejected_before_device_work(pkg):
                  (pts, -1.0, [0.0]), (pts, 0.0, [0.0])):
         with pytest.raises(ValueError):
             eng.BorGpuProblem(*args)
+
+
+def test_mode_runs_groups_live_modes(pkg):
+    """The refinement corrects only the modes still above the floor, as runs of
+    consecutive modes (one batched launch per run)."""
+    runs = pkg.engine.mode_runs
+    assert runs(np.array([1, 1, 0, 1, 0, 0, 1, 1, 1], bool)) == [(0, 2), (3, 4), (6, 9)]
+    assert runs(np.zeros(5, bool)) == []
+    assert runs(np.ones(4, bool)) == [(0, 4)]
+    rng = np.random.default_rng(3)
+    for _ in range(50):
+        live = rng.random(rng.integers(1, 40)) < 0.5
+        got = np.zeros_like(live)
+        for a, b in runs(live):
+            assert a < b and not got[a:b].any()
+            got[a:b] = True
+        assert np.array_equal(got, live)
