@@ -28,6 +28,13 @@
 //
 // The near band is added to Z_far before the split (A = Z_far + band), so the
 // epilogue only forms R = B - P in FP64 and zeroes the masked rows.
+//
+// Kernel (one CTA per 128 rows x 24 complex right-hand sides): warp 0 streams
+// the A and Bt slices of each 64-wide K stage through a two-stage ring (TMA);
+// warp 1 issues the 14 slice-pair MMAs per 16 K into one of two TMEM
+// accumulator sets (5 levels x 48 columns each), alternating per K chunk;
+// warps 2..9 fold a finished chunk into the double-float accumulators while
+// the MMAs of the next chunk run.  All waits are bounded.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -39,21 +46,23 @@ namespace {
 constexpr int XSA = 5;                   // slices of A (Z_far rows)
 constexpr int XS = 4;                    // slices of Bt (the FP32 solution: 4 slices hold it exactly)
 constexpr int XBM = 128;                 // tile rows
-constexpr int XBN = 64;                  // tile real columns (32 complex rhs)
+constexpr int XBN = 48;                  // tile real columns (24 complex rhs)
 constexpr int XBK = 64;                  // real K per stage (64 bf16 = one 128-byte swizzle row)
 constexpr int XCHUNK = 3;                // stages per exact accumulation (K = 192)
 constexpr int XLEV = 5;                  // levels s + t = 2..6
-constexpr uint32_t XTMEM_COLS = 512;     // power of two >= XLEV * XBN
-constexpr int XTHREADS = 256;            // 8 warps: warps w and w + 4 share TMEM lanes, split the columns
-constexpr int XCOLS = XBN / 2;           // real columns per thread in the fold
+constexpr int XSET = XLEV * XBN;         // TMEM columns of one accumulator set
+constexpr uint32_t XTMEM_COLS = 512;     // two accumulator sets (2 x 240 columns)
+// warps: 0 TMA, 1 MMA, 2..9 fold; the fold of chunk c overlaps the MMAs of chunk c + 1
+constexpr int XW_FOLD0 = 2, XNFOLD = 8;
+constexpr int XTHREADS = (XW_FOLD0 + XNFOLD) * 32;
+constexpr int XCOLS = XBN / 2;           // real columns per fold thread
 constexpr int XA_TILE = XBM * XBK;       // bf16 elements
 constexpr int XB_TILE = XBN * XBK;
 
 struct __align__(1024) XSmem {
     __nv_bfloat16 a[2][XSA][XA_TILE];    // 2 stages x 5 slices x 16 KB
-    __nv_bfloat16 b[2][XS][XB_TILE];     // 2 stages x 4 slices x 8 KB
-    unsigned long long full[2];
-    unsigned long long mma[2];
+    __nv_bfloat16 b[2][XS][XB_TILE];     // 2 stages x 4 slices x 6 KB
+    unsigned long long full[2], empty[2], tfull[2], tempty[2], drain;
     uint32_t tmem_base;
     int failed;
 };
@@ -262,7 +271,13 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int i = 0; i < 2; ++i) { mbar_init(&s.full[i], 1); mbar_init(&s.mma[i], 1); }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&s.full[i], 1);
+            mbar_init(&s.empty[i], 1);
+            mbar_init(&s.tfull[i], 1);
+            mbar_init(&s.tempty[i], XNFOLD);
+        }
+        mbar_init(&s.drain, 1);
         s.failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -270,109 +285,123 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = s.tmem_base;
-    const uint32_t stage_bytes = (uint32_t)((XSA * XA_TILE + XS * XB_TILE) * 2);
+    volatile int *vfailed = &s.failed;
+    auto fail = [&]() {
+        *vfailed = 1;
+        atomicExch(err, 1);
+    };
 
-    // producer state (thread 0 only)
-    uint32_t full_phase[2] = {0, 0}, mma_phase[2] = {0, 0};
-    bool pending[2] = {false, false};
-    bool ok = true;
-    auto load_stage = [&](int ks) {
-        const int st = ks & 1;
-        mbar_expect_tx(&s.full[st], stage_bytes);
+    if (warp == 0) {
+        // ---------------- TMA: the A and Bt slices of each K stage into a 2-stage ring
+        if (lane == 0) {
+            const uint32_t stage_bytes = (uint32_t)((XSA * XA_TILE + XS * XB_TILE) * 2);
+            int ks = 0;
+            for (; ks < nst && !*vfailed; ++ks) {
+                const int st = ks & 1;
+                if (ks >= 2 && !mbar_wait(&s.empty[st], (uint32_t)(((ks >> 1) - 1) & 1))) { fail(); break; }
+                mbar_expect_tx(&s.full[st], stage_bytes);
 #pragma unroll
-        for (int q = 0; q < XSA; ++q) tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
+                for (int q = 0; q < XSA; ++q) tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
 #pragma unroll
-        for (int q = 0; q < XS; ++q) tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
-    };
-    auto wait_mma = [&](int st) {
-        if (!pending[st]) return;
-        if (!mbar_wait(&s.mma[st], mma_phase[st])) ok = false;
-        mma_phase[st] ^= 1u;
-        pending[st] = false;
-    };
-    if (tid == 0) {
-        load_stage(0);
-        if (nst > 1) load_stage(1);
+                for (int q = 0; q < XS; ++q) tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
+            }
+            // drain: every issued copy has landed before the CTA may exit
+            for (int st = 0; st < 2; ++st) {
+                const int n_issued = (ks - st + 1) / 2;
+                if (n_issued > 0 && !mbar_wait(&s.full[st], (uint32_t)((n_issued - 1) & 1))) fail();
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA: chunk c into accumulator set c % 2
+        if (lane == 0) {
+            int ks = 0;
+            bool ok = true;
+            for (int c = 0; c < nch && ok && !*vfailed; ++c) {
+                const int set = c & 1;
+                if (c >= 2 && !mbar_wait(&s.tempty[set], (uint32_t)(((c >> 1) - 1) & 1))) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc_base = tmem + (uint32_t)(set * XSET);
+                const int k_lo = c * XCHUNK, k_hi = min(nst, k_lo + XCHUNK);
+                for (; ks < k_hi; ++ks) {
+                    const int st = ks & 1;
+                    if (!mbar_wait(&s.full[st], (uint32_t)((ks >> 1) & 1))) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                    for (int L = 0; L < XLEV; ++L) {
+                        const int lev = L + 2;
+                        // A slice sa (1..XSA) with Bt slice lev - sa (1..XS)
+                        const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XSA ? lev - 1 : XSA;
+                        for (int sa = s_lo; sa <= s_hi; ++sa) {
+                            const int sb = lev - sa;
+                            const uint32_t ab = smem_u32(s.a[st][sa - 1]), bb = smem_u32(s.b[st][sb - 1]);
+#pragma unroll
+                            for (int kk = 0; kk < XBK / 16; ++kk) {    // 16 bf16 = 32 bytes per MMA
+                                const uint32_t acc = (ks > k_lo || sa > s_lo || kk > 0) ? 1u : 0u;
+                                umma_bf16(acc_base + (uint32_t)(L * XBN), umma_desc_sw128(ab + kk * 32),
+                                          umma_desc_sw128(bb + kk * 32), acc);
+                            }
+                        }
+                    }
+                    umma_commit(&s.empty[st]);          // the stage may be refilled once these MMAs are done
+                }
+                if (!ok) break;
+                umma_commit(&s.tfull[set]);             // the chunk's accumulators are complete
+            }
+            if (!ok) fail();
+            // drain: every issued MMA has completed before TMEM is freed
+            umma_commit(&s.drain);
+            if (!mbar_wait(&s.drain, 0)) fail();
+        }
     }
 
-    // double-float accumulators of this thread's row (TMEM lane 32 (warp % 4) + lane)
-    // and 32 of the tile's 64 real columns (half warp / 4)
-    const int quad = warp & 3, chalf = warp >> 2;
+    // ---------------- fold: each chunk's five exact levels into double-float
+    // (hi, lo) accumulators of this thread's row and 24 of the tile's 48 real
+    // columns.  A warp reads the TMEM lanes of its rank in its warpgroup,
+    // 32 (warp % 4) .. + 31; fold warps 2..5 and 6..9 cover the four quarters
+    // for the two column halves
+    const int fw = warp - XW_FOLD0;
+    const int quad = warp & 3, chalf = fw >> 2;
     float hi[XCOLS], lo[XCOLS];
 #pragma unroll
     for (int c = 0; c < XCOLS; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
-
-    for (int ch = 0; ch < nch; ++ch) {
-        if (tid == 0 && ok) {
-            const int k_lo = ch * XCHUNK, k_hi = min(nst, k_lo + XCHUNK);
-            for (int ks = k_lo; ks < k_hi && ok; ++ks) {
-                const int st = ks & 1;
-                if (!mbar_wait(&s.full[st], full_phase[st])) { ok = false; break; }
-                full_phase[st] ^= 1u;
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-                for (int L = 0; L < XLEV; ++L) {
-                    const int lev = L + 2;
-                    // A slice sa (1..XSA) with Bt slice lev - sa (1..XS)
-                    const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XSA ? lev - 1 : XSA;
-                    for (int sa = s_lo; sa <= s_hi; ++sa) {
-                        const int sb = lev - sa;
-                        const uint32_t ab = smem_u32(s.a[st][sa - 1]), bb = smem_u32(s.b[st][sb - 1]);
-#pragma unroll
-                        for (int kk = 0; kk < XBK / 16; ++kk) {    // 16 bf16 = 32 bytes per MMA
-                            const uint32_t acc = (ks > k_lo || sa > s_lo || kk > 0) ? 1u : 0u;
-                            umma_bf16(tmem + (uint32_t)(L * XBN), umma_desc_sw128(ab + kk * 32),
-                                      umma_desc_sw128(bb + kk * 32), acc);
-                        }
-                    }
-                }
-                umma_commit(&s.mma[st]);
-                pending[st] = true;
-                if (ks + 2 < nst) {
-                    wait_mma(st);                 // the buffer is refilled after its MMAs read it
-                    if (!ok) break;
-                    load_stage(ks + 2);
-                }
-            }
-            // every MMA of this chunk must be complete before its accumulators are read
-            if (ok) wait_mma(0);
-            if (ok) wait_mma(1);
-            if (!ok) {
-                s.failed = 1;
-                atomicExch(err, 1);
-            }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (!s.failed) {
-            const uint32_t row_addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(chalf * XCOLS);
+    if (warp >= XW_FOLD0) {
+        for (int c = 0; c < nch && !*vfailed; ++c) {
+            const int set = c & 1;
+            if (!mbar_wait(&s.tfull[set], (uint32_t)((c >> 1) & 1))) { fail(); break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t row_addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(set * XSET + chalf * XCOLS);
 #pragma unroll
             for (int L = 0; L < XLEV; ++L) {
                 const float sc = ldexpf(1.0f, -14 - 8 * L);
-                float v[32];
-                tmem_ld32(row_addr + (uint32_t)(L * XBN), v);
+                uint32_t u16[16], u8[8];
+                tmem_ld16(row_addr + (uint32_t)(L * XBN), u16);
+                tmem_ld8(row_addr + (uint32_t)(L * XBN + 16), u8);
+                tmem_wait_ld();
 #pragma unroll
-                for (int c = 0; c < XCOLS; ++c) {
+                for (int q = 0; q < XCOLS; ++q) {
                     // x is exact (an integer times a power of two); a two-sum keeps
                     // every level exact in (hi, lo), so lo only collects rounding
                     // errors of hi (~2^-24 |hi|) and stays precise
-                    const float x = v[c] * sc;
-                    const float t = hi[c] + x;
-                    const float bb2 = t - hi[c];
-                    lo[c] += (hi[c] - (t - bb2)) + (x - bb2);
-                    hi[c] = t;
+                    const float x = __uint_as_float(q < 16 ? u16[q] : u8[q - 16]) * sc;
+                    const float t = hi[q] + x;
+                    const float bb2 = t - hi[q];
+                    lo[q] += (hi[q] - (t - bb2)) + (x - bb2);
+                    hi[q] = t;
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&s.tempty[set]);    // the set may take chunk c + 2
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();                         // accumulators consumed: the next chunk may overwrite them
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();                             // every copy, MMA and fold is done: the stages are free
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     // P = 2^(e_i + f_j) (hi + lo) through shared memory (the operand buffers are free)
     double (*Ps)[XBN + 1] = reinterpret_cast<double (*)[XBN + 1]>(&s.a[0][0][0]);
-    if (!s.failed) {
+    const bool good = !*vfailed;
+    if (good && warp >= XW_FOLD0) {
         const int r = quad * 32 + lane;
         const int i = m0 + r;
         const int e = (i < n) ? ex[(size_t)b * n + i] : 0;
@@ -385,41 +414,45 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
         }
     }
     __syncthreads();
-    // R = B - P (the near band is inside the slices), masked rows zero; each warp
-    // 16 rows, lane = complex column; norms in FP32 (reported, not refined)
+    // R = B - P (the near band is inside the slices), masked rows zero; the 8 fold
+    // warps take 16 rows each, lane = complex column (24 per tile); norms in FP32
+    // (reported, not refined)
     float rn = 0.f, bn = 0.f;
-    if (!s.failed) {
+    if (good && warp >= XW_FOLD0) {
         const int *mr = mask_rows + 4 * b;
         const double2 *Bb = B + (size_t)b * sbb;
         const int j = (n0 >> 1) + lane;
-        for (int rr = 0; rr < XBM / 8; ++rr) {
-            const int r = warp * (XBM / 8) + rr;
-            const int i = m0 + r;
-            if (i >= n || j >= nrhs) continue;
-            const double2 bv = Bb[(size_t)i * ldb + j];
-            double2 rv = make_double2(bv.x - Ps[r][2 * lane], bv.y - Ps[r][2 * lane + 1]);
-            if (row_masked(mr, i)) rv = make_double2(0.0, 0.0);
-            if (R) R[(size_t)b * sbb + (size_t)i * ldb + j] = rv;
-            const float2 r32 = make_float2((float)rv.x, (float)rv.y);
-            if (R32) R32[(size_t)b * sbb + (size_t)i * ldb + j] = r32;
-            const float2 b32 = make_float2((float)bv.x, (float)bv.y);
-            rn = fmaf(r32.x, r32.x, fmaf(r32.y, r32.y, rn));
-            bn = fmaf(b32.x, b32.x, fmaf(b32.y, b32.y, bn));
-        }
+        if (lane < XBN / 2)
+            for (int rr = 0; rr < XBM / XNFOLD; ++rr) {
+                const int r = fw * (XBM / XNFOLD) + rr;
+                const int i = m0 + r;
+                if (i >= n || j >= nrhs) continue;
+                const double2 bv = Bb[(size_t)i * ldb + j];
+                double2 rv = make_double2(bv.x - Ps[r][2 * lane], bv.y - Ps[r][2 * lane + 1]);
+                if (row_masked(mr, i)) rv = make_double2(0.0, 0.0);
+                if (R) R[(size_t)b * sbb + (size_t)i * ldb + j] = rv;
+                const float2 r32 = make_float2((float)rv.x, (float)rv.y);
+                if (R32) R32[(size_t)b * sbb + (size_t)i * ldb + j] = r32;
+                const float2 b32 = make_float2((float)bv.x, (float)bv.y);
+                rn = fmaf(r32.x, r32.x, fmaf(r32.y, r32.y, rn));
+                bn = fmaf(b32.x, b32.x, fmaf(b32.y, b32.y, bn));
+            }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         rn += __shfl_xor_sync(0xffffffffu, rn, off);
         bn += __shfl_xor_sync(0xffffffffu, bn, off);
     }
-    if (lane == 0 && !s.failed) {
+    if (lane == 0 && good && warp >= XW_FOLD0) {
         atomicAdd(norms + 2 * b, (double)rn);
         atomicAdd(norms + 2 * b + 1, (double)bn);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(XTMEM_COLS));
+    }
 }
 
 // K-major [batch][rows][Kp] bf16 operand, box 64 x box_rows, 128-byte swizzle
