@@ -29,12 +29,14 @@
 // The near band is added to Z_far before the split (A = Z_far + band), so the
 // epilogue only forms R = B - P in FP64 and zeroes the masked rows.
 //
-// Kernel (one CTA per 128 rows x 24 complex right-hand sides): warp 0 streams
-// the A and Bt slices of each 64-wide K stage through a two-stage ring (TMA);
-// warp 1 issues the 14 slice-pair MMAs per 16 K into one of two TMEM
-// accumulator sets (5 levels x 48 columns each), alternating per K chunk;
-// warps 2..9 fold a finished chunk into the double-float accumulators while
-// the MMAs of the next chunk run.  All waits are bounded.
+// Kernel (one CTA per 128 rows x 48 complex right-hand sides): warp 0 streams
+// the A and Bt slices of each 32-deep K stage through a three-stage ring (TMA,
+// 64-byte swizzle); warp 1 issues the 14 slice-pair MMAs (M = 128, N = 96) per
+// 16 K into the five level accumulators (5 x 96 TMEM columns); warps 2..13 fold
+// each finished K chunk into the double-float accumulators and release TMEM as
+// soon as the chunk is in registers.  The wide N halves the shared-memory
+// reads of the A slices per output column, which bound the MMA issue rate at
+// N = 48.  All waits are bounded.
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -46,30 +48,55 @@ namespace {
 constexpr int XSA = 5;                   // slices of A (Z_far rows)
 constexpr int XS = 4;                    // slices of Bt (the FP32 solution: 4 slices hold it exactly)
 constexpr int XBM = 128;                 // tile rows
-constexpr int XBN = 48;                  // tile real columns (24 complex rhs)
-constexpr int XBK = 64;                  // real K per stage (64 bf16 = one 128-byte swizzle row)
-constexpr int XCHUNK = 3;                // stages per exact accumulation (K = 192)
+constexpr int XBN = 96;                  // tile real columns (48 complex rhs)
+constexpr int XBK = 32;                  // real K per stage (32 bf16 = one 64-byte swizzle row)
+constexpr int XSTAGES = 3;               // operand ring depth
+constexpr int XCHUNK = 6;                // stages per exact accumulation (K = 192)
 constexpr int XLEV = 5;                  // levels s + t = 2..6
-constexpr int XSET = XLEV * XBN;         // TMEM columns of one accumulator set
-constexpr uint32_t XTMEM_COLS = 512;     // two accumulator sets (2 x 240 columns)
-// warps: 0 TMA, 1 MMA, 2..9 fold; the fold of chunk c overlaps the MMAs of chunk c + 1
-constexpr int XW_FOLD0 = 2, XNFOLD = 8;
+constexpr uint32_t XTMEM_COLS = 512;     // one accumulator set of 5 x 96 columns
+// warps: 0 TMA, 1 MMA, 2..13 fold.  A fold warp reads the TMEM lanes of its rank
+// in its warpgroup, 32 (warp % 4) .. + 31, and one of three 32-column groups
+// (14 warps: at most 4 per SM sub-partition, 128 registers each)
+constexpr int XW_FOLD0 = 2, XNFOLD = 12;
 constexpr int XTHREADS = (XW_FOLD0 + XNFOLD) * 32;
-constexpr int XCOLS = XBN / 2;           // real columns per fold thread
+constexpr int XCOLS = XBN / 3;           // real columns per fold thread
+// the slice pairs (A slice, Bt slice) with s + t = 2..6, level by level, and
+// whether a pair is the first of its level (its first MMA of a chunk overwrites)
+constexpr int XPAIRS = 14;
+__device__ constexpr int kPairA[XPAIRS] = {1, 1, 2, 1, 2, 3, 1, 2, 3, 4, 2, 3, 4, 5};
+__device__ constexpr int kPairB[XPAIRS] = {1, 2, 1, 3, 2, 1, 4, 3, 2, 1, 4, 3, 2, 1};
+__device__ constexpr bool kPairFirst[XPAIRS] = {true, true, false, true, false, false, true, false, false, false,
+                                                true, false, false, false};
 constexpr int XA_TILE = XBM * XBK;       // bf16 elements
 constexpr int XB_TILE = XBN * XBK;
 
 struct __align__(1024) XSmem {
-    __nv_bfloat16 a[2][XSA][XA_TILE];    // 2 stages x 5 slices x 16 KB
-    __nv_bfloat16 b[2][XS][XB_TILE];     // 2 stages x 4 slices x 6 KB
-    unsigned long long full[2], empty[2], tfull[2], tempty[2], drain;
+    __nv_bfloat16 a[XSTAGES][XSA][XA_TILE];    // 3 stages x 5 slices x 8 KB
+    __nv_bfloat16 b[XSTAGES][XS][XB_TILE];     // 3 stages x 4 slices x 6 KB
+    unsigned long long full[XSTAGES], empty[XSTAGES], tfull, tempty, drain;
     uint32_t tmem_base;
     int failed;
 };
+static_assert(sizeof(XSmem) + 1024 <= 227 * 1024, "exact residual shared memory");
+static_assert(XBM * (XBN + 1) * sizeof(double) <= sizeof(__nv_bfloat16) * XSTAGES * XSA * XA_TILE,
+              "the P tile fits in the A stages");
 
 // instruction descriptor: D f32, A/B bf16 (kind::f16), both K-major, M = 128, N = 64
 constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XBN >> 3) << 17) |
                                 ((uint32_t)(XBM >> 4) << 24);
+
+// UMMA shared-memory descriptor: K-major operand, 64-byte swizzle, 8-row
+// groups 512 bytes apart (SBO), version 1
+__device__ __forceinline__ uint64_t umma_desc_sw64x(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;
+    d |= (uint64_t)((512u >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    d |= (uint64_t)4u << 61;             // SWIZZLE_64B
+    return d;
+}
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
 {
@@ -251,7 +278,7 @@ struct XMaps {
     CUtensorMap b[XS];
 };
 
-__global__ void __launch_bounds__(XTHREADS)
+__global__ void __launch_bounds__(XTHREADS, 1)
 exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int Kp,
                       const int *__restrict__ ex, const int *__restrict__ fx, const int *__restrict__ mask_rows,
                       const double2 *__restrict__ B, long long ldb, long long sbb,
@@ -271,12 +298,12 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < XSTAGES; ++i) {
             mbar_init(&s.full[i], 1);
             mbar_init(&s.empty[i], 1);
-            mbar_init(&s.tfull[i], 1);
-            mbar_init(&s.tempty[i], XNFOLD);
         }
+        mbar_init(&s.tfull, 1);
+        mbar_init(&s.tempty, XNFOLD);
         mbar_init(&s.drain, 1);
         s.failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -292,13 +319,14 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
     };
 
     if (warp == 0) {
-        // ---------------- TMA: the A and Bt slices of each K stage into a 2-stage ring
+        // ---------------- TMA: the A and Bt slices of each 32-deep K stage into a 3-stage ring
         if (lane == 0) {
             const uint32_t stage_bytes = (uint32_t)((XSA * XA_TILE + XS * XB_TILE) * 2);
             int ks = 0;
             for (; ks < nst && !*vfailed; ++ks) {
-                const int st = ks & 1;
-                if (ks >= 2 && !mbar_wait(&s.empty[st], (uint32_t)(((ks >> 1) - 1) & 1))) { fail(); break; }
+                const int st = ks % XSTAGES;
+                const int use = ks / XSTAGES;
+                if (use > 0 && !mbar_wait(&s.empty[st], (uint32_t)((use - 1) & 1))) { fail(); break; }
                 mbar_expect_tx(&s.full[st], stage_bytes);
 #pragma unroll
                 for (int q = 0; q < XSA; ++q) tma_load_3d(s.a[st][q], &maps.a[q], ks * XBK, m0, b, &s.full[st]);
@@ -306,46 +334,50 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
                 for (int q = 0; q < XS; ++q) tma_load_3d(s.b[st][q], &maps.b[q], ks * XBK, n0, b, &s.full[st]);
             }
             // drain: every issued copy has landed before the CTA may exit
-            for (int st = 0; st < 2; ++st) {
-                const int n_issued = (ks - st + 1) / 2;
+            for (int st = 0; st < XSTAGES; ++st) {
+                const int n_issued = ks > st ? (ks - st + XSTAGES - 1) / XSTAGES : 0;
                 if (n_issued > 0 && !mbar_wait(&s.full[st], (uint32_t)((n_issued - 1) & 1))) fail();
             }
         }
     } else if (warp == 1) {
-        // ---------------- MMA: chunk c into accumulator set c % 2
+        // ---------------- MMA: the K chunks into the accumulator set, one chunk at a time
         if (lane == 0) {
             int ks = 0;
             bool ok = true;
+            // stage-0 descriptors; stage st lies st times a fixed number of 16-byte units further
+            uint64_t adesc[XSA], bdesc[XS];
+#pragma unroll
+            for (int q = 0; q < XSA; ++q) adesc[q] = umma_desc_sw64x(smem_u32(s.a[0][q]));
+#pragma unroll
+            for (int q = 0; q < XS; ++q) bdesc[q] = umma_desc_sw64x(smem_u32(s.b[0][q]));
+            constexpr uint32_t kAStage = XSA * XA_TILE * 2 / 16, kBStage = XS * XB_TILE * 2 / 16;
             for (int c = 0; c < nch && ok && !*vfailed; ++c) {
-                const int set = c & 1;
-                if (c >= 2 && !mbar_wait(&s.tempty[set], (uint32_t)(((c >> 1) - 1) & 1))) { ok = false; break; }
+                // the fold has read the previous chunk's accumulators
+                if (c >= 1 && !mbar_wait(&s.tempty, (uint32_t)((c - 1) & 1))) { ok = false; break; }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t acc_base = tmem + (uint32_t)(set * XSET);
                 const int k_lo = c * XCHUNK, k_hi = min(nst, k_lo + XCHUNK);
                 for (; ks < k_hi; ++ks) {
-                    const int st = ks & 1;
-                    if (!mbar_wait(&s.full[st], (uint32_t)((ks >> 1) & 1))) { ok = false; break; }
+                    const int st = ks % XSTAGES;
+                    if (!mbar_wait(&s.full[st], (uint32_t)((ks / XSTAGES) & 1))) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const bool first = ks == k_lo;
+                    const uint32_t aoff = (uint32_t)st * kAStage, boff = (uint32_t)st * kBStage;
+                    // 14 slice pairs by level; the descriptors step by 32 bytes (2 units)
+                    // per 16-deep MMA
 #pragma unroll
-                    for (int L = 0; L < XLEV; ++L) {
-                        const int lev = L + 2;
-                        // A slice sa (1..XSA) with Bt slice lev - sa (1..XS)
-                        const int s_lo = lev - XS > 1 ? lev - XS : 1, s_hi = lev - 1 < XSA ? lev - 1 : XSA;
-                        for (int sa = s_lo; sa <= s_hi; ++sa) {
-                            const int sb = lev - sa;
-                            const uint32_t ab = smem_u32(s.a[st][sa - 1]), bb = smem_u32(s.b[st][sb - 1]);
+                    for (int pr = 0; pr < XPAIRS; ++pr) {
+                        const int sa = kPairA[pr], sb = kPairB[pr], L = sa + sb - 2;
+                        const uint64_t ad = adesc[sa - 1] + aoff, bd = bdesc[sb - 1] + boff;
 #pragma unroll
-                            for (int kk = 0; kk < XBK / 16; ++kk) {    // 16 bf16 = 32 bytes per MMA
-                                const uint32_t acc = (ks > k_lo || sa > s_lo || kk > 0) ? 1u : 0u;
-                                umma_bf16(acc_base + (uint32_t)(L * XBN), umma_desc_sw128(ab + kk * 32),
-                                          umma_desc_sw128(bb + kk * 32), acc);
-                            }
+                        for (int kk = 0; kk < XBK / 16; ++kk) {
+                            const uint32_t acc = (!first || !kPairFirst[pr] || kk > 0) ? 1u : 0u;
+                            umma_bf16(tmem + (uint32_t)(L * XBN), ad + 2u * kk, bd + 2u * kk, acc);
                         }
                     }
                     umma_commit(&s.empty[st]);          // the stage may be refilled once these MMAs are done
                 }
                 if (!ok) break;
-                umma_commit(&s.tfull[set]);             // the chunk's accumulators are complete
+                umma_commit(&s.tfull);                  // the chunk's accumulators are complete
             }
             if (!ok) fail();
             // drain: every issued MMA has completed before TMEM is freed
@@ -355,43 +387,43 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
     }
 
     // ---------------- fold: each chunk's five exact levels into double-float
-    // (hi, lo) accumulators of this thread's row and 24 of the tile's 48 real
-    // columns.  A warp reads the TMEM lanes of its rank in its warpgroup,
-    // 32 (warp % 4) .. + 31; fold warps 2..5 and 6..9 cover the four quarters
-    // for the two column halves
+    // (hi, lo) accumulators of this thread's row (TMEM lane 32 (warp % 4) + lane)
+    // and 32 of the tile's 96 real columns; the TMA warp keeps loading the next
+    // chunk's stages meanwhile, and the MMAs of the next chunk start as soon as
+    // the last level is in registers
     const int fw = warp - XW_FOLD0;
-    const int quad = warp & 3, chalf = fw >> 2;
+    const int quad = warp & 3, cg = fw >> 2;        // fold warps 2..13: every (quad, cg) once
     float hi[XCOLS], lo[XCOLS];
 #pragma unroll
     for (int c = 0; c < XCOLS; ++c) { hi[c] = 0.f; lo[c] = 0.f; }
     if (warp >= XW_FOLD0) {
         for (int c = 0; c < nch && !*vfailed; ++c) {
-            const int set = c & 1;
-            if (!mbar_wait(&s.tfull[set], (uint32_t)((c >> 1) & 1))) { fail(); break; }
+            if (!mbar_wait(&s.tfull, (uint32_t)(c & 1))) { fail(); break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t row_addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(set * XSET + chalf * XCOLS);
+            const uint32_t row_addr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(cg * XCOLS);
 #pragma unroll
             for (int L = 0; L < XLEV; ++L) {
+                float v[32];
+                tmem_ld32(row_addr + (uint32_t)(L * XBN), v);
+                if (L == XLEV - 1) {
+                    // every level of this chunk is read: the set may take the next chunk
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&s.tempty);
+                }
                 const float sc = ldexpf(1.0f, -14 - 8 * L);
-                uint32_t u16[16], u8[8];
-                tmem_ld16(row_addr + (uint32_t)(L * XBN), u16);
-                tmem_ld8(row_addr + (uint32_t)(L * XBN + 16), u8);
-                tmem_wait_ld();
 #pragma unroll
                 for (int q = 0; q < XCOLS; ++q) {
                     // x is exact (an integer times a power of two); a two-sum keeps
                     // every level exact in (hi, lo), so lo only collects rounding
                     // errors of hi (~2^-24 |hi|) and stays precise
-                    const float x = __uint_as_float(q < 16 ? u16[q] : u8[q - 16]) * sc;
+                    const float x = v[q] * sc;
                     const float t = hi[q] + x;
                     const float bb2 = t - hi[q];
                     lo[q] += (hi[q] - (t - bb2)) + (x - bb2);
                     hi[q] = t;
                 }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&s.tempty[set]);    // the set may take chunk c + 2
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -407,28 +439,27 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
         const int e = (i < n) ? ex[(size_t)b * n + i] : 0;
 #pragma unroll
         for (int c = 0; c < XCOLS; ++c) {
-            const int cc = chalf * XCOLS + c;
+            const int cc = cg * XCOLS + c;
             const int j = (n0 + cc) >> 1;
             const int f = (j < nrhs) ? fx[(size_t)b * nrhs + j] : 0;
             Ps[r][cc] = ((double)hi[c] + (double)lo[c]) * exp2i(e + f);
         }
     }
     __syncthreads();
-    // R = B - P (the near band is inside the slices), masked rows zero; the 8 fold
-    // warps take 16 rows each, lane = complex column (24 per tile); norms in FP32
-    // (reported, not refined)
+    // R = B - P (the near band is inside the slices), masked rows zero; fold warp
+    // fw takes rows fw, fw + 12, ..., lane = complex column (48 per tile, two
+    // passes); norms in FP32 (reported, not refined)
     float rn = 0.f, bn = 0.f;
     if (good && warp >= XW_FOLD0) {
         const int *mr = mask_rows + 4 * b;
         const double2 *Bb = B + (size_t)b * sbb;
-        const int j = (n0 >> 1) + lane;
-        if (lane < XBN / 2)
-            for (int rr = 0; rr < XBM / XNFOLD; ++rr) {
-                const int r = fw * (XBM / XNFOLD) + rr;
+        for (int jc = lane; jc < XBN / 2; jc += 32) {
+            const int j = (n0 >> 1) + jc;
+            for (int r = fw; r < XBM; r += XNFOLD) {
                 const int i = m0 + r;
                 if (i >= n || j >= nrhs) continue;
                 const double2 bv = Bb[(size_t)i * ldb + j];
-                double2 rv = make_double2(bv.x - Ps[r][2 * lane], bv.y - Ps[r][2 * lane + 1]);
+                double2 rv = make_double2(bv.x - Ps[r][2 * jc], bv.y - Ps[r][2 * jc + 1]);
                 if (row_masked(mr, i)) rv = make_double2(0.0, 0.0);
                 if (R) R[(size_t)b * sbb + (size_t)i * ldb + j] = rv;
                 const float2 r32 = make_float2((float)rv.x, (float)rv.y);
@@ -437,6 +468,7 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
                 rn = fmaf(r32.x, r32.x, fmaf(r32.y, r32.y, rn));
                 bn = fmaf(b32.x, b32.x, fmaf(b32.y, b32.y, bn));
             }
+        }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -455,7 +487,7 @@ exact_residual_kernel(const __grid_constant__ XMaps maps, int n, int nrhs, int K
     }
 }
 
-// K-major [batch][rows][Kp] bf16 operand, box 64 x box_rows, 128-byte swizzle
+// K-major [batch][rows][Kp] bf16 operand, box 32 x box_rows, 64-byte swizzle
 bool make_map_bf16(CUtensorMap *map, const __nv_bfloat16 *base, int rows, int Kp, int batch, int box_rows)
 {
     auto enc = get_encode();
@@ -465,7 +497,7 @@ bool make_map_bf16(CUtensorMap *map, const __nv_bfloat16 *base, int rows, int Kp
     const cuuint32_t box[3] = {XBK, (cuuint32_t)box_rows, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims, strides, box,
-               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
