@@ -544,9 +544,11 @@ def roofline(res, peaks, workload):
             samples = float(4 * prob.N) ** 2 * (prob.n_xi // 2 + 1)
             out["fp32_pipe"]["samples_per_s"] = float(f"{samples * len(ks[name]) / t_sum:.4g}")
         if name == "near_fill":
-            out["note"] = ("near fill: 4 flops per azimuth node and order of the cos(m xi) projection; each "
-                           "is a double-float multiply-add on the FP32 pipe (~30 FP32 instructions with the "
-                           "recurrence), and every node's transcendentals run in double-float as well")
+            out["note"] = ("near fill (CUDA cores, FP32 pipe; no tensor-core work -- the schema's compute roof "
+                           "is the bf16 one, fp32_pipe holds the pipe that bounds it): 4 flops per azimuth node "
+                           "and order of the cos(m xi) projection; each is a double-float multiply-add on the "
+                           "FP32 pipe (~20 FP32 instructions with the recurrence), and every node's "
+                           "transcendentals run in double-float as well")
         else:
             out["note"] = ("far fill: 4 flops per far Gauss-point pair, sample and order of the DCT (all "
                            "P^2 pairs; the kernel samples each symmetric pair once and runs the DCT as "
@@ -562,16 +564,17 @@ def roofline(res, peaks, workload):
 # (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of the named workload;
 # None where not captured.
 TRAFFIC = {     # (kernel, workload) -> bytes per launch
-    ("near_fill", "cone_sphere_ka40"): 65.76e9 + 38.90e9,  # per-CTA node scratch
+    ("near_fill", "cone_sphere_ka40"): 21.18e6 + 0.07e6,   # inputs only: nodes stay on chip
+    ("far_fill", "cone_sphere_ka40"): 13.87e9 + 13.06e9,   # Z_far by FP64 atomics (4.7 GB once)
 }
 
 # ncu pipe counters of the fills on the 600-segment cone-sphere (ka = 20), the
 # profiles under profiles/ (the same kernels as the bench runs)
 FILL_COUNTERS = {
-    "far_fill": {"fma_pipe_busy_pct_ncu": 46.9, "issue_active_pct_ncu": 61.9,
-                 "profile": "profiles/far_efie_cone_sphere_ka20.md"},
-    "near_fill": {"fma_pipe_busy_pct_ncu": 47.5, "issue_active_pct_ncu": 37.8,
-                  "profile": "profiles/near_efie_cone_sphere_ka20.md"},
+    "far_fill": {"fma_pipe_busy_pct_ncu": 50.9, "issue_active_pct_ncu": 46.5, "tensor_pipe_pct_ncu": 5.95,
+                 "profile": "profiles/far_efie_tc_cone_sphere_ka20.md"},
+    "near_fill": {"fma_pipe_busy_pct_ncu": 54.4, "issue_active_pct_ncu": 51.7,
+                  "profile": "profiles/near_efie_group_cone_sphere_ka20.md"},
 }
 
 
