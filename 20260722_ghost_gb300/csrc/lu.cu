@@ -143,6 +143,216 @@ panel_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long lo
     }
 }
 
+// ---------------------------------------------------------------------------
+// blocked panel factorisation, FP32 (one CTA per batch matrix): the panel is
+// factored in sub-blocks of PW columns held in registers (each of the 256
+// threads holds rows k0 + t + 256 s, s < RPT), so the pivot search, the row
+// interchanges and the rank-1 updates of a sub-block touch no memory; the
+// sub-block is then written back, its interchanges are applied to the other
+// panel columns, and the rest of the panel gets one rank-PW update
+// (U12 = L11^-1 A12, A22 -= L21 U12) -- one pass over it per sub-block instead
+// of one per column.  Same pivots (LAPACK izamax rule) as panel_kernel.
+// ---------------------------------------------------------------------------
+constexpr int PB_THREADS = 256;
+template <int RPT, int PW>    // rows per thread, columns per sub-block
+__global__ void __launch_bounds__(PB_THREADS, 2)
+panel_blocked_kernel(int n, int k0, int nb, float2 *__restrict__ A, long long lda, long long sa,
+                     int *__restrict__ ipiv, int *__restrict__ info)
+{
+    using CT = float2;
+    const int b = blockIdx.x;
+    CT *Ab = A + (size_t)b * sa;
+    int *piv = ipiv + (size_t)b * n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = PB_THREADS / 32;
+    __shared__ float s_val[NW];
+    __shared__ int s_idx[NW];
+    __shared__ int s_piv;
+    __shared__ CT s_rowp[PW], s_rowc[PW];
+    __shared__ CT s_l11[PW][PW];
+    __shared__ CT s_u12[PW][64];
+
+    for (int c0 = k0; c0 < k0 + nb; c0 += PW) {
+        const int w = min(PW, k0 + nb - c0);
+        CT blk[RPT][PW];
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) {
+            const int i = k0 + tid + PB_THREADS * s;
+#pragma unroll
+            for (int q = 0; q < PW; ++q)
+                blk[s][q] = (i < n && q < w) ? Ab[(size_t)i * lda + c0 + q] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int jj = 0; jj < PW; ++jj) {
+            if (jj >= w) break;
+            const int col = c0 + jj;
+            // --- pivot search over rows >= col: max |re|+|im|, smallest index on ties
+            float best = -1.f;
+            int bi = n;
+#pragma unroll
+            for (int s = 0; s < RPT; ++s) {
+                const int i = k0 + tid + PB_THREADS * s;
+                if (i >= col && i < n) {
+                    const float v = cabs1(blk[s][jj]);
+                    if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+                }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                const float ov = __shfl_down_sync(0xffffffffu, best, off);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+            }
+            if (lane == 0) { s_val[warp] = best; s_idx[warp] = bi; }
+            __syncthreads();
+            if (warp == 0) {
+                best = lane < NW ? s_val[lane] : -1.f;
+                bi = lane < NW ? s_idx[lane] : n;
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float ov = __shfl_down_sync(0xffffffffu, best, off);
+                    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+                }
+                if (lane == 0) {
+                    const int p = (bi < n) ? bi : col;
+                    s_piv = p;
+                    piv[col] = p;
+                    if (!(best > 0.f) && info[b] == 0) info[b] = col + 1;
+                }
+            }
+            __syncthreads();
+            const int p = s_piv;
+            // --- interchange rows col and p of the sub-block (through shared memory)
+            const int oc = (col - k0) % PB_THREADS, sc = (col - k0) / PB_THREADS;
+            const int op = (p - k0) % PB_THREADS, sp = (p - k0) / PB_THREADS;
+#pragma unroll
+            for (int s = 0; s < RPT; ++s) {
+                if (tid == op && s == sp)
+#pragma unroll
+                    for (int q = 0; q < PW; ++q) s_rowp[q] = blk[s][q];
+                if (tid == oc && s == sc)
+#pragma unroll
+                    for (int q = 0; q < PW; ++q) s_rowc[q] = blk[s][q];
+            }
+            __syncthreads();
+            if (p != col) {
+#pragma unroll
+                for (int s = 0; s < RPT; ++s) {
+                    if (tid == oc && s == sc)
+#pragma unroll
+                        for (int q = 0; q < PW; ++q) blk[s][q] = s_rowp[q];
+                    if (tid == op && s == sp)
+#pragma unroll
+                        for (int q = 0; q < PW; ++q) blk[s][q] = s_rowc[q];
+                }
+            }
+            // --- multipliers and the rank-1 update of the sub-block (pivot row = s_rowp)
+            const CT pv = s_rowp[jj];
+            if (pv.x != 0.f || pv.y != 0.f) {
+                const float den = pv.x * pv.x + pv.y * pv.y;
+                const CT inv = make_float2(pv.x / den, -pv.y / den);
+#pragma unroll
+                for (int s = 0; s < RPT; ++s) {
+                    const int i = k0 + tid + PB_THREADS * s;
+                    if (i > col && i < n) {
+                        const CT l = cmul(blk[s][jj], inv);
+                        blk[s][jj] = l;
+#pragma unroll
+                        for (int q = 0; q < PW; ++q)
+                            if (q > jj && q < w) blk[s][q] = cfms(l, s_rowp[q], blk[s][q]);
+                    }
+                }
+            }
+            __syncthreads();                     // s_rowp / s_rowc are reused by the next column
+        }
+        // --- the sub-block back to memory; L11 to shared memory
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) {
+            const int i = k0 + tid + PB_THREADS * s;
+            if (i < n)
+#pragma unroll
+                for (int q = 0; q < PW; ++q)
+                    if (q < w) Ab[(size_t)i * lda + c0 + q] = blk[s][q];
+            if (i >= c0 && i < c0 + w)
+#pragma unroll
+                for (int q = 0; q < PW; ++q) s_l11[i - c0][q] = blk[s][q];
+        }
+        __syncthreads();
+        // --- the sub-block's interchanges on the panel's other columns, in order
+        const int nother = nb - w;
+        for (int jj = 0; jj < w; ++jj) {
+            const int r = c0 + jj, pr = piv[r];
+            if (pr != r)
+                for (int t = tid; t < nother; t += PB_THREADS) {
+                    const int c = k0 + (t < c0 - k0 ? t : t + w);
+                    const CT x = Ab[(size_t)r * lda + c];
+                    Ab[(size_t)r * lda + c] = Ab[(size_t)pr * lda + c];
+                    Ab[(size_t)pr * lda + c] = x;
+                }
+            __syncthreads();
+        }
+        // --- rest of the panel: U12 = L11^-1 A12 (rows c0..c0+w-1), A22 -= L21 U12
+        const int cr = c0 + w, ncol = k0 + nb - cr;
+        if (ncol > 0) {
+            for (int j = tid; j < ncol; j += PB_THREADS) {
+                CT x[PW];
+#pragma unroll
+                for (int r = 0; r < PW; ++r) {
+                    if (r < w) {
+                        CT v = Ab[(size_t)(c0 + r) * lda + cr + j];
+#pragma unroll
+                        for (int q = 0; q < PW; ++q)
+                            if (q < r) v = cfms(s_l11[r][q], x[q], v);
+                        x[r] = v;
+                        Ab[(size_t)(c0 + r) * lda + cr + j] = v;
+                        s_u12[r][j] = v;
+                    }
+                }
+            }
+            __syncthreads();
+            // warps over groups of 32 rows, lanes over the panel's remaining columns
+            // (coalesced); each lane loads the PW multipliers of one row of the group
+            // (the sub-block just written, L2-resident), and a batch of 8 rows' values
+            // is loaded before the first store, so a batch costs one memory latency
+            for (int i0 = cr + 32 * warp; i0 < n; i0 += 32 * NW) {
+                const int ir = i0 + lane;
+                CT lmine[PW];
+#pragma unroll
+                for (int q = 0; q < PW; ++q)
+                    lmine[q] = (ir < n && q < w) ? Ab[(size_t)ir * lda + c0 + q] : make_float2(0.f, 0.f);
+                const int rows = min(32, n - i0);
+                CT *rows0 = Ab + (size_t)i0 * lda + cr;
+                for (int jc = 0; jc < ncol; jc += 32) {
+                    const int j = jc + lane;
+                    const bool act = j < ncol;
+                    CT u[PW];
+#pragma unroll
+                    for (int q = 0; q < PW; ++q) u[q] = act ? s_u12[q][j] : make_float2(0.f, 0.f);
+                    constexpr int QB = RPT >= 12 ? 4 : 8;             // rows per batch of loads
+#pragma unroll 1
+                    for (int q0 = 0; q0 < 32; q0 += QB) {
+                        CT v[QB];
+#pragma unroll
+                        for (int qq = 0; qq < QB; ++qq)
+                            if (act && q0 + qq < rows) v[qq] = rows0[(size_t)(q0 + qq) * lda + j];
+#pragma unroll
+                        for (int qq = 0; qq < QB; ++qq) {
+#pragma unroll
+                            for (int q = 0; q < PW; ++q) {
+                                CT l;
+                                l.x = __shfl_sync(0xffffffffu, lmine[q].x, q0 + qq);
+                                l.y = __shfl_sync(0xffffffffu, lmine[q].y, q0 + qq);
+                                if (q < w) v[qq] = cfms(l, u[q], v[qq]);
+                            }
+                            if (act && q0 + qq < rows) rows0[(size_t)(q0 + qq) * lda + j] = v[qq];
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // apply the panel's interchanges to the columns outside [k0, k0 + nb)
 template <class R>
 __global__ void laswp_kernel(int n, int k0, int nb, C<R> *__restrict__ A, long long lda, long long sa,
@@ -403,6 +613,33 @@ bool look_ahead(LookAhead &L)
     return true;
 }
 
+// the panel of one step: the register-blocked FP32 kernel while its rows fit
+// (n - k0 <= 256 x 24 rows; sub-blocks of 4 columns up to 3072 rows, of 2
+// above), else the column-by-column kernel
+template <class R>
+int panel_launch(int batch, int n, int k0, int nb, C<R> *A, long long lda, long long sa, int *ipiv, int *info,
+                 cudaStream_t st)
+{
+    if constexpr (sizeof(R) == 4) {
+        const int rows = n - k0;
+        if (nb <= 64 && rows <= PB_THREADS * 24) {
+            if (rows <= PB_THREADS * 4)
+                panel_blocked_kernel<4, 4><<<batch, PB_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+            else if (rows <= PB_THREADS * 8)
+                panel_blocked_kernel<8, 4><<<batch, PB_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+            else if (rows <= PB_THREADS * 12)
+                panel_blocked_kernel<12, 4><<<batch, PB_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+            else if (rows <= PB_THREADS * 16)
+                panel_blocked_kernel<16, 2><<<batch, PB_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+            else
+                panel_blocked_kernel<24, 2><<<batch, PB_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+            return check_launch("getrf: blocked panel");
+        }
+    }
+    panel_kernel<R><<<batch, PANEL_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
+    return check_launch("getrf: panel");
+}
+
 // Right-looking blocked LU with one step of look-ahead: the trailing update of
 // step k is split into the next panel's NB columns (caller's stream) and the
 // remaining columns (side stream), so the panel of step k + 1 -- a
@@ -423,8 +660,7 @@ int getrf_impl(int batch, int n, C<R> *A, long long lda, long long sa, int *ipiv
     int rc;
     for (int k0 = 0; k0 < n; k0 += NB) {
         const int nb = min(NB, n - k0);
-        panel_kernel<R><<<batch, PANEL_THREADS, 0, st>>>(n, k0, nb, A, lda, sa, ipiv, info);
-        if ((rc = check_launch("getrf: panel"))) return rc;
+        if ((rc = panel_launch<R>(batch, n, k0, nb, A, lda, sa, ipiv, info, st))) return rc;
         if (rest_pending) {
             // the row swaps below touch the columns the side stream is updating
             if (cudaStreamWaitEvent(st, L.rest, 0) != cudaSuccess) return check_launch("getrf: wait");

@@ -198,6 +198,60 @@ def test_singular_pivot_reported(pkg, torch):
     assert int(info.cpu()[0]) == 41
 
 
+@pytest.mark.parametrize("n", [700, 1500, 2900, 3200, 6002])
+def test_blocked_panel_lu_sizes(pkg, torch, n):
+    """The FP32 LU with the register-blocked panel (256 threads holding 4, 8,
+    12, 16 or 24 rows each, sub-blocks of 4 or 2 columns) on the
+    tensor-core path: solution vs numpy, the pivoting bound, and the pivots of
+    an FP64 LU of the same matrix where no near-tie decides them."""
+    nat = pkg._native
+    rng = np.random.default_rng(n)
+    batch, nrhs = 2, 8
+    A = rng.standard_normal((batch, n, n)) + 1j * rng.standard_normal((batch, n, n))
+    A[:, : n // 3, :] *= 1e-2                   # pivots come from below
+    B = rng.standard_normal((batch, n, nrhs)) + 1j * rng.standard_normal((batch, n, nrhs))
+    X_ref = np.linalg.solve(A, B)
+    p = nat.F32
+    dA = torch.as_tensor(A, device="cuda").to(torch.complex64).contiguous()
+    dB = torch.as_tensor(B, device="cuda").to(torch.complex64).contiguous()
+    ipiv = torch.empty((batch, n), dtype=torch.int32, device="cuda")
+    info = torch.empty((batch,), dtype=torch.int32, device="cuda")
+    st = nat.stream_handle()
+    lib = nat.load()
+    wf = torch.empty(int(lib.ghost_bor_getrf_workspace(p, batch, n)), dtype=torch.uint8, device="cuda")
+    ws = torch.empty(int(lib.ghost_bor_getrs_workspace(p, batch, n, nrhs)), dtype=torch.uint8, device="cuda")
+    nat.call("ghost_bor_getrf", p, batch, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info), nat.ptr(wf), st)
+    nat.call("ghost_bor_getrs", p, batch, n, nrhs, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(dB),
+             nrhs, n * nrhs, nat.ptr(ws), st)
+    torch.cuda.synchronize()
+    assert int(wf[:4].view(torch.int32)[0].cpu()) == 0 and int(ws[:4].view(torch.int32)[0].cpu()) == 0
+    assert np.all(info.cpu().numpy() == 0)
+    X = dB.cpu().numpy()
+    # FP32 LU of a random n x n system: error ~ n eps_32 kappa
+    assert rel(X, X_ref) < 2e-2, rel(X, X_ref)
+    L = np.tril(dA.cpu().numpy(), -1)
+    assert np.max(np.abs(L)) <= math.sqrt(2.0) * (1.0 + 1e-5)
+    # the first panel's pivots equal those of the FP64 LU (no near-ties at this scale)
+    dA64 = torch.as_tensor(A, device="cuda").contiguous()
+    ip64 = torch.empty_like(ipiv)
+    nat.call("ghost_bor_getrf", nat.F64, batch, n, nat.ptr(dA64), n, n * n, nat.ptr(ip64), nat.ptr(info), 0, st)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ipiv.cpu().numpy()[:, :16], ip64.cpu().numpy()[:, :16])
+
+
+def test_singular_pivot_reported_blocked_panel(pkg, torch):
+    nat = pkg._native
+    n = 300
+    A = np.eye(n, dtype=np.complex64)
+    A[40, 40] = 0.0
+    dA = torch.as_tensor(A[None], device="cuda").contiguous()
+    ipiv = torch.empty((1, n), dtype=torch.int32, device="cuda")
+    info = torch.empty((1,), dtype=torch.int32, device="cuda")
+    nat.call("ghost_bor_getrf", nat.F32, 1, n, nat.ptr(dA), n, n * n, nat.ptr(ipiv), nat.ptr(info), 0,
+             nat.stream_handle())
+    assert int(info.cpu()[0]) == 41
+
+
 def test_bessel_rhs_against_scipy(pkg, torch):
     """Miller-recurrence Bessel tables inside the excitation kernel vs scipy jv,
     through rhs_mode at large orders and arguments."""
