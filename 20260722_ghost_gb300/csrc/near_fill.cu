@@ -592,7 +592,8 @@ __device__ __forceinline__ void project_group2(float4 (&dacc)[kOrdG], int nord, 
     float2 C0h = make_float2(cc0.x, cc1.x), C0l = make_float2(cc0.y, cc1.y);
 #pragma unroll
     for (int n = 0; n < kOrdG; ++n) {
-        if (n < nord) {
+        if (n >= nord) break;                  // uniform across the warp: no predicated tail
+        {
             float2 Sh = make_float2(dacc[n].x, dacc[n].y), Sl = make_float2(dacc[n].z, dacc[n].w);
             p2_df_mac(Sh, Sl, Gh0, Gl0, NGh0, make_float2(C0h.x, C0h.x), make_float2(C0l.x, C0l.x));
             p2_df_mac(Sh, Sl, Gh1, Gl1, NGh1, make_float2(C0h.y, C0h.y), make_float2(C0l.y, C0l.y));
