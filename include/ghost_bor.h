@@ -145,10 +145,12 @@ int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k,
                           void *work, long long work_bytes,
                           void *Z, long long ldz, long long mode_stride, void *stream);
 
-/* Persistent grid of the near fills: CTAs per SM (default 2; 0 restores it,
- * at most 8).  The workspace size (ghost_bor_near_workspace,
- * ghost_bor_near_mfie_workspace) depends on it: query it after a change.  A
- * tuning knob, process-wide.  No counterpart in the reference. */
+/* Persistent grid of the near fills: CTAs per SM (default: 2 for the
+ * per-thread kernels, every resident CTA for the grouped double-float EFIE
+ * kernel; 0 restores the defaults, at most 8).  The workspace size
+ * (ghost_bor_near_workspace, ghost_bor_near_mfie_workspace) depends on it:
+ * query it after a change.  A tuning knob, process-wide.  No counterpart in
+ * the reference. */
 int ghost_bor_set_near_grid(int ctas_per_sm);
 
 /* ------------------------------------------------------------------------
@@ -166,13 +168,16 @@ int ghost_bor_set_near_grid(int ctas_per_sm);
  * dense complex double Z[m].  `prec` selects the arithmetic: GHOST_BOR_F64 =
  * FP64 throughout; GHOST_BOR_F32 = double-float (two FP32 words, ~48-bit) on
  * the FP32 pipe for the azimuth-node transcendentals, the cos(m xi) projection
- * and the order GEMM (agrees with the FP64 result to ~1e-13 of the band).
+ * and the order GEMM (agrees with the FP64 result to ~3e-11 of each mode's
+ * largest band entry).  For m_max + 2 <= 256 the F32 fill runs a grouped
+ * kernel: 2..16 lanes share a point pair, each holding every G-th order in
+ * registers, so the azimuth nodes never leave the chip; otherwise (and for
+ * F64) each CTA of the persistent grid keeps the nodes of its 128 point pairs
+ * in the workspace, so the transcendental functions still run once per node.
  * work: ghost_bor_near_workspace(n_tail_max) bytes, 256-byte aligned, where
  * n_tail_max >= every n_tail of `tails`; its first int is a status word set to
- * 1 if a pair had a larger n_tail (that pair is then skipped).  Each CTA of the
- * persistent grid keeps the azimuth nodes of its 128 point pairs there (and
- * the double-float tail rule of its current pair), so the transcendental
- * functions run once per node.
+ * 1 if a pair had a larger n_tail (that pair is then skipped); it also holds
+ * the double-float tail rule of each CTA's current pair.
  * Replaces _near_pair_data + modal_kernels_near + the near loop of
  * assemble_mode (bor_solver.py:270-336, bor_kernels.py:170-257).
  */
