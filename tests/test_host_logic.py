@@ -201,3 +201,46 @@ def test_mode_runs_groups_live_modes(pkg):
             assert a < b and not got[a:b].any()
             got[a:b] = True
         assert np.array_equal(got, live)
+
+
+def test_far_blocks_mirror_relation(oracle):
+    """The relation the tensor-core far fill writes the mirror pair with: for
+    node pairs reached only by far element pairs (|i - j| >= 3), the EFIE
+    operator of every mode satisfies Z_tt^T = Z_tt, Z_ff^T = Z_ff and
+    Z_tf^T = -Z_ft, so the blocks of (f, e) are b0, -b2, -b1, b3 of (e, f)."""
+    D = load_golden("conesphere_n40")
+    s = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    M = int(D["m_max"])
+    s.prepare(M, efie=True)
+    Nn = s.geo.Nn
+    far = np.abs(np.arange(Nn)[:, None] - np.arange(Nn)[None, :]) >= 3
+    for m in (0, 1, 4, M):
+        Z = s.assemble_efie(m, M)
+        tt, tf, ft, ff = Z[:Nn, :Nn], Z[:Nn, Nn:], Z[Nn:, :Nn], Z[Nn:, Nn:]
+        top = np.max(np.abs(Z))
+        assert np.max(np.abs((tt - tt.T)[far])) <= 1e-13 * top, m
+        assert np.max(np.abs((ff - ff.T)[far])) <= 1e-13 * top, m
+        assert np.max(np.abs((tf + ft.T)[far])) <= 1e-13 * top, m
+
+
+def test_step_g_chebyshev_recurrence_covers_every_order():
+    """The grouped near kernel's order mapping: lane q of G starts the step-G
+    recurrence c_{n+G} = 2 cos(G xi) c_n - c_{n-G} from (cos((G - q) xi),
+    cos(q xi)) (cos((q - G) xi) = cos((G - q) xi)) and visits n = q, q + G, ...;
+    every order is visited once and gets cos(n xi)."""
+    rng = np.random.default_rng(4)
+    for G in (2, 4, 8, 16):
+        Mp = 16 * G - 3
+        xi = rng.uniform(0.0, np.pi, 64)
+        T = np.cos(np.arange(G + 1)[:, None] * xi[None, :])        # the evaluating lane's ladder
+        got = np.full((Mp, xi.size), np.nan)
+        for q in range(G):
+            cm, c0, t = T[G - q], T[q], 2.0 * T[G]
+            for i in range((Mp + G - 1) // G):
+                n = q + i * G
+                if n < Mp:
+                    assert np.all(np.isnan(got[n]))
+                    got[n] = c0
+                cm, c0 = c0, t * c0 - cm
+        assert not np.any(np.isnan(got))
+        np.testing.assert_allclose(got, np.cos(np.arange(Mp)[:, None] * xi[None, :]), rtol=0, atol=1e-11)
