@@ -318,7 +318,7 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
                 }
             }
         }
-        __syncthreads();      // every job of this round has read its orders
+        __syncthreads();      // every job of this pass has read its orders
         if constexpr (sizeof(R) == 4) {
             if (doit) {
                 // mode-local parts in double-float (the FP64 pipe is ~1/64 of FP32)
