@@ -33,6 +33,7 @@ SIGNATURES = {
     "ghost_bor_far_efie_tc_workspace": (_ll, [_i, _i, _i]),
     "ghost_bor_far_efie_tc_tables": (_i, [_i, _i, _vp, _vp, _vp, _ll, _vp]),
     "ghost_bor_far_efie_tc": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _ll, _vp, _ll, _ll, _vp]),
+    "ghost_bor_far_efie_tc_masked": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _ll, _vp, _ll, _ll, _vp]),
     "ghost_bor_set_near_grid": (_i, [_i]),
     "ghost_bor_near_workspace": (_ll, [_i]),
     "ghost_bor_near_efie": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _i,

@@ -350,13 +350,28 @@ __device__ __forceinline__ TileGeo tile_of(long long t, int N, int fgroups)
 // far element pairs are visited once, as (e, f) with f >= e + 2; the mirror
 // (f, e) reuses the same transform
 __device__ __forceinline__ bool pair_active(int e, int f, int N) { return f < N && f >= e + 2; }
+// with an element mask (NULL: every pair): only the pairs that touch a masked
+// element, and only the tiles that hold one (every warp role applies the same test)
+__device__ __forceinline__ bool pair_active(int e, int f, int N, const unsigned char *mask)
+{
+    return pair_active(e, f, N) && (!mask || mask[e] || mask[f]);
+}
 // a tile with at least one visited pair
 __device__ __forceinline__ bool tile_live(const TileGeo &g, int N) { return g.f0 + 3 >= g.e + 2 && g.f0 < N; }
+__device__ __forceinline__ bool tile_live(const TileGeo &g, int N, const unsigned char *mask)
+{
+    if (!tile_live(g, N)) return false;
+    if (!mask || mask[g.e]) return true;
+    for (int j = 0; j < 4; ++j)
+        if (pair_active(g.e, g.f0 + j, N) && mask[g.f0 + j]) return true;
+    return false;
+}
 
 template <int N>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int M, int h, float2 kf,
                    float2 ik2f, float2 sre, float2 sim, const float2 *__restrict__ geo,
+                   const unsigned char *__restrict__ emask,
                    const float2 *__restrict__ s2f, const int *__restrict__ hdr, int bA,
                    double2 *__restrict__ Z, long long ldz, long long mode_stride, int *__restrict__ status)
 {
@@ -407,7 +422,7 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
             long long gs = 0;                                  // global stage counter
             for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
                 const TileGeo tg = tile_of(t, NE, fgroups);
-                if (!tile_live(tg, NE)) continue;
+                if (!tile_live(tg, NE, emask)) continue;
                 const int o0 = max(0, tg.row * (N - 2) - 1);
                 for (int ks = 0; ks < nst; ++ks, ++gs) {
                     const int st = (int)(gs & 1);
@@ -429,7 +444,7 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
         if (lane == 0) {
             long long gs = 0, ti = 0;
             for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
-                if (!tile_live(tile_of(t, NE, fgroups), NE)) continue;
+                if (!tile_live(tile_of(t, NE, fgroups), NE, emask)) continue;
                 const int set = (int)(ti % NSET);
                 const long long tuse = ti / NSET;
                 ++ti;
@@ -478,9 +493,9 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
         long long gs = 0;
         for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
             const TileGeo tg = tile_of(t, NE, fgroups);
-            if (!tile_live(tg, NE)) continue;
+            if (!tile_live(tg, NE, emask)) continue;
             const int f = tg.f0 + ep;
-            const bool act = pair_active(tg.e, f, NE);
+            const bool act = pair_active(tg.e, f, NE, emask);
             TcGreen smp;
             float sc = 0.f;
             if (act) {
@@ -539,9 +554,9 @@ far_efie_tc_kernel(const __grid_constant__ CUtensorMap bmap, int NE, int Nn, int
         long long ti = 0;
         for (long long t = blockIdx.x; t < ntiles && !*vfailed; t += gridDim.x) {
             const TileGeo tg = tile_of(t, NE, fgroups);
-            if (!tile_live(tg, NE)) continue;
+            if (!tile_live(tg, NE, emask)) continue;
             const int e = tg.e, f = tg.f0 + ep;
-            const bool act = pair_active(e, f, NE);
+            const bool act = pair_active(e, f, NE, emask);
             const int m0 = tg.row * (N - 2);
             const int m1 = min(M, m0 + N - 3);
             const int o0 = max(0, m0 - 1);
@@ -809,7 +824,8 @@ TcLayout tc_layout(int n_elem, int m_max, int nxi)
 
 template <int N>
 int launch_tc(const TcLayout &L, int NE, int M, int h, float2 kf, float2 ik2f, float2 sre, float2 sim,
-              unsigned char *w, int bA, double2 *Z, long long ldz, long long ms, cudaStream_t st)
+              const unsigned char *emask, unsigned char *w, int bA, double2 *Z, long long ldz, long long ms,
+              cudaStream_t st)
 {
     auto enc = get_encode();
     if (!enc) {
@@ -846,7 +862,7 @@ int launch_tc(const TcLayout &L, int NE, int M, int h, float2 kf, float2 ik2f, f
     const long long ntiles = (long long)nrows * NE * fgroups;
     const int grid = (int)(ntiles < nsm ? ntiles : nsm);
     kern<<<grid, TC_THREADS, smem, st>>>(map, NE, NE + 1, M, h, kf, ik2f, sre, sim,
-                                         reinterpret_cast<const float2 *>(w + L.geo_off),
+                                         reinterpret_cast<const float2 *>(w + L.geo_off), emask,
                                          reinterpret_cast<const float2 *>(w + L.s2_off),
                                          reinterpret_cast<const int *>(w), bA, Z, ldz, ms,
                                          reinterpret_cast<int *>(w));
@@ -884,9 +900,10 @@ extern "C" int ghost_bor_far_efie_tc_tables(int m_max, int nxi, const double *dc
     return check_launch("far_efie_tc: table digits");
 }
 
-extern "C" int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k, double scale_re, double scale_im,
-                                     const double *geo, void *work, long long work_bytes,
-                                     void *Z, long long ldz, long long mode_stride, void *stream)
+extern "C" int ghost_bor_far_efie_tc_masked(int n_elem, int m_max, int nxi, double k, double scale_re,
+                                            double scale_im, const double *geo, const unsigned char *elem_mask,
+                                            void *work, long long work_bytes, void *Z, long long ldz,
+                                            long long mode_stride, void *stream)
 {
     using namespace gb;
     if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !Z || !work ||
@@ -912,7 +929,15 @@ extern "C" int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k, d
     };
     const float2 kf = split(k), ik2f = split(1.0 / (k * k)), sre = split(scale_re), sim = split(scale_im);
     double2 *Zd = reinterpret_cast<double2 *>(Z);
-    if (L.N == 32) return launch_tc<32>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
-    if (L.N == 64) return launch_tc<64>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
-    return launch_tc<128>(L, n_elem, m_max, h, kf, ik2f, sre, sim, w, bA, Zd, ldz, mode_stride, st);
+    if (L.N == 32) return launch_tc<32>(L, n_elem, m_max, h, kf, ik2f, sre, sim, elem_mask, w, bA, Zd, ldz, mode_stride, st);
+    if (L.N == 64) return launch_tc<64>(L, n_elem, m_max, h, kf, ik2f, sre, sim, elem_mask, w, bA, Zd, ldz, mode_stride, st);
+    return launch_tc<128>(L, n_elem, m_max, h, kf, ik2f, sre, sim, elem_mask, w, bA, Zd, ldz, mode_stride, st);
+}
+
+extern "C" int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k, double scale_re, double scale_im,
+                                     const double *geo, void *work, long long work_bytes,
+                                     void *Z, long long ldz, long long mode_stride, void *stream)
+{
+    return ghost_bor_far_efie_tc_masked(n_elem, m_max, nxi, k, scale_re, scale_im, geo, nullptr, work, work_bytes,
+                                        Z, ldz, mode_stride, stream);
 }

@@ -145,6 +145,16 @@ int ghost_bor_far_efie_tc(int n_elem, int m_max, int nxi, double k,
                           void *work, long long work_bytes,
                           void *Z, long long ldz, long long mode_stride, void *stream);
 
+/* ghost_bor_far_efie_tc restricted to the far pairs (e, f) with elem_mask[e]
+ * or elem_mask[f] nonzero (n_elem bytes on the device; NULL = all pairs): the
+ * tiles without such a pair are skipped.  Used by the adjoint gradient for the
+ * operator change of a local shape perturbation.  No counterpart in the
+ * reference. */
+int ghost_bor_far_efie_tc_masked(int n_elem, int m_max, int nxi, double k,
+                                 double scale_re, double scale_im, const double *geo,
+                                 const unsigned char *elem_mask, void *work, long long work_bytes,
+                                 void *Z, long long ldz, long long mode_stride, void *stream);
+
 /* Persistent grid of the near fills: CTAs per SM (default: 2 for the
  * per-thread kernels, every resident CTA for the grouped double-float EFIE
  * kernel; 0 restores the defaults, at most 8).  The workspace size
