@@ -24,9 +24,10 @@ dZ/dp and dV/dp are recomputed in the backward pass (nothing of size n^2 is
 stored per parameter): for parameter p the generatrix nodes move by
 +-h dnodes/dp, and the operator change is filled by the GPU kernels directly
 into one buffer as (Z(+h) - Z(-h)) / 2h, restricted to the element pairs that
-touch a moved element (ghost_bor_far_efie_masked for far pairs, a subset of
-the near-pair table for near pairs); dV likewise from two excitation
-launches.  The quadrature orders (n_xi, near tail orders) stay those of the
+touch a moved element (far pairs: ghost_bor_far_efie_tc_masked for FP32+IR
+sweeps, ghost_bor_far_efie_masked in FP64 for FP64 sweeps; near pairs: a
+subset of the near-pair table through the double-float or the FP64 near
+kernel); dV likewise from two FP64 excitation launches.  The quadrature orders (n_xi, near tail orders) stay those of the
 unperturbed body, so the derivative is that of the discrete operator.
 
 Shape parameters of the benchmark body (bodies.bspline_body): the control radii
