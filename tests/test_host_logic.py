@@ -203,6 +203,16 @@ def test_mode_runs_groups_live_modes(pkg):
         assert np.array_equal(got, live)
 
 
+def test_refine_for_currents_settings(pkg):
+    """The surface-current refinement: every correction updated with exact
+    products, each mode refined to 1e-11 of its right-hand side."""
+    eng = pkg.engine
+    prob = object.__new__(eng.BorGpuProblem)
+    prob.exact_update_iters, prob.refine_floor = 1, 2e-9
+    prob.refine_for_currents()
+    assert prob.exact_update_iters is None and prob.refine_floor == 1e-11
+
+
 def test_far_blocks_mirror_relation(oracle):
     """The relation the tensor-core far fill writes the mirror pair with: for
     node pairs reached only by far element pairs (|i - j| >= 3), the EFIE
