@@ -42,8 +42,12 @@ SIGNATURES = {
     "ghost_bor_near_mfie_workspace": (_ll, [_i]),
     "ghost_bor_near_mfie": (_i, [_i, _i, _d, _d, _d, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i,
                                  _vp, _vp, _i, _vp, _vp, _ll, _ll, _i, _vp, _ll, _vp]),
+    "ghost_bor_far_ibc": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
+    "ghost_bor_near_ibc": (_i, [_i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i,
+                                _vp, _vp, _i, _vp, _vp, _ll, _ll, _i, _vp, _ll, _vp]),
     "ghost_bor_rhs_workspace": (_ll, [_i, _i, _i]),
     "ghost_bor_rhs": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp]),
+    "ghost_bor_rhs_weighted": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_rhs_noalloc_capacity": (_ll, []),
     "ghost_bor_rhs_noalloc": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_cgemm_tc_workspace": (_ll, [_i, _i, _i, _i]),

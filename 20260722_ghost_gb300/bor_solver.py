@@ -74,25 +74,47 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
     if asm not in ("auto", "tables", "streaming"):
         raise ValueError("assembly must be 'auto', 'tables', or 'streaming'.")
     precision = _precision_of(table_precision)
-    if zs is not None and np.any(np.abs(np.asarray(zs, dtype=complex)) > 0.0):
-        raise NotImplementedError("surface impedance (IBC-EFIE) is not on the GPU path yet")
     if check_abort is not None:
         check_abort()
     thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
     prob = BorGpuProblem(points, freq_hz, thetas, m_max=n_modes, gauss_order=gauss_order,
-                         formulation=form, cfie_alpha=cfie_alpha)
+                         formulation=form, cfie_alpha=cfie_alpha, zs=zs)
+    # interior-resonance guard of the reference (bor_solver.py:955-985): a
+    # closed body on the EFIE with a lossless (purely reactive) Z_s
+    warnings: List[str] = []
+    closed = prob.gen.node_on_axis(0) and prob.gen.node_on_axis(prob.Nn - 1)
+    lossless = (prob.zs is not None and
+                float(np.max(np.abs(np.real(prob.zs)))) < 1e-3 * float(np.max(np.abs(prob.zs))))
+    prob.monitor_cond = form == "efie" and closed and lossless
+    if prob.monitor_cond:
+        warnings.append(
+            "Closed body with a lossless (purely reactive) surface impedance "
+            "on the EFIE: interior cavity resonances are undamped, and "
+            "results at resonant frequencies may be silently corrupted. "
+            "Inspect max_cond across the frequency sweep for spikes, add "
+            "loss to Z_s, or avoid closed-body reactive IBC.")
     t_setup = time.perf_counter()
     res = prob.sweep(precision=precision, check_abort=check_abort)
-    return _result(prob, res, thetas, form, precision, mode_tol, progress, t_wall, t_setup)
+    return _result(prob, res, thetas, form, precision, mode_tol, progress, t_wall, t_setup, warnings)
 
 
 def _result(prob: BorGpuProblem, res, thetas, form: str, precision: str, mode_tol: float,
-            progress: Optional[Callable], t_wall: float, t_setup: float) -> Dict:
+            progress: Optional[Callable], t_wall: float, t_setup: float,
+            warnings: Optional[List[str]] = None) -> Dict:
     """The reference's result dict of one sweep (bor_solver.py:987-1004)."""
     F, modes_used = replay_truncation(res.dF, mode_tol)
     if progress is not None:
         progress(modes_used, prob.m_max)
-    warnings: List[str] = []
+    warnings = [] if warnings is None else list(warnings)
+    stats: Dict = {}
+    if res.cond is not None:
+        conds = res.cond[: modes_used + 1]
+        stats = {"max_cond": float(np.max(conds)), "median_cond": float(np.median(conds))}
+        if stats["max_cond"] > 1e5:
+            warnings.append(
+                f"Mode-system conditioning reached {stats['max_cond']:.1e}: an "
+                "interior resonance is likely at or near this frequency; the "
+                "result is untrustworthy there.")
     bad = np.flatnonzero(res.info != 0)
     if bad.size:
         warnings.append(f"Zero pivot in the LU of mode(s) {bad.tolist()}: singular mode system.")
@@ -119,6 +141,7 @@ def _result(prob: BorGpuProblem, res, thetas, form: str, precision: str, mode_to
         "refine_iters": int(res.refine_iters),
         "refine_residual": lin_res,
         "timings": timings,
+        **stats,
     }
 
 
@@ -190,8 +213,11 @@ class BorPecSolver:
     Operators are built on the GPU for all modes 0..m_max at once (FP64) and
     returned per mode as complex128 NumPy arrays for compatibility; mode -m is
     D Z(m) D for both operators.  The EFIE and MFIE operators, the mass
-    blocks, the plane-wave excitations (E and H) and the PEC far field are
-    provided; the IBC / PMCHWT operators raise NotImplementedError.
+    blocks, the plane-wave excitations (E and H), the surface-impedance
+    (IBC) operator addition and the far field with the impedance surface's
+    magnetic current are provided; the PMCHWT operators raise
+    NotImplementedError.  Z_s is per element (constant on each element, as
+    solve_bor builds it).
     """
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,
@@ -222,6 +248,7 @@ class BorPecSolver:
         self._stream = None
         self._ops: Optional[Tuple[int, object]] = None
         self._mops: Optional[Tuple[int, object]] = None
+        self._iops: Optional[Tuple[int, bytes, object]] = None
         self._single = bool(single_tables)
 
     # -- operator cache ----------------------------------------------------
@@ -242,9 +269,8 @@ class BorPecSolver:
     def prepare_operators(self, m_max: int, efie: bool = True, mfie: bool = False,
                           ibc: bool = False, workers: int = 1) -> None:
         """Build the FP64 operators of every mode 0..m_max on the GPU
-        (bor_solver.py:578-608); modes -m follow by symmetry."""
-        if ibc:
-            raise NotImplementedError("IBC operators are not on the GPU path yet")
+        (bor_solver.py:578-608); modes -m follow by symmetry.  The IBC
+        addition depends on Z_s and is built by assemble_ibc_extra."""
         if efie and (self._ops is None or self._ops[0] < m_max):
             prob = self._problem(m_max)
             self._ops = (m_max, prob.assemble_modes_fp64())
@@ -270,6 +296,36 @@ class BorPecSolver:
         self.prepare_operators(max(m_max, abs(m)), efie=False, mfie=True)
         return self._mode(self._mops, m)
 
+    def _zs_elem(self, zs_pt, zs_elem=None) -> np.ndarray:
+        """Z_s per element from the per-Gauss-point values (and the per-element
+        array, which must agree with them)."""
+        pt = np.asarray(zs_pt, dtype=complex)
+        if pt.shape != (self.P,):
+            raise ValueError("zs_pt must have one entry per Gauss point.")
+        per = pt.reshape(self.gen.n_elems, -1)
+        if np.any(per != per[:, :1]):
+            raise NotImplementedError("the GPU IBC fill takes Z_s constant on each element")
+        ze = per[:, 0].copy()
+        if zs_elem is not None and not np.array_equal(np.asarray(zs_elem, dtype=complex), ze):
+            raise ValueError("zs_pt and zs_elem disagree")
+        return ze
+
+    def assemble_ibc_extra(self, m: int, m_max: int, zs_pt: np.ndarray,
+                           zs_elem: np.ndarray) -> np.ndarray:
+        """IBC-EFIE addition Z_s (M/2) + B of mode m: the Z_s-weighted mass term
+        plus the rotated principal-value brackets with Z_s at the source
+        (bor_solver.py:534-552)."""
+        ze = self._zs_elem(zs_pt, zs_elem)
+        if not np.any(ze != 0.0):
+            return np.zeros((2 * self.Nn, 2 * self.Nn), dtype=np.complex128)
+        mm = max(m_max, abs(m))
+        key = ze.tobytes()
+        if self._iops is None or self._iops[0] < mm or self._iops[1] != key:
+            prob = BorGpuProblem(self._points, self.freq_hz, (0.0,), m_max=mm,
+                                 gauss_order=self.gauss_order, zs=ze)
+            self._iops = (mm, key, prob.assemble_ibc_modes_fp64())
+        return self._mode((self._iops[0], self._iops[2]), m)
+
     def basis_mask(self, m: int) -> np.ndarray:
         return _basis_mask(self.gen, m)
 
@@ -283,13 +339,14 @@ class BorPecSolver:
         return 2.0 * np.pi * (self.B_T * wgt[None, :]) @ self.B_T.T
 
     # -- excitation / far field (GPU kernels, one angle) --------------------
-    def _excitation(self, m: int, theta_inc_deg: float, coef_e: float, coef_h: float):
+    def _excitation(self, m: int, theta_inc_deg: float, coef_e: float, coef_h: float, h_weight=None):
         import torch
         am = abs(m)
         prob = self._problem(am, thetas=(float(theta_inc_deg),))
         prob.d_masks.fill_(-1)
         B = torch.empty((am + 1, prob.n, 2), dtype=torch.complex128, device=prob.device)
-        prob.excitation(B, coef_e, coef_h, nat.stream_handle())
+        hw = None if h_weight is None else torch.as_tensor(h_weight, dtype=torch.complex128, device=prob.device)
+        prob.excitation(B, coef_e, coef_h, nat.stream_handle(), h_weight=hw)
         V = B[am].cpu().numpy()       # [2Nn, 2] (VV, HH)
         if m < 0:
             # V(-m) = D V(m) for VV and -D V(m) for HH
@@ -320,13 +377,19 @@ class BorPecSolver:
     def farfield_mode(self, m: int, sol: np.ndarray, theta_s_deg: float,
                       zs_pt: Optional[np.ndarray] = None,
                       msol: Optional[np.ndarray] = None) -> Tuple[complex, complex]:
-        """Modal far field (F_theta, F_phi) of a PEC current by reciprocity:
-        F_theta = c (D V_VV)^T x, F_phi = -c (D V_HH)^T x, c = -j k eta0/(4 pi)
-        (equal to the reference's projection, bor_solver.py:659-708)."""
-        if zs_pt is not None or msol is not None:
-            raise NotImplementedError("magnetic-current radiation (IBC / PMCHWT) is not on the GPU path")
+        """Modal far field (F_theta, F_phi) by reciprocity:
+        F_theta = c (D V_VV)^T x, F_phi = -c (D V_HH)^T x, c = -j k eta0/(4 pi),
+        V = V_E for a PEC current and V_E - V_H^Zs with the magnetic current
+        M = -Z_s n x J of an impedance surface (equal to the reference's
+        projection, bor_solver.py:659-708)."""
+        if msol is not None:
+            raise NotImplementedError("PMCHWT magnetic-current radiation is not on the GPU path")
         import torch
-        V = torch.as_tensor(self._excitation(m, theta_s_deg, 1.0, 0.0), device="cuda")
+        if zs_pt is None:
+            Vh = self._excitation(m, theta_s_deg, 1.0, 0.0)
+        else:
+            Vh = self._excitation(m, theta_s_deg, 1.0, -1.0, h_weight=self._zs_elem(zs_pt))
+        V = torch.as_tensor(Vh, device="cuda")
         x = torch.as_tensor(np.asarray(sol, dtype=np.complex128), device="cuda")
         Nn = self.Nn
         d = torch.ones(2 * Nn, dtype=torch.float64, device="cuda")

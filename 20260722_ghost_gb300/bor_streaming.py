@@ -5,9 +5,11 @@
 GPU sweep by the fused far-fill kernels (ghost_bor_far_efie,
 ghost_bor_far_mfie) instead of tile-by-tile CPU sampling + FFT + einsum.
 ``efie_blocks(m)`` returns the four nodal EFIE blocks WITHOUT the
-C = j k eta 2 pi factor and ``bracket_blocks("mfie", m)`` the four MFIE
-bracket blocks K (2 pi Galerkin factor included, no mass term), exactly as the
-reference (same/adjacent element pairs contribute zero; the near path adds
+C = j k eta 2 pi factor, ``bracket_blocks("mfie", m)`` the four MFIE
+bracket blocks K (2 pi Galerkin factor included, no mass term) and
+``bracket_blocks("ibc", m)`` the four rotated principal-value blocks B with
+the surface impedance in the source weights (ghost_bor_far_ibc), exactly as
+the reference (same/adjacent element pairs contribute zero; the near path adds
 them).  Blocks are held on the device; accessors copy one mode to the host.
 """
 
@@ -42,8 +44,6 @@ class StreamingFarBlocks:
                  ibc_zs_pt: Optional[np.ndarray] = None, dtype=np.complex128,
                  tile_budget_gb: float = 1.0, workers: int = 1,
                  mode_block: Optional[int] = None):
-        if ibc_zs_pt is not None:
-            raise NotImplementedError("IBC bracket blocks are not on the GPU path yet")
         import torch
         self.solver = solver
         self.m_max = int(m_max)
@@ -57,6 +57,15 @@ class StreamingFarBlocks:
         single = np.dtype(dtype) == np.complex64
         prec = nat.F32 if single else nat.F64
         self.Z = self.K = self.B = None
+        if ibc_zs_pt is not None:
+            # Z_s per element (constant on each element, as solve_bor builds it)
+            ze = solver._zs_elem(ibc_zs_pt)
+            B = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
+            if np.any(ze != 0.0):
+                bprob = BorGpuProblem(solver._points, solver.freq_hz, (0.0,), m_max=self.m_max,
+                                      gauss_order=solver.gauss_order, zs=ze)
+                bprob.fill_far_ibc(B, prec, 1.0 + 0.0j, nat.stream_handle())
+            self.B = B
         if efie:
             Z = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
             prob.fill_far(Z, prec, 1.0 + 0.0j, nat.stream_handle())
@@ -88,13 +97,16 @@ class StreamingFarBlocks:
         return self._blocks(self.Z, m)
 
     def bracket_blocks(self, which: str, m: int):
-        """Far MFIE bracket blocks K_tt, K_tf, K_ft, K_ff of mode m
-        (bor_streaming.py:409-414); K(-m) = D K(m) D."""
-        if which != "mfie":
-            raise NotImplementedError("IBC bracket blocks are not on the GPU path yet")
-        if self.K is None:
-            raise ValueError("MFIE bracket blocks were not built")
-        return self._blocks(self.K, m)
+        """Far bracket blocks (tt, tf, ft, ff) of mode m, ``which`` = "mfie"
+        (K) or "ibc" (B, Z_s in the source weights) (bor_streaming.py:409-414);
+        both obey X(-m) = D X(m) D."""
+        if which not in ("mfie", "ibc"):
+            raise ValueError(f"unknown bracket kind {which!r}")
+        store = self.K if which == "mfie" else self.B
+        if store is None:
+            raise ValueError(f"{which.upper()} bracket blocks were not built")
+        return self._blocks(store, m)
 
     def memory_gb(self) -> float:
-        return float(sum(t.numel() * t.element_size() for t in (self.Z, self.K) if t is not None)) / 1e9
+        return float(sum(t.numel() * t.element_size() for t in (self.Z, self.K, self.B)
+                         if t is not None)) / 1e9

@@ -25,8 +25,18 @@
 // per-sample products of the reference, which cancel for nearby points, are
 // never formed.  The combinations c0 C[p] + c1 C[p s2] lose at most a
 // factor ~2 to cancellation.
+//
+// Surface impedance (IBC-EFIE).  The reference's extra operator
+// Z_s (M/2) + B (bor_solver.py:499-552: the Z_s-weighted mass term plus the
+// rotated principal-value brackets with Z_s at the source, far part from
+// bor_kernels.py:449-511 / bor_stream_kernel.c:108-150, near part from
+// bor_kernels.py:514-560 on the same graded cells) is the same three
+// transforms with another coefficient set (brackets.cuh), the opposite sign
+// of the bracket term and a complex weight per source element: the IBC
+// instantiations of both kernels below.
 #include "common.cuh"
 #include "samplers.cuh"
+#include "brackets.cuh"
 
 namespace gb {
 namespace {
@@ -57,35 +67,12 @@ template <class R> struct MfieSmem {
     }
 };
 
-// per Gauss-point pair bracket coefficients (see the file header):
-// K_tt = k0 C[p] + k1 C[p s2], K_ff = k2 C[p] + k3 C[p s2],
-// K_tf = -j k4 S, K_ft = -j k5 S
-__device__ __forceinline__ void bracket_coefs(double rp, double zp, double trp, double tzp,
-                                              double rq, double zq, double trq, double tzq,
-                                              double *c)
-{
-    const double dr = rp - rq, dz = zp - zq;
-    const double X0 = trp * tzq - tzp * trq;
-    const double N0 = trp * dz - tzp * dr;
-    const double A0 = trp * dr + tzp * dz;
-    const double D0 = trp * trq + tzp * tzq;
-    const double c0 = dr * tzq - dz * trq;
-    const double c1 = 2.0 * (A0 * tzp * trq + trp * rq * X0 + D0 * tzp * rq + trp * trq * N0);
-    const double e0 = rq * X0 + trq * N0;
-    c[0] = -c0;
-    c[1] = -c1;
-    c[2] = N0;
-    c[3] = -2.0 * (N0 - rq * tzp);
-    c[4] = dz;
-    c[5] = -e0;
-}
-
-template <class R>
+template <class R, bool IBC>
 __global__ void __launch_bounds__(MTPB)
 far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ tab,
-                const double *__restrict__ sin2, double2 *__restrict__ Z,
-                long long ldz, long long mode_stride)
+                const double *__restrict__ sin2, const double2 *__restrict__ wsrc,
+                double2 *__restrict__ Z, long long ldz, long long mode_stride)
 {
     using CT = C<R>;
     using Samp = BracketSampler<R>;
@@ -123,8 +110,8 @@ far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     for (int i = tid; i < MEPB * 16; i += MTPB) {
         const int el = min(f0 + i / 16, N - 1);
         const int p = 4 * e + ((i & 15) >> 2), q = 4 * el + (i & 3);
-        bracket_coefs(geo[p], geo[P + p], geo[(size_t)9 * P + p], geo[(size_t)10 * P + p],
-                      geo[q], geo[P + q], geo[(size_t)9 * P + q], geo[(size_t)10 * P + q], coef + 6 * i);
+        bracket_coefs<IBC>(geo[p], geo[P + p], geo[(size_t)9 * P + p], geo[(size_t)10 * P + p],
+                           geo[q], geo[P + q], geo[(size_t)9 * P + q], geo[(size_t)10 * P + q], coef + 6 * i);
     }
 
     Samp smp;
@@ -202,15 +189,22 @@ far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
             ktf.x += w * cf[4] * sxx; ktf.y += w * cf[4] * sxy;
             kft.x += w * cf[5] * sxx; kft.y += w * cf[5] * sxy;
         }
-        // K_tf = -j ktf, K_ft = -j kft; the block value is -scale * K
+        // K_tf = -j ktf, K_ft = -j kft; the block value is -scale K (MFIE) or
+        // +scale Z_s(f) K (IBC, Z_s of the source element)
         const double2 K[4] = {ktt, make_double2(ktf.y, -ktf.x), make_double2(kft.y, -kft.x), kff};
+        double s_re = sc_re, s_im = sc_im;
+        if (IBC && wsrc) {
+            const double2 w = wsrc[ff];
+            s_re = sc_re * w.x - sc_im * w.y;
+            s_im = sc_re * w.y + sc_im * w.x;
+        }
         double2 *Zm = Z + (size_t)(m0 + n) * mode_stride;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const long long row = e + a + (q >> 1) * Nn, col = ff + b + (q & 1) * Nn;
-            const double2 v = make_double2(-(sc_re * K[q].x - sc_im * K[q].y),
-                                           -(sc_re * K[q].y + sc_im * K[q].x));
-            catomic_add(Zm + row * ldz + col, v);
+            double v[2];
+            bracket_entry<IBC>(K[q].x, K[q].y, 0.0, s_re, s_im, v);
+            catomic_add(Zm + row * ldz + col, make_double2(v[0], v[1]));
         }
     }
 }
@@ -253,8 +247,10 @@ __device__ __forceinline__ void project3(double2 (&acc)[3][NCM], double2 p, doub
     }
 }
 
+template <bool IBC>
 __global__ void __launch_bounds__(NTPB, 2)
 near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
+                 const double2 *__restrict__ wsrc,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
                  const double *__restrict__ emass, int n_pairs,
                  const int *__restrict__ pairs, const int *__restrict__ tails,
@@ -374,7 +370,7 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     gSm[q] = -sx; gS0[q] = 0.0;
                 }
                 double cf[6];
-                bracket_coefs(rp, zp, tre, tze, rq, zq, trf, tzf, cf);
+                bracket_coefs<IBC>(rp, zp, tre, tze, rq, zq, trf, tzf, cf);
                 const double Tp[2] = {1.0 - s, s}, Tq[2] = {1.0 - sp, sp};
                 const double rr = 2.0 * GB_PI * rp * rq * w;
 #pragma unroll
@@ -437,7 +433,14 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
         }
         __syncthreads();
 
-        // blocks: Z_M = M/2 - K; K_tt = O0 + O1, K_ff = O2 + O3, K_tf = -j O4, K_ft = -j O5
+        // blocks: Z_M = M/2 - K (MFIE) or Z_s(f) (M/2 + B) (IBC);
+        // K_tt = O0 + O1, K_ff = O2 + O3, K_tf = -j O4, K_ft = -j O5
+        double s_re = sc_re, s_im = sc_im;
+        if (IBC && wsrc) {
+            const double2 w = wsrc[f];
+            s_re = sc_re * w.x - sc_im * w.y;
+            s_im = sc_re * w.y + sc_im * w.x;
+        }
         for (int job = tid; job < Mo * 16; job += NTPB) {
             const int m = job / 16, blk = (job / 4) % 4, ab = job % 4;
             const int a = ab >> 1, b = ab & 1;
@@ -450,9 +453,10 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                 const double2 u = Prim[((blk == 1 ? 4 : 5) * 4 + ab) * Mo + m];
                 K = make_double2(u.y, -u.x);
             }
-            double2 v = make_double2(-K.x, -K.y);
-            if (e == f && (blk == 0 || blk == 3)) v.x += 0.5 * emass[4 * e + ab];
-            const double2 sv = make_double2(sc_re * v.x - sc_im * v.y, sc_re * v.y + sc_im * v.x);
+            const double mh = (e == f && (blk == 0 || blk == 3)) ? 0.5 * emass[4 * e + ab] : 0.0;
+            double sv2[2];
+            bracket_entry<IBC>(K.x, K.y, mh, s_re, s_im, sv2);
+            const double2 sv = make_double2(sv2[0], sv2[1]);
             const int i = e + a, j = f + b;
             if (band) {
                 double2 *dst = band + (((size_t)m * 4 + blk) * Nn + i) * 5 + (j - i + 2);
@@ -465,21 +469,67 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     }
 }
 
-template <class R>
-int launch_far_mfie(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
-                    const double *tab, const double *sin2, void *Z, long long ldz, long long ms,
-                    cudaStream_t st)
+template <class R, bool IBC>
+int launch_far_bracket(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
+                       const double *tab, const double *sin2, const double *wsrc, void *Z, long long ldz,
+                       long long ms, cudaStream_t st)
 {
     const size_t smem = MfieSmem<R>::bytes();
-    auto kern = far_mfie_kernel<R>;
+    auto kern = far_mfie_kernel<R, IBC>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("far_mfie: smem attribute");
     const int fgroups = (N + MEPB - 1) / MEPB;
     const int nchunks = (M + 1 + MNOB - 1) / MNOB;
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, MTPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, tab, sin2,
+                                   reinterpret_cast<const double2 *>(wsrc),
                                    reinterpret_cast<double2 *>(Z), ldz, ms);
-    return check_launch("far_mfie");
+    return check_launch(IBC ? "far_ibc" : "far_mfie");
+}
+
+template <bool IBC>
+int far_bracket(int prec, int n_elem, int m_max, int nxi, double k, double sre, double sim,
+                const double *geo, const double *tab, const double *sin2, const double *wsrc,
+                void *Z, long long ldz, long long ms, void *stream)
+{
+    if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !tab || !sin2 || !Z ||
+        ldz < 2LL * (n_elem + 1) || ms < ldz * 2LL * (n_elem + 1) || !(k > 0.0))
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (prec == GHOST_BOR_F32)
+        return launch_far_bracket<float, IBC>(n_elem, m_max, nxi, k, sre, sim, geo, tab, sin2, wsrc, Z, ldz, ms, st);
+    if (prec == GHOST_BOR_F64)
+        return launch_far_bracket<double, IBC>(n_elem, m_max, nxi, k, sre, sim, geo, tab, sin2, wsrc, Z, ldz, ms, st);
+    return GHOST_BOR_EINVAL;
+}
+
+template <bool IBC>
+int near_bracket(int n_elem, int m_max, double k, double sre, double sim, const double *wsrc,
+                 const double *nodes, const double *elem, const double *emass, int n_pairs, const int *pairs,
+                 const int *tails, const double *cells, int n_cells_total, const double *core_gl,
+                 const double *tail_gl, int n_tail_total, double *band, void *Z, long long ldz, long long ms,
+                 int n_tail_max, void *work, long long work_bytes, long long work_need, void *stream)
+{
+    if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !emass || !pairs || !tails ||
+        !cells || !core_gl || !tail_gl || !(k > 0.0) || n_tail_max < 0 || !work ||
+        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < work_need)
+        return GHOST_BOR_EINVAL;
+    if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
+    const size_t smem = NearMfieSmem::bytes(m_max + 1);
+    if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    auto kern = near_mfie_kernel<IBC>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("near_mfie: smem attribute");
+    int *status = reinterpret_cast<int *>(work);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_mfie: memset");
+    const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
+    kern<<<grid, NTPB, smem, st>>>(
+        n_elem, n_elem + 1, m_max, k, sre, sim, reinterpret_cast<const double2 *>(wsrc), nodes, elem, emass,
+        n_pairs, pairs, tails, cells, n_cells_total, core_gl, tail_gl, n_tail_total, NCORE_M + n_tail_max,
+        reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, ms,
+        reinterpret_cast<unsigned char *>(work) + 256, status);
+    return check_launch(IBC ? "near_ibc" : "near_mfie");
 }
 
 }  // namespace
@@ -490,16 +540,17 @@ extern "C" int ghost_bor_far_mfie(int prec, int n_elem, int m_max, int nxi, doub
                                   const double *geo, const double *tab, const double *sin2,
                                   void *Z, long long ldz, long long mode_stride, void *stream)
 {
-    using namespace gb;
-    if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !tab || !sin2 || !Z ||
-        ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k > 0.0))
-        return GHOST_BOR_EINVAL;
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (prec == GHOST_BOR_F32)
-        return launch_far_mfie<float>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, tab, sin2, Z, ldz, mode_stride, st);
-    if (prec == GHOST_BOR_F64)
-        return launch_far_mfie<double>(n_elem, m_max, nxi, k, scale_re, scale_im, geo, tab, sin2, Z, ldz, mode_stride, st);
-    return GHOST_BOR_EINVAL;
+    return gb::far_bracket<false>(prec, n_elem, m_max, nxi, k, scale_re, scale_im, geo, tab, sin2, nullptr,
+                                  Z, ldz, mode_stride, stream);
+}
+
+extern "C" int ghost_bor_far_ibc(int prec, int n_elem, int m_max, int nxi, double k,
+                                 double scale_re, double scale_im, const double *zs_elem,
+                                 const double *geo, const double *tab, const double *sin2,
+                                 void *Z, long long ldz, long long mode_stride, void *stream)
+{
+    return gb::far_bracket<true>(prec, n_elem, m_max, nxi, k, scale_re, scale_im, geo, tab, sin2, zs_elem,
+                                 Z, ldz, mode_stride, stream);
 }
 
 extern "C" long long ghost_bor_near_mfie_workspace(int n_tail_max)
@@ -516,25 +567,22 @@ extern "C" int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale
                                    double *band, void *Z, long long ldz, long long mode_stride,
                                    int n_tail_max, void *work, long long work_bytes, void *stream)
 {
-    using namespace gb;
-    if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !emass || !pairs || !tails ||
-        !cells || !core_gl || !tail_gl || !(k > 0.0) || n_tail_max < 0 || !work ||
-        (reinterpret_cast<uintptr_t>(work) & 255) || work_bytes < ghost_bor_near_mfie_workspace(n_tail_max))
-        return GHOST_BOR_EINVAL;
-    if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
-    const size_t smem = NearMfieSmem::bytes(m_max + 1);
-    if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (cudaFuncSetAttribute(near_mfie_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-        return check_launch("near_mfie: smem attribute");
-    int *status = reinterpret_cast<int *>(work);
-    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_mfie: memset");
-    const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
-    near_mfie_kernel<<<grid, NTPB, smem, st>>>(
-        n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, emass, n_pairs, pairs, tails, cells,
-        n_cells_total, core_gl, tail_gl, n_tail_total, NCORE_M + n_tail_max,
-        reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, mode_stride,
-        reinterpret_cast<unsigned char *>(work) + 256, status);
-    return check_launch("near_mfie");
+    return gb::near_bracket<false>(n_elem, m_max, k, scale_re, scale_im, nullptr, nodes, elem, emass, n_pairs,
+                                   pairs, tails, cells, n_cells_total, core_gl, tail_gl, n_tail_total, band, Z,
+                                   ldz, mode_stride, n_tail_max, work, work_bytes,
+                                   ghost_bor_near_mfie_workspace(n_tail_max), stream);
+}
+
+extern "C" int ghost_bor_near_ibc(int n_elem, int m_max, double k, double scale_re, double scale_im,
+                                  const double *zs_elem, const double *nodes, const double *elem,
+                                  const double *emass, int n_pairs, const int *pairs, const int *tails,
+                                  const double *cells, int n_cells_total,
+                                  const double *core_gl, const double *tail_gl, int n_tail_total,
+                                  double *band, void *Z, long long ldz, long long mode_stride,
+                                  int n_tail_max, void *work, long long work_bytes, void *stream)
+{
+    return gb::near_bracket<true>(n_elem, m_max, k, scale_re, scale_im, zs_elem, nodes, elem, emass, n_pairs,
+                                  pairs, tails, cells, n_cells_total, core_gl, tail_gl, n_tail_total, band, Z,
+                                  ldz, mode_stride, n_tail_max, work, work_bytes,
+                                  ghost_bor_near_mfie_workspace(n_tail_max), stream);
 }

@@ -84,6 +84,7 @@ __device__ __forceinline__ double2 ipow_times(int n, double v)
 
 // B[m][row][2 it + pol]: one thread per (it), nodes striding over grid y, blockIdx.z = m
 __global__ void rhs_kernel(int N, int Nn, int Mp, int T, double k, double ce, double ch,
+                           const double2 *__restrict__ hw,
                            const double *__restrict__ geo, const double *__restrict__ thetas,
                            const double *__restrict__ Jtab, const double2 *__restrict__ Ph,
                            const int *__restrict__ mask_rows, double2 *__restrict__ B,
@@ -125,7 +126,19 @@ __global__ void rhs_kernel(int N, int Nn, int Mp, int T, double k, double ce, do
             double2 efh = Ic;
             double2 tv = make_double2(ce * etv.x, ce * etv.y), fv = make_double2(ce * efv.x, ce * efv.y);
             double2 thh = make_double2(ce * eth.x, ce * eth.y), fh = make_double2(ce * efh.x, ce * efh.y);
-            if (ch != 0.0) {
+            if (hw) {
+                // n x H parts with the complex weight of the element (Z_s for the
+                // far field of an impedance surface): c2 = ch w(el) / eta0
+                const double2 w = hw[el];
+                const double2 c2 = make_double2(ch / ETA0 * w.x, ch / ETA0 * w.y);
+                const double2 a = cmul(c2, Ic), b = cmul(c2, Is);
+                const double2 h = cmul(c2, make_double2(ct * tr * Ic.x - st * tz * I1.x,
+                                                        ct * tr * Ic.y - st * tz * I1.y));
+                tv.x += a.x; tv.y += a.y;
+                fv.x -= tr * b.x; fv.y -= tr * b.y;
+                thh.x += ct * b.x; thh.y += ct * b.y;
+                fh.x += h.x; fh.y += h.y;
+            } else if (ch != 0.0) {
                 const double c2 = ch / ETA0;
                 // MFIE parts: VV et = Ic, ef = -t_rho Is ; HH et = ct Is, ef = ct t_rho Ic - st t_z I1
                 tv.x += c2 * Ic.x; tv.y += c2 * Ic.y;
@@ -191,13 +204,14 @@ extern "C" long long ghost_bor_rhs_workspace(int n_elem, int m_max, int n_theta)
     return P * (m_max + 2) * n_theta * 8 + P * n_theta * 16 + 256;
 }
 
-extern "C" int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
-                             double coef_e, double coef_h,
-                             const double *geo, const double *thetas_deg,
-                             const int *mask_rows, double *B, long long ldb, long long mode_stride,
-                             void *work, void *stream)
+namespace gb {
+namespace {
+
+int rhs_launch(int n_elem, int m_max, int n_theta, double k, double coef_e, double coef_h,
+               const double *h_weight, const double *geo, const double *thetas_deg,
+               const int *mask_rows, double *B, long long ldb, long long mode_stride,
+               void *work, void *stream)
 {
-    using namespace gb;
     const int Mp = m_max + 2;
     if (n_elem < 1 || m_max < 0 || Mp > MAX_ORD || n_theta < 1 || !geo || !thetas_deg || !mask_rows ||
         !B || !work || ldb < 2LL * n_theta || mode_stride < ldb * 2LL * (n_elem + 1))
@@ -212,9 +226,34 @@ extern "C" int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
     int rc = check_launch("rhs: bessel");
     if (rc) return rc;
     dim3 g2((n_theta + 63) / 64, n_elem + 1 < kMaxGridY ? n_elem + 1 : kMaxGridY, m_max + 1);
-    rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, n_theta, k, coef_e, coef_h, geo, thetas_deg,
+    rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, n_theta, k, coef_e, coef_h,
+                                  reinterpret_cast<const double2 *>(h_weight), geo, thetas_deg,
                                   Jtab, Ph, mask_rows, reinterpret_cast<double2 *>(B), ldb, mode_stride);
     return check_launch("rhs");
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
+                             double coef_e, double coef_h,
+                             const double *geo, const double *thetas_deg,
+                             const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                             void *work, void *stream)
+{
+    return gb::rhs_launch(n_elem, m_max, n_theta, k, coef_e, coef_h, nullptr, geo, thetas_deg, mask_rows, B,
+                          ldb, mode_stride, work, stream);
+}
+
+extern "C" int ghost_bor_rhs_weighted(int n_elem, int m_max, int n_theta, double k,
+                                      double coef_e, double coef_h, const double *h_weight,
+                                      const double *geo, const double *thetas_deg,
+                                      const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                                      void *work, void *stream)
+{
+    if (!h_weight) return GHOST_BOR_EINVAL;
+    return gb::rhs_launch(n_elem, m_max, n_theta, k, coef_e, coef_h, h_weight, geo, thetas_deg, mask_rows, B,
+                          ldb, mode_stride, work, stream);
 }
 
 extern "C" int ghost_bor_farfield(int prec, int batch, int n, int nrhs, int Nn, double k,
@@ -328,7 +367,8 @@ extern "C" int ghost_bor_rhs_noalloc(int n_elem, int m_max, int n_theta, double 
         int rc = check_launch("rhs_noalloc: bessel");
         if (rc) return rc;
         dim3 g2((T + 63) / 64, n_elem + 1 < kMaxGridY ? n_elem + 1 : kMaxGridY, m_max + 1);
-        rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, T, k, coef_e, coef_h, geo, thetas_deg + it0,
+        rhs_kernel<<<g2, 64, 0, st>>>(n_elem, n_elem + 1, Mp, T, k, coef_e, coef_h, nullptr, geo,
+                                      thetas_deg + it0,
                                       Jtab, Ph, mask_rows, reinterpret_cast<double2 *>(B) + 2 * (size_t)it0,
                                       ldb, mode_stride);
         if ((rc = check_launch("rhs_noalloc"))) return rc;

@@ -68,6 +68,8 @@ class SweepResult:
     res_history_modes: Optional[np.ndarray] = None
     # device seconds of single launches, bracketed by CUDA events on the launch stream
     kernel_s: Dict[str, List[float]] = field(default_factory=dict)
+    # [M+1] 2-norm condition number of each mode's reduced system (monitor_cond)
+    cond: Optional[np.ndarray] = None
 
 
 class BorGpuProblem:
@@ -75,7 +77,7 @@ class BorGpuProblem:
 
     def __init__(self, points, freq_hz: float, thetas_deg, m_max: Optional[int] = None,
                  gauss_order: int = 4, device=None, formulation: str = "efie",
-                 cfie_alpha: float = 0.5):
+                 cfie_alpha: float = 0.5, zs=None):
         if gauss_order != 4:
             raise NotImplementedError("the GPU kernels are specialised for gauss_order=4")
         # non-finite inputs would reach the kernels' index arithmetic (tail
@@ -86,11 +88,27 @@ class BorGpuProblem:
             raise ValueError("aspect angles must be finite")
         if not (math.isfinite(float(freq_hz)) and float(freq_hz) > 0.0):
             raise ValueError("freq_hz must be a positive finite frequency")
+        self.gen = Generatrix(points)
+        self.N = self.gen.n_elems
+        if self.N < 3:
+            raise ValueError("the GPU path needs at least 3 generatrix elements")
+        # A = alpha Z_EFIE + (1 - alpha) eta0 Z_MFIE (bor_solver.py:929-938)
+        form = formulation.strip().lower()
+        if form not in ("efie", "cfie", "mfie"):
+            raise ValueError(f"unknown formulation {formulation!r}")
+        self.formulation = form
+        self.alpha = float(cfie_alpha) if form == "cfie" else (1.0 if form == "efie" else 0.0)
+        # surface impedance per element (bor_solver.py:848-866): the EFIE gains
+        # Z_s (M/2) + B and the far field the radiation of M = -Z_s n x J
+        self.zs = impedance_per_element(zs, self.N)
+        if self.zs is not None and form == "cfie":
+            raise ValueError("CFIE with surface impedance is not supported in phase 2; "
+                             "use formulation='efie' (lossy Z_s suppresses resonances).")
+        self.ibc = self.zs is not None and self.alpha > 0.0
         torch = _torch()
         nat.load()
         self.torch = torch
         self.device = torch.device("cuda" if device is None else device)
-        self.gen = Generatrix(points)
         self.g = gauss_on_generatrix(self.gen, gauss_order)
         self.freq_hz = float(freq_hz)
         self.k = 2.0 * math.pi * self.freq_hz / C0
@@ -99,9 +117,6 @@ class BorGpuProblem:
         if m_max is None:
             m_max = default_n_modes(self.k, self.rho_max, self.thetas)
         self.m_max = int(m_max)
-        self.N = self.gen.n_elems
-        if self.N < 3:
-            raise ValueError("the GPU path needs at least 3 generatrix elements")
         self.Nn = self.gen.n_nodes
         self.n = 2 * self.Nn
         self.P = 4 * self.N
@@ -134,15 +149,10 @@ class BorGpuProblem:
         w[0] = 1.0
         self.d_mode_w = torch.as_tensor(w, dtype=f64, device=dev)
         self.C = 1j * self.k * ETA0 * 2.0 * math.pi          # bor_solver.py:338
-        # A = alpha Z_EFIE + (1 - alpha) eta0 Z_MFIE (bor_solver.py:929-938)
-        form = formulation.strip().lower()
-        if form not in ("efie", "cfie", "mfie"):
-            raise ValueError(f"unknown formulation {formulation!r}")
-        self.formulation = form
-        self.alpha = float(cfie_alpha) if form == "cfie" else (1.0 if form == "efie" else 0.0)
+        self.d_zs = None if self.zs is None else torch.as_tensor(self.zs, dtype=torch.complex128, device=dev)
         self.d_btab = self.d_bsin2 = self.d_emass = None
         self.n_xi_b = 0
-        if self.alpha < 1.0:
+        if self.alpha < 1.0 or self.ibc:
             self.n_xi_b = n_xi_bracket(self.k, self.rho_max, self.m_max)
             btab, bs2 = bracket_tables(self.n_xi_b, self.m_max)
             self.d_btab = torch.as_tensor(btab, dtype=f64, device=dev)
@@ -174,20 +184,25 @@ class BorGpuProblem:
         # digit products); False selects the SIMT FP32 transform of far_fill.cu
         self.far_tc = True
         self._far_tc_ws = None
+        # condition numbers of the mode systems in the sweep result (the
+        # reference monitors them for closed bodies with a lossless Z_s)
+        self.monitor_cond = False
 
     def h2d_bytes(self) -> int:
         """Bytes of host tables copied to the device for one problem."""
         return int(sum(t.numel() * t.element_size() for t in (
             self.d_geo, self.d_dct, self.d_sin2, self.d_nodes, self.d_elem, self.d_pairs,
             self.d_tails, self.d_cells, self.d_core, self.d_tail, self.d_masks, self.d_thetas,
-            self.d_mode_w) + tuple(t for t in (self.d_btab, self.d_bsin2, self.d_emass) if t is not None)))
+            self.d_mode_w) + tuple(t for t in (self.d_btab, self.d_bsin2, self.d_emass, self.d_zs)
+                                   if t is not None)))
 
     # -- memory -----------------------------------------------------------
     def bytes_needed(self, precision: str) -> int:
         Mb = self.m_max + 1
         nn = self.n * self.n
         rhs = self.n * self.nrhs
-        ve = Mb * rhs * 16 if self.alpha < 1.0 else 0       # separate V_E for the far field
+        # separate far-field vector (V_E, or V_E - V_H^Zs for an impedance surface)
+        ve = Mb * rhs * 16 if (self.alpha < 1.0 or self.zs is not None) else 0
         if precision == "fp64":
             return Mb * (2 * nn * 16 + 3 * rhs * 16) + ve
         tc = 4 * 128 * Mb * (2 * self.n + 4 * max(self.n, self.nrhs)) * 2
@@ -276,28 +291,55 @@ class BorGpuProblem:
                  nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
                  self.n_tail_max, nat.ptr(work), nbytes, stream)
 
+    def fill_far_ibc(self, Z, precision: int, scale: complex, stream: int):
+        nat.call("ghost_bor_far_ibc", precision, self.N, self.m_max, self.n_xi_b, self.k,
+                 scale.real, scale.imag, nat.ptr(self.d_zs), nat.ptr(self.d_geo), nat.ptr(self.d_btab),
+                 nat.ptr(self.d_bsin2), nat.ptr(Z), Z.shape[-1], Z.stride(0), stream)
+
+    def fill_near_ibc(self, scale: complex, stream: int, band=None, Z=None):
+        ld = 0 if Z is None else Z.shape[-1]
+        ms = 0 if Z is None else Z.stride(0)
+        work, nbytes = self._near_work("ghost_bor_near_mfie_workspace")
+        nat.call("ghost_bor_near_ibc", self.N, self.m_max, self.k, scale.real, scale.imag,
+                 nat.ptr(self.d_zs), nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(self.d_emass),
+                 len(self.near.pairs), nat.ptr(self.d_pairs), nat.ptr(self.d_tails),
+                 nat.ptr(self.d_cells), self.near.cells.shape[1], nat.ptr(self.d_core),
+                 nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
+                 self.n_tail_max, nat.ptr(work), nbytes, stream)
+
     def fill_operator_far(self, Z, precision: int, stream: int):
-        """Far parts of A = alpha C Z_E + (1 - alpha) eta0 Z_M into Z."""
+        """Far parts of A = alpha (C Z_E + Z_s-terms) + (1 - alpha) eta0 Z_M into Z."""
         if self.alpha > 0.0:
             self.fill_far(Z, precision, self.alpha * self.C, stream)
+        if self.ibc:
+            self.fill_far_ibc(Z, precision, complex(self.alpha), stream)
         if self.alpha < 1.0:
             self.fill_far_mfie(Z, precision, complex((1.0 - self.alpha) * ETA0), stream)
 
     def fill_operator_near(self, stream: int, band=None, Z=None, precision: int = nat.F64):
-        """Near/self parts (and the MFIE mass term) of A into the band or Z."""
+        """Near/self parts (and the mass terms) of A into the band or Z."""
         if self.alpha > 0.0:
             self.fill_near(self.alpha * self.C, stream, band=band, Z=Z, precision=precision)
+        if self.ibc:
+            self.fill_near_ibc(complex(self.alpha), stream, band=band, Z=Z)
         if self.alpha < 1.0:
             self.fill_near_mfie(complex((1.0 - self.alpha) * ETA0), stream, band=band, Z=Z)
 
-    def excitation(self, B, coef_e: float, coef_h: float, stream: int):
+    def excitation(self, B, coef_e: float, coef_h: float, stream: int, h_weight=None):
+        """B = coef_e <W, E_inc> + coef_h <W, w n x H_inc> for every mode, angle
+        and polarisation; w = 1, or the complex per-element h_weight (device)."""
         torch = self.torch
         lib = nat.load()
         nbytes = int(lib.ghost_bor_rhs_workspace(self.N, self.m_max, self.T))
         work = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
-        nat.call("ghost_bor_rhs", self.N, self.m_max, self.T, self.k, coef_e, coef_h,
-                 nat.ptr(self.d_geo), nat.ptr(self.d_thetas), nat.ptr(self.d_masks),
-                 nat.ptr(B), B.shape[-1], B.stride(0), nat.ptr(work), stream)
+        if h_weight is None:
+            nat.call("ghost_bor_rhs", self.N, self.m_max, self.T, self.k, coef_e, coef_h,
+                     nat.ptr(self.d_geo), nat.ptr(self.d_thetas), nat.ptr(self.d_masks),
+                     nat.ptr(B), B.shape[-1], B.stride(0), nat.ptr(work), stream)
+        else:
+            nat.call("ghost_bor_rhs_weighted", self.N, self.m_max, self.T, self.k, coef_e, coef_h,
+                     nat.ptr(h_weight), nat.ptr(self.d_geo), nat.ptr(self.d_thetas), nat.ptr(self.d_masks),
+                     nat.ptr(B), B.shape[-1], B.stride(0), nat.ptr(work), stream)
         return work
 
     def excitation_coefs(self):
@@ -306,8 +348,15 @@ class BorGpuProblem:
                 (1.0 - self.alpha) * ETA0 if self.alpha < 1.0 else 0.0)
 
     def _far_excitation(self, B, stream: int):
-        """The EFIE excitation V_E that the reciprocity far field needs: B itself
-        for EFIE, a second excitation for CFIE / MFIE (whose B mixes in n x H)."""
+        """The vector the reciprocity far field dots with each solution: V_E
+        (B itself for a PEC EFIE, a second excitation for CFIE / MFIE, whose B
+        mixes in n x H); for an impedance surface V_E - V_H^Zs, the rotated
+        n x H excitation weighted by Z_s / eta0, which adds the radiation of
+        M = -Z_s n x J (bor_solver.py:659-708)."""
+        if self.zs is not None:
+            Ve = self.torch.empty_like(B)
+            self._ve_work = self.excitation(Ve, 1.0, -1.0, stream, h_weight=self.d_zs)
+            return Ve
         if self.alpha >= 1.0:
             return B
         Ve = self.torch.empty_like(B)
@@ -327,6 +376,19 @@ class BorGpuProblem:
         self.check_near_status()
         return Z
 
+    def assemble_ibc_modes_fp64(self, stream: Optional[int] = None):
+        """Dense FP64 Z_s (M/2) + B(m), m = 0..M, unmasked: the
+        assemble_ibc_extra operator of the reference for every m >= 0."""
+        torch = self.torch
+        if self.zs is None or self.d_btab is None:
+            raise ValueError("this problem was built without a surface impedance")
+        st = nat.stream_handle() if stream is None else stream
+        Z = torch.zeros((self.m_max + 1, self.n, self.n), dtype=torch.complex128, device=self.device)
+        self.fill_far_ibc(Z, nat.F64, 1.0 + 0.0j, st)
+        self.fill_near_ibc(1.0 + 0.0j, st, Z=Z)
+        self.check_near_status()
+        return Z
+
     def assemble_modes_fp64(self, stream: Optional[int] = None):
         """Dense FP64 Z(m), m = 0..M, unmasked, C factor applied: the
         assemble_mode operator of the reference for every m >= 0."""
@@ -339,6 +401,22 @@ class BorGpuProblem:
         return Z
 
     # -- the sweep ---------------------------------------------------------
+    def mode_conds(self, Aop) -> np.ndarray:
+        """2-norm condition number of every mode's reduced system (the rows and
+        columns of its basis mask removed) from its singular values on the
+        device: the figure np.linalg.cond gives the reference's monitor of
+        lossless impedance surfaces (bor_solver.py:745-800).  Aop is the masked
+        operator of the sweep (FP64, or its FP32 composition)."""
+        torch = self.torch
+        out = np.zeros(self.m_max + 1)
+        for m in range(self.m_max + 1):
+            drop = {int(r) for r in self.masks[m] if r >= 0}
+            keep = torch.as_tensor([i for i in range(self.n) if i not in drop], device=self.device)
+            A = Aop[m].index_select(0, keep).index_select(1, keep).to(torch.complex128)
+            sv = torch.linalg.svdvals(A)
+            out[m] = float(sv[0] / sv[-1])
+        return out
+
     def refine_for_currents(self) -> None:
         """Refinement for surface currents within 1e-4 of the FP64 solve, not only
         the far field: every correction updates the residual with exact products
@@ -399,6 +477,7 @@ class BorGpuProblem:
             self.fill_operator_near(st, Z=Z); mark("near")
             nat.call("ghost_bor_mask64", Mb, n, nat.ptr(self.d_masks), nat.ptr(Z), n, Z.stride(0), st)
             Zc = Z.clone()
+            conds = self.mode_conds(Zc) if self.monitor_cond else None
             mark("compose"); abort()
             work = self.excitation(B, *self.excitation_coefs(), st)
             Ve = self._far_excitation(B, st); mark("rhs")
@@ -420,7 +499,9 @@ class BorGpuProblem:
             mark("near")
             A = torch.empty((Mb, n, n), dtype=c64, device=self.device)
             nat.call("ghost_bor_compose", Mb, n, Nn, nat.ptr(Zf), n, Zf.stride(0), nat.ptr(band),
-                     nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st); mark("compose"); abort()
+                     nat.ptr(self.d_masks), nat.ptr(A), n, A.stride(0), st)
+            conds = self.mode_conds(A) if self.monitor_cond else None
+            mark("compose"); abort()
             work = self.excitation(B, *self.excitation_coefs(), st)
             Ve = self._far_excitation(B, st); mark("rhs")
             X32 = torch.empty((Mb, n, nrhs), dtype=c64, device=self.device)
@@ -589,13 +670,33 @@ class BorGpuProblem:
         out = SweepResult(dF=np.ascontiguousarray(dF_h), residual=res, refine_iters=iters, timings=tm,
                           info=info_h, res_history=history if precision == "fp32ir" else [], kernel_s=ks,
                           res_history_modes=(torch.stack(hist_modes).cpu().numpy() if precision == "fp32ir"
-                                             else None))
+                                             else None), cond=conds)
         if keep:
             out.X = X
             out.B = B
             out.Ve = Ve
             out.lu = lu          # factors, pivots and the unfactored (masked) operator
         return out
+
+
+def impedance_per_element(zs, n_elem: int) -> Optional[np.ndarray]:
+    """Z_s per generatrix element as the reference reads it (bor_solver.py:
+    848-862): None, a complex scalar or one complex value per element; None
+    when every value is zero (a PEC body)."""
+    if zs is None:
+        return None
+    arr = np.asarray(zs, dtype=complex)
+    if arr.ndim == 0:
+        out = np.full(n_elem, complex(arr))
+    else:
+        if arr.ndim != 1 or len(arr) != n_elem:
+            raise ValueError("zs array must have one entry per generatrix element.")
+        out = arr.astype(complex)
+    if not np.all(np.isfinite(out)):
+        raise ValueError("zs must be finite")
+    if np.all(np.abs(out) == 0.0):
+        return None
+    return np.ascontiguousarray(out)
 
 
 def mode_runs(live: np.ndarray) -> List[Tuple[int, int]]:

@@ -249,6 +249,36 @@ int ghost_bor_near_mfie(int n_elem, int m_max, double k, double scale_re, double
                         int n_tail_max, void *work, long long work_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
+ * Surface-impedance (IBC-EFIE) operator addition Z_s (M/2) + B for
+ * m = 0..m_max: the Z_s-weighted mass term plus the rotated principal-value
+ * brackets B_uv = p(R) W_u . [R x (n' x f_v)] with Z_s at the source.  Both
+ * fills ADD scale * Z_s(f) * (block) for every pair (e, f), Z_s(f) the complex
+ * impedance of the source element:
+ *   zs_elem [n_elem] complex (interleaved re, im), or NULL for Z_s = 1
+ * ghost_bor_far_ibc: the far pairs |e - f| >= 2, arguments otherwise as in
+ *   ghost_bor_far_mfie (same tables, same bracket rule for nxi).
+ *   Replaces sample_ibc + the streamed IBC blocks and _rot_pv_blocks' far
+ *   part (bor_stream_kernel.c:108-150, bor_kernels.py:449-511,
+ *   bor_solver.py:499-519).
+ * ghost_bor_near_ibc: the near pairs |e - f| <= 1 on the graded cells and the
+ *   mass term (self pairs), arguments otherwise as in ghost_bor_near_mfie
+ *   (workspace ghost_bor_near_mfie_workspace).  Replaces ibc_kernels_near,
+ *   _near_ibc_data, the near loop of _rot_pv_blocks and mass_blocks(weight)
+ *   (bor_kernels.py:514-560, bor_solver.py:481-497, 520-552).
+ */
+int ghost_bor_far_ibc(int prec, int n_elem, int m_max, int nxi, double k,
+                      double scale_re, double scale_im, const double *zs_elem,
+                      const double *geo, const double *tab, const double *sin2,
+                      void *Z, long long ldz, long long mode_stride, void *stream);
+int ghost_bor_near_ibc(int n_elem, int m_max, double k, double scale_re, double scale_im,
+                       const double *zs_elem, const double *nodes, const double *elem,
+                       const double *emass, int n_pairs, const int *pairs, const int *tails,
+                       const double *cells, int n_cells_total,
+                       const double *core_gl, const double *tail_gl, int n_tail_total,
+                       double *band, void *Z, long long ldz, long long mode_stride,
+                       int n_tail_max, void *work, long long work_bytes, void *stream);
+
+/* ------------------------------------------------------------------------
  * Excitation for all modes 0..m_max, angles and both polarisations:
  *   B[m][row][2*it + pol] (complex double, row stride ldb, mode stride),
  *   pol 0 = VV (theta), 1 = HH (phi).  Rows flagged in mask_rows[m][4]
@@ -266,6 +296,19 @@ int ghost_bor_rhs(int n_elem, int m_max, int n_theta, double k,
                   const double *geo, const double *thetas_deg,
                   const int *mask_rows, double *B, long long ldb, long long mode_stride,
                   void *work, void *stream);
+
+/* ghost_bor_rhs with a complex weight per element on the n x H part:
+ * coef_e <W, E_inc> + coef_h <W, h_weight(el) n x H_inc>, h_weight
+ * [n_elem] complex (interleaved re, im, not NULL).  With coef_e = 1,
+ * coef_h = -1 and h_weight = Z_s this is the reciprocity vector of the far
+ * field of an impedance surface, J plus the eliminated M = -Z_s n x J
+ * (farfield_mode with zs_pt, bor_solver.py:659-708).
+ */
+int ghost_bor_rhs_weighted(int n_elem, int m_max, int n_theta, double k,
+                           double coef_e, double coef_h, const double *h_weight,
+                           const double *geo, const double *thetas_deg,
+                           const int *mask_rows, double *B, long long ldb, long long mode_stride,
+                           void *work, void *stream);
 
 /* Allocation-free variant of ghost_bor_rhs for callers that cannot allocate
  * device memory during a solve (a service that reserves all GPU memory up front,

@@ -155,8 +155,6 @@ def test_drop_in_arguments_and_no_cpu_fallback(pkg):
         bs.solve_bor(pts, f, [0.0], assembly="fmm")
     with pytest.raises(ValueError):
         bs.solve_bor_batch([{"points": pts, "freq_hz": f}], [0.0], table_precision="quad")
-    with pytest.raises(NotImplementedError):
-        bs.solve_bor(pts, f, [0.0], zs=50.0)
 
     def abort():
         raise InterruptedError("cancelled")
@@ -168,6 +166,8 @@ def test_drop_in_arguments_and_no_cpu_fallback(pkg):
     if not torch.cuda.is_available():
         with pytest.raises(RuntimeError, match="no CPU fallback"):
             bs.solve_bor(pts, f, [0.0, 90.0])
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            bs.solve_bor(pts, f, [0.0], zs=50.0)
         with pytest.raises(RuntimeError, match="no CPU fallback"):
             bs.BorPecSolver(pts, f).assemble_mode(0, 2)
 

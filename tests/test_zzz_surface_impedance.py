@@ -1,0 +1,136 @@
+"""Surface impedance (IBC-EFIE) on the GPU against the reference.
+
+tests/golden/ibc_conesphere_n40.npz holds the reference's own FP64 results
+(tests/golden/make_ibc_golden.py): the per-mode IBC operator additions
+Z_s (M/2) + B for a tapered complex Z_s with a bare (Z_s = 0) nose, and the
+full-solve amplitudes with that taper and with a scalar Z_s.  The GPU path
+(ghost_bor_far_ibc, ghost_bor_near_ibc, ghost_bor_rhs_weighted) must give the
+operator to 1e-11 of its largest entry, the FP64 solve to 1e-10 relative
+amplitude and the FP32 + refinement solve to 1e-4 and 0.01 dB.  The far
+bracket blocks and the far field with the eliminated magnetic current are
+checked against the oracle, the lossless-Z_s resonance monitor against the
+oracle's condition numbers, and impedance spheres against the Mie series.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def D():
+    return load_golden("ibc_conesphere_n40")
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def db_err(a, b):
+    a, b = np.abs(np.asarray(a)) ** 2, np.abs(np.asarray(b)) ** 2
+    return float(np.max(np.abs(10 * np.log10(a / b))))
+
+
+def test_ibc_operator_matches_reference(pkg, D):
+    """assemble_ibc_extra (far + near brackets + Z_s mass) of modes 0, 1, -4."""
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]))
+    zs = D["zs_taper"]
+    M = int(D["m_max"])
+    for m in D["modes"]:
+        m = int(m)
+        err = rel(s.assemble_ibc_extra(m, M, zs[s.g.elem], zs), D[f"Zi_{m}"])
+        print(f"\nmode {m}: {err:.2e}")
+        assert err < 1e-11, (m, err)
+
+
+def test_ibc_far_bracket_blocks(pkg, oracle, D):
+    """Streamed IBC far blocks with Z_s in the source weights (FP64 and FP32
+    transforms) vs the oracle's, every mode -M..M."""
+    M = int(D["m_max"])
+    zs = D["zs_taper"]
+    o = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    o.build_far(M, efie=False, ibc_zs_pt=zs[o.geo.elem])
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]))
+    for dtype, tol in ((np.complex128, 1e-12), (np.complex64, 1e-5)):
+        s.enable_streaming(M, efie=False, ibc_zs_pt=zs[s.g.elem], single_blocks=dtype == np.complex64)
+        for m in range(-M, M + 1):
+            got = s._stream.bracket_blocks("ibc", m)
+            want = [o.Bb[uv, m + M] for uv in range(4)]
+            scale = max(np.max(np.abs(w)) for w in want)
+            err = max(np.max(np.abs(g - w)) for g, w in zip(got, want)) / scale
+            assert err < tol, (dtype, m, err)
+
+
+@pytest.mark.parametrize("tag", ["taper", "scalar"])
+@pytest.mark.parametrize("precision,rel_tol,db_tol", [("double", 1e-10, 1e-6), ("auto", 1e-4, 0.01)])
+def test_ibc_solve_matches_reference(pkg, D, tag, precision, rel_tol, db_tol):
+    zs = D["zs_taper"] if tag == "taper" else 120.0 - 80.0j
+    r = pkg.bor_solver.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], formulation="efie",
+                                 zs=zs, n_modes=int(D["m_max"]), mode_tol=0.0, table_precision=precision)
+    for pol in ("vv", "hh"):
+        a, b = r[f"amp_{pol}"], D[f"amp_{pol}_{tag}"]
+        print(f"\n{tag} {precision} {pol}: rel {rel(a, b):.2e}, dB {db_err(a, b):.2e}")
+        assert rel(a, b) < rel_tol
+        assert db_err(a, b) < db_tol
+    assert "max_cond" not in r          # lossy Z_s: no resonance monitor
+
+
+def test_ibc_farfield_mode_matches_oracle(pkg, oracle, D):
+    """Far field of J plus the eliminated M = -Z_s n x J by reciprocity
+    (V_E - V_H^Zs from ghost_bor_rhs_weighted) vs the oracle's projection."""
+    zs = D["zs_taper"]
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]))
+    o = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    rng = np.random.default_rng(4)
+    for m in (0, 1, -3):
+        for th in (20.0, 90.0, 151.0):
+            x = rng.standard_normal(2 * s.Nn) + 1j * rng.standard_normal(2 * s.Nn)
+            got = s.farfield_mode(m, x, th, zs_pt=zs[s.g.elem])
+            fth, fph = o.farfield(m, x[None, :], [th], zs_pt=zs[o.geo.elem])
+            want = np.array([fth[0], fph[0]])
+            assert np.max(np.abs(np.array(got) - want)) <= 1e-12 * np.max(np.abs(want)), (m, th)
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-6), ("auto", 1e-2)])
+def test_lossless_ibc_resonance_monitor(pkg, oracle, D, precision, tol):
+    """A closed body with a purely reactive Z_s on the EFIE: the warning and the
+    per-mode condition numbers (max, median over the modes used) of the
+    reference's monitor, against np.linalg.cond of the oracle's systems."""
+    zs = -50j
+    M = int(D["m_max"])
+    r = pkg.bor_solver.solve_bor(D["points"], float(D["freq_hz"]), D["thetas"], formulation="efie",
+                                 zs=zs, n_modes=M, mode_tol=0.0, table_precision=precision)
+    assert any("lossless" in w for w in r["warnings"])
+    o = oracle.OracleSolver(D["points"], float(D["freq_hz"]))
+    ze = np.full(o.geo.ne, zs)
+    o.prepare(M, efie=True, mfie=False, workers=4, ibc_zs_pt=ze[o.geo.elem])
+    conds = []
+    for m in range(M + 1):
+        A = o.assemble_efie(m, M) + o.assemble_ibc_extra(m, M, ze[o.geo.elem], ze)
+        keep = o.basis_mask(m)
+        conds.append(np.linalg.cond(A[np.ix_(keep, keep)]))
+    print(f"\n{precision}: max_cond {r['max_cond']:.6e} vs {max(conds):.6e}, "
+          f"median {r['median_cond']:.6e} vs {np.median(conds):.6e}")
+    assert abs(r["max_cond"] - max(conds)) <= tol * max(conds)
+    assert abs(r["median_cond"] - np.median(conds)) <= tol * np.median(conds)
+
+
+@pytest.mark.parametrize("a,f,zs", [(0.5, 3e8, 50 - 20j), (0.3, 1e9, 100 + 100j)])
+def test_impedance_sphere_matches_mie(pkg, a, f, zs):
+    """Backscatter of a 120-segment impedance sphere vs the impedance-sphere
+    Mie series (oracle.mie, pinned to the reference's): the mesh's own
+    discretisation error is 0.0024 and 0.0063 dB for these two cases."""
+    from oracle import mie
+    pts = pkg.bodies.sphere_generatrix(a, 120)
+    want = mie.sigma_impedance_sphere(a, f, zs)
+    for precision in ("double", "auto"):
+        r = pkg.bor_solver.solve_bor(pts, f, [0.0, 60.0, 120.0], zs=zs, mode_tol=0.0,
+                                     table_precision=precision)
+        s = np.array(r["sigma_vv"] + r["sigma_hh"])
+        err = float(np.max(np.abs(10 * np.log10(s / want))))
+        print(f"\n{precision}: {err:.4f} dB")
+        assert err < 0.01, (precision, err)
