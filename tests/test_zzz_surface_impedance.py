@@ -11,7 +11,6 @@ bracket blocks and the far field with the eliminated magnetic current are
 checked against the oracle, the lossless-Z_s resonance monitor against the
 oracle's condition numbers, and impedance spheres against the Mie series.
 """
-import math
 
 import numpy as np
 import pytest
