@@ -14,11 +14,14 @@ frequency is then solved on the GPU by ``bor_solver.solve_bor``.  Several
 frequencies go through ``bor_solver.solve_bor_batch``, which builds the next
 frequency's problem on a host thread while the GPU sweeps the current one.
 
-Scope: bodies whose segments are all TYPE 2 conductors without impedance
-flags (PEC, CFIE or EFIE).  Impedance (IBC) flags and the penetrable kinds
-(TYPE 3 dielectric, TYPE 3+4 coated, TYPE 2+3+4 partial coating, TYPE 3+4+5
-layered) are recognised and rejected with NotImplementedError; malformed
-snapshots raise ValueError as in the reference.
+Scope: bodies whose segments are all TYPE 2 conductors: PEC (CFIE, or EFIE
+when cfie_alpha <= 0) and conductors with surface-impedance (IBC) flags,
+whose Z_s per element comes from the snapshot's material tables
+(materials.MaterialLibrary) and which are solved with the IBC-EFIE.  The
+penetrable kinds (TYPE 3 dielectric, TYPE 3+4 coated, TYPE 2+3+4 partial
+coating, TYPE 3+4+5 layered) are recognised and rejected with
+NotImplementedError; malformed snapshots and material tables raise as in the
+reference.
 """
 
 from __future__ import annotations
@@ -34,6 +37,7 @@ import numpy as np
 
 from .bor_solver import solve_bor, solve_bor_batch
 from .geometry import C0
+from .materials import MaterialLibrary
 
 DEFAULT_ELEMENTS_PER_WAVELENGTH = 20
 MAX_ELEMENTS_DEFAULT = 50_000
@@ -299,9 +303,6 @@ def prepare_snapshot(snapshot: Dict[str, Any], geometry_units: str = "inches"):
     run = generatrix_run(chains, "TYPE 2", max(1e-12, 1e-9 * diag))
     axis_tol = 1e-6 * diag
     preflight(run, "body", axis_tol)
-    if any(c.ibc_flag > 0 for c in run):
-        raise NotImplementedError("surface-impedance (IBC) flags on TYPE 2 segments are not "
-                                  "on the GPU path; only PEC bodies are.")
     return kind, run, axis_tol
 
 
@@ -388,10 +389,16 @@ def solve_monostatic_rcs_bor(
     if any(a < 0.0 or a > 180.0 for a in aspects):
         raise ValueError("Aspect angles must lie in [0, 180] degrees from +z.")
     pol = canonical_polarization(polarization)
+    _meters_per_unit(geometry_units)
     if workers is None:
         workers = max(1, (os.cpu_count() or 2) - 1)
+    # material tables first, as the reference reads them (bor_dispatch.py:389-393)
+    materials = MaterialLibrary.from_entries(geometry_snapshot.get("ibcs", []) or [],
+                                             geometry_snapshot.get("dielectrics", []) or [],
+                                             base_dir=material_base_dir or os.getcwd())
     kind, run, axis_tol = prepare_snapshot(geometry_snapshot, geometry_units)
     form = "efie" if cfie_alpha <= 0.0 else "cfie"
+    label = f"BoR-MoM PEC {form.upper()}"
 
     def check_abort():
         if abort_event is not None and abort_event.is_set():
@@ -404,13 +411,45 @@ def solve_monostatic_rcs_bor(
             except Exception:                      # a failing callback never stops a solve
                 pass
 
-    def mesh(freq_ghz):
+    def mesh(freq_ghz, full=False):
         ghz = float(mesh_reference_ghz) if mesh_reference_ghz else freq_ghz
-        return mesh_generatrix(run, C0 / (ghz * 1e9), max_elements, axis_tol)[0]
+        m = mesh_generatrix(run, C0 / (ghz * 1e9), max_elements, axis_tol)
+        return m if full else m[0]
 
-    check_abort()
     common = dict(formulation=form, cfie_alpha=cfie_alpha, mode_tol=mode_tol,
                   table_precision=table_precision)
+    if any(c.ibc_flag > 0 for c in run):
+        # impedance flags: Z_s per element at each frequency (material warnings
+        # in the reference's order), one IBC-EFIE solve per frequency
+        # (bor_dispatch.py:504-537)
+        outs = []
+        for fi, f in enumerate(freqs):
+            check_abort()
+            pts, seg_of, arc_of = mesh(f, full=True)
+            zs = np.zeros(len(pts) - 1, dtype=complex)
+            for ei in range(len(zs)):
+                c = run[seg_of[ei]]
+                if c.ibc_flag > 0:
+                    zs[ei] = materials.get_impedance(c.ibc_flag, f, arc_s=float(arc_of[ei]))
+            has_ibc = bool(np.any(np.abs(zs) > 0.0))
+            form_f = "efie" if (has_ibc or cfie_alpha <= 0.0) else "cfie"
+
+            def report(done, cap, fi=fi, f=f):
+                notify(fi, f"{f:g} GHz: mode {done}/{cap}")
+
+            out = solve_bor(pts, f * 1e9, aspects, formulation=form_f, cfie_alpha=cfie_alpha,
+                            zs=zs if has_ibc else None, n_modes=n_modes, mode_tol=mode_tol,
+                            workers=workers, progress=report, check_abort=check_abort,
+                            table_precision=table_precision, assembly=assembly)
+            label = "BoR-MoM IBC-EFIE (Leontovich)" if has_ibc else f"BoR-MoM PEC {form_f.upper()}"
+            for w in out.get("warnings", []) or []:
+                materials.warn_once(str(w))
+            outs.append(out)
+            notify(fi + 1, f"Solved {f:g} GHz")
+        return _sweep_result(freqs, outs, aspects, pol, kind, label, cfie_alpha, workers,
+                             materials, expand_to_360, warnings_done=True)
+
+    check_abort()
     if len(freqs) == 1:
         f0 = freqs[0]
 
@@ -429,14 +468,20 @@ def solve_monostatic_rcs_bor(
             check_abort()
 
         outs = solve_bor_batch(bodies, aspects, progress=done, **common)
+    return _sweep_result(freqs, outs, aspects, pol, kind, label, cfie_alpha, workers, materials,
+                         expand_to_360, warnings_done=False)
 
+
+def _sweep_result(freqs, outs, aspects, pol, kind, label, cfie_alpha, workers,
+                  materials: MaterialLibrary, expand_to_360: bool, warnings_done: bool):
+    """The result layout of solve_monostatic_rcs_bor (bor_dispatch.py:640-702);
+    the solves' warnings join the material warnings once each, in order."""
     samples: List[Dict[str, Any]] = []
     per_freq: List[Dict[str, Any]] = []
-    warnings: List[str] = []
     for f, out in zip(freqs, outs):
-        for w in out.get("warnings", []) or []:
-            if str(w) not in warnings:
-                warnings.append(str(w))
+        if not warnings_done:
+            for w in out.get("warnings", []) or []:
+                materials.warn_once(str(w))
         samples += _samples_of(out, f, aspects, pol)
         residual = float(out.get("linear_residual", 0.0))
         per_freq.append({
@@ -456,13 +501,13 @@ def solve_monostatic_rcs_bor(
         "rcs_linear_quantity": "sigma_3d",
         "samples": samples,
         "metadata": {
-            "formulation": f"BoR-MoM PEC {form.upper()}",
+            "formulation": label,
             "geometry_kind": kind,
             "expanded_to_360": bool(expand_to_360),
             "per_frequency": per_freq,
             "cfie_alpha": float(cfie_alpha),
             "workers": int(workers),
-            "warnings": warnings,
+            "warnings": list(materials.warnings),
         },
     }
 

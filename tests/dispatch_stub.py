@@ -11,11 +11,14 @@ module, so both sides see identical solver outputs.
 """
 import copy
 import math
+import os
 import threading
 
 import numpy as np
 
 C0 = 299_792_458.0
+# mat.<flag> table files of the impedance cases
+MATERIALS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "materials")
 
 
 class Recorder:
@@ -28,10 +31,13 @@ class Recorder:
                  zs=None, n_modes=None, mode_tol=1e-6, table_precision="auto", **_kw):
         pts = np.asarray(points, dtype=float)
         th = np.radians(np.asarray(thetas_deg, dtype=float))
+        zrec = None if zs is None else [[float(z.real), float(z.imag)]
+                                        for z in np.atleast_1d(np.asarray(zs, dtype=complex))]
         self.calls.append({"points": pts.tolist(), "freq_hz": float(freq_hz),
                            "thetas": np.degrees(th).tolist(), "formulation": formulation,
                            "cfie_alpha": float(cfie_alpha), "n_modes": n_modes,
-                           "mode_tol": float(mode_tol), "table_precision": table_precision})
+                           "mode_tol": float(mode_tol), "table_precision": table_precision,
+                           "zs": zrec})
         k = 2.0 * math.pi * float(freq_hz) / C0
         n = len(pts)
         sig = float(np.sum(pts[:, 0]) - 0.5 * np.sum(pts[:, 1]))
@@ -104,7 +110,30 @@ def snapshots():
                                   ["2", "junk"])]}
     ogive["segments"][1]["point_pairs"][0]["x1"] = ogive["segments"][0]["point_pairs"][-1]["x2"]
     ogive["segments"][1]["point_pairs"][0]["y1"] = ogive["segments"][0]["point_pairs"][-1]["y2"]
-    return {"sphere_in": sphere, "cone_sphere_m": cone_sphere, "ogive_in": ogive}
+    # impedance flags: the cone-sphere with a constant Z_s on the flank, a
+    # linear taper on one cap and a frequency table (tests/golden/materials/
+    # mat.51) on the other; unused medium rows are parsed too
+    cone_ibc = copy.deepcopy(cone_sphere)
+    cone_ibc["segments"][0]["properties"] = ["2", "-12", "51", "0", "0"]
+    cone_ibc["segments"][1]["properties"] = ["2", "3", "1", "", ""]
+    cone_ibc["segments"][2]["properties"] = ["2.0", "5", "mat.2"]
+    cone_ibc["ibcs"] = [["1", "constant", "50", "-20", "0", "0"],
+                        ["mat.2", "Linear", "0", "0", "100", "-50"], ["51"], [], ["0", "x"]]
+    cone_ibc["dielectrics"] = [["3", "4.0", "-0.1", "1", "0"], ["4", "0", "0"], ["5"]]
+    # a sphere in two segments: a raised-cosine taper from PEC and a geometric
+    # taper, in inches
+    top, bottom = arc(6.0, 0.0, 0.0, 100.0, 7), arc(6.0, 0.0, 100.0, 180.0, 5)
+    sphere_ibc = {"segments": [segment("top", top, ["2", "0", "4"]),
+                               segment("bottom", bottom, ["2", "-8", "5"])],
+                  "ibcs": [["4", "cosine", "0", "0", "80", "10"],
+                           ["5", "exp", "30", "0", "300", "-40"]]}
+    # an impedance flag without a model: a PEC body
+    sphere_unknown = {"segments": [segment("sphere", arc(6.0, 0.0, 0.0, 180.0, 12),
+                                           ["2", "0", "7", "0", "0"])],
+                      "ibcs": [["6", "constant", "10", "0", "0", "0"]]}
+    return {"sphere_in": sphere, "cone_sphere_m": cone_sphere, "ogive_in": ogive,
+            "cone_sphere_ibc_m": cone_ibc, "sphere_ibc_in": sphere_ibc,
+            "sphere_unknown_flag_in": sphere_unknown}
 
 
 def cases():
@@ -125,6 +154,17 @@ def cases():
               polarization="TE", geometry_units="m", cfie_alpha=0.3)),
         ("ogive", "ogive_in",
          dict(frequencies_ghz=[2.2], elevations_deg=th, polarization="", workers=3)),
+        ("cone_sphere_ibc", "cone_sphere_ibc_m",
+         dict(frequencies_ghz=[0.5, 2.0, 2.5, 4.0], elevations_deg=[0.0, 30.0, 90.0, 150.0],
+              polarization="VV", geometry_units="meters", material_base_dir=MATERIALS)),
+        ("sphere_ibc_tapers", "sphere_ibc_in",
+         dict(frequencies_ghz=[1.0, 2.0], elevations_deg=th, polarization="HH",
+              mesh_reference_ghz=2.0, expand_to_360=True, mode_tol=0.0)),
+        ("sphere_ibc_single_freq", "sphere_ibc_in",
+         dict(frequencies_ghz=[1.3], elevations_deg=[0.0, 90.0], polarization="VV", cfie_alpha=0.0)),
+        ("sphere_unknown_impedance_flag", "sphere_unknown_flag_in",
+         dict(frequencies_ghz=[1.5, 2.0], elevations_deg=[0.0, 90.0], polarization="VV",
+              cfie_alpha=0.4)),
     ]
 
 
@@ -157,7 +197,24 @@ def bad_inputs():
                               seg("b", arc_[3:], ["3", "0", "0", "2"]))
     aborted = threading.Event()
     aborted.set()
+
+    def with_ibcs(ibcs, dielectrics=None):
+        snap = copy.deepcopy(ok)
+        snap["segments"][0]["properties"] = ["2", "0", "1", "0", "0"]
+        snap["ibcs"] = ibcs
+        if dielectrics is not None:
+            snap["dielectrics"] = dielectrics
+        return snap
+
+    in_mat = dict(base, material_base_dir=MATERIALS)
     return [
+        ("ibc_too_few_tokens", with_ibcs([["1", "linear", "1", "2"]]), base),
+        ("ibc_unknown_taper", with_ibcs([["1", "spline", "1", "2", "3", "4"]]), base),
+        ("ibc_nonfinite_taper", with_ibcs([["1", "linear", "1", "inf", "0", "0"]]), base),
+        ("ibc_table_missing", with_ibcs([["77"]]), in_mat),
+        ("ibc_table_nonfinite", with_ibcs([["52"]]), in_mat),
+        ("dielectric_nonfinite", with_ibcs([], [["3", "nan", "0"]]), base),
+        ("dielectric_table_missing", with_ibcs([], [["mat.78"]]), in_mat),
         ("no_frequencies", ok, dict(base, frequencies_ghz=[])),
         ("no_aspects", ok, dict(base, elevations_deg=[])),
         ("negative_frequency", ok, dict(base, frequencies_ghz=[1.0, -2.0])),

@@ -64,25 +64,33 @@ def test_sweep_matches_reference(fx, rec, name):
 @pytest.mark.parametrize("name", [c[0] for c in stub.bad_inputs()])
 def test_bad_inputs_raise_like_reference(fx, rec, name):
     _, snap, kw = next(c for c in stub.bad_inputs() if c[0] == name)
-    exc = {"ValueError": ValueError, "InterruptedError": InterruptedError}[fx["errors"][name]]
+    exc = {"ValueError": ValueError, "InterruptedError": InterruptedError,
+           "FileNotFoundError": FileNotFoundError}[fx["errors"][name]]
     with pytest.raises(exc):
         D.solve_monostatic_rcs_bor(geometry_snapshot=snap, **kw)
     assert not rec.calls
 
 
 def test_kinds_off_the_gpu_path_are_named(rec):
-    """Valid dielectric bodies and impedance flags raise NotImplementedError."""
+    """Valid dielectric bodies raise NotImplementedError; a conductor with an
+    impedance flag goes to the solver (an IBC-EFIE when the flag has a model)."""
     arc = stub.arc(0.2, 0.0, 0.0, 180.0, 8)
     kw = dict(frequencies_ghz=[1.0], elevations_deg=[0.0], polarization="VV",
               geometry_units="meters")
     diel = {"segments": [stub.segment("d", arc, ["3", "0", "0", "1"])]}
     with pytest.raises(NotImplementedError, match="dielectric"):
         D.solve_monostatic_rcs_bor(diel, **kw)
-    ibc = {"segments": [stub.segment("c", arc[:5], ["2", "0", "1"]),
-                        stub.segment("c2", arc[4:], ["2"])]}
-    with pytest.raises(NotImplementedError, match="IBC"):
-        D.solve_monostatic_rcs_bor(ibc, **kw)
     assert not rec.calls
+    ibc = {"segments": [stub.segment("c", arc[:5], ["2", "0", "1"]),
+                        stub.segment("c2", arc[4:], ["2"])],
+           "ibcs": [["1", "constant", "120", "-30", "0", "0"]]}
+    res = D.solve_monostatic_rcs_bor(ibc, **kw)
+    assert res["metadata"]["formulation"] == "BoR-MoM IBC-EFIE (Leontovich)"
+    (call,) = rec.calls
+    zs = np.array([complex(*z) for z in call["zs"]])
+    n_top = int(np.sum(np.asarray(call["points"])[:, 1] >= arc[4, 1] - 1e-12)) - 1
+    assert call["formulation"] == "efie"
+    assert np.all(zs[:n_top] == 120 - 30j) and np.all(zs[n_top:] == 0)
 
 
 def test_one_mesh_per_frequency_goes_to_one_batch(monkeypatch):
