@@ -28,6 +28,7 @@ SIGNATURES = {
     "ghost_bor_launch_count": (_ll, []),
     "ghost_bor_sample_g": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _d, _vp, _vp, _vp]),
     "ghost_bor_sample_mfie": (_i, [_i, _i, _i] + [_vp] * 8 + [_d, _vp, _vp] + [_vp] * 4 + [_vp]),
+    "ghost_bor_sample_ibc": (_i, [_i, _i, _i] + [_vp] * 8 + [_d, _vp, _vp] + [_vp] * 4 + [_vp]),
     "ghost_bor_far_efie": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_far_efie_masked": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp, _vp]),
     "ghost_bor_far_efie_tc_workspace": (_ll, [_i, _i, _i]),

@@ -63,6 +63,32 @@ GB_HD void ibc_bracket_coefs(double rp, double zp, double trp, double tzp,
     c[5] = dz;
 }
 
+// Geometric factors f_uv of the four IBC brackets at one azimuth sample for the
+// device sampler (the reference's per-sample form, bor_stream_kernel.c:108-150):
+// test point (rho, z) with tangent t at phi = 0, source (rho', z') with tangent
+// t' and outward normal n' = (-t'_z, t'_rho) at phi' = -xi, cx = cos xi,
+// sx = sin xi, dz = z - z', D = rho cos xi - rho':
+//   f_uv = (W_u . n')(R . f'_v) - (W_u . f'_v)(R . n'),  uv = tt, tf, ft, ff;
+// the bracket sample is p(R) f_uv.
+GB_HD void ibc_sample_factors(double rp, double rq, double dz, double trp, double tzp,
+                              double trq, double tzq, double cx, double sx, double *f)
+{
+    const double wt_n = -trp * tzq * cx + tzp * trq;
+    const double wf_n = tzq * sx;
+    const double D = rp * cx - rq;
+    const double r_t = trq * D + tzq * dz;
+    const double r_f = rp * sx;
+    const double r_n = -tzq * D + trq * dz;
+    const double wt_t = trp * trq * cx + tzp * tzq;
+    const double wt_f = trp * sx;
+    const double wf_t = -trq * sx;
+    const double wf_f = cx;
+    f[0] = wt_n * r_t - wt_t * r_n;
+    f[1] = wt_n * r_f - wt_f * r_n;
+    f[2] = wf_n * r_t - wf_t * r_n;
+    f[3] = wf_n * r_f - wf_f * r_n;
+}
+
 template <bool IBC>
 GB_HD void bracket_coefs(double rp, double zp, double trp, double tzp,
                          double rq, double zq, double trq, double tzq, double *c)

@@ -1,7 +1,9 @@
 // capi.cu -- library-level entry points: version, error text, and the
 // drop-in device samplers with the reference's ctypes argument meaning
-// (bor_stream_kernel.c:26-48 sample_g, :51-106 sample_mfie).
+// (bor_stream_kernel.c:26-48 sample_g, :51-106 sample_mfie, :108-150
+// sample_ibc).
 #include "common.cuh"
+#include "brackets.cuh"
 
 #include <stdio.h>
 #include <string.h>
@@ -91,6 +93,40 @@ __global__ void sample_mfie_kernel(int nr, int np_, int nxi,
     }
 }
 
+__global__ void sample_ibc_kernel(int nr, int np_, int nxi,
+                                  const double *__restrict__ rho_p, const double *__restrict__ z_p,
+                                  const double *__restrict__ tr_p, const double *__restrict__ tz_p,
+                                  const double *__restrict__ rho_q, const double *__restrict__ z_q,
+                                  const double *__restrict__ tr_q, const double *__restrict__ tz_q,
+                                  double k, const double *__restrict__ cx_tab, const double *__restrict__ sx_tab,
+                                  double2 *__restrict__ o_tt, double2 *__restrict__ o_tf,
+                                  double2 *__restrict__ o_ft, double2 *__restrict__ o_ff)
+{
+    const long long pair = blockIdx.y * (long long)gridDim.z + blockIdx.z;
+    if (pair >= (long long)nr * np_) return;
+    const int i = (int)(pair / np_), j = (int)(pair % np_);
+    const double Rz = z_p[i] - z_q[j];
+    const double rp = rho_p[i], rq = rho_q[j];
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < nxi; l += gridDim.x * blockDim.x) {
+        const double cx = cx_tab[l], sx = sx_tab[l];
+        const double Rx = rp - rq * cx, Ry = rq * sx;
+        double R = sqrt(Rx * Rx + Ry * Ry + Rz * Rz);
+        if (R < R_MIN) R = R_MIN;
+        const double amp = 1.0 / (4.0 * GB_PI * R * R * R);
+        const double kr = k * R;
+        double sn, cs;
+        sincos(kr, &sn, &cs);
+        const double pr = amp * (cs + kr * sn), pim = amp * (kr * cs - sn);
+        double f[4];
+        ibc_sample_factors(rp, rq, Rz, tr_p[i], tz_p[i], tr_q[j], tz_q[j], cx, sx, f);
+        const long long o = pair * nxi + l;
+        o_tt[o] = make_double2(f[0] * pr, f[0] * pim);
+        o_tf[o] = make_double2(f[1] * pr, f[1] * pim);
+        o_ft[o] = make_double2(f[2] * pr, f[2] * pim);
+        o_ff[o] = make_double2(f[3] * pr, f[3] * pim);
+    }
+}
+
 dim3 pair_grid(int nr, int np_, int nxi)
 {
     const long long pairs = (long long)nr * np_;
@@ -146,4 +182,24 @@ extern "C" int ghost_bor_sample_mfie(int nr, int np_, int nxi,
         reinterpret_cast<double2 *>(o_tt), reinterpret_cast<double2 *>(o_tf),
         reinterpret_cast<double2 *>(o_ft), reinterpret_cast<double2 *>(o_ff));
     return check_launch("sample_mfie");
+}
+
+extern "C" int ghost_bor_sample_ibc(int nr, int np_, int nxi,
+                                    const double *rho_p, const double *z_p,
+                                    const double *tr_p, const double *tz_p,
+                                    const double *rho_q, const double *z_q,
+                                    const double *tr_q, const double *tz_q,
+                                    double k, const double *cos_tab, const double *sin_tab,
+                                    double *o_tt, double *o_tf, double *o_ft, double *o_ff, void *stream)
+{
+    if (nr < 0 || np_ < 0 || nxi < 1) return GHOST_BOR_EINVAL;
+    if ((long long)nr * np_ == 0) return GHOST_BOR_OK;
+    if (!rho_p || !z_p || !tr_p || !tz_p || !rho_q || !z_q || !tr_q || !tz_q || !cos_tab || !sin_tab ||
+        !o_tt || !o_tf || !o_ft || !o_ff || (long long)nr * np_ > 65535LL * 65535LL)
+        return GHOST_BOR_EINVAL;
+    sample_ibc_kernel<<<pair_grid(nr, np_, nxi), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        nr, np_, nxi, rho_p, z_p, tr_p, tz_p, rho_q, z_q, tr_q, tz_q, k, cos_tab, sin_tab,
+        reinterpret_cast<double2 *>(o_tt), reinterpret_cast<double2 *>(o_tf),
+        reinterpret_cast<double2 *>(o_ft), reinterpret_cast<double2 *>(o_ff));
+    return check_launch("sample_ibc");
 }

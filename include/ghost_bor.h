@@ -76,6 +76,18 @@ int ghost_bor_sample_mfie(int nr, int np_, int nxi,
                           double *o_tt, double *o_tf, double *o_ft, double *o_ff,
                           void *stream);
 
+/* Replaces sample_ibc (bor_stream_kernel.c:108-150): the four rotated
+ * principal-value (IBC) brackets p(R) [(W_u . n')(R . f_v) - (W_u . f_v)(R . n')]
+ * with the source normal n', same arguments and layout as ghost_bor_sample_mfie. */
+int ghost_bor_sample_ibc(int nr, int np_, int nxi,
+                         const double *rho_p, const double *z_p,
+                         const double *tr_p, const double *tz_p,
+                         const double *rho_q, const double *z_q,
+                         const double *tr_q, const double *tz_q,
+                         double k, const double *cos_tab, const double *sin_tab,
+                         double *o_tt, double *o_tf, double *o_ft, double *o_ff,
+                         void *stream);
+
 /* ------------------------------------------------------------------------
  * Fused EFIE far fill: for every far element pair (|e - f| >= 2) sample the
  * Green's function on the half azimuth grid xi_j = pi j / (nxi/2), take the

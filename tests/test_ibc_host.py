@@ -13,7 +13,9 @@ pinned to the reference's IBC operator (tests/test_oracle_ibc.py):
   and the entry rule reproduces the oracle's Z_s-weighted far IBC blocks;
 * the entry rule is -s K + s M/2 for the MFIE and s Z_s (K + M/2) for the IBC;
 * the per-element mass contributions weighted by Z_s give the oracle's
-  Z_s mass term.
+  Z_s mass term;
+* the device IBC sampler's loop body (ghost_bor_sample_ibc) equals the
+  reference's own compiled sample_ibc and the oracle's brackets.
 
 Plus the host side of solve_bor(zs=...): Z_s parsing and its errors, before
 any device work.
@@ -47,7 +49,13 @@ def shim(tmp_path_factory):
     for name in ("host_bracket_coefs", "host_bracket_entry"):
         getattr(lib, name).argtypes = [ctypes.c_int, ctypes.c_int, dp, dp]
         getattr(lib, name).restype = None
+    lib.host_sample_ibc.argtypes = SAMPLER_ARGS
+    lib.host_sample_ibc.restype = None
     return lib
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+SAMPLER_ARGS = [ctypes.c_int] * 3 + [_dp] * 8 + [ctypes.c_double, _dp, _dp] + [_dp] * 4
 
 
 def _ptr(a):
@@ -90,6 +98,44 @@ def test_bracket_coefficients_reproduce_oracle_samples(oracle, shim, kind):
     scale = np.abs(p) * (1.0 + np.abs(dz) + rp[:, None] + rq[:, None])
     for g_, w_ in zip(got, want):
         assert np.max(np.abs(g_ - w_) / scale) < 1e-13
+
+
+def _run_sampler(fn):
+    rng = np.random.default_rng(2)
+    nr, npp, nx = 5, 9, 32
+    a = [np.ascontiguousarray(rng.uniform(0.01, 1, nr)) for _ in range(4)]
+    b = [np.ascontiguousarray(rng.uniform(0.01, 1, npp)) for _ in range(4)]
+    xi = 2 * np.pi * np.arange(nx) / nx - np.pi
+    cx, sx = np.ascontiguousarray(np.cos(xi)), np.ascontiguousarray(np.sin(xi))
+    outs = [np.empty((nr, npp, nx), np.complex128) for _ in range(4)]
+    fn(nr, npp, nx, *[_ptr(v) for v in a], *[_ptr(v) for v in b], 7.5, _ptr(cx), _ptr(sx),
+       *[_ptr(o) for o in outs])
+    return a, b, xi, outs
+
+
+def test_ibc_sampler_matches_reference_and_oracle(oracle, shim):
+    """The device IBC sampler's loop body (ghost_bor_sample_ibc, factors from
+    csrc/brackets.cuh) run on the host: equal to the reference's own compiled
+    sample_ibc (oracle/_ref, when the reference tree was available to build it)
+    to rounding, and to the oracle's NumPy brackets."""
+    a, b, xi, outs = _run_sampler(shim.host_sample_ibc)
+    nr, npp, nx = outs[0].shape
+    one = np.ones((nr, npp))
+    F = oracle._ibc_bracket_grid(*[(v[:, None] * one).ravel() for v in a],
+                                 *[(v[None, :] * one).ravel() for v in b], 7.5,
+                                 np.broadcast_to(xi, (nr * npp, nx)))
+    for o, f in zip(outs, F):
+        f = f.reshape(nr, npp, nx)
+        assert np.max(np.abs(o - f)) <= 1e-13 * np.max(np.abs(f))
+    ref_path = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "bor_stream_kernel.so")
+    if not os.path.exists(ref_path):
+        pytest.skip("reference sampler not built (reference tree absent)")
+    ref = ctypes.CDLL(ref_path)
+    ref.sample_ibc.argtypes = SAMPLER_ARGS
+    ref.sample_ibc.restype = None
+    _, _, _, routs = _run_sampler(ref.sample_ibc)
+    for o, r in zip(outs, routs):
+        assert np.max(np.abs(o - r)) <= 1e-15 * np.max(np.abs(r))
 
 
 def test_bracket_entry_rule(shim):

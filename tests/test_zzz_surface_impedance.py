@@ -46,6 +46,35 @@ def test_ibc_operator_matches_reference(pkg, D):
         assert err < 1e-11, (m, err)
 
 
+def test_sample_ibc_matches_oracle(pkg, oracle):
+    """Drop-in device IBC sampler (sample_ibc's argument list) vs the oracle's
+    brackets, FP64."""
+    import torch
+    nat = pkg._native
+    rng = np.random.default_rng(1)
+    nr, npp, nx = 6, 13, 48
+    a = [rng.uniform(0.01, 1, nr) for _ in range(4)]
+    b = [rng.uniform(0.01, 1, npp) for _ in range(4)]
+    xi = 2 * np.pi * np.arange(nx) / nx - np.pi
+    keep = []
+
+    def d(v):
+        t = torch.as_tensor(np.ascontiguousarray(v), dtype=torch.float64, device="cuda")
+        keep.append(t)
+        return t
+
+    outs = [torch.empty((nr, npp, nx), dtype=torch.complex128, device="cuda") for _ in range(4)]
+    args = [nat.ptr(d(v)) for v in a] + [nat.ptr(d(v)) for v in b]
+    nat.call("ghost_bor_sample_ibc", nr, npp, nx, *args, 7.5, nat.ptr(d(np.cos(xi))),
+             nat.ptr(d(np.sin(xi))), *[nat.ptr(o) for o in outs], nat.stream_handle())
+    one = np.ones((nr, npp))
+    F = oracle._ibc_bracket_grid(*[(v[:, None] * one).ravel() for v in a],
+                                 *[(v[None, :] * one).ravel() for v in b], 7.5,
+                                 np.broadcast_to(xi, (nr * npp, nx)))
+    for o, f in zip(outs, F):
+        assert rel(o.cpu().numpy(), f.reshape(nr, npp, nx)) < 1e-13
+
+
 def test_ibc_far_bracket_blocks(pkg, oracle, D):
     """Streamed IBC far blocks with Z_s in the source weights (FP64 and FP32
     transforms) vs the oracle's, every mode -M..M."""
