@@ -166,3 +166,22 @@ def test_drop_in_impedance_operators(pkg, calls):
         assert len(s._stream.bracket_blocks("ibc", -3)) == 4
     with pytest.raises(ValueError):
         s._stream.bracket_blocks("mfie", 0)
+
+
+def test_batched_sweep_and_adjoint_calls(pkg, calls):
+    """The size-class batch (without graph capture) and the adjoint gradient
+    make only declared calls too."""
+    bodies = pkg.bodies
+    bs = pkg.bor_solver
+    items = [{"points": bodies.cone_sphere_generatrix(0.3, 15.0, n), "freq_hz": 1e9, "n_modes": 4}
+             for n in (24, 30, 40)]
+    out = bs.solve_bor_batch(items, [0.0, 45.0, 90.0], use_graphs=False, autotune=False)
+    assert len(out) == 3 and all(len(r["amp_vv"]) == 3 for r in out)
+    assert "ghost_bor_getrf" in calls
+    del calls[:]
+    adj = importlib.import_module("20260722_ghost_gb300.adjoint")
+    r = torch.full((12,), 0.45, dtype=torch.float64, requires_grad=True)
+    J = adj.bspline_rcs(r, 60, 1.5e9, np.arange(30.0, 40.01, 5.0), pol="HH", m_max=4)
+    J.backward()
+    assert r.grad is not None and r.grad.shape == (12,)
+    assert "ghost_bor_far_efie_masked" in calls or "ghost_bor_far_efie_tc_masked" in calls
