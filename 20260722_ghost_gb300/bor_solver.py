@@ -1,4 +1,5 @@
-"""Drop-in replacement for the reference module ``bor_solver`` (PEC path).
+"""Drop-in replacement for the reference module ``bor_solver`` (PEC and
+surface-impedance bodies).
 
 Same entry points, keyword arguments and result keys as the reference
 (bor_solver.py:820-1004 ``solve_bor``, :1007 ``solve_bor_pec``, :175-708
@@ -9,10 +10,12 @@ CUDA device every call raises.
 Precision mapping of ``table_precision``:
   "double"          -> plain FP64 GPU path (far fill, LU and solves in FP64)
   "auto" / "single" -> FP32 far fill + FP32 LU, FP64 near/self blocks, FP64
-                       residual refinement (<= 3 passes) and FP64 mode sum
+                       residual refinement per mode (at most 5 corrections,
+                       typically 3) and FP64 mode sum
 ``assembly``, ``workers`` and ``stream_budget_gb`` are accepted for
 compatibility; the GPU fill is always a streamed (never tabulated) fill and the
-memory gate is the free device memory.
+memory gate is the free device memory.  ``zs`` (surface impedance, scalar or
+per element) selects the IBC-EFIE as in the reference.
 """
 
 from __future__ import annotations

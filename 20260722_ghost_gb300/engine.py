@@ -2,20 +2,27 @@
 
 Stages (each a C-ABI call on one CUDA stream):
 
-  far fill      ghost_bor_far_efie   alpha C Z_E far blocks, m = 0..M (FP32 or FP64
-                ghost_bor_far_mfie   sampling + transforms, FP64 contraction and storage)
-                                     and (1 - alpha) eta0 (-K) MFIE far brackets
-  near fill     ghost_bor_near_efie  FP64 near/self blocks (band store or dense),
-                ghost_bor_near_mfie  MFIE near brackets and the mass term M/2
-  compose       ghost_bor_compose    A32 = fl32(Z_far + Z_near), masked
-  excitation    ghost_bor_rhs        B = alpha V_E + (1 - alpha) eta0 V_H (FP64); for
-                                     CFIE / MFIE also V_E alone for the far field
-  LU + solve    ghost_bor_getrf/getrs  (FP32, trailing updates on tcgen05)
+  far fill      ghost_bor_far_efie_tc   alpha C Z_E far blocks, m = 0..M: FP32+IR,
+                                        the azimuth transform exact on the bf16
+                                        tensor cores; ghost_bor_far_efie_masked
+                                        in FP64 (the comparator)
+                ghost_bor_far_mfie      (1 - alpha) eta0 (-K) MFIE far brackets
+                ghost_bor_far_ibc       Z_s B far brackets of an impedance surface
+  near fill     ghost_bor_near_efie     near/self blocks (FP32+IR: double-float into
+                                        the band; FP64: dense)
+                ghost_bor_near_mfie     MFIE near brackets and the mass term M/2
+                ghost_bor_near_ibc      Z_s (M/2 + B) near part of the IBC
+  compose       ghost_bor_compose       A32 = fl32(Z_far + Z_near), masked
+  excitation    ghost_bor_rhs           B = alpha V_E + (1 - alpha) eta0 V_H (FP64); the
+                                        far-field vector separately for CFIE / MFIE
+                                        (V_E) and IBC (V_E - V_H^Zs, _weighted)
+  LU + solve    ghost_bor_getrf/getrs   (FP32, trailing updates on tcgen05)
   refinement    ghost_bor_residual_exact  R0 = B - (Z_far + Z_near) X0 with exact
-                                     products of 8-bit slices on the bf16 tensor
-                                     cores, then per correction D = A32^-1 R:
-                                     X += D, R -= fl32(Z) D (ghost_bor_cgemm_tc)
-  far field     ghost_bor_farfield   dF[m][col] by reciprocity
+                                        products of 8-bit slices on the bf16 tensor
+                                        cores; per correction D = A32^-1 R, X += D,
+                                        R -= Z D exactly for the first correction
+                                        and with fl32(Z) on ghost_bor_cgemm_tc after
+  far field     ghost_bor_farfield      dF[m][col] by reciprocity
 
 Only modes m >= 0 are factored: Z(-m) = D Z(m) D with D = diag(I, -I) for the
 EFIE and the MFIE operator, and the excitation obeys V(-m) = +-D V(m), so each
@@ -26,7 +33,13 @@ the tests).
 Precisions: "fp64" is the plain FP64 path (the comparator); "fp32ir" samples
 and transforms the far kernels and factors in FP32, keeps the near/self blocks,
 the far-block contraction, the first residual and the mode sum in FP64-class
-arithmetic, and refines up to three times.
+arithmetic, and refines each mode until its residual is below the floor or no
+longer halves (at most max_refine corrections).
+
+A surface impedance Z_s per element (IBC-EFIE) adds the impedance fills
+ghost_bor_far_ibc / ghost_bor_near_ibc to the EFIE operator and takes the far
+field with V_E - V_H^Zs (ghost_bor_rhs_weighted); the LU, solves and
+refinement are unchanged.
 """
 
 from __future__ import annotations
