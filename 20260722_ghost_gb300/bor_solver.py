@@ -203,6 +203,43 @@ def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: f
     return out
 
 
+def solve_bor_dielectric(points, freq_hz: float, thetas_deg, eps_r, mu_r=1.0,
+                         n_modes: Optional[int] = None, gauss_order: int = 4,
+                         mode_tol: float = 1e-6, workers: int = 1,
+                         progress: Optional[Callable] = None,
+                         check_abort: Optional[Callable] = None) -> Dict:
+    """Monostatic RCS of a closed homogeneous penetrable body by per-mode
+    PMCHWT on the GPU (bor_solver.py:1019-1095): FP64 fills, LU and far field
+    of J and M; lossless media (real eps_r, mu_r > 0) -- lossy ones raise
+    NotImplementedError.  Returns the reference's result dict."""
+    from .penetrable import DielectricBorProblem
+    t_wall = time.perf_counter()
+    if gauss_order != 4:
+        raise NotImplementedError("the GPU kernels are specialised for gauss_order=4")
+    if check_abort is not None:
+        check_abort()
+    thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
+    prob = DielectricBorProblem(points, freq_hz, thetas, eps_r, mu_r, m_max=n_modes)
+    res = prob.sweep(check_abort=check_abort)
+    F, modes_used = replay_truncation(res.dF, mode_tol)
+    if progress is not None:
+        progress(modes_used, prob.m_max)
+    return {
+        "theta_deg": thetas.tolist(),
+        "sigma_vv": (4.0 * math.pi * np.abs(F[0]) ** 2).tolist(),
+        "sigma_hh": (4.0 * math.pi * np.abs(F[1]) ** 2).tolist(),
+        "amp_vv": F[0].tolist(),
+        "amp_hh": F[1].tolist(),
+        "modes_used": int(modes_used),
+        "n_unknowns": int(prob.n),
+        "formulation": "pmchwt",
+        "eps_r": complex(eps_r),
+        "mu_r": complex(mu_r),
+        "linear_residual": float(np.max(res.residual[: modes_used + 1])),
+        "timings": {"wall_s": time.perf_counter() - t_wall, **res.timings},
+    }
+
+
 def solve_bor_pec(points, freq_hz: float, thetas_deg, n_modes: Optional[int] = None,
                   gauss_order: int = 4, mode_tol: float = 1e-6) -> Dict:
     """PEC EFIE entry point (bor_solver.py:1007-1016)."""
@@ -225,15 +262,17 @@ class BorPecSolver:
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,
                  near_depth: int = 4, medium=None, single_tables: bool = False):
-        if medium is not None:
-            raise NotImplementedError("penetrable media (PMCHWT operators) are not on the GPU path")
         if near_depth != 4:
             raise NotImplementedError("the GPU near kernel uses the reference's depth-4 grading")
+        from .penetrable import lossless_medium
+        # medium=(eps_r, mu_r): the operators (T, P, MFIE) in that lossless
+        # medium, i.e. of the same generatrix at the frequency f n; excitation and
+        # far field stay in air (bor_solver.py:175-200)
+        self._n_index, self.eta = (1.0, ETA0) if medium is None else lossless_medium(*medium)
         self.gen = Generatrix(np.asarray(points, dtype=float))
         self.g: GaussData = gauss_on_generatrix(self.gen, gauss_order)
         self.freq_hz = float(freq_hz)
-        self.k = 2.0 * math.pi * self.freq_hz / C0
-        self.eta = ETA0
+        self.k = 2.0 * math.pi * self.freq_hz / C0 * self._n_index
         self.gauss_order = gauss_order
         self.near_depth = near_depth
         self.Nn = self.gen.n_nodes
@@ -252,12 +291,17 @@ class BorPecSolver:
         self._ops: Optional[Tuple[int, object]] = None
         self._mops: Optional[Tuple[int, object]] = None
         self._iops: Optional[Tuple[int, bytes, object]] = None
+        self._pops: Optional[Tuple[int, object]] = None
         self._single = bool(single_tables)
 
     # -- operator cache ----------------------------------------------------
-    def _problem(self, m_max: int, thetas=(0.0,), formulation: str = "efie"):
-        return BorGpuProblem(self._points, self.freq_hz, thetas, m_max=m_max,
-                             gauss_order=self.gauss_order, formulation=formulation)
+    def _problem(self, m_max: int, thetas=(0.0,), formulation: str = "efie", air: bool = False,
+                 zs=None):
+        """The GPU problem of this surface: in its medium (frequency f n), or in
+        air for the excitation and the far field."""
+        f = self.freq_hz if air else self.freq_hz * self._n_index
+        return BorGpuProblem(self._points, f, thetas, m_max=m_max, gauss_order=self.gauss_order,
+                             formulation=formulation, zs=zs)
 
     def enable_streaming(self, m_max: int, efie: bool = True, mfie: bool = False,
                          ibc_zs_pt: Optional[np.ndarray] = None, single_blocks: bool = False,
@@ -276,7 +320,10 @@ class BorPecSolver:
         addition depends on Z_s and is built by assemble_ibc_extra."""
         if efie and (self._ops is None or self._ops[0] < m_max):
             prob = self._problem(m_max)
-            self._ops = (m_max, prob.assemble_modes_fp64())
+            Z = prob.assemble_modes_fp64()
+            if self.eta != ETA0:
+                Z *= self.eta / ETA0            # C = j k eta 2 pi with this medium's eta
+            self._ops = (m_max, Z)
         if mfie and (self._mops is None or self._mops[0] < m_max):
             prob = self._problem(m_max, formulation="mfie")
             self._mops = (m_max, prob.assemble_mfie_modes_fp64())
@@ -329,6 +376,24 @@ class BorPecSolver:
             self._iops = (mm, key, prob.assemble_ibc_modes_fp64())
         return self._mode((self._iops[0], self._iops[2]), m)
 
+    def assemble_pmchwt_P(self, m: int, m_max: int) -> np.ndarray:
+        """The PMCHWT rotated principal-value operator P of mode m in this
+        medium: the unit-weight IBC brackets B without mass term, source columns
+        remapped P = [[-B_tf, B_tt], [-B_ff, B_ft]] (bor_solver.py:554-576)."""
+        mm = max(m_max, abs(m))
+        if self._pops is None or self._pops[0] < mm:
+            prob = self._problem(mm, zs=1.0)
+            st = nat.stream_handle()
+            import torch
+            B = torch.zeros((mm + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
+            prob.fill_far_ibc(B, nat.F64, 1.0 + 0.0j, st)
+            prob.fill_near_ibc(1.0 + 0.0j, st, Z=B, mass=False)
+            prob.check_near_status()
+            self._pops = (mm, B)
+        B = self._mode(self._pops, m)
+        Nn = self.Nn
+        return np.concatenate([-B[:, Nn:], B[:, :Nn]], axis=1)
+
     def basis_mask(self, m: int) -> np.ndarray:
         return _basis_mask(self.gen, m)
 
@@ -345,7 +410,7 @@ class BorPecSolver:
     def _excitation(self, m: int, theta_inc_deg: float, coef_e: float, coef_h: float, h_weight=None):
         import torch
         am = abs(m)
-        prob = self._problem(am, thetas=(float(theta_inc_deg),))
+        prob = self._problem(am, thetas=(float(theta_inc_deg),), air=True)
         prob.d_masks.fill_(-1)
         B = torch.empty((am + 1, prob.n, 2), dtype=torch.complex128, device=prob.device)
         hw = None if h_weight is None else torch.as_tensor(h_weight, dtype=torch.complex128, device=prob.device)
@@ -397,7 +462,7 @@ class BorPecSolver:
         Nn = self.Nn
         d = torch.ones(2 * Nn, dtype=torch.float64, device="cuda")
         d[Nn:] = -1.0
-        c = -1j * self.k * ETA0 / (4.0 * math.pi)
+        c = -1j * (self.k / self._n_index) * ETA0 / (4.0 * math.pi)
         fth = c * complex(torch.sum(d * V[:, 0] * x).cpu())
         fph = -c * complex(torch.sum(d * V[:, 1] * x).cpu())
         return fth, fph

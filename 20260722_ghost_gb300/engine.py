@@ -245,7 +245,7 @@ class BorGpuProblem:
             raise RuntimeError("a bounded tensor-core wait gave up in the far fill")
 
     def fill_far(self, Z, precision: int, scale: complex, stream: int):
-        ld = Z.shape[-1]
+        ld = Z.stride(-2)                  # row stride: Z may be a block of a larger system
         if precision == nat.F32 and self.far_tc:
             ws = self._far_tc_work(stream)
             nat.call("ghost_bor_far_efie_tc", self.N, self.m_max, self.n_xi, self.k, scale.real, scale.imag,
@@ -277,7 +277,7 @@ class BorGpuProblem:
                 raise RuntimeError(f"near kernel scratch too small ({name})")
 
     def fill_near(self, scale: complex, stream: int, band=None, Z=None, precision: int = nat.F64):
-        ld = 0 if Z is None else Z.shape[-1]
+        ld = 0 if Z is None else Z.stride(-2)
         ms = 0 if Z is None else Z.stride(0)
         work, nbytes = self._near_work("ghost_bor_near_workspace")
         nat.call("ghost_bor_near_efie", precision, self.N, self.m_max, self.k, scale.real, scale.imag,
@@ -288,13 +288,13 @@ class BorGpuProblem:
                  self.n_tail_max, nat.ptr(work), nbytes, stream)
 
     def fill_far_mfie(self, Z, precision: int, scale: complex, stream: int):
-        ld = Z.shape[-1]
+        ld = Z.stride(-2)                  # row stride: Z may be a block of a larger system
         nat.call("ghost_bor_far_mfie", precision, self.N, self.m_max, self.n_xi_b, self.k,
                  scale.real, scale.imag, nat.ptr(self.d_geo), nat.ptr(self.d_btab),
                  nat.ptr(self.d_bsin2), nat.ptr(Z), ld, Z.stride(0), stream)
 
     def fill_near_mfie(self, scale: complex, stream: int, band=None, Z=None):
-        ld = 0 if Z is None else Z.shape[-1]
+        ld = 0 if Z is None else Z.stride(-2)
         ms = 0 if Z is None else Z.stride(0)
         work, nbytes = self._near_work("ghost_bor_near_mfie_workspace")
         nat.call("ghost_bor_near_mfie", self.N, self.m_max, self.k, scale.real, scale.imag,
@@ -307,14 +307,21 @@ class BorGpuProblem:
     def fill_far_ibc(self, Z, precision: int, scale: complex, stream: int):
         nat.call("ghost_bor_far_ibc", precision, self.N, self.m_max, self.n_xi_b, self.k,
                  scale.real, scale.imag, nat.ptr(self.d_zs), nat.ptr(self.d_geo), nat.ptr(self.d_btab),
-                 nat.ptr(self.d_bsin2), nat.ptr(Z), Z.shape[-1], Z.stride(0), stream)
+                 nat.ptr(self.d_bsin2), nat.ptr(Z), Z.stride(-2), Z.stride(0), stream)
 
-    def fill_near_ibc(self, scale: complex, stream: int, band=None, Z=None):
-        ld = 0 if Z is None else Z.shape[-1]
+    def fill_near_ibc(self, scale: complex, stream: int, band=None, Z=None, mass: bool = True):
+        """Near IBC part Z_s (M/2 + B); mass=False leaves the mass term out (the
+        bare brackets B, as the PMCHWT operator P takes them)."""
+        ld = 0 if Z is None else Z.stride(-2)
         ms = 0 if Z is None else Z.stride(0)
         work, nbytes = self._near_work("ghost_bor_near_mfie_workspace")
+        emass = self.d_emass
+        if not mass:
+            if getattr(self, "_zero_emass", None) is None:
+                self._zero_emass = self.torch.zeros_like(self.d_emass)
+            emass = self._zero_emass
         nat.call("ghost_bor_near_ibc", self.N, self.m_max, self.k, scale.real, scale.imag,
-                 nat.ptr(self.d_zs), nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(self.d_emass),
+                 nat.ptr(self.d_zs), nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(emass),
                  len(self.near.pairs), nat.ptr(self.d_pairs), nat.ptr(self.d_tails),
                  nat.ptr(self.d_cells), self.near.cells.shape[1], nat.ptr(self.d_core),
                  nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,

@@ -7,100 +7,20 @@ the real call -- and each formulation calls its own entry points.  Device
 tensors are CPU tensors here and the entry points do nothing, so no number is
 checked: the numerics are the GPU tests' business.
 """
-import ctypes
 import importlib
 
 import numpy as np
 import pytest
 import torch
 
+import mock_device
 from conftest import load_golden
-
-_REAL_DEVICE = torch.device
-
-
-def _cpu(d):
-    return "cpu" if d is not None and str(d).startswith("cuda") else d
-
-
-class _Event:
-    def __init__(self, *a, **k):
-        pass
-
-    def record(self, *a, **k):
-        pass
-
-    def elapsed_time(self, other):
-        return 1.0
-
-
-class _Stream:
-    cuda_stream = 0
-
 
 @pytest.fixture
 def calls(monkeypatch, pkg):
-    """Route torch's CUDA allocations to zero-filled CPU tensors, fake the
-    CUDA events and streams, and record the entry points called."""
-    zero_for = {"empty": torch.zeros, "empty_like": torch.zeros_like}
-    for name in ("zeros", "ones", "as_tensor", "tensor", "full", "arange", "zeros_like", "empty",
-                 "empty_like"):
-        fn = zero_for.get(name, getattr(torch, name))
-
-        def wrapped(*a, _fn=fn, **k):
-            if "device" in k:
-                k["device"] = _cpu(k["device"])
-            return _fn(*a, **k)
-        monkeypatch.setattr(torch, name, wrapped)
-    to = torch.Tensor.to
-
-    def tensor_to(self, *a, **k):
-        a = tuple(_cpu(x) if isinstance(x, (str, _REAL_DEVICE)) else x for x in a)
-        if "device" in k:
-            k["device"] = _cpu(k["device"])
-        return to(self, *a, **k)
-    monkeypatch.setattr(torch.Tensor, "to", tensor_to)
-    for name, val in (("is_available", lambda: True), ("mem_get_info", lambda *a: (1 << 40, 1 << 40)),
-                      ("memory_reserved", lambda *a: 0), ("memory_allocated", lambda *a: 0),
-                      ("Event", _Event), ("synchronize", lambda *a: None),
-                      ("current_stream", lambda *a: _Stream())):
-        monkeypatch.setattr(torch.cuda, name, val)
-
-    nat, eng = pkg._native, pkg.engine
-
-    class TorchOnCpu:
-        def __getattr__(self, n):
-            return getattr(torch, n)
-
-        def device(self, d=None, *a):
-            return _REAL_DEVICE(_cpu(d) if d is not None else "cpu", *a)
-
-    monkeypatch.setattr(eng, "_torch", lambda: TorchOnCpu())
-    log = []
-    protos = {}
-    for name, (res, args) in nat.SIGNATURES.items():
-        if res in (ctypes.c_int, ctypes.c_longlong):
-            ret = (1 << 20) if res is ctypes.c_longlong else 0
-            protos[name] = ctypes.CFUNCTYPE(res, *args)(lambda *a, _r=ret: _r)
-
-    class Lib:
-        def __getattr__(self, name):
-            fn = protos[name]
-
-            def g(*a):
-                log.append(name)
-                return fn(*a)
-            return g
-
-    def call(name, *args):
-        res, argt = nat.SIGNATURES[name]
-        assert len(args) == len(argt), (name, len(args), len(argt))
-        log.append(name)
-        return protos[name](*args)
-
-    monkeypatch.setattr(nat, "load", lambda *a, **k: Lib())
-    monkeypatch.setattr(nat, "call", call)
-    return log
+    """CPU tensors for device memory, fake events and streams, and the entry
+    points called (tests/mock_device.py)."""
+    return mock_device.install(monkeypatch, pkg)
 
 
 IBC_CALLS = {"ghost_bor_far_ibc", "ghost_bor_near_ibc", "ghost_bor_rhs_weighted"}

@@ -1,4 +1,5 @@
-"""Surface impedance (IBC-EFIE) on the GPU against the reference.
+"""Surface impedance (IBC-EFIE) and lossless penetrable bodies (PMCHWT) on
+the GPU against the reference.
 
 tests/golden/ibc_conesphere_n40.npz holds the reference's own FP64 results
 (tests/golden/make_ibc_golden.py): the per-mode IBC operator additions
@@ -10,6 +11,12 @@ amplitude and the FP32 + refinement solve to 1e-4 and 0.01 dB.  The far
 bracket blocks and the far field with the eliminated magnetic current are
 checked against the oracle, the lossless-Z_s resonance monitor against the
 oracle's condition numbers, and impedance spheres against the Mie series.
+
+tests/golden/pmchwt_sphere_n24.npz holds the reference's exterior PMCHWT
+operator P and its solve_bor_dielectric amplitudes; the GPU dielectric path
+(lossless media: every block from the fills above) must give P to 1e-11 and
+the eps_r = 4 solve to 1e-10, the operators in a medium must equal the
+oracle's, and a dielectric sphere must match the Mie series.
 """
 
 import numpy as np
@@ -162,3 +169,59 @@ def test_impedance_sphere_matches_mie(pkg, a, f, zs):
         err = float(np.max(np.abs(10 * np.log10(s / want))))
         print(f"\n{precision}: {err:.4f} dB")
         assert err < 0.01, (precision, err)
+
+
+# ---------------------------------------------------------------------------
+# lossless penetrable bodies (PMCHWT)
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def P24():
+    return load_golden("pmchwt_sphere_n24")
+
+
+def test_pmchwt_P_matches_reference(pkg, P24):
+    """The exterior rotated principal-value operator (unit-weight IBC brackets
+    without mass term, columns remapped) of modes 0 and 2."""
+    s = pkg.bor_solver.BorPecSolver(P24["points"], float(P24["freq_hz"]))
+    M = int(P24["m_max"])
+    for m in P24["modes"]:
+        err = rel(s.assemble_pmchwt_P(int(m), M), P24[f"Pe_{int(m)}"])
+        print(f"\nP_e mode {int(m)}: {err:.2e}")
+        assert err < 1e-11, (int(m), err)
+
+
+def test_operators_in_a_medium_match_oracle(pkg, oracle, P24):
+    """T and P of a lossless medium (eps_r = 4): the generatrix at f n with the
+    medium's eta, vs the oracle's complex-medium solver."""
+    M = int(P24["m_max"])
+    s = pkg.bor_solver.BorPecSolver(P24["points"], float(P24["freq_hz"]), medium=(4.0, 1.0))
+    o = oracle.OracleSolver(P24["points"], float(P24["freq_hz"]), medium=(4.0, 1.0))
+    o.prepare(M, efie=True, workers=4, ibc_zs_pt=np.ones(o.geo.P))
+    for m in (0, 2, -3):
+        assert rel(s.assemble_mode(m, M), o.assemble_efie(m, M)) < 1e-11, m
+        assert rel(s.assemble_pmchwt_P(m, M), o.pmchwt_P(m, M)) < 1e-11, m
+
+
+def test_dielectric_solve_matches_reference(pkg, P24):
+    r = pkg.bor_solver.solve_bor_dielectric(P24["points"], float(P24["freq_hz"]), P24["thetas"], 4.0, 1.0,
+                                            n_modes=int(P24["m_max"]), mode_tol=0.0)
+    for pol in ("vv", "hh"):
+        a, b = r[f"amp_{pol}"], P24[f"amp_{pol}_1"]
+        print(f"\n{pol}: rel {rel(a, b):.2e}, dB {db_err(a, b):.2e}")
+        assert rel(a, b) < 1e-10
+    assert r["linear_residual"] < 1e-10
+
+
+def test_dielectric_sphere_matches_mie(pkg):
+    """A 60-segment eps_r = 2.5 sphere, ka = pi: the oracle's own error against
+    the Mie series is 0.0085 dB at this mesh."""
+    from oracle import mie
+    a, f, eps = 0.5, 3e8, 2.5
+    r = pkg.bor_solver.solve_bor_dielectric(pkg.bodies.sphere_generatrix(a, 60), f, [0.0, 60.0, 120.0],
+                                            eps, 1.0, mode_tol=0.0)
+    want = mie.sigma_dielectric_sphere(a, eps, 1.0, f)
+    s = np.array(r["sigma_vv"] + r["sigma_hh"])
+    err = float(np.max(np.abs(10 * np.log10(s / want))))
+    print(f"\n{err:.4f} dB")
+    assert err < 0.02
