@@ -14,14 +14,14 @@ frequency is then solved on the GPU by ``bor_solver.solve_bor``.  Several
 frequencies go through ``bor_solver.solve_bor_batch``, which builds the next
 frequency's problem on a host thread while the GPU sweeps the current one.
 
-Scope: bodies whose segments are all TYPE 2 conductors: PEC (CFIE, or EFIE
+Scope: bodies whose segments are all TYPE 2 conductors -- PEC (CFIE, or EFIE
 when cfie_alpha <= 0) and conductors with surface-impedance (IBC) flags,
 whose Z_s per element comes from the snapshot's material tables
-(materials.MaterialLibrary) and which are solved with the IBC-EFIE.  The
-penetrable kinds (TYPE 3 dielectric, TYPE 3+4 coated, TYPE 2+3+4 partial
-coating, TYPE 3+4+5 layered) are recognised and rejected with
-NotImplementedError; malformed snapshots and material tables raise as in the
-reference.
+(materials.MaterialLibrary) and which are solved with the IBC-EFIE -- and
+homogeneous TYPE 3 dielectric bodies (PMCHWT, lossless media on the GPU).
+The multi-region kinds (TYPE 3+4 coated, TYPE 2+3+4 partial coating, TYPE
+3+4+5 layered) are recognised and rejected with NotImplementedError;
+malformed snapshots and material tables raise as in the reference.
 """
 
 from __future__ import annotations
@@ -35,7 +35,7 @@ from typing import Any, Callable, Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
-from .bor_solver import solve_bor, solve_bor_batch
+from .bor_solver import solve_bor, solve_bor_batch, solve_bor_dielectric
 from .geometry import C0
 from .materials import MaterialLibrary
 
@@ -43,7 +43,6 @@ DEFAULT_ELEMENTS_PER_WAVELENGTH = 20
 MAX_ELEMENTS_DEFAULT = 50_000
 
 _NOT_ON_GPU = {
-    "dielectric": "homogeneous dielectric bodies (PMCHWT)",
     "coated": "coated PEC bodies (multi-region PMCHWT)",
     "partial": "partially coated PEC bodies (PMCHWT with junctions)",
     "layered": "layered coated PEC bodies (PMCHWT)",
@@ -290,17 +289,29 @@ def mesh_generatrix(run: Sequence[Chain], lam: float, max_elements: int,
     return pts, np.concatenate(seg_of), np.concatenate(arc_of)
 
 
+def causal_index(eps_r: complex, mu_r: complex) -> complex:
+    """Refractive index sqrt(eps_r mu_r) on the causal branch (Im <= 0, then
+    Re >= 0), as the reference picks it (bor_solver.py:161-172)."""
+    m = complex(np.sqrt(complex(eps_r) * complex(mu_r)))
+    if m.imag > 0.0:
+        m = -m
+    if m.real < 0.0:
+        m = -m
+    return m
+
+
 def prepare_snapshot(snapshot: Dict[str, Any], geometry_units: str = "inches"):
     """Parse, classify and check a snapshot.  Returns (kind, run, axis_tol)
-    for a conductor body; other kinds raise NotImplementedError."""
+    for a conductor or a homogeneous dielectric body; other kinds raise
+    NotImplementedError."""
     chains = chains_from_snapshot(snapshot, _meters_per_unit(geometry_units))
     kind = classify(chains)
-    if kind != "conductor":
+    if kind not in ("conductor", "dielectric"):
         raise NotImplementedError(f"{_NOT_ON_GPU[kind]} are not on the GPU path; "
-                                  "only PEC (TYPE 2) bodies are.")
+                                  "conductors (TYPE 2) and homogeneous dielectric bodies (TYPE 3) are.")
     extent = np.ptp(np.vstack([c.pts for c in chains]), axis=0).max()
     diag = max(float(extent), 1e-9)
-    run = generatrix_run(chains, "TYPE 2", max(1e-12, 1e-9 * diag))
+    run = generatrix_run(chains, "TYPE 2" if kind == "conductor" else "TYPE 3", max(1e-12, 1e-9 * diag))
     axis_tol = 1e-6 * diag
     preflight(run, "body", axis_tol)
     return kind, run, axis_tol
@@ -418,6 +429,28 @@ def solve_monostatic_rcs_bor(
 
     common = dict(formulation=form, cfie_alpha=cfie_alpha, mode_tol=mode_tol,
                   table_precision=table_precision)
+    if kind == "dielectric":
+        # one PMCHWT solve per frequency, meshed for the wavelength inside the
+        # medium (bor_dispatch.py:540-549)
+        outs = []
+        for fi, f in enumerate(freqs):
+            check_abort()
+            eps, mu = materials.get_medium(run[0].pos_mat, f)
+            ghz = float(mesh_reference_ghz) if mesh_reference_ghz else f
+            lam = C0 / (ghz * 1e9) / max(1.0, abs(causal_index(eps, mu)))
+            pts = mesh_generatrix(run, lam, max_elements, axis_tol)[0]
+
+            def report(done, cap, fi=fi, f=f):
+                notify(fi, f"{f:g} GHz: mode {done}/{cap}")
+
+            out = solve_bor_dielectric(pts, f * 1e9, aspects, eps, mu, n_modes=n_modes, mode_tol=mode_tol,
+                                       workers=workers, progress=report, check_abort=check_abort)
+            for w in out.get("warnings", []) or []:
+                materials.warn_once(str(w))
+            outs.append(out)
+            notify(fi + 1, f"Solved {f:g} GHz")
+        return _sweep_result(freqs, outs, aspects, pol, kind, "BoR-MoM PMCHWT (homogeneous dielectric)",
+                             cfie_alpha, workers, materials, expand_to_360, warnings_done=True)
     if any(c.ibc_flag > 0 for c in run):
         # impedance flags: Z_s per element at each frequency (material warnings
         # in the reference's order), one IBC-EFIE solve per frequency

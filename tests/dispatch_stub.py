@@ -57,6 +57,22 @@ class Recorder:
             "linear_residual": 1e-13 * n, "warnings": warnings,
         }
 
+    def dielectric(self, points, freq_hz, thetas_deg, eps_r, mu_r=1.0, n_modes=None, mode_tol=1e-6,
+                   **_kw):
+        """Stand-in for solve_bor_dielectric: logged with the medium, the same
+        smooth amplitude model scaled by the medium."""
+        out = self(points, freq_hz, thetas_deg, formulation="pmchwt", n_modes=n_modes, mode_tol=mode_tol)
+        call = self.calls[-1]
+        call["eps_r"] = [complex(eps_r).real, complex(eps_r).imag]
+        call["mu_r"] = [complex(mu_r).real, complex(mu_r).imag]
+        g = abs(complex(eps_r) * complex(mu_r)) ** 0.25
+        for key in ("amp_vv", "amp_hh"):
+            out[key] = [a * g for a in out[key]]
+        for key, amp in (("sigma_vv", "amp_vv"), ("sigma_hh", "amp_hh")):
+            out[key] = [4.0 * math.pi * abs(a) ** 2 for a in out[amp]]
+        out["n_unknowns"] = 2 * out["n_unknowns"]
+        return out
+
     def batch(self, bodies, thetas_deg, formulation="efie", cfie_alpha=0.5, mode_tol=1e-6,
               table_precision="auto", progress=None):
         """Stand-in for solve_bor_batch: one call per body, in order."""
@@ -131,9 +147,17 @@ def snapshots():
     sphere_unknown = {"segments": [segment("sphere", arc(6.0, 0.0, 0.0, 180.0, 12),
                                            ["2", "0", "7", "0", "0"])],
                       "ibcs": [["6", "constant", "10", "0", "0", "0"]]}
+    # homogeneous dielectric bodies (TYPE 3): an inline lossless medium, and a
+    # frequency table of eps and mu (tests/golden/materials/mat.53)
+    diel = {"segments": [segment("d1", arc(6.0, 0.0, 0.0, 90.0, 6), ["3", "0", "0", "3", "0"]),
+                         segment("d2", arc(6.0, 0.0, 90.0, 180.0, 6), ["3", "-10", "0", "3", "0"])],
+            "dielectrics": [["3", "4.0", "0", "1.0", "0"]]}
+    diel_table = {"segments": [segment("d", arc(0.15, 0.0, 0.0, 180.0, 9), ["3", "0", "0", "mat.53"])],
+                  "dielectrics": [["53"]]}
     return {"sphere_in": sphere, "cone_sphere_m": cone_sphere, "ogive_in": ogive,
             "cone_sphere_ibc_m": cone_ibc, "sphere_ibc_in": sphere_ibc,
-            "sphere_unknown_flag_in": sphere_unknown}
+            "sphere_unknown_flag_in": sphere_unknown, "dielectric_sphere_in": diel,
+            "dielectric_table_m": diel_table}
 
 
 def cases():
@@ -165,6 +189,15 @@ def cases():
         ("sphere_unknown_impedance_flag", "sphere_unknown_flag_in",
          dict(frequencies_ghz=[1.5, 2.0], elevations_deg=[0.0, 90.0], polarization="VV",
               cfie_alpha=0.4)),
+        ("dielectric_sphere", "dielectric_sphere_in",
+         dict(frequencies_ghz=[1.0, 1.8], elevations_deg=[0.0, 45.0, 90.0], polarization="HH",
+              n_modes=7, mode_tol=0.0)),
+        ("dielectric_table", "dielectric_table_m",
+         dict(frequencies_ghz=[0.5, 1.5, 2.5, 3.5], elevations_deg=[10.0, 170.0], polarization="VV",
+              geometry_units="meters", material_base_dir=MATERIALS, expand_to_360=True)),
+        ("dielectric_mesh_reference", "dielectric_sphere_in",
+         dict(frequencies_ghz=[1.0, 2.0], elevations_deg=[30.0], polarization="VV",
+              mesh_reference_ghz=1.5)),
     ]
 
 

@@ -44,10 +44,12 @@ def main():
     for name, snap, kw in stub.cases():
         rec = stub.Recorder()
         rd.solve_bor = rec
+        rd.solve_bor_dielectric = rec.dielectric
         res = rd.solve_monostatic_rcs_bor(geometry_snapshot=snaps[snap], **kw)
         out["cases"][name] = {"calls": rec.calls, "result": res}
     for name, snap, kw in stub.bad_inputs():
         rd.solve_bor = stub.Recorder()
+        rd.solve_bor_dielectric = rd.solve_bor.dielectric
         try:
             rd.solve_monostatic_rcs_bor(geometry_snapshot=snap, **kw)
             out["errors"][name] = None

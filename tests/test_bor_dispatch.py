@@ -32,6 +32,7 @@ def rec(monkeypatch):
     r = stub.Recorder()
     monkeypatch.setattr(D, "solve_bor", r)
     monkeypatch.setattr(D, "solve_bor_batch", r.batch)
+    monkeypatch.setattr(D, "solve_bor_dielectric", r.dielectric)
     return r
 
 
@@ -72,14 +73,16 @@ def test_bad_inputs_raise_like_reference(fx, rec, name):
 
 
 def test_kinds_off_the_gpu_path_are_named(rec):
-    """Valid dielectric bodies raise NotImplementedError; a conductor with an
+    """Valid coated bodies raise NotImplementedError; a conductor with an
     impedance flag goes to the solver (an IBC-EFIE when the flag has a model)."""
     arc = stub.arc(0.2, 0.0, 0.0, 180.0, 8)
+    core = stub.arc(0.1, 0.0, 0.0, 180.0, 6)
     kw = dict(frequencies_ghz=[1.0], elevations_deg=[0.0], polarization="VV",
               geometry_units="meters")
-    diel = {"segments": [stub.segment("d", arc, ["3", "0", "0", "1"])]}
-    with pytest.raises(NotImplementedError, match="dielectric"):
-        D.solve_monostatic_rcs_bor(diel, **kw)
+    coated = {"segments": [stub.segment("o", arc, ["3", "0", "0", "1"]),
+                           stub.segment("c", core, ["4", "0", "0", "1"])]}
+    with pytest.raises(NotImplementedError, match="coated"):
+        D.solve_monostatic_rcs_bor(coated, **kw)
     assert not rec.calls
     ibc = {"segments": [stub.segment("c", arc[:5], ["2", "0", "1"]),
                         stub.segment("c2", arc[4:], ["2"])],
