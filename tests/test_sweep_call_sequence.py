@@ -105,3 +105,20 @@ def test_batched_sweep_and_adjoint_calls(pkg, calls):
     J.backward()
     assert r.grad is not None and r.grad.shape == (12,)
     assert "ghost_bor_far_efie_masked" in calls or "ghost_bor_far_efie_tc_masked" in calls
+
+
+def test_dielectric_solve_calls(pkg, calls):
+    """solve_bor_dielectric: the EFIE fills of both media into the diagonal
+    blocks of the 4 Nn systems (row stride 4 Nn), the bracket fills without
+    mass term, one excitation, the FP64 LU and two far-field calls."""
+    D = load_golden("pmchwt_sphere_n24")
+    r = pkg.bor_solver.solve_bor_dielectric(D["points"], float(D["freq_hz"]), D["thetas"][:3], 4.0, 1.0,
+                                            n_modes=3, mode_tol=0.0)
+    assert r["n_unknowns"] == 4 * len(D["points"])
+    used = [c for c in calls if not c.endswith("_workspace")]
+    assert used.count("ghost_bor_far_efie_masked") == 4 and used.count("ghost_bor_near_efie") == 4
+    assert used.count("ghost_bor_far_ibc") == 2 and used.count("ghost_bor_near_ibc") == 2
+    assert used.count("ghost_bor_farfield") == 2 and used.count("ghost_bor_rhs") == 1
+    assert {"ghost_bor_getrf", "ghost_bor_getrs", "ghost_bor_residual64"} <= set(used)
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]), medium=(4.0, 1.0))
+    assert s.assemble_mode(1, 3).shape == s.assemble_pmchwt_P(-1, 3).shape == (2 * s.Nn, 2 * s.Nn)
