@@ -1,5 +1,5 @@
-"""Drop-in replacement for the reference module ``bor_solver`` (PEC and
-surface-impedance bodies).
+"""Drop-in replacement for the reference module ``bor_solver`` (PEC,
+surface-impedance and homogeneous lossless dielectric bodies).
 
 Same entry points, keyword arguments and result keys as the reference
 (bor_solver.py:820-1004 ``solve_bor``, :1007 ``solve_bor_pec``, :175-708
@@ -254,10 +254,12 @@ class BorPecSolver:
     returned per mode as complex128 NumPy arrays for compatibility; mode -m is
     D Z(m) D for both operators.  The EFIE and MFIE operators, the mass
     blocks, the plane-wave excitations (E and H), the surface-impedance
-    (IBC) operator addition and the far field with the impedance surface's
-    magnetic current are provided; the PMCHWT operators raise
-    NotImplementedError.  Z_s is per element (constant on each element, as
-    solve_bor builds it).
+    (IBC) operator addition, the far field with the impedance surface's
+    magnetic current and the PMCHWT operator P are provided.  Z_s is per
+    element (constant on each element, as solve_bor builds it).  With
+    medium=(eps_r, mu_r) the operators are those of that medium (lossless
+    media; complex ones raise NotImplementedError), the excitation and the
+    far field stay in air.
     """
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,

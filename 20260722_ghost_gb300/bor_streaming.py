@@ -52,7 +52,9 @@ class StreamingFarBlocks:
         self.mode_block = self.m_max + 1
         self.n_sweeps = 1
         self.lo, self.hi = 0, self.m_max
-        prob = BorGpuProblem(solver._points, solver.freq_hz, (0.0,), m_max=self.m_max,
+        # the operators of the solver's medium: its generatrix at f n
+        f = solver.freq_hz * getattr(solver, "_n_index", 1.0)
+        prob = BorGpuProblem(solver._points, f, (0.0,), m_max=self.m_max,
                              gauss_order=solver.gauss_order, formulation="mfie" if mfie else "efie")
         single = np.dtype(dtype) == np.complex64
         prec = nat.F32 if single else nat.F64
@@ -62,7 +64,7 @@ class StreamingFarBlocks:
             ze = solver._zs_elem(ibc_zs_pt)
             B = torch.zeros((self.m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
             if np.any(ze != 0.0):
-                bprob = BorGpuProblem(solver._points, solver.freq_hz, (0.0,), m_max=self.m_max,
+                bprob = BorGpuProblem(solver._points, f, (0.0,), m_max=self.m_max,
                                       gauss_order=solver.gauss_order, zs=ze)
                 bprob.fill_far_ibc(B, prec, 1.0 + 0.0j, nat.stream_handle())
             self.B = B
