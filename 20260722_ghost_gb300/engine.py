@@ -332,7 +332,11 @@ class BorGpuProblem:
         if self.alpha > 0.0:
             self.fill_far(Z, precision, self.alpha * self.C, stream)
         if self.ibc:
-            self.fill_far_ibc(Z, precision, complex(self.alpha), stream)
+            # FP64 in both precisions: the refinement converges to the operator it
+            # is given, and the IBC-EFIE of a closed body is far less well
+            # conditioned than the CFIE, so the FP32 bracket transform's ~1e-6
+            # would remain in the solution
+            self.fill_far_ibc(Z, nat.F64, complex(self.alpha), stream)
         if self.alpha < 1.0:
             self.fill_far_mfie(Z, precision, complex((1.0 - self.alpha) * ETA0), stream)
 
