@@ -360,45 +360,67 @@ class NearTables:
     n_tail: np.ndarray = field(default=None)
 
 
+_NEAR_CELLS: Dict[int, tuple] = {}
+
+
+def _near_cells(gorder: int = 4):
+    """Cell points of the three near kinds, once per process: {kind: (offset,
+    count, s, s')} and the concatenated [3, n_cells_total] table."""
+    if gorder not in _NEAR_CELLS:
+        kinds = {}
+        off = 0
+        blocks = []
+        for kind in _NEAR_KINDS:
+            s, sp_, w = cell_points(kind, gorder)
+            kinds[kind] = (off, len(s), s, sp_)
+            blocks.append(np.stack([s, sp_, w]))
+            off += len(s)
+        _NEAR_CELLS[gorder] = (kinds, np.ascontiguousarray(np.concatenate(blocks, axis=1)))
+    return _NEAR_CELLS[gorder]
+
+
 def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> NearTables:
     """Element pairs |e - f| <= 1, their cell sets and the tail Gauss order
     n_tail = clip(ceil(4 (max|k| a / pi + m_max + 2)), 64, 1024) with
     a = sqrt(4 rho rho') over the pair's non-axis point pairs, bit-identical to
-    the reference's choice (bor_kernels.py:199-204, 238-240)."""
+    the reference's choice (bor_kernels.py:199-204, 238-240).  The maximum is
+    taken over 4 rho rho' before the (monotone, correctly rounded) square root
+    and scaling, which gives the same value with one pass less per point."""
     ne = gen.n_elems
-    kinds = {}
-    off = 0
-    blocks = []
-    for kind in _NEAR_KINDS:
-        s, sp_, w = cell_points(kind)
-        kinds[kind] = (off, len(s), s, sp_)
-        blocks.append(np.stack([s, sp_, w]))
-        off += len(s)
-    cells = np.ascontiguousarray(np.concatenate(blocks, axis=1))
-    pairs = []
-    ntails = []
-    x0 = gen.nodes[:-1]
-    x1 = gen.nodes[1:]
+    kinds, cells = _near_cells()
+    cells = cells.copy()
+    kabs = abs(complex(k))
+    x0 = gen.nodes[:-1, 0]
+    dx = gen.nodes[1:, 0] - x0
+    cols = []
+    ntl = []
     for kind, df in (("diag", 0), ("corner10", 1), ("corner01", -1)):
         e = np.arange(max(0, -df), ne - max(0, df))
         f = e + df
         coff, cnt, s, sp_ = kinds[kind]
-        rho_p = x0[e, 0][:, None] + s[None, :] * (x1[e, 0] - x0[e, 0])[:, None]
-        rho_q = x0[f, 0][:, None] + sp_[None, :] * (x1[f, 0] - x0[f, 0])[:, None]
-        rr4 = 4.0 * rho_p * rho_q
-        a = np.sqrt(np.where(rr4 > 1e-30, rr4, 0.0))
-        osc = np.max(abs(complex(k)) * a, axis=1) / math.pi + (m_max + 2)
+        mx = np.empty(len(e))
+        # row blocks small enough to stay in cache
+        for r0 in range(0, len(e), 64):
+            eb, fb = e[r0:r0 + 64], f[r0:r0 + 64]
+            rr4 = np.multiply.outer(dx[eb], s)
+            rr4 += x0[eb][:, None]                  # rho on the test element
+            rq = np.multiply.outer(dx[fb], sp_)
+            rq += x0[fb][:, None]                   # rho' on the source element
+            rr4 *= 4.0
+            rr4 *= rq
+            mx[r0:r0 + 64] = rr4.max(axis=1)
+        on = mx > 1e-30                             # some point pair off the axis
+        osc = kabs * np.sqrt(np.where(on, mx, 0.0)) / math.pi + (m_max + 2)
         nt = np.minimum(1024, np.maximum(64, np.ceil(4.0 * osc))).astype(np.int64)
-        nt[~np.any(rr4 > 1e-30, axis=1)] = 0
-        for i in range(len(e)):
-            pairs.append((int(e[i]), int(f[i]), coff, cnt))
-            ntails.append(int(nt[i]))
-    pairs = np.asarray(pairs, dtype=np.int32)
-    ntails = np.asarray(ntails, dtype=np.int64)
+        nt[~on] = 0
+        cols.append(np.stack([e, f, np.full(len(e), coff), np.full(len(e), cnt)], axis=1))
+        ntl.append(nt)
+    pairs = np.concatenate(cols).astype(np.int32)
+    ntails = np.concatenate(ntl)
     order = np.lexsort((pairs[:, 1], pairs[:, 0]))
     pairs = pairs[order]
     ntails = ntails[order]
-    uniq = sorted(set(int(n) for n in ntails if n > 0))
+    uniq = [int(n) for n in np.unique(ntails[ntails > 0])]
     tab_u, tab_w, offs = [], [], {}
     o = 0
     for n in uniq:
@@ -418,7 +440,14 @@ def near_tables(gen: Generatrix, k: float, m_max: int, core_order: int = 48) -> 
                                                  np.cos(0.5 * xi)]))
     else:
         tail_gl = np.zeros((4, 1))
-    tails = np.asarray([(offs.get(int(n), 0), int(n)) for n in ntails], dtype=np.int32)
+    if uniq:
+        u_arr = np.asarray(uniq, dtype=np.int64)
+        o_arr = np.asarray([offs[n] for n in uniq], dtype=np.int64)
+        pos = np.minimum(np.searchsorted(u_arr, ntails), len(uniq) - 1)
+        toff = np.where(ntails > 0, o_arr[pos], 0)
+    else:
+        toff = np.zeros(len(ntails), dtype=np.int64)
+    tails = np.stack([toff, ntails], axis=1).astype(np.int32)
     xc, wc = _leggauss(core_order)
     core_gl = np.ascontiguousarray(np.stack([0.5 * (xc + 1.0), 0.5 * wc]))
     return NearTables(pairs=np.ascontiguousarray(pairs), tails=np.ascontiguousarray(tails),
