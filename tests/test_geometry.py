@@ -207,3 +207,35 @@ def test_bspline_body_definition(pkg):
     assert pts[0, 1] == pytest.approx(1.0) and pts[-1, 1] == pytest.approx(-1.0)
     assert np.all(np.diff(pts[:, 1]) < 0)
     assert np.all(pts[1:-1, 0] > 0.0) and pts[:, 0].max() <= radii.max() + 1e-12
+
+
+def test_near_tail_orders_equal_the_pointwise_rule(pkg):
+    """The tail order of every near pair (row maxima of 4 rho rho' taken
+    before the square root, in row blocks) equals the pointwise rule
+    clip(ceil(4 (max_points |k| sqrt(4 rho rho') / pi + m_max + 2)), 64, 1024),
+    points with 4 rho rho' <= 1e-30 left out and 0 for pairs wholly on the
+    axis, exactly; the pairs come sorted by (e, f)."""
+    import math
+    geom = pkg.geometry
+    rng = np.random.default_rng(5)
+    for trial in range(4):
+        N = int(rng.integers(8, 300))
+        t = np.linspace(0.0, 1.0, N + 1)
+        rho = rng.uniform(0.2, 0.6) * np.sin(np.pi * t) * (1 + 0.1 * np.sin(5 * np.pi * t))
+        gen = geom.Generatrix(np.stack([rho, 1.3 * (0.5 - t)], axis=1))
+        k, M = float(rng.uniform(3, 90)), int(rng.integers(2, 60))
+        nt = geom.near_tables(gen, k, M)
+        x0, x1 = gen.nodes[:-1], gen.nodes[1:]
+        cells = nt.cells
+        for (e, f, coff, cnt), (toff, n) in zip(nt.pairs, nt.tails):
+            s, sp = cells[0, coff:coff + cnt], cells[1, coff:coff + cnt]
+            rp = x0[e, 0] + s * (x1[e, 0] - x0[e, 0])
+            rq = x0[f, 0] + sp * (x1[f, 0] - x0[f, 0])
+            rr4 = 4.0 * rp * rq
+            if not np.any(rr4 > 1e-30):
+                assert n == 0
+                continue
+            osc = np.max(k * np.sqrt(np.where(rr4 > 1e-30, rr4, 0.0))) / math.pi + (M + 2)
+            assert n == min(1024, max(64, math.ceil(4.0 * osc))), (e, f)
+            assert np.array_equal(nt.tail_gl[0, toff:toff + n], 0.5 * (geom._leggauss(n)[0] + 1.0))
+        assert np.all(np.diff(nt.pairs[:, 0] * 4 + nt.pairs[:, 1] - nt.pairs[:, 0]) > 0)
