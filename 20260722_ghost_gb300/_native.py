@@ -46,6 +46,12 @@ SIGNATURES = {
     "ghost_bor_far_ibc": (_i, [_i, _i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
     "ghost_bor_near_ibc": (_i, [_i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i,
                                 _vp, _vp, _i, _vp, _vp, _ll, _ll, _i, _vp, _ll, _vp]),
+    "ghost_bor_far_efie_ck": (_i, [_i, _i, _i, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
+    "ghost_bor_near_efie_ck": (_i, [_i, _i, _d, _d, _d, _d, _vp, _vp, _i, _vp, _vp, _vp, _i,
+                                    _vp, _vp, _i, _vp, _vp, _ll, _ll, _i, _vp, _ll, _vp]),
+    "ghost_bor_far_ibc_ck": (_i, [_i, _i, _i, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp]),
+    "ghost_bor_near_ibc_ck": (_i, [_i, _i, _d, _d, _d, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _i,
+                                   _vp, _vp, _i, _vp, _vp, _ll, _ll, _i, _vp, _ll, _vp]),
     "ghost_bor_rhs_workspace": (_ll, [_i, _i, _i]),
     "ghost_bor_rhs": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp]),
     "ghost_bor_rhs_weighted": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _vp, _vp, _ll, _ll, _vp, _vp]),

@@ -210,8 +210,9 @@ def solve_bor_dielectric(points, freq_hz: float, thetas_deg, eps_r, mu_r=1.0,
                          check_abort: Optional[Callable] = None) -> Dict:
     """Monostatic RCS of a closed homogeneous penetrable body by per-mode
     PMCHWT on the GPU (bor_solver.py:1019-1095): FP64 fills, LU and far field
-    of J and M; lossless media (real eps_r, mu_r > 0) -- lossy ones raise
-    NotImplementedError.  Returns the reference's result dict."""
+    of J and M; lossless media take the real-k fills, lossy ones the
+    complex-k fills (a purely imaginary index raises NotImplementedError).
+    Returns the reference's result dict."""
     from .penetrable import DielectricBorProblem
     t_wall = time.perf_counter()
     if gauss_order != 4:
@@ -257,24 +258,34 @@ class BorPecSolver:
     (IBC) operator addition, the far field with the impedance surface's
     magnetic current and the PMCHWT operator P are provided.  Z_s is per
     element (constant on each element, as solve_bor builds it).  With
-    medium=(eps_r, mu_r) the operators are those of that medium (lossless
-    media; complex ones raise NotImplementedError), the excitation and the
-    far field stay in air.
+    medium=(eps_r, mu_r) the operators T and P are those of that medium (a
+    lossy medium's through the complex-wave-number fills; its MFIE operator
+    raises NotImplementedError), the excitation and the far field stay in
+    air.
     """
 
     def __init__(self, points, freq_hz: float, gauss_order: int = 4,
                  near_depth: int = 4, medium=None, single_tables: bool = False):
         if near_depth != 4:
             raise NotImplementedError("the GPU near kernel uses the reference's depth-4 grading")
-        from .penetrable import lossless_medium
-        # medium=(eps_r, mu_r): the operators (T, P, MFIE) in that lossless
-        # medium, i.e. of the same generatrix at the frequency f n; excitation and
-        # far field stay in air (bor_solver.py:175-200)
-        self._n_index, self.eta = (1.0, ETA0) if medium is None else lossless_medium(*medium)
+        from .penetrable import medium_index
+        # medium=(eps_r, mu_r): the operators (T, P) in that medium, i.e. of the
+        # same generatrix at the frequency f |m| (whose rules set n_xi and the
+        # near tables) with the wave number k0 m (complex for a lossy medium);
+        # excitation and far field stay in air (bor_solver.py:175-200)
+        self.freq_hz = float(freq_hz)
+        self._k0 = 2.0 * math.pi * self.freq_hz / C0
+        if medium is None:
+            self._lossy, self._n_index, self._k_medium, self.eta = False, 1.0, self._k0, ETA0
+        else:
+            m_idx, eta = medium_index(*medium)
+            self._lossy = not (m_idx.imag == 0.0 and eta.imag == 0.0)
+            self._n_index = abs(m_idx) if self._lossy else m_idx.real
+            self._k_medium = self._k0 * m_idx
+            self.eta = eta if self._lossy else eta.real
         self.gen = Generatrix(np.asarray(points, dtype=float))
         self.g: GaussData = gauss_on_generatrix(self.gen, gauss_order)
-        self.freq_hz = float(freq_hz)
-        self.k = 2.0 * math.pi * self.freq_hz / C0 * self._n_index
+        self.k = self._k_medium if self._lossy else self._k0 * self._n_index
         self.gauss_order = gauss_order
         self.near_depth = near_depth
         self.Nn = self.gen.n_nodes
@@ -322,10 +333,22 @@ class BorPecSolver:
         addition depends on Z_s and is built by assemble_ibc_extra."""
         if efie and (self._ops is None or self._ops[0] < m_max):
             prob = self._problem(m_max)
-            Z = prob.assemble_modes_fp64()
-            if self.eta != ETA0:
-                Z *= self.eta / ETA0            # C = j k eta 2 pi with this medium's eta
+            if self._lossy:
+                import torch
+                k = complex(self._k_medium)
+                C = 1j * k * self.eta * 2.0 * math.pi
+                st = nat.stream_handle()
+                Z = torch.zeros((m_max + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
+                prob.fill_far_ck(Z, k, C, st)
+                prob.fill_near_ck(k, C, st, Z=Z)
+                prob.check_near_status()
+            else:
+                Z = prob.assemble_modes_fp64()
+                if self.eta != ETA0:
+                    Z *= self.eta / ETA0            # C = j k eta 2 pi with this medium's eta
             self._ops = (m_max, Z)
+        if mfie and self._lossy:
+            raise NotImplementedError("the MFIE operator of a lossy medium is not on the GPU path")
         if mfie and (self._mops is None or self._mops[0] < m_max):
             prob = self._problem(m_max, formulation="mfie")
             self._mops = (m_max, prob.assemble_mfie_modes_fp64())
@@ -388,8 +411,13 @@ class BorPecSolver:
             st = nat.stream_handle()
             import torch
             B = torch.zeros((mm + 1, prob.n, prob.n), dtype=torch.complex128, device=prob.device)
-            prob.fill_far_ibc(B, nat.F64, 1.0 + 0.0j, st)
-            prob.fill_near_ibc(1.0 + 0.0j, st, Z=B, mass=False)
+            if self._lossy:
+                k = complex(self._k_medium)
+                prob.fill_far_ibc_ck(B, k, 1.0 + 0.0j, st)
+                prob.fill_near_ibc_ck(k, 1.0 + 0.0j, st, Z=B, mass=False)
+            else:
+                prob.fill_far_ibc(B, nat.F64, 1.0 + 0.0j, st)
+                prob.fill_near_ibc(1.0 + 0.0j, st, Z=B, mass=False)
             prob.check_near_status()
             self._pops = (mm, B)
         B = self._mode(self._pops, m)
@@ -464,7 +492,7 @@ class BorPecSolver:
         Nn = self.Nn
         d = torch.ones(2 * Nn, dtype=torch.float64, device="cuda")
         d[Nn:] = -1.0
-        c = -1j * (self.k / self._n_index) * ETA0 / (4.0 * math.pi)
+        c = -1j * self._k0 * ETA0 / (4.0 * math.pi)
         fth = c * complex(torch.sum(d * V[:, 0] * x).cpu())
         fph = -c * complex(torch.sum(d * V[:, 1] * x).cpu())
         return fth, fph

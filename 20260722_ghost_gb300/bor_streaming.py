@@ -45,6 +45,9 @@ class StreamingFarBlocks:
                  tile_budget_gb: float = 1.0, workers: int = 1,
                  mode_block: Optional[int] = None):
         import torch
+        if getattr(solver, "_lossy", False):
+            raise NotImplementedError("streamed far blocks of a lossy medium are not on the GPU path "
+                                      "(its operators come from assemble_mode / assemble_pmchwt_P)")
         self.solver = solver
         self.m_max = int(m_max)
         self.dtype = dtype

@@ -30,6 +30,8 @@
 // FP32 path R^2, R and k R are carried as double-float so the phase is exact
 // to ~1e-7 rad before an accurate sincosf, and the DCT is summed in blocks
 // of 8 samples folded in with Kahan compensation.
+#include <type_traits>
+
 #include "common.cuh"
 #include "samplers.cuh"
 #include "df_math.cuh"
@@ -63,16 +65,18 @@ template <class R, int NT, int OG> struct SmemLayout {
     }
 };
 
-template <class R, int NT, int OG>
+// CK: complex wave number k + j ki (FP64 only; a lossy medium's interior)
+template <class R, int NT, int OG, bool CK = false>
 __global__ void __launch_bounds__(TPB, 2)
 far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ dct,
                 const double *__restrict__ sin2, double2 *__restrict__ Z,
                 long long ldz, long long mode_stride, const unsigned char *__restrict__ emask,
-                const float *__restrict__ dct32)
+                const float *__restrict__ dct32, double ki)
 {
+    static_assert(!CK || sizeof(R) == 8, "complex wave numbers on the FP64 path only");
     using CT = C<R>;
-    using Samp = GreenSampler<R>;
+    using Samp = typename std::conditional<CK, GreenSamplerC, GreenSampler<R>>::type;
     using S2 = typename Samp::S2;
     constexpr int NOB = OG * NT;
     constexpr int EPB = 16 / OG, PPB = EPB * 16;
@@ -125,7 +129,10 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         const double rp = geo[p], zp = geo[P + p];
         const double rq = geo[q], zq = geo[P + q];
         const double dr = rp - rq, dz = zp - zq;
-        smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
+        if constexpr (CK)
+            smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k, ki);
+        else
+            smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
     }
 
     CT acc[NT];          // running sums of this thread's NT orders
@@ -347,16 +354,38 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
             const double fm = o * ik2;               // jm/k^2 magnitude
             const double fm2 = (double)o * o * ik2;  // m^2/k^2
             double2 *zl = Gs + (jep * NOB + n) * SLAB;
+            if constexpr (CK) {
+                // the same parts with the complex 1/k^2
+                double q[2];
+                ck_inv_k2(k, ki, q);
+                const double2 c1 = make_double2(q[0], q[1]);
+                const double2 cm = make_double2(o * q[0], o * q[1]);
+                const double2 cm2 = make_double2((double)o * o * q[0], (double)o * o * q[1]);
 #pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                const int ab = a * 2 + b;
-                const double2 p11 = out[0][a], pdd = out[1][a], pds = out[2][a], psd = out[3][a], pss = out[4][a];
-                P11s[(jep * NOB + n) * 4 + ab] = p11;
-                // mode-local parts (mode m = o)
-                zl[0 * 4 + ab] = make_double2(tt * p11.x - ik2 * pdd.x, tt * p11.y - ik2 * pdd.y);
-                zl[1 * 4 + ab] = make_double2(fm * pds.y, -fm * pds.x);       // -(j o/k^2) pds
-                zl[2 * 4 + ab] = make_double2(-fm * psd.y, fm * psd.x);       // +(j o/k^2) psd
-                zl[3 * 4 + ab] = make_double2(-fm2 * pss.x, -fm2 * pss.y);
+                for (int a = 0; a < 2; ++a) {
+                    const int ab = a * 2 + b;
+                    const double2 p11 = out[0][a], pdd = out[1][a], pds = out[2][a], psd = out[3][a],
+                                  pss = out[4][a];
+                    P11s[(jep * NOB + n) * 4 + ab] = p11;
+                    const double2 d = cmul(c1, pdd), x = cmul(cm, pds), y = cmul(cm, psd), w = cmul(cm2, pss);
+                    zl[0 * 4 + ab] = make_double2(tt * p11.x - d.x, tt * p11.y - d.y);
+                    zl[1 * 4 + ab] = make_double2(x.y, -x.x);                 // -(j o/k^2) pds
+                    zl[2 * 4 + ab] = make_double2(-y.y, y.x);                 // +(j o/k^2) psd
+                    zl[3 * 4 + ab] = make_double2(-w.x, -w.y);
+                }
+            } else {
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    const int ab = a * 2 + b;
+                    const double2 p11 = out[0][a], pdd = out[1][a], pds = out[2][a], psd = out[3][a],
+                                  pss = out[4][a];
+                    P11s[(jep * NOB + n) * 4 + ab] = p11;
+                    // mode-local parts (mode m = o)
+                    zl[0 * 4 + ab] = make_double2(tt * p11.x - ik2 * pdd.x, tt * p11.y - ik2 * pdd.y);
+                    zl[1 * 4 + ab] = make_double2(fm * pds.y, -fm * pds.x);       // -(j o/k^2) pds
+                    zl[2 * 4 + ab] = make_double2(-fm * psd.y, fm * psd.x);       // +(j o/k^2) psd
+                    zl[3 * 4 + ab] = make_double2(-fm2 * pss.x, -fm2 * pss.y);
+                }
             }
         }
         __syncthreads();
@@ -432,14 +461,14 @@ far_efie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
     }
 }
 
-template <class R, int NT, int OG>
+template <class R, int NT, int OG, bool CK = false>
 int launch_far(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                const double *dct, const double *sin2, void *Z, long long ldz, long long ms,
-               const unsigned char *emask, const float *dct32, cudaStream_t st)
+               const unsigned char *emask, const float *dct32, cudaStream_t st, double ki = 0.0)
 {
     constexpr int EPB = 16 / OG;
     const size_t smem = SmemLayout<R, NT, OG>::bytes();
-    auto kern = far_efie_kernel<R, NT, OG>;
+    auto kern = far_efie_kernel<R, NT, OG, CK>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("far_efie: smem attribute");
     constexpr int NOB = OG * NT;
@@ -447,8 +476,8 @@ int launch_far(int N, int M, int nxi, double k, double sre, double sim, const do
     const int nchunks = (M + 1 + (NOB - 2) - 1) / (NOB - 2);
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, TPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, dct, sin2,
-                                  reinterpret_cast<double2 *>(Z), ldz, ms, emask, dct32);
-    return check_launch("far_efie");
+                                  reinterpret_cast<double2 *>(Z), ldz, ms, emask, dct32, ki);
+    return check_launch(CK ? "far_efie (complex k)" : "far_efie");
 }
 
 }  // namespace
@@ -486,4 +515,22 @@ extern "C" int ghost_bor_far_efie(int prec, int n_elem, int m_max, int nxi, doub
 {
     return ghost_bor_far_efie_masked(prec, n_elem, m_max, nxi, k, scale_re, scale_im, geo, dct, sin2, Z,
                                      ldz, mode_stride, nullptr, nullptr, stream);
+}
+
+extern "C" int ghost_bor_far_efie_ck(int n_elem, int m_max, int nxi, double k_re, double k_im,
+                                     double scale_re, double scale_im,
+                                     const double *geo, const double *dct, const double *sin2,
+                                     void *Z, long long ldz, long long mode_stride, void *stream)
+{
+    using namespace gb;
+    if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !dct || !sin2 || !Z ||
+        ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k_re > 0.0) ||
+        !(k_im <= 0.0) || !isfinite(k_re) || !isfinite(k_im))
+        return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (m_max + 1 <= 30)
+        return launch_far<double, 8, 4, true>(n_elem, m_max, nxi, k_re, scale_re, scale_im, geo, dct, sin2, Z, ldz,
+                                              mode_stride, nullptr, nullptr, st, k_im);
+    return launch_far<double, 16, 4, true>(n_elem, m_max, nxi, k_re, scale_re, scale_im, geo, dct, sin2, Z, ldz,
+                                           mode_stride, nullptr, nullptr, st, k_im);
 }

@@ -34,6 +34,8 @@
 // transforms with another coefficient set (brackets.cuh), the opposite sign
 // of the bracket term and a complex weight per source element: the IBC
 // instantiations of both kernels below.
+#include <type_traits>
+
 #include "common.cuh"
 #include "samplers.cuh"
 #include "brackets.cuh"
@@ -67,15 +69,17 @@ template <class R> struct MfieSmem {
     }
 };
 
-template <class R, bool IBC>
+// CK: complex wave number k + j ki (FP64 only; a lossy medium's interior)
+template <class R, bool IBC, bool CK = false>
 __global__ void __launch_bounds__(MTPB)
 far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_im,
                 const double *__restrict__ geo, const double *__restrict__ tab,
                 const double *__restrict__ sin2, const double2 *__restrict__ wsrc,
-                double2 *__restrict__ Z, long long ldz, long long mode_stride)
+                double2 *__restrict__ Z, long long ldz, long long mode_stride, double ki)
 {
+    static_assert(!CK || sizeof(R) == 8, "complex wave numbers on the FP64 path only");
     using CT = C<R>;
-    using Samp = BracketSampler<R>;
+    using Samp = typename std::conditional<CK, BracketSamplerC, BracketSampler<R>>::type;
     using S2 = typename Samp::S2;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CT *gsm = reinterpret_cast<CT *>(smem_raw);
@@ -121,7 +125,10 @@ far_mfie_kernel(int N, int Nn, int M, int h, double k, double sc_re, double sc_i
         const double rp = geo[p], zp = geo[P + p];
         const double rq = geo[q], zq = geo[P + q];
         const double dr = rp - rq, dz = zp - zq;
-        smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
+        if constexpr (CK)
+            smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k, ki);
+        else
+            smp.init(dr * dr + dz * dz, 4.0 * rp * rq, k);
     }
 
     CT acc[3][MNT];
@@ -247,9 +254,9 @@ __device__ __forceinline__ void project3(double2 (&acc)[3][NCM], double2 p, doub
     }
 }
 
-template <bool IBC>
+template <bool IBC, bool CK = false>
 __global__ void __launch_bounds__(NTPB, 2)
-near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
+near_mfie_kernel(int N, int Nn, int M, double k, double ki, double sc_re, double sc_im,
                  const double2 *__restrict__ wsrc,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
                  const double *__restrict__ emass, int n_pairs,
@@ -337,7 +344,14 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const double amp = 2.0 * wv * dxi * ik4pi * ir * ir * ir;   // x2: +xi and -xi
                     const size_t q = (size_t)i * NTPB + tid;
                     const double sx = 2.0 * sv * cv;
-                    gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    if constexpr (CK) {
+                        // (1 + j k R) e^{-j k R} with k = k_r + j k_i:
+                        // (1 - k_i R + j k_r R) e^{k_i R} (cos k_r R - j sin k_r R)
+                        const double u = 1.0 - ki * R, ea = amp * exp(ki * R);
+                        gP[q] = make_double2((u * cs + kr * sn) * ea, (kr * cs - u * sn) * ea);
+                    } else {
+                        gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    }
                     gS2[q] = sv * sv;
                     gSx[q] = sx;
                     gCm[q] = 1.0 - 2.0 * sv * sv; gC0[q] = 1.0;    // cos(-xi), cos(0)
@@ -363,7 +377,12 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const double amp = 2.0 * wt * ik4pi * ir * ir * ir;
                     const size_t q = (size_t)(NCORE_M + i) * NTPB + tid;
                     const double sx = 2.0 * st * ct;
-                    gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    if constexpr (CK) {
+                        const double u = 1.0 - ki * R, ea = amp * exp(ki * R);
+                        gP[q] = make_double2((u * cs + kr * sn) * ea, (kr * cs - u * sn) * ea);
+                    } else {
+                        gP[q] = make_double2(fma(kr, sn, cs) * amp, fma(kr, cs, -sn) * amp);
+                    }
                     gS2[q] = st * st;
                     gSx[q] = sx;
                     gCm[q] = 1.0 - 2.0 * st * st; gC0[q] = 1.0;
@@ -469,13 +488,13 @@ near_mfie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
     }
 }
 
-template <class R, bool IBC>
+template <class R, bool IBC, bool CK = false>
 int launch_far_bracket(int N, int M, int nxi, double k, double sre, double sim, const double *geo,
                        const double *tab, const double *sin2, const double *wsrc, void *Z, long long ldz,
-                       long long ms, cudaStream_t st)
+                       long long ms, cudaStream_t st, double ki = 0.0)
 {
     const size_t smem = MfieSmem<R>::bytes();
-    auto kern = far_mfie_kernel<R, IBC>;
+    auto kern = far_mfie_kernel<R, IBC, CK>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("far_mfie: smem attribute");
     const int fgroups = (N + MEPB - 1) / MEPB;
@@ -483,8 +502,8 @@ int launch_far_bracket(int N, int M, int nxi, double k, double sre, double sim, 
     dim3 grid((unsigned)(N * fgroups), (unsigned)nchunks);
     kern<<<grid, MTPB, smem, st>>>(N, N + 1, M, nxi / 2, k, sre, sim, geo, tab, sin2,
                                    reinterpret_cast<const double2 *>(wsrc),
-                                   reinterpret_cast<double2 *>(Z), ldz, ms);
-    return check_launch(IBC ? "far_ibc" : "far_mfie");
+                                   reinterpret_cast<double2 *>(Z), ldz, ms, ki);
+    return check_launch(CK ? "far_ibc (complex k)" : IBC ? "far_ibc" : "far_mfie");
 }
 
 template <bool IBC>
@@ -503,12 +522,13 @@ int far_bracket(int prec, int n_elem, int m_max, int nxi, double k, double sre, 
     return GHOST_BOR_EINVAL;
 }
 
-template <bool IBC>
+template <bool IBC, bool CK = false>
 int near_bracket(int n_elem, int m_max, double k, double sre, double sim, const double *wsrc,
                  const double *nodes, const double *elem, const double *emass, int n_pairs, const int *pairs,
                  const int *tails, const double *cells, int n_cells_total, const double *core_gl,
                  const double *tail_gl, int n_tail_total, double *band, void *Z, long long ldz, long long ms,
-                 int n_tail_max, void *work, long long work_bytes, long long work_need, void *stream)
+                 int n_tail_max, void *work, long long work_bytes, long long work_need, void *stream,
+                 double ki = 0.0)
 {
     if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !emass || !pairs || !tails ||
         !cells || !core_gl || !tail_gl || !(k > 0.0) || n_tail_max < 0 || !work ||
@@ -518,18 +538,18 @@ int near_bracket(int n_elem, int m_max, double k, double sre, double sim, const 
     const size_t smem = NearMfieSmem::bytes(m_max + 1);
     if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    auto kern = near_mfie_kernel<IBC>;
+    auto kern = near_mfie_kernel<IBC, CK>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("near_mfie: smem attribute");
     int *status = reinterpret_cast<int *>(work);
     if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_mfie: memset");
     const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
     kern<<<grid, NTPB, smem, st>>>(
-        n_elem, n_elem + 1, m_max, k, sre, sim, reinterpret_cast<const double2 *>(wsrc), nodes, elem, emass,
+        n_elem, n_elem + 1, m_max, k, ki, sre, sim, reinterpret_cast<const double2 *>(wsrc), nodes, elem, emass,
         n_pairs, pairs, tails, cells, n_cells_total, core_gl, tail_gl, n_tail_total, NCORE_M + n_tail_max,
         reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, ms,
         reinterpret_cast<unsigned char *>(work) + 256, status);
-    return check_launch(IBC ? "near_ibc" : "near_mfie");
+    return check_launch(CK ? "near_ibc (complex k)" : IBC ? "near_ibc" : "near_mfie");
 }
 
 }  // namespace
@@ -585,4 +605,35 @@ extern "C" int ghost_bor_near_ibc(int n_elem, int m_max, double k, double scale_
                                   pairs, tails, cells, n_cells_total, core_gl, tail_gl, n_tail_total, band, Z,
                                   ldz, mode_stride, n_tail_max, work, work_bytes,
                                   ghost_bor_near_mfie_workspace(n_tail_max), stream);
+}
+
+extern "C" int ghost_bor_far_ibc_ck(int n_elem, int m_max, int nxi, double k_re, double k_im,
+                                    double scale_re, double scale_im, const double *zs_elem,
+                                    const double *geo, const double *tab, const double *sin2,
+                                    void *Z, long long ldz, long long mode_stride, void *stream)
+{
+    using namespace gb;
+    if (n_elem < 3 || m_max < 0 || nxi < 2 || (nxi & 1) || !geo || !tab || !sin2 || !Z ||
+        ldz < 2LL * (n_elem + 1) || mode_stride < ldz * 2LL * (n_elem + 1) || !(k_re > 0.0) ||
+        !(k_im <= 0.0) || !isfinite(k_re) || !isfinite(k_im))
+        return GHOST_BOR_EINVAL;
+    return launch_far_bracket<double, true, true>(n_elem, m_max, nxi, k_re, scale_re, scale_im, geo, tab, sin2,
+                                                  zs_elem, Z, ldz, mode_stride,
+                                                  reinterpret_cast<cudaStream_t>(stream), k_im);
+}
+
+extern "C" int ghost_bor_near_ibc_ck(int n_elem, int m_max, double k_re, double k_im,
+                                     double scale_re, double scale_im, const double *zs_elem,
+                                     const double *nodes, const double *elem, const double *emass,
+                                     int n_pairs, const int *pairs, const int *tails,
+                                     const double *cells, int n_cells_total,
+                                     const double *core_gl, const double *tail_gl, int n_tail_total,
+                                     double *band, void *Z, long long ldz, long long mode_stride,
+                                     int n_tail_max, void *work, long long work_bytes, void *stream)
+{
+    if (!(k_im <= 0.0) || !isfinite(k_im)) return GHOST_BOR_EINVAL;
+    return gb::near_bracket<true, true>(n_elem, m_max, k_re, scale_re, scale_im, zs_elem, nodes, elem, emass,
+                                        n_pairs, pairs, tails, cells, n_cells_total, core_gl, tail_gl,
+                                        n_tail_total, band, Z, ldz, mode_stride, n_tail_max, work, work_bytes,
+                                        ghost_bor_near_mfie_workspace(n_tail_max), stream, k_im);
 }

@@ -21,6 +21,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "medium.cuh"
 #include "df_math.cuh"
 
 namespace gb {
@@ -316,7 +317,9 @@ __device__ __forceinline__ void near_chunk(int n0, bool more, bool valid, bool o
 // DF = true (FP32+IR path): every node's transcendental functions, the cos(m xi)
 // recurrence, the projection and the order GEMM run in double-float (two FP32
 // words, ~48 bits) on the FP32 pipe; DF = false is the plain FP64 path.
-template <bool DF, int NC>
+// CK: complex wave number k + j ki on the FP64 path (a lossy medium's
+// interior): every sample of g gains e^{ki R}, and 1/k^2 is complex.
+template <bool DF, int NC, bool CK = false>
 __global__ void __launch_bounds__(TPBN, 2)
 near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                  const double *__restrict__ nodes, const double *__restrict__ elem,
@@ -324,8 +327,10 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                  const double *__restrict__ cells, int ncells_total,
                  const double *__restrict__ core_gl, const double *__restrict__ tail_gl, int ntail_total,
                  int nmax, double2 *__restrict__ band, double2 *__restrict__ Z, long long ldz,
-                 long long mode_stride, unsigned char *__restrict__ scratch, int *__restrict__ status)
+                 long long mode_stride, unsigned char *__restrict__ scratch, int *__restrict__ status,
+                 double ki)
 {
+    static_assert(!(CK && DF), "complex wave numbers on the FP64 path only");
     using NA = typename NodeT<DF>::A;
     using NB = typename NodeT<DF>::B;
     using Acc = typename std::conditional<DF, float4, double2>::type;
@@ -418,7 +423,8 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                     const double R0 = sqrt(d2);
                     double sn, cs;
                     sincos(kk * R0, &sn, &cs);
-                    const double amp = 2.0 * GB_PI / (4.0 * GB_PI * fmax(R0, 1e-300));
+                    double amp = 2.0 * GB_PI / (4.0 * GB_PI * fmax(R0, 1e-300));
+                    if constexpr (CK) amp *= exp(ki * R0);
                     axis0 = make_double2(amp * cs, -amp * sn);
                 } else {
                     const double d = sqrt(fmax(d2, 1e-300));
@@ -455,7 +461,8 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         const double dxi = 2.0 * da * ch2 * rsqrt(fmax(1.0 - sv * sv, 1e-15));
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
-                        const double gw = 2.0 * wv * dxi * (1.0 / (4.0 * GB_PI)) * iR;
+                        double gw = 2.0 * wv * dxi * (1.0 / (4.0 * GB_PI)) * iR;
+                        if constexpr (CK) gw *= exp(ki * R);
                         put_node(gA, gC, gS0, gS1, (size_t)i * TPBN + tid, gw * cs, -gw * sn,
                                  1.0 - 2.0 * sv * sv);
                     }
@@ -475,7 +482,8 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
                         const double R = R2 * iR;
                         double sn, cs;
                         sincos(kk * R, &sn, &cs);
-                        const double gw = 2.0 * wt * (1.0 / (4.0 * GB_PI)) * iR;
+                        double gw = 2.0 * wt * (1.0 / (4.0 * GB_PI)) * iR;
+                        if constexpr (CK) gw *= exp(ki * R);
                         put_node(gA, gC, gS0, gS1, (size_t)(NCORE + i) * TPBN + tid, gw * cs, -gw * sn,
                                  1.0 - 2.0 * st * st);
                     }
@@ -536,7 +544,28 @@ near_efie_kernel(int N, int Nn, int M, double k, double sc_re, double sc_im,
             const double2 Gs = make_double2(Dh.y, -Dh.x);                                       // A1(Gs) = Dh / j
             const double fm = m * ik2, fm2 = (double)m * m * ik2;
             double2 v;
-            if (blk == 0) {
+            if constexpr (CK) {
+                // the same blocks with the complex 1/k^2: c1 = 1/k^2, cm = m/k^2, cm2 = m^2/k^2
+                double q[2];
+                ck_inv_k2(kk, ki, q);
+                const double2 c1 = make_double2(q[0], q[1]);
+                const double2 cm = make_double2(m * q[0], m * q[1]);
+                const double2 cm2 = make_double2((double)m * m * q[0], (double)m * m * q[1]);
+                if (blk == 0) {
+                    const double2 d = cmul(c1, Prim[(1 * 4 + ab) * Mp + m]);
+                    v = make_double2(tre * trf * S.x + tze * tzf * A1.x - d.x,
+                                     tre * trf * S.y + tze * tzf * A1.y - d.y);
+                } else if (blk == 1) {
+                    const double2 x = cmul(cm, Prim[(2 * 4 + ab) * Mp + m]);
+                    v = make_double2(tre * Gs.x + x.y, tre * Gs.y - x.x);       // - j (m/k^2) Ads
+                } else if (blk == 2) {
+                    const double2 y = cmul(cm, Prim[(3 * 4 + ab) * Mp + m]);
+                    v = make_double2(-trf * Gs.x - y.y, -trf * Gs.y + y.x);     // + j (m/k^2) Asd
+                } else {
+                    const double2 w = cmul(cm2, Prim[(4 * 4 + ab) * Mp + m]);
+                    v = make_double2(S.x - w.x, S.y - w.y);
+                }
+            } else if (blk == 0) {
                 const double2 Add = Prim[(1 * 4 + ab) * Mp + m];
                 v = make_double2(tre * trf * S.x + tze * tzf * A1.x - ik2 * Add.x,
                                  tre * trf * S.y + tze * tzf * A1.y - ik2 * Add.y);
@@ -984,6 +1013,44 @@ extern "C" int ghost_bor_near_efie(int prec, int n_elem, int m_max, double k,
         n_elem, n_elem + 1, m_max, k, scale_re, scale_im, nodes, elem, n_pairs, pairs, tails, cells,
         n_cells_total, core_gl, tail_gl, n_tail_total, NCORE + n_tail_max,
         reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, mode_stride,
-        reinterpret_cast<unsigned char *>(work) + 256, status);
+        reinterpret_cast<unsigned char *>(work) + 256, status, 0.0);
     return check_launch("near_efie");
+}
+
+extern "C" int ghost_bor_near_efie_ck(int n_elem, int m_max, double k_re, double k_im,
+                                      double scale_re, double scale_im,
+                                      const double *nodes, const double *elem,
+                                      int n_pairs, const int *pairs, const int *tails,
+                                      const double *cells, int n_cells_total,
+                                      const double *core_gl, const double *tail_gl, int n_tail_total,
+                                      double *band, void *Z, long long ldz, long long mode_stride,
+                                      int n_tail_max, void *work, long long work_bytes, void *stream)
+{
+    using namespace gb;
+    if (n_elem < 1 || m_max < 0 || n_pairs < 1 || !nodes || !elem || !pairs || !tails || !cells ||
+        !core_gl || !tail_gl || !(k_re > 0.0) || !(k_im <= 0.0) || !isfinite(k_re) || !isfinite(k_im) ||
+        n_tail_max < 0 || !work || (reinterpret_cast<uintptr_t>(work) & 255) ||
+        work_bytes < ghost_bor_near_workspace(n_tail_max))
+        return GHOST_BOR_EINVAL;
+    if (!band && (!Z || ldz < 2LL * (n_elem + 1))) return GHOST_BOR_EINVAL;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int Mp = m_max + 2;
+    const size_t smem = NearSmem::bytes(Mp, kNc64);
+    if (smem > 227 * 1024) return GHOST_BOR_EUNSUPPORTED;
+    auto kern = near_efie_kernel<false, kNc64, true>;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
+            return check_launch("near_efie_ck: smem attribute");
+        attr = true;
+    }
+    int *status = reinterpret_cast<int *>(work);
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return check_launch("near_efie_ck: memset");
+    const int grid = n_pairs < near_grid() ? n_pairs : near_grid();
+    kern<<<grid, TPBN, smem, st>>>(
+        n_elem, n_elem + 1, m_max, k_re, scale_re, scale_im, nodes, elem, n_pairs, pairs, tails, cells,
+        n_cells_total, core_gl, tail_gl, n_tail_total, NCORE + n_tail_max,
+        reinterpret_cast<double2 *>(band), reinterpret_cast<double2 *>(Z), ldz, mode_stride,
+        reinterpret_cast<unsigned char *>(work) + 256, status, k_im);
+    return check_launch("near_efie (complex k)");
 }

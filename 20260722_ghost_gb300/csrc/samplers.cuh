@@ -9,6 +9,7 @@
 // phase is exact to ~1e-7 rad before an accurate sincosf.
 #pragma once
 #include "common.cuh"
+#include "medium.cuh"
 
 namespace gb {
 namespace {
@@ -106,6 +107,33 @@ template <> struct GreenSampler<float> {
         const float ir = __frcp_rn(ph.r);
         const float amp = ir * fmaf(-ph.rl, ir, 1.0f);  // 1/(4 pi) is folded into the tables
         return make_float2(amp * ph.cs, -amp * ph.sn);
+    }
+};
+
+// FP64 samplers with a complex wave number k_r + j k_i (lossy media)
+struct GreenSamplerC {
+    using S2 = double;
+    double d2, a2, kr, ki;
+    __device__ void init(double d2_, double a2_, double kr_, double ki_) { d2 = d2_; a2 = a2_; kr = kr_; ki = ki_; }
+    static __device__ __forceinline__ double load_s2(const double *t, int j) { return t[j]; }
+    __device__ __forceinline__ double2 operator()(double s2) const {
+        const double R = fmax(sqrt(fma(a2, s2, d2)), 1e-30);
+        double o[2];
+        ck_green(R, kr, ki, 1.0, o);                 // 1/(4 pi) is folded into the tables
+        return make_double2(o[0], o[1]);
+    }
+};
+
+struct BracketSamplerC {
+    using S2 = double;
+    double d2, a2, kr, ki;
+    __device__ void init(double d2_, double a2_, double kr_, double ki_) { d2 = d2_; a2 = a2_; kr = kr_; ki = ki_; }
+    static __device__ __forceinline__ double load_s2(const double *t, int j) { return t[j]; }
+    __device__ __forceinline__ double2 operator()(double s2) const {
+        const double R = fmax(sqrt(fma(a2, s2, d2)), 1e-30);
+        double o[2];
+        ck_bracket(R, kr, ki, 1.0, o);
+        return make_double2(o[0], o[1]);
     }
 };
 

@@ -327,6 +327,47 @@ class BorGpuProblem:
                  nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
                  self.n_tail_max, nat.ptr(work), nbytes, stream)
 
+    # -- FP64 fills with a complex wave number (a lossy medium's interior; the
+    # problem is built at the frequency of |k|, whose rules set n_xi and the
+    # near tables as the reference forms them for a complex k)
+    def fill_far_ck(self, Z, k: complex, scale: complex, stream: int):
+        nat.call("ghost_bor_far_efie_ck", self.N, self.m_max, self.n_xi, k.real, k.imag, scale.real, scale.imag,
+                 nat.ptr(self.d_geo), nat.ptr(self.d_dct), nat.ptr(self.d_sin2), nat.ptr(Z), Z.stride(-2),
+                 Z.stride(0), stream)
+
+    def fill_near_ck(self, k: complex, scale: complex, stream: int, Z=None, band=None):
+        ld = 0 if Z is None else Z.stride(-2)
+        ms = 0 if Z is None else Z.stride(0)
+        work, nbytes = self._near_work("ghost_bor_near_workspace")
+        nat.call("ghost_bor_near_efie_ck", self.N, self.m_max, k.real, k.imag, scale.real, scale.imag,
+                 nat.ptr(self.d_nodes), nat.ptr(self.d_elem), len(self.near.pairs),
+                 nat.ptr(self.d_pairs), nat.ptr(self.d_tails), nat.ptr(self.d_cells),
+                 self.near.cells.shape[1], nat.ptr(self.d_core), nat.ptr(self.d_tail),
+                 self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
+                 self.n_tail_max, nat.ptr(work), nbytes, stream)
+
+    def fill_far_ibc_ck(self, Z, k: complex, scale: complex, stream: int):
+        nat.call("ghost_bor_far_ibc_ck", self.N, self.m_max, self.n_xi_b, k.real, k.imag,
+                 scale.real, scale.imag, nat.ptr(self.d_zs), nat.ptr(self.d_geo), nat.ptr(self.d_btab),
+                 nat.ptr(self.d_bsin2), nat.ptr(Z), Z.stride(-2), Z.stride(0), stream)
+
+    def fill_near_ibc_ck(self, k: complex, scale: complex, stream: int, Z=None, band=None,
+                         mass: bool = True):
+        ld = 0 if Z is None else Z.stride(-2)
+        ms = 0 if Z is None else Z.stride(0)
+        work, nbytes = self._near_work("ghost_bor_near_mfie_workspace")
+        emass = self.d_emass
+        if not mass:
+            if getattr(self, "_zero_emass", None) is None:
+                self._zero_emass = self.torch.zeros_like(self.d_emass)
+            emass = self._zero_emass
+        nat.call("ghost_bor_near_ibc_ck", self.N, self.m_max, k.real, k.imag, scale.real, scale.imag,
+                 nat.ptr(self.d_zs), nat.ptr(self.d_nodes), nat.ptr(self.d_elem), nat.ptr(emass),
+                 len(self.near.pairs), nat.ptr(self.d_pairs), nat.ptr(self.d_tails),
+                 nat.ptr(self.d_cells), self.near.cells.shape[1], nat.ptr(self.d_core),
+                 nat.ptr(self.d_tail), self.near.tail_gl.shape[1], nat.ptr(band), nat.ptr(Z), ld, ms,
+                 self.n_tail_max, nat.ptr(work), nbytes, stream)
+
     def fill_operator_far(self, Z, precision: int, stream: int):
         """Far parts of A = alpha (C Z_E + Z_s-terms) + (1 - alpha) eta0 Z_M into Z."""
         if self.alpha > 0.0:

@@ -1,6 +1,5 @@
 """Homogeneous penetrable bodies of revolution: per-mode PMCHWT on the GPU
-(the reference's solve_bor_dielectric, bor_solver.py:1019-1095), for lossless
-media.
+(the reference's solve_bor_dielectric, bor_solver.py:1019-1095).
 
 Unknowns per mode are J (2 Nn) and M' = M / eta0 (2 Nn); with T the EFIE
 operator and P the rotated principal-value operator of each medium (exterior
@@ -10,13 +9,16 @@ e = free space, interior i):
     [ eta0 (P_e + P_i)     T_e + r T_i       ] [M'] = [ eta0 <W, H_inc> ],
     r = (eta0 / eta_i)^2.
 
-Every block is a fill that exists for the PEC and impedance paths.  With real
-eps_r, mu_r > 0 the interior wave number k_i = k0 sqrt(eps_r mu_r) is real, so
-T_i is the EFIE fill of the same generatrix at the frequency f sqrt(eps_r mu_r)
-with the factor j k_i eta_i 2 pi, and P the impedance bracket fill
-(ghost_bor_far_ibc / ghost_bor_near_ibc) with unit weights and no mass term,
-its source columns remapped P = [[-B_tf, B_tt], [-B_ff, B_ft]] (n x t = phi,
-n x phi = -t; bor_solver.py:554-576).  The right-hand side and the far field
+Every block is a fill of the PEC and impedance paths.  The interior
+problem is the same generatrix at the frequency f |m| (m the refractive index
+on the reference's causal branch), whose rules set n_xi and the near tables as
+the reference forms them from |k_i|.  T_i is the EFIE fill with the wave
+number k_i = k0 m and the factor j k_i eta_i 2 pi, P the impedance bracket
+fill (ghost_bor_far_ibc / ghost_bor_near_ibc) with unit weights and no mass
+term, its source columns remapped P = [[-B_tf, B_tt], [-B_ff, B_ft]]
+(n x t = phi, n x phi = -t; bor_solver.py:554-576).  A lossless medium (real
+m and eta_i) takes the real-k fills; a lossy one their complex-wave-number
+variants (ghost_bor_*_ck, csrc/medium.cuh).  The right-hand side and the far field
 come from the exterior EFIE excitation alone: the H-field excitation is the
 E-field excitation of the other polarisation over eta0 (bor_solver.py:647-657),
 so the columns are VV: [V_VV; -V_HH], HH: [V_HH; V_VV], and these same columns
@@ -26,8 +28,8 @@ F_theta = c sum D (B_VV . x), F_phi = -c sum D (B_HH . x), D = diag(I, -I, I,
 Z(-m) = S Z(m) S with S = diag(I, -I, -I, I) and B(-m) = +-S B(m), so only
 m >= 0 is factored and m > 0 counts twice, as for the PEC sweep.
 
-Lossy or negative media need complex-wavenumber fills, which the kernels do
-not have: they raise NotImplementedError.
+A purely imaginary index (an evanescent interior, Re k_i = 0) raises
+NotImplementedError.
 """
 
 from __future__ import annotations
@@ -43,16 +45,33 @@ from .engine import BorGpuProblem, SweepResult
 from .geometry import ETA0
 
 
+def medium_index(eps_r, mu_r):
+    """(m, eta_i): refractive index on the causal branch (Im m <= 0, then
+    Re m >= 0) and the medium's impedance eta0 mu_r / m, as the reference forms
+    them (bor_solver.py:161-172).  A medium whose wave number has no real part
+    (Re m = 0, an evanescent interior) raises NotImplementedError."""
+    eps, mu = complex(eps_r), complex(mu_r)
+    if not all(math.isfinite(v) for v in (eps.real, eps.imag, mu.real, mu.imag)):
+        raise ValueError("eps_r and mu_r must be finite")
+    m = complex(np.sqrt(eps * mu))
+    if m.imag > 0.0:
+        m = -m
+    if m.real < 0.0:
+        m = -m
+    if not m.real > 0.0:
+        raise NotImplementedError("a medium with a purely imaginary refractive index (evanescent interior) "
+                                  "is not on the GPU path")
+    return m, ETA0 * (mu / m)
+
+
 def lossless_medium(eps_r, mu_r):
-    """(refractive index, eta_i) of a lossless medium; NotImplementedError for
-    the media the GPU path does not take."""
+    """(refractive index, eta_i) of a lossless medium (real eps_r, mu_r > 0);
+    NotImplementedError for any other."""
     eps, mu = complex(eps_r), complex(mu_r)
     if not all(math.isfinite(v) for v in (eps.real, eps.imag, mu.real, mu.imag)):
         raise ValueError("eps_r and mu_r must be finite")
     if eps.imag != 0.0 or mu.imag != 0.0 or eps.real <= 0.0 or mu.real <= 0.0:
-        raise NotImplementedError("lossy or negative media need complex-wavenumber fills, which the "
-                                  "GPU path does not have; it takes real eps_r > 0 and mu_r > 0")
-    # index and relative impedance as the reference forms them (bor_solver.py:161-172)
+        raise NotImplementedError("not a lossless medium: real eps_r > 0 and mu_r > 0 take the real-k fills")
     n = math.sqrt(eps.real * mu.real)
     return n, ETA0 * (mu.real / n)
 
@@ -95,18 +114,24 @@ def farfield_fp64(prob: BorGpuProblem, V, X, stream: int):
 
 
 class DielectricBorProblem:
-    """One homogeneous lossless body at one frequency: the exterior problem
-    (free space) and the interior one (the same generatrix at f n), with their
+    """One homogeneous body at one frequency: the exterior problem (free
+    space) and the interior one (the same generatrix at f |m|), with their
     tables on the device."""
 
     def __init__(self, points, freq_hz: float, thetas_deg, eps_r, mu_r=1.0,
                  m_max: Optional[int] = None):
-        self.n_index, self.eta_i = lossless_medium(eps_r, mu_r)
+        self.m_index, self.eta_i = medium_index(eps_r, mu_r)
+        # a real index and impedance: the real-k fills (also a double-negative medium)
+        self.lossless = self.m_index.imag == 0.0 and self.eta_i.imag == 0.0
+        self.n_index = self.m_index.real if self.lossless else abs(self.m_index)
         self.eps_r, self.mu_r = complex(eps_r), complex(mu_r)
-        # unit Z_s: the bracket tables and unit source weights for P
+        # unit Z_s: the bracket tables and unit source weights for P.  The
+        # interior problem is the generatrix at f |m|: its n_xi and near tables
+        # follow |k_i|; a lossy medium's fills take the complex k_i = k0 m
         self.ext = BorGpuProblem(points, freq_hz, thetas_deg, m_max=m_max, zs=1.0)
         self.int = BorGpuProblem(points, float(freq_hz) * self.n_index, thetas_deg,
                                  m_max=self.ext.m_max, zs=1.0)
+        self.k_int = self.ext.k * self.m_index
         self.m_max = self.ext.m_max
         self.Nn = self.ext.Nn
         self.n = 2 * self.ext.n           # 4 Nn unknowns per mode
@@ -136,17 +161,27 @@ class DielectricBorProblem:
         c128 = torch.complex128
         Z = torch.zeros((Mb, n, n), dtype=c128, device=e.device)
         Ce = e.C
-        Ci = 1j * i.k * self.eta_i * 2.0 * math.pi
+        ki = self.k_int
+        Ci = 1j * (i.k if self.lossless else ki) * self.eta_i * 2.0 * math.pi
         r2 = (ETA0 / self.eta_i) ** 2
         for blk, ci in ((Z[:, :h, :h], Ci), (Z[:, h:, h:], Ci * r2)):
             e.fill_far(blk, nat.F64, Ce, stream)
             e.fill_near(Ce, stream, Z=blk)
-            i.fill_far(blk, nat.F64, ci, stream)
-            i.fill_near(ci, stream, Z=blk)
+            if self.lossless:
+                i.fill_far(blk, nat.F64, ci, stream)
+                i.fill_near(ci, stream, Z=blk)
+            else:
+                i.fill_far_ck(blk, ki, ci, stream)
+                i.fill_near_ck(ki, ci, stream, Z=blk)
         Bt = torch.zeros((Mb, h, h), dtype=c128, device=e.device)
-        for p in (e, i):
-            p.fill_far_ibc(Bt, nat.F64, 1.0 + 0.0j, stream)
-            p.fill_near_ibc(1.0 + 0.0j, stream, Z=Bt, mass=False)
+        e.fill_far_ibc(Bt, nat.F64, 1.0 + 0.0j, stream)
+        e.fill_near_ibc(1.0 + 0.0j, stream, Z=Bt, mass=False)
+        if self.lossless:
+            i.fill_far_ibc(Bt, nat.F64, 1.0 + 0.0j, stream)
+            i.fill_near_ibc(1.0 + 0.0j, stream, Z=Bt, mass=False)
+        else:
+            i.fill_far_ibc_ck(Bt, ki, 1.0 + 0.0j, stream)
+            i.fill_near_ibc_ck(ki, 1.0 + 0.0j, stream, Z=Bt, mass=False)
         P = ETA0 * torch.cat([-Bt[:, :, Nn:], Bt[:, :, :Nn]], dim=2)
         del Bt
         Z[:, :h, h:] -= P

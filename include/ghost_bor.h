@@ -291,6 +291,41 @@ int ghost_bor_near_ibc(int n_elem, int m_max, double k, double scale_re, double 
                        int n_tail_max, void *work, long long work_bytes, void *stream);
 
 /* ------------------------------------------------------------------------
+ * FP64 fills with a complex wave number k = k_re + j k_im, k_im <= 0 (the
+ * interior of a lossy medium, for the PMCHWT operators T_i and P_i;
+ * bor_solver.py:161-200): the samples gain e^{k_im R}, p(R) becomes
+ * (1 - k_im R + j k_re R) e^{k_im R} (cos - j sin) / R^3 and 1/k^2 is complex.
+ * Arguments as in ghost_bor_far_efie (FP64, no element mask),
+ * ghost_bor_near_efie (FP64 path), ghost_bor_far_ibc and ghost_bor_near_ibc;
+ * nxi, the cells and the tail orders come from |k| as the reference forms
+ * them for a complex k.
+ */
+int ghost_bor_far_efie_ck(int n_elem, int m_max, int nxi, double k_re, double k_im,
+                          double scale_re, double scale_im,
+                          const double *geo, const double *dct, const double *sin2,
+                          void *Z, long long ldz, long long mode_stride, void *stream);
+int ghost_bor_near_efie_ck(int n_elem, int m_max, double k_re, double k_im,
+                           double scale_re, double scale_im,
+                           const double *nodes, const double *elem,
+                           int n_pairs, const int *pairs, const int *tails,
+                           const double *cells, int n_cells_total,
+                           const double *core_gl, const double *tail_gl, int n_tail_total,
+                           double *band, void *Z, long long ldz, long long mode_stride,
+                           int n_tail_max, void *work, long long work_bytes, void *stream);
+int ghost_bor_far_ibc_ck(int n_elem, int m_max, int nxi, double k_re, double k_im,
+                         double scale_re, double scale_im, const double *zs_elem,
+                         const double *geo, const double *tab, const double *sin2,
+                         void *Z, long long ldz, long long mode_stride, void *stream);
+int ghost_bor_near_ibc_ck(int n_elem, int m_max, double k_re, double k_im,
+                          double scale_re, double scale_im, const double *zs_elem,
+                          const double *nodes, const double *elem, const double *emass,
+                          int n_pairs, const int *pairs, const int *tails,
+                          const double *cells, int n_cells_total,
+                          const double *core_gl, const double *tail_gl, int n_tail_total,
+                          double *band, void *Z, long long ldz, long long mode_stride,
+                          int n_tail_max, void *work, long long work_bytes, void *stream);
+
+/* ------------------------------------------------------------------------
  * Excitation for all modes 0..m_max, angles and both polarisations:
  *   B[m][row][2*it + pol] (complex double, row stride ldb, mode stride),
  *   pol 0 = VV (theta), 1 = HH (phi).  Rows flagged in mask_rows[m][4]

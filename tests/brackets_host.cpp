@@ -67,3 +67,20 @@ void host_sample_ibc(int nr, int np_, int nxi, const double *rho_p, const double
 }
 
 }
+
+#include "medium.cuh"
+
+extern "C" {
+
+// in [n][3] = (R, k_r, k_i); out [n][6] = g (re, im), p (re, im), 1/k^2 (re, im)
+void host_complex_k(int n, const double *in, double *out)
+{
+    for (int i = 0; i < n; ++i) {
+        const double *v = in + 3 * i;
+        gb::ck_green(v[0], v[1], v[2], 1.0, out + 6 * i);
+        gb::ck_bracket(v[0], v[1], v[2], 1.0, out + 6 * i + 2);
+        gb::ck_inv_k2(v[1], v[2], out + 6 * i + 4);
+    }
+}
+
+}

@@ -39,8 +39,24 @@ def emulated(monkeypatch, pkg, oracle):
             cache[key] = o
         return cache[key]
 
-    def blocks(prob, kind):
-        o = orc(prob)
+    media = []                       # (f in air, eps_r, mu_r) of the lossy media of a test
+
+    def orc_ck(prob, k):
+        for f, eps, mu in media:
+            key = ("ck", round(f, 6), eps, mu)
+            m_idx = complex(np.sqrt(complex(eps) * complex(mu)))
+            m_idx = -m_idx if m_idx.imag > 0 else m_idx
+            m_idx = -m_idx if m_idx.real < 0 else m_idx
+            if abs(2 * math.pi * f / oracle.C0 * m_idx - k) <= 1e-9 * abs(k):
+                if key not in cache:
+                    o = oracle.OracleSolver(prob.gen.nodes, f, medium=(eps, mu))
+                    o.prepare(prob.m_max, efie=True, workers=4, ibc_zs_pt=np.ones(o.geo.P))
+                    cache[key] = o
+                return cache[key]
+        raise AssertionError(f"no medium registered for k = {k}")
+
+    def blocks(prob, kind, o=None):
+        o = orc(prob) if o is None else o
         M, Nn = prob.m_max, prob.Nn
         C = 1j * o.k * o.eta * 2.0 * math.pi
         out = []
@@ -74,6 +90,18 @@ def emulated(monkeypatch, pkg, oracle):
         assert not mass
         add(Z, scale, blocks(self, "ibc_near"))
     monkeypatch.setattr(eng.BorGpuProblem, "fill_near_ibc", near_ibc)
+    monkeypatch.setattr(eng.BorGpuProblem, "fill_far_ck",
+                        lambda self, Z, k, scale, st: add(Z, scale, blocks(self, "far", orc_ck(self, k))))
+    monkeypatch.setattr(eng.BorGpuProblem, "fill_near_ck",
+                        lambda self, k, scale, st, Z=None, band=None:
+                        add(Z, scale, blocks(self, "near", orc_ck(self, k))))
+    monkeypatch.setattr(eng.BorGpuProblem, "fill_far_ibc_ck",
+                        lambda self, Z, k, scale, st: add(Z, scale, blocks(self, "ibc_far", orc_ck(self, k))))
+
+    def near_ibc_ck(self, k, scale, st, Z=None, band=None, mass=True):
+        assert not mass
+        add(Z, scale, blocks(self, "ibc_near", orc_ck(self, k)))
+    monkeypatch.setattr(eng.BorGpuProblem, "fill_near_ibc_ck", near_ibc_ck)
 
     def excitation(self, B, coef_e, coef_h, st, h_weight=None):
         o = orc(self)
@@ -106,6 +134,7 @@ def emulated(monkeypatch, pkg, oracle):
     monkeypatch.setattr(pen, "solve_fp64", solve)
     monkeypatch.setattr(pen, "residual_fp64", residual)
     monkeypatch.setattr(pen, "farfield_fp64", farfield)
+    cache["media"] = media
     return cache
 
 
@@ -120,18 +149,41 @@ def test_dielectric_orchestration_matches_reference(pkg, emulated):
     assert r["n_unknowns"] == 4 * len(D["points"]) and r["formulation"] == "pmchwt"
     assert r["linear_residual"] < 1e-12
     # the interior problem is the generatrix at f n
-    assert sorted(emulated) == sorted([round(float(D["freq_hz"]), 6), round(2.0 * float(D["freq_hz"]), 6)])
+    assert sorted(k for k in emulated if k != "media") == sorted([round(float(D["freq_hz"]), 6),
+                                                                  round(2.0 * float(D["freq_hz"]), 6)])
 
 
-def test_lossy_media_are_named(pkg):
+@pytest.mark.parametrize("case", [0, 2])
+def test_lossy_dielectric_orchestration_matches_reference(pkg, emulated, case):
+    """Lossy media (eps_r = 2.5 - 0.2j; eps_r = 2 - 0.1j with mu_r = 1.5 - 0.2j):
+    the complex-wave-number fills of the interior, the rest as for a lossless
+    body, against the reference's amplitudes."""
+    D = load_golden("pmchwt_sphere_n24")
+    eps, mu = (complex(x) for x in D["media"][case])
+    f = float(D["freq_hz"])
+    emulated["media"].append((f, eps, mu))
+    r = pkg.bor_solver.solve_bor_dielectric(D["points"], f, D["thetas"], eps, mu,
+                                            n_modes=int(D["m_max"]), mode_tol=0.0)
+    for pol in ("vv", "hh"):
+        a, b = np.asarray(r[f"amp_{pol}"]), D[f"amp_{pol}_{case}"]
+        assert np.max(np.abs(a - b)) <= 1e-10 * np.max(np.abs(b)), pol
+
+
+def test_medium_index_branch(pkg):
+    """Index and impedance on the reference's causal branch (Im m <= 0, then
+    Re m >= 0); a purely imaginary index (evanescent interior) is not taken."""
     pen = pkg.penetrable
-    n, eta = pen.lossless_medium(4.0, 1.0)
-    assert n == 2.0 and eta == pytest.approx(376.730313668 / 2.0, rel=1e-15)
-    for eps, mu in ((2.5 - 0.2j, 1.0), (2.0, 1.5 - 0.2j), (-2.0, 1.0)):
-        with pytest.raises(NotImplementedError, match="complex-wavenumber"):
-            pen.lossless_medium(eps, mu)
+    m, eta = pen.medium_index(4.0, 1.0)
+    assert m == 2.0 and eta == pytest.approx(376.730313668 / 2.0, rel=1e-15)
+    for eps, mu in ((2.5 - 0.2j, 1.0), (2.0, 1.5 - 0.2j), (-2.0 - 1j, 1.0), (-2.0, -1.0)):
+        m, eta = pen.medium_index(eps, mu)
+        assert m.imag <= 0.0 and m.real > 0.0
+        assert abs(m * m - complex(eps) * complex(mu)) <= 1e-14 * abs(m * m)
+        assert eta == pytest.approx(376.730313668 * complex(mu) / m, rel=1e-15)
+    with pytest.raises(NotImplementedError, match="imaginary"):
+        pen.medium_index(-2.0, 1.0)
     with pytest.raises(ValueError):
-        pen.lossless_medium(float("nan"), 1.0)
+        pen.medium_index(float("nan"), 1.0)
 
 
 def test_drop_in_medium_operators(pkg, oracle, emulated):
@@ -151,3 +203,23 @@ def test_drop_in_medium_operators(pkg, oracle, emulated):
     for m in D["modes"]:
         P = se.assemble_pmchwt_P(int(m), M)
         assert np.max(np.abs(P - D[f"Pe_{int(m)}"])) <= 1e-11 * np.max(np.abs(P)), m
+
+
+def test_drop_in_lossy_medium_operators(pkg, oracle, emulated):
+    """BorPecSolver(medium=(2.5 - 0.2j, 1)): T and P through the complex-k
+    fills equal the reference's (tests/golden/pmchwt_sphere_n24.npz, modes 0
+    and 2); its MFIE operator and streamed blocks are not provided."""
+    D = load_golden("pmchwt_sphere_n24")
+    M, f = int(D["m_max"]), float(D["freq_hz"])
+    eps, mu = (complex(x) for x in D["media"][0])
+    emulated["media"].append((f, eps, mu))
+    s = pkg.bor_solver.BorPecSolver(D["points"], f, medium=(eps, mu))
+    for m in D["modes"]:
+        m = int(m)
+        T, P = s.assemble_mode(m, M), s.assemble_pmchwt_P(m, M)
+        assert np.max(np.abs(T - D[f"Ti_{m}"])) <= 1e-11 * np.max(np.abs(T)), m
+        assert np.max(np.abs(P - D[f"Pi_{m}"])) <= 1e-11 * np.max(np.abs(P)), m
+    with pytest.raises(NotImplementedError):
+        s.assemble_mfie_mode(0, M)
+    with pytest.raises(NotImplementedError):
+        s.enable_streaming(M)

@@ -162,12 +162,14 @@ def test_drop_in_arguments_and_no_cpu_fallback(pkg):
     with pytest.raises(InterruptedError):
         bs.solve_bor(pts, f, [0.0], check_abort=abort)
     with pytest.raises(NotImplementedError):
-        bs.BorPecSolver(pts, f, medium=(2.0 - 0.1j, 1.0))       # lossy: complex wave number
+        bs.BorPecSolver(pts, f, medium=(-2.0, 1.0))              # evanescent: Re m = 0
     with pytest.raises(NotImplementedError):
-        bs.solve_bor_dielectric(pts, f, [0.0], 2.0 - 0.1j, 1.0)
+        bs.solve_bor_dielectric(pts, f, [0.0], -2.0, 1.0)
     if not torch.cuda.is_available():
         with pytest.raises(RuntimeError, match="no CPU fallback"):
             bs.solve_bor_dielectric(pts, f, [0.0], 2.0, 1.0)
+        with pytest.raises(RuntimeError, match="no CPU fallback"):
+            bs.solve_bor_dielectric(pts, f, [0.0], 2.0 - 0.1j, 1.0)
         with pytest.raises(RuntimeError, match="no CPU fallback"):
             bs.solve_bor(pts, f, [0.0, 90.0])
         with pytest.raises(RuntimeError, match="no CPU fallback"):

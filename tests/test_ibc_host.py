@@ -51,6 +51,8 @@ def shim(tmp_path_factory):
         getattr(lib, name).restype = None
     lib.host_sample_ibc.argtypes = SAMPLER_ARGS
     lib.host_sample_ibc.restype = None
+    lib.host_complex_k.argtypes = [ctypes.c_int, dp, dp]
+    lib.host_complex_k.restype = None
     return lib
 
 
@@ -238,3 +240,20 @@ def test_impedance_parsing_and_errors(pkg):
         s._zs_elem(np.arange(s.P, dtype=complex))          # not constant on each element
     ze = np.arange(12, dtype=complex)
     np.testing.assert_array_equal(s._zs_elem(ze[s.g.elem], ze), ze)
+
+
+def test_complex_wave_number_samples(shim):
+    """The lossy-medium fills' samples (csrc/medium.cuh, compiled for the
+    host): e^{-jkR}/R, (1 + jkR) e^{-jkR}/R^3 and 1/k^2 for k = k_r + j k_i,
+    k_i <= 0, equal the complex formulas."""
+    rng = np.random.default_rng(8)
+    n = 500
+    v = np.ascontiguousarray(np.stack([rng.uniform(1e-3, 3.0, n), rng.uniform(0.5, 200.0, n),
+                                       -rng.uniform(0.0, 30.0, n)], axis=1))
+    out = np.empty((n, 6))
+    shim.host_complex_k(n, _ptr(v), _ptr(out))
+    R, k = v[:, 0], v[:, 1] + 1j * v[:, 2]
+    for got, want in ((out[:, 0] + 1j * out[:, 1], np.exp(-1j * k * R) / R),
+                      (out[:, 2] + 1j * out[:, 3], (1 + 1j * k * R) * np.exp(-1j * k * R) / R ** 3),
+                      (out[:, 4] + 1j * out[:, 5], 1.0 / k ** 2)):
+        assert np.max(np.abs(got - want) / np.abs(want)) < 1e-13

@@ -122,3 +122,19 @@ def test_dielectric_solve_calls(pkg, calls):
     assert {"ghost_bor_getrf", "ghost_bor_getrs", "ghost_bor_residual64"} <= set(used)
     s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]), medium=(4.0, 1.0))
     assert s.assemble_mode(1, 3).shape == s.assemble_pmchwt_P(-1, 3).shape == (2 * s.Nn, 2 * s.Nn)
+
+
+def test_lossy_dielectric_calls(pkg, calls):
+    """A lossy medium's interior goes through the complex-wave-number fills."""
+    D = load_golden("pmchwt_sphere_n24")
+    pkg.bor_solver.solve_bor_dielectric(D["points"], float(D["freq_hz"]), D["thetas"][:2], 2.5 - 0.2j, 1.0,
+                                        n_modes=3, mode_tol=0.0)
+    used = [c for c in calls if not c.endswith("_workspace")]
+    assert used.count("ghost_bor_far_efie_ck") == 2 and used.count("ghost_bor_near_efie_ck") == 2
+    assert used.count("ghost_bor_far_ibc_ck") == 1 and used.count("ghost_bor_near_ibc_ck") == 1
+    assert used.count("ghost_bor_far_efie_masked") == 2 and used.count("ghost_bor_far_ibc") == 1
+    s = pkg.bor_solver.BorPecSolver(D["points"], float(D["freq_hz"]), medium=(2.5 - 0.2j, 1.0))
+    del calls[:]
+    assert s.assemble_mode(1, 3).shape == s.assemble_pmchwt_P(-1, 3).shape == (2 * s.Nn, 2 * s.Nn)
+    assert {"ghost_bor_far_efie_ck", "ghost_bor_near_efie_ck", "ghost_bor_far_ibc_ck",
+            "ghost_bor_near_ibc_ck"} <= set(calls)
