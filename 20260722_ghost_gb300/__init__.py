@@ -2,8 +2,8 @@
 
 Drop-in modules mirroring the reference project's entry points:
 
-    bor_solver     solve_bor (PEC and surface impedance), solve_bor_dielectric (lossless
-                   PMCHWT), solve_bor_pec, solve_bor_batch, BorPecSolver, sphere_generatrix, ...
+    bor_solver     solve_bor (PEC and surface impedance), solve_bor_dielectric
+                   (PMCHWT), solve_bor_pec, solve_bor_batch, BorPecSolver, sphere_generatrix, ...
     batch          BorGpuBatch (size classes, CUDA-graph replay), Autotuner
     bor_streaming  StreamingFarBlocks, estimate_streaming_gb
     adjoint        bspline_rcs (torch.autograd.Function), ShapeGradient

@@ -18,7 +18,7 @@ Scope: bodies whose segments are all TYPE 2 conductors -- PEC (CFIE, or EFIE
 when cfie_alpha <= 0) and conductors with surface-impedance (IBC) flags,
 whose Z_s per element comes from the snapshot's material tables
 (materials.MaterialLibrary) and which are solved with the IBC-EFIE -- and
-homogeneous TYPE 3 dielectric bodies (PMCHWT, lossless media on the GPU).
+homogeneous TYPE 3 dielectric bodies (PMCHWT).
 The multi-region kinds (TYPE 3+4 coated, TYPE 2+3+4 partial coating, TYPE
 3+4+5 layered) are recognised and rejected with NotImplementedError;
 malformed snapshots and material tables raise as in the reference.

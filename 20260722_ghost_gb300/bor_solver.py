@@ -1,5 +1,5 @@
 """Drop-in replacement for the reference module ``bor_solver`` (PEC,
-surface-impedance and homogeneous lossless dielectric bodies).
+surface-impedance and homogeneous dielectric bodies).
 
 Same entry points, keyword arguments and result keys as the reference
 (bor_solver.py:820-1004 ``solve_bor``, :1007 ``solve_bor_pec``, :175-708

@@ -64,18 +64,6 @@ def medium_index(eps_r, mu_r):
     return m, ETA0 * (mu / m)
 
 
-def lossless_medium(eps_r, mu_r):
-    """(refractive index, eta_i) of a lossless medium (real eps_r, mu_r > 0);
-    NotImplementedError for any other."""
-    eps, mu = complex(eps_r), complex(mu_r)
-    if not all(math.isfinite(v) for v in (eps.real, eps.imag, mu.real, mu.imag)):
-        raise ValueError("eps_r and mu_r must be finite")
-    if eps.imag != 0.0 or mu.imag != 0.0 or eps.real <= 0.0 or mu.real <= 0.0:
-        raise NotImplementedError("not a lossless medium: real eps_r > 0 and mu_r > 0 take the real-k fills")
-    n = math.sqrt(eps.real * mu.real)
-    return n, ETA0 * (mu.real / n)
-
-
 def solve_fp64(Z, X, stream: int):
     """X <- Z^-1 X for every mode (ghost_bor_getrf / getrs, FP64; Z is
     overwritten by its factors).  Returns the per-mode LU info."""
