@@ -82,23 +82,27 @@ def solve_bor(points, freq_hz: float, thetas_deg, formulation: str = "efie",
     thetas = np.atleast_1d(np.asarray(thetas_deg, dtype=float))
     prob = BorGpuProblem(points, freq_hz, thetas, m_max=n_modes, gauss_order=gauss_order,
                          formulation=form, cfie_alpha=cfie_alpha, zs=zs)
-    # interior-resonance guard of the reference (bor_solver.py:955-985): a
-    # closed body on the EFIE with a lossless (purely reactive) Z_s
-    warnings: List[str] = []
+    warnings = _resonance_monitor(prob, form)
+    t_setup = time.perf_counter()
+    res = prob.sweep(precision=precision, check_abort=check_abort)
+    return _result(prob, res, thetas, form, precision, mode_tol, progress, t_wall, t_setup, warnings)
+
+
+def _resonance_monitor(prob: BorGpuProblem, form: str) -> List[str]:
+    """Interior-resonance guard of the reference (bor_solver.py:955-985): a
+    closed body on the EFIE with a lossless (purely reactive) Z_s gets the
+    per-mode condition numbers and a warning."""
     closed = prob.gen.node_on_axis(0) and prob.gen.node_on_axis(prob.Nn - 1)
     lossless = (prob.zs is not None and
                 float(np.max(np.abs(np.real(prob.zs)))) < 1e-3 * float(np.max(np.abs(prob.zs))))
     prob.monitor_cond = form == "efie" and closed and lossless
-    if prob.monitor_cond:
-        warnings.append(
-            "Closed body with a lossless (purely reactive) surface impedance "
+    if not prob.monitor_cond:
+        return []
+    return ["Closed body with a lossless (purely reactive) surface impedance "
             "on the EFIE: interior cavity resonances are undamped, and "
             "results at resonant frequencies may be silently corrupted. "
             "Inspect max_cond across the frequency sweep for spikes, add "
-            "loss to Z_s, or avoid closed-body reactive IBC.")
-    t_setup = time.perf_counter()
-    res = prob.sweep(precision=precision, check_abort=check_abort)
-    return _result(prob, res, thetas, form, precision, mode_tol, progress, t_wall, t_setup, warnings)
+            "loss to Z_s, or avoid closed-body reactive IBC."]
 
 
 def _result(prob: BorGpuProblem, res, thetas, form: str, precision: str, mode_tol: float,
@@ -155,11 +159,13 @@ def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: f
     """Monostatic RCS of many bodies of revolution on one GPU.
 
     ``bodies``: iterable of dicts with ``points``, ``freq_hz`` and optionally
-    ``n_modes`` (or ``m_max``).  FP32+IR EFIE sweeps run as size classes
+    ``n_modes`` (or ``m_max``) and ``zs`` (surface impedance, as in
+    solve_bor).  FP32+IR EFIE sweeps of PEC bodies run as size classes
     (batch.BorGpuBatch): the bodies of a class share one LU, one set of
     substitutions and one refinement for all their modes, and each class's
     sweep is a captured CUDA graph; the class width and the near-fill grid come
-    from the autotuner's cache.  FP64 and CFIE / MFIE sweeps run body by body,
+    from the autotuner's cache.  FP64, CFIE / MFIE and impedance sweeps run
+    body by body,
     the next body's host set-up overlapping the current sweep.  Returns one
     ``solve_bor`` result dict per body, in order.  No counterpart in the
     reference (its callers loop over bodies).
@@ -174,11 +180,13 @@ def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: f
         t0 = time.perf_counter()
         m = b.get("n_modes", b.get("m_max"))
         prob = BorGpuProblem(b["points"], float(b["freq_hz"]), thetas, m_max=m,
-                             formulation=form, cfie_alpha=cfie_alpha)
+                             formulation=form, cfie_alpha=cfie_alpha, zs=b.get("zs"))
         return prob, t0, time.perf_counter()
 
     out: List[Dict] = []
-    if precision == "fp32ir" and form == "efie" and items:
+    pec = all(b.get("zs") is None or not np.any(np.abs(np.asarray(b["zs"], dtype=complex)) > 0.0)
+              for b in items)
+    if precision == "fp32ir" and form == "efie" and items and pec:
         from .batch import Autotuner, BorGpuBatch
         with ThreadPoolExecutor(max_workers=4) as ex:
             made = list(ex.map(setup, items))
@@ -195,8 +203,9 @@ def solve_bor_batch(bodies, thetas_deg, formulation: str = "efie", cfie_alpha: f
         for i in range(len(items)):
             prob, t0, t1 = nxt.result()
             nxt = ex.submit(setup, items[i + 1]) if i + 1 < len(items) else None
+            warnings = _resonance_monitor(prob, form)
             res = prob.sweep(precision=precision)
-            out.append(_result(prob, res, thetas, form, precision, mode_tol, None, t0, t1))
+            out.append(_result(prob, res, thetas, form, precision, mode_tol, None, t0, t1, warnings))
             if progress is not None:
                 progress(i + 1, len(items))
             del prob, res

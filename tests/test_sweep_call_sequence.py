@@ -138,3 +138,17 @@ def test_lossy_dielectric_calls(pkg, calls):
     assert s.assemble_mode(1, 3).shape == s.assemble_pmchwt_P(-1, 3).shape == (2 * s.Nn, 2 * s.Nn)
     assert {"ghost_bor_far_efie_ck", "ghost_bor_near_efie_ck", "ghost_bor_far_ibc_ck",
             "ghost_bor_near_ibc_ck"} <= set(calls)
+
+
+def test_batch_with_impedance_bodies(pkg, calls):
+    """solve_bor_batch with a per-body Z_s: the impedance bodies are swept one
+    by one (their fills and far-field vector), the lossless-Z_s monitor as in
+    solve_bor."""
+    D = load_golden("ibc_conesphere_n40")
+    items = [{"points": D["points"], "freq_hz": float(D["freq_hz"]), "n_modes": 3, "zs": D["zs_taper"]},
+             {"points": D["points"], "freq_hz": float(D["freq_hz"]), "n_modes": 3, "zs": -40j}]
+    out = pkg.bor_solver.solve_bor_batch(items, [0.0, 90.0])
+    assert len(out) == 2
+    assert "max_cond" not in out[0] and "max_cond" in out[1]
+    assert any("lossless" in w for w in out[1]["warnings"])
+    assert IBC_CALLS <= set(calls)
